@@ -1,0 +1,362 @@
+"""Benchmark: Mpaths/s of the wavefront path tracer on the 1M-triangle scene.
+
+Workload (one step = one progressive frame): 12 instances of a level-6
+icosphere (81,920 triangles each) + a 2-triangle ground plane + 100k
+alpha-tested quads (64 distinct 512x512 RGBA8 value-noise masks, 50% cut
+out), Hosek-Wilkie sky (sun elevation 30 deg, turbidity 3) baked to a
+2048x1024 FP16 lat-long map with importance sampling, 4 point lights;
+1920x1080, 1 sample per pixel per frame, max depth 8, reference shading
+policy.  Synthetic, seeded procedural data.
+
+value     = paths / device time of K frames (CUDA events on the library stream)
+e2e       = the same through the C-ABI with the frame constants passed from
+            the host and the tone-mapped RGBA8 frame copied to pinned host
+            memory every step (host wall clock)
+roofline  = closest-hit traversal kernel: algorithmic bytes per launch / its
+            mean launch time (bytes = rays x (ray 36 B + hit 16 B) +
+            node fetches x 80 B + triangle tests x 48 B, counted in a separate
+            counting pass of the same frame)
+
+--impl reference times the oracle's scalar transcription of the reference
+shaders (the reference's Vulkan path cannot run without a graphics stack) on
+all host cores, on a bounded sample of the same frame.
+"""
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WIDTH, HEIGHT, DEPTH = 1920, 1080, 8
+METRIC = "Mpaths/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Dist:
+    """Host-side barrier / max-reduce across replica ranks (gloo); no data-path collective."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def allreduce(self, x, op):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX if op == "max" else self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+def workload_config():
+    return {"workload": "icospheres_1M_alpha_quads_sky_1080p_1spp_depth8", "scene": "12 x level-6 icosphere "
+            "(983,040 tris) + 2-tri ground + 100k alpha quads (200k tris; 64 masks 512^2, 50% cutout)",
+            "width": WIDTH, "height": HEIGHT, "spp_per_step": 1, "max_depth": DEPTH, "policy": "reference + "
+            "importance-sampled environment", "env": "Hosek-Wilkie sun 30 deg turbidity 3, 2048x1024 FP16",
+            "l2": "per-frame working set (path state 2.07M x 176 B + BVH/scene) larger than L2; no flush"}
+
+
+def make_scene(hx):
+    return hx.HostScene(hx.SCENE_ICOSPHERES)
+
+
+def make_policy(hx):
+    pol = hx.policy_reference()
+    pol.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
+    return pol
+
+
+def idesc(hx, pol):
+    d = hx.IntegratorDesc()
+    d.width, d.height, d.max_ray_bounces, d.max_samples = WIDTH, HEIGHT, DEPTH, 1 << 30
+    d.policy = pol
+    return d
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(hs, hx, pol, seconds, threads=0):
+    """Oracle (scalar FP32 transcription of the reference shaders) on whole
+    image rows of the same frame until the time budget is used."""
+    from oracle import binding as ob
+    osc = ob.OracleScene(hs)
+    d = idesc(hx, pol)
+    f = hx.frame_desc(hs.camera(), WIDTH, HEIGHT)
+    paths = segs = 0
+    secs = 0.0
+    row = HEIGHT // 2 - 8
+    rows_done = 0
+    chunk = 8
+    thr = 0
+    while secs < seconds and rows_done < HEIGHT:
+        r0 = (row + rows_done) % HEIGHT
+        n = min(chunk, HEIGHT - r0)
+        import numpy as np
+        pix = (np.arange(r0, r0 + n)[:, None] * WIDTH + np.arange(WIDTH)[None, :]).ravel().astype(np.uint32)
+        _, cnt = osc.render(d, f, 1, precision=32, pixels=pix, threads=threads)
+        paths += cnt.paths
+        segs += cnt.extension_rays + cnt.shadow_rays
+        secs += cnt.seconds
+        thr = cnt.threads
+        rows_done += n
+        chunk = min(64, chunk * 2)
+    osc.close()
+    return {"paths": paths, "segments": segs, "seconds": secs, "threads": thr, "rows": rows_done}
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return
+    import helios_gb300 as hx
+    hs = make_scene(hx)
+    pol = make_policy(hx)
+    per_step = []
+    total_paths = 0
+    total_secs = 0.0
+    thr = 0
+    budget = max(1.0, args.cpu_seconds / 4)
+    for k in range(args.warmup + args.steps):
+        r = cpu_sample(hs, hx, pol, budget)
+        if k >= args.warmup:
+            per_step.append(r["seconds"] * 1000.0)
+            total_paths += r["paths"]
+            total_secs += r["seconds"]
+            thr = r["threads"]
+    value = total_paths / total_secs / 1e6
+    sample = "%d frame rows of 1920 px per step (%.1f s budget), 1 spp, depth 8" % (r["rows"], budget)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(per_step),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": thr, "kind": "port", "sample": sample,
+                             "cpu": cpu_model()},
+            "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, dist):
+    import numpy as np
+    import helios_gb300 as hx
+    ctx = hx.Context(dist.local)
+    hs = make_scene(hx)
+    scene = hx.Scene(ctx, hs)
+    info = scene.info()
+    pol = make_policy(hx)
+    it = hx.PathIntegrator(ctx, scene, WIDTH, HEIGHT, max_ray_bounces=DEPTH, max_samples=1 << 30, policy=pol)
+    frame = hx.frame_desc(hs.camera(), WIDTH, HEIGHT)
+    paths_per_step = WIDTH * HEIGHT
+
+    # 1) stage breakdown + segment counts (timing mode syncs per stage: not the timed region)
+    it.set_timing(True)
+    it.render(frame)
+    st = it.stats()
+    segs_per_step = st.extension_rays + st.shadow_rays
+    ms_trace_per_launch = st.ms_trace / max(1, st.trace_launches)
+    stage = {"raygen": st.ms_raygen, "trace": st.ms_trace, "shade": st.ms_shade, "shadow": st.ms_shadow,
+             "accumulate": st.ms_accumulate}
+    it.set_timing(False)
+    # 2) counting pass: node fetches and triangle tests of the closest-hit launches
+    it.set_counting(True)
+    it.render(frame)
+    ct = it.stats()
+    it.set_counting(False)
+    ext_rays = ct.extension_rays
+    trav_bytes = ct.node_visits * 80 + ct.tri_tests * 48
+    alg_bytes_per_launch = (ext_rays * (36 + 16) + trav_bytes) / max(1, ct.trace_launches)
+
+    # 3) warm-up, then K device-timed frames
+    for _ in range(args.warmup):
+        it.render(frame)
+    ctx.synchronize()
+    events = [hx.Event(ctx) for _ in range(args.steps + 1)]
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    ctx.synchronize()
+    clocks.start()
+    launches_before = 0
+    events[0].record()
+    launches = 0
+    for k in range(args.steps):
+        it.render(frame)
+        launches += it.stats().kernel_launches
+        events[k + 1].record()
+    frame_ms = [events[k].elapsed_ms(events[k + 1]) for k in range(args.steps)]
+    ctx.synchronize()
+    clk = clocks.stop()
+    total_ms = events[0].elapsed_ms(events[-1])
+    total_ms = dist.allreduce(total_ms, "max")
+    paths_all = dist.allreduce(paths_per_step * args.steps, "sum")
+    value = paths_all / (total_ms / 1000.0) / 1e6
+    seg_rate = dist.allreduce(segs_per_step * args.steps, "sum") / (total_ms / 1000.0) / 1e6
+
+    # 4) end to end through the C-ABI: frame constants from the host, tone-mapped frame to pinned host memory
+    out = hx.PinnedBuffer((HEIGHT, WIDTH, 4), np.uint8)
+    for _ in range(2):
+        it.render(frame)
+        hx.check(hx.lib().hx_integrator_tonemap(it.handle, hx.TONEMAP_ACES, 1.0, out.array.ctypes.data))
+    dist.barrier()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        it.render(frame)
+        hx.check(hx.lib().hx_integrator_tonemap(it.handle, hx.TONEMAP_ACES, 1.0, out.array.ctypes.data))
+    ctx.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_s = dist.allreduce(e2e_s, "max")
+    e2e_value = paths_all / e2e_s / 1e6
+    launches_e2e = launches + args.steps  # + one tone-map launch per step
+    out.close()
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes_per_launch / (ms_trace_per_launch / 1000.0) / 1e9
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "trace_kernel_traffic.json")))
+        traffic = prof["dram_bytes_per_extension_ray"] * ext_rays / max(1, ct.trace_launches)
+    except Exception:
+        pass
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        r = cpu_sample(hs, hx, pol, args.cpu_seconds)
+        cpu = {"value": r["paths"] / r["seconds"] / 1e6, "unit": "Mpaths/s", "cores": r["threads"], "kind": "port",
+               "sample": "%d rows x 1920 px of the same frame, 1 spp, depth 8 (%.1f s)" % (r["rows"], r["seconds"]),
+               "cpu": cpu_model(), "mray_segments_per_s": r["segments"] / r["seconds"] / 1e6}
+
+    it.close()
+    scene.close()
+    if dist.rank == 0:
+        fs = sorted(frame_ms)
+        line = {"metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": dist.world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": dict(workload_config(), parallelism="replicas" if dist.world > 1 else "single"),
+                "mray_segments_per_s": seg_rate,
+                "frame_latency_ms": {"p50": float(np.percentile(fs, 50)), "p99": float(np.percentile(fs, 99)),
+                                     "max": fs[-1]},
+                "segments_per_path": segs_per_step / paths_per_step,
+                "stage_ms_per_frame": stage,
+                "scene": {"triangles": info.num_triangles, "bvh8_nodes": info.num_bvh8_nodes,
+                          "build_ms": info.build_ms, "device_mb": info.device_bytes / 2**20},
+                "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 128,
+                        "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
+                "gpu_launches": launches_e2e,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": achieved / hbm_peak, "traffic": traffic,
+                             "kernel": "k_trace (closest hit)", "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                             "bytes_per_launch": alg_bytes_per_launch, "ms_per_launch": ms_trace_per_launch,
+                             "node_fetches_per_ray": ct.node_visits / max(1, ext_rays),
+                             "tri_tests_per_ray": ct.tri_tests / max(1, ext_rays)},
+                "clocks": clk,
+                "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,537 @@
+"""helios_gb300 — Python view of the helios-gb300 C-ABI (include/hx.h).
+
+The product is the CUDA library ``libhx.so`` (sm_103a); this module is a thin
+ctypes mirror of its C-ABI plus the engine-shaped classes the reference
+exposes to its renderer (``PathIntegrator``, ``Renderer``, ``Scene``).  There
+is no CPU fallback: every call goes to the CUDA library and fails loudly when
+it is missing or when no GB300 is present.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libhx.so")
+
+# status codes (hx_status)
+HX_OK, HX_ERR_INVALID_ARG, HX_ERR_OOM_BUDGET, HX_ERR_TIMEOUT, HX_ERR_DEVICE, HX_ERR_NOT_READY, \
+    HX_ERR_UNSUPPORTED, HX_ERR_CANCELLED = range(8)
+LIGHT_DIRECTIONAL, LIGHT_SPOT, LIGHT_POINT, LIGHT_ENVIRONMENT, LIGHT_AREA = range(5)
+ENV_NONE, ENV_EQUIRECT, ENV_HOSEK_WILKIE = range(3)
+RNG_XOROSHIRO64STAR, RNG_PCG = 0, 1
+ACCUM_RUNNING_MEAN, ACCUM_KAHAN = 0, 1
+ENV_SAMPLE_COSINE, ENV_SAMPLE_IMPORTANCE = 0, 1
+PAYLOAD_FP32, PAYLOAD_FP16 = 0, 1
+TONEMAP_ACES, TONEMAP_REINHARD, TONEMAP_NONE = 0, 1, 2
+SCENE_BOX, SCENE_ICOSPHERES = 0, 1
+SUBMESH_NON_OPAQUE = 1
+NO_HIT = 0xFFFFFFFF
+
+
+class HxError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("hx status %d: %s" % (status, msg))
+        self.status = status
+
+
+# ---------------------------------------------------------------------------
+# Struct mirrors (layouts of include/hx.h)
+# ---------------------------------------------------------------------------
+class Vertex(C.Structure):
+    _fields_ = [("position", C.c_float * 4), ("tex_coord", C.c_float * 4), ("normal", C.c_float * 4),
+                ("tangent", C.c_float * 4), ("bitangent", C.c_float * 4)]
+
+
+class Submesh(C.Structure):
+    _fields_ = [("base_index", C.c_uint32), ("index_count", C.c_uint32), ("material", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("vertices", C.POINTER(Vertex)), ("num_vertices", C.c_uint32),
+                ("indices", C.POINTER(C.c_uint32)), ("num_indices", C.c_uint32),
+                ("submeshes", C.POINTER(Submesh)), ("num_submeshes", C.c_uint32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("texture_indices0", C.c_int32 * 4), ("texture_indices1", C.c_int32 * 4),
+                ("albedo", C.c_float * 4), ("emissive", C.c_float * 4), ("roughness_metallic", C.c_float * 4)]
+
+
+class Light(C.Structure):
+    _fields_ = [("data0", C.c_float * 4), ("data1", C.c_float * 4), ("data2", C.c_float * 4),
+                ("data3", C.c_float * 4)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("model_matrix", C.c_float * 16), ("normal_matrix", C.c_float * 16), ("mesh_index", C.c_uint32),
+                ("material_override", C.c_int32), ("padding", C.c_float * 2)]
+
+
+class TextureDesc(C.Structure):
+    _fields_ = [("rgba8", C.POINTER(C.c_uint8)), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class EnvironmentDesc(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("rgba32f", C.POINTER(C.c_float)), ("sun_direction", C.c_float * 4), ("coeffs", C.c_float * 40)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("meshes", C.POINTER(MeshDesc)), ("num_meshes", C.c_uint32),
+                ("instances", C.POINTER(Instance)), ("num_instances", C.c_uint32),
+                ("materials", C.POINTER(Material)), ("num_materials", C.c_uint32),
+                ("textures", C.POINTER(TextureDesc)), ("num_textures", C.c_uint32),
+                ("punctual_lights", C.POINTER(Light)), ("num_punctual_lights", C.c_uint32),
+                ("environment", EnvironmentDesc)]
+
+
+class Policy(C.Structure):
+    _fields_ = [("rng", C.c_uint32), ("rr_start_depth", C.c_uint32), ("rr_clamp", C.c_uint32),
+                ("radiance_clamp", C.c_float), ("accumulation", C.c_uint32), ("area_count_from_x", C.c_uint32),
+                ("area_w_one", C.c_uint32), ("env_sampling", C.c_uint32), ("payload", C.c_uint32),
+                ("reserved", C.c_uint32 * 3)]
+
+
+class IntegratorDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("max_ray_bounces", C.c_uint32),
+                ("max_samples", C.c_uint32), ("shadow_ray_bias", C.c_float), ("tiled", C.c_uint32),
+                ("max_paths_in_flight", C.c_uint32), ("reserved", C.c_uint32), ("policy", Policy)]
+
+
+class FrameDesc(C.Structure):
+    _fields_ = [("view_proj_inverse", C.c_float * 16), ("camera_pos", C.c_float * 4),
+                ("up_direction", C.c_float * 4), ("right_direction", C.c_float * 4),
+                ("focal_plane", C.c_float * 4), ("focal_length", C.c_float), ("aperture_radius", C.c_float),
+                ("reserved", C.c_float * 2)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_y_degrees", C.c_float), ("near_plane", C.c_float), ("far_plane", C.c_float),
+                ("focal_length", C.c_float), ("aperture_radius", C.c_float)]
+
+
+class Hit(C.Structure):
+    _fields_ = [("t", C.c_float), ("prim", C.c_uint32), ("u", C.c_float), ("v", C.c_float)]
+
+
+HIT_DTYPE = np.dtype([("t", np.float32), ("prim", np.uint32), ("u", np.float32), ("v", np.float32)])
+
+
+class Stats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("ms_total", C.c_double), ("ms_raygen", C.c_double), ("ms_trace", C.c_double),
+                ("ms_shade", C.c_double), ("ms_shadow", C.c_double), ("ms_accumulate", C.c_double),
+                ("trace_launches", C.c_uint32), ("kernel_launches", C.c_uint32),
+                ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint32), ("num_bvh8_nodes", C.c_uint32), ("num_binary_nodes", C.c_uint32),
+                ("num_lights", C.c_uint32), ("device_bytes", C.c_uint64), ("build_ms", C.c_double),
+                ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3)]
+
+
+class ProceduralParams(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("num_alpha_quads", C.c_uint32),
+                ("mask_pool", C.c_uint32), ("mask_size", C.c_uint32), ("icosphere_level", C.c_uint32),
+                ("env_width", C.c_uint32), ("env_height", C.c_uint32), ("sun_elevation_deg", C.c_float),
+                ("turbidity", C.c_float)]
+
+
+BVH8_NODE_BYTES = 80
+BVH8_DTYPE = np.dtype([("origin", np.float32, 3), ("exponent", np.int8, 3), ("internal_mask", np.uint8),
+                       ("child_base", np.uint32), ("prim_base", np.uint32), ("meta", np.uint8, 8),
+                       ("qlo", np.uint8, (3, 8)), ("qhi", np.uint8, (3, 8))])
+assert BVH8_DTYPE.itemsize == BVH8_NODE_BYTES
+
+# C-ABI entry points: name -> (restype, argtypes)
+_P = C.c_void_p
+_SIGS = {
+    "hx_version": (C.c_char_p, []),
+    "hx_last_error_string": (C.c_char_p, []),
+    "hx_policy_reference": (None, [C.POINTER(Policy)]),
+    "hx_policy_spec": (None, [C.POINTER(Policy)]),
+    "hx_camera_to_frame_desc": (C.c_int, [C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(FrameDesc)]),
+    "hx_context_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_P)]),
+    "hx_context_destroy": (C.c_int, [_P]),
+    "hx_context_synchronize": (C.c_int, [_P]),
+    "hx_context_memory": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "hx_scene_upload": (C.c_int, [_P, C.POINTER(SceneDesc), C.POINTER(_P)]),
+    "hx_scene_destroy": (C.c_int, [_P]),
+    "hx_scene_info_get": (C.c_int, [_P, C.POINTER(SceneInfo)]),
+    "hx_scene_lights": (C.c_int, [_P, C.POINTER(Light), C.c_uint32, C.POINTER(C.c_uint32)]),
+    "hx_scene_export_bvh": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+    "hx_scene_trace": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P]),
+    "hx_integrator_create": (C.c_int, [_P, _P, C.POINTER(IntegratorDesc), C.POINTER(_P)]),
+    "hx_integrator_destroy": (C.c_int, [_P]),
+    "hx_integrator_render": (C.c_int, [_P, C.POINTER(FrameDesc)]),
+    "hx_integrator_render_frames": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32]),
+    "hx_integrator_restart_bake": (C.c_int, [_P]),
+    "hx_integrator_set_max_ray_bounces": (C.c_int, [_P, C.c_uint32]),
+    "hx_integrator_set_max_samples": (C.c_int, [_P, C.c_uint32]),
+    "hx_integrator_set_shadow_ray_bias": (C.c_int, [_P, C.c_float]),
+    "hx_integrator_set_tiled": (C.c_int, [_P, C.c_uint32]),
+    "hx_integrator_set_policy": (C.c_int, [_P, C.POINTER(Policy)]),
+    "hx_integrator_progress": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "hx_integrator_tonemap": (C.c_int, [_P, C.c_uint32, C.c_float, _P]),
+    "hx_integrator_read_accumulation": (C.c_int, [_P, _P]),
+    "hx_integrator_set_timing": (C.c_int, [_P, C.c_uint32]),
+    "hx_integrator_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "hx_integrator_set_counting": (C.c_int, [_P, C.c_uint32]),
+    "hx_event_create": (C.c_int, [_P, C.POINTER(_P)]),
+    "hx_event_record": (C.c_int, [_P]),
+    "hx_event_elapsed": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
+    "hx_event_destroy": (C.c_int, [_P]),
+    "hx_pinned_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
+    "hx_pinned_free": (C.c_int, [_P]),
+    "hx_scene_export_env": (C.c_int, [_P, _P]),
+    "hx_integrator_primary_hits": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
+    "hx_integrator_sample_radiance": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
+    "hx_rng_streams": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P]),
+    "hx_procedural_defaults": (None, [C.c_uint32, C.POINTER(ProceduralParams)]),
+    "hx_procedural_scene_create": (C.c_int, [C.POINTER(ProceduralParams), C.POINTER(_P)]),
+    "hx_host_scene_desc": (C.POINTER(SceneDesc), [_P]),
+    "hx_host_scene_camera": (C.c_int, [_P, C.POINTER(Camera)]),
+    "hx_host_scene_destroy": (C.c_int, [_P]),
+    "hx_hosek_wilkie_coefficients": (C.c_int, [C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_float)]),
+}
+
+_lib_handle = None
+
+
+def lib():
+    """Loads libhx.so (built in-tree by ``__graft_entry__.build()``)."""
+    global _lib_handle
+    if _lib_handle is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("helios_gb300: CUDA library %s is missing; build it with "
+                               "python -c 'import __graft_entry__ as g; g.build()'" % LIB_PATH)
+        h = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(h, name)
+            f.restype = res
+            f.argtypes = args
+        _lib_handle = h
+    return _lib_handle
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def check(status):
+    if status != HX_OK:
+        raise HxError(status, lib().hx_last_error_string().decode())
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def policy_reference():
+    p = Policy()
+    lib().hx_policy_reference(C.byref(p))
+    return p
+
+
+def policy_spec():
+    p = Policy()
+    lib().hx_policy_spec(C.byref(p))
+    return p
+
+
+def frame_desc(camera, width, height):
+    f = FrameDesc()
+    check(lib().hx_camera_to_frame_desc(C.byref(camera), width, height, C.byref(f)))
+    return f
+
+
+def hosek_wilkie_coefficients(sun_direction, turbidity=3.0, normalized_sun_y=1.15):
+    d = (C.c_float * 3)(*sun_direction)
+    out = (C.c_float * 40)()
+    check(lib().hx_hosek_wilkie_coefficients(d, turbidity, normalized_sun_y, out))
+    return np.array(out[:], dtype=np.float32).reshape(10, 4)[:, :3]
+
+
+class HostScene:
+    """Seeded procedural scene (host arrays in the hx.h layouts)."""
+
+    def __init__(self, kind=SCENE_BOX, **overrides):
+        p = ProceduralParams()
+        lib().hx_procedural_defaults(kind, C.byref(p))
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        self.params = p
+        h = C.c_void_p()
+        check(lib().hx_procedural_scene_create(C.byref(p), C.byref(h)))
+        self.handle = h
+
+    @property
+    def desc(self):
+        return lib().hx_host_scene_desc(self.handle)
+
+    def camera(self):
+        c = Camera()
+        check(lib().hx_host_scene_camera(self.handle, C.byref(c)))
+        return c
+
+    def close(self):
+        if self.handle:
+            lib().hx_host_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One GPU + stream + HBM budget (the role of vk::Backend)."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0):
+        h = C.c_void_p()
+        check(lib().hx_context_create(device, hbm_budget_bytes, C.byref(h)))
+        self.handle = h
+
+    def synchronize(self):
+        check(lib().hx_context_synchronize(self.handle))
+
+    def memory(self):
+        u, b = C.c_uint64(), C.c_uint64()
+        check(lib().hx_context_memory(self.handle, C.byref(u), C.byref(b)))
+        return u.value, b.value
+
+    def rng_streams(self, kind, seeds, draws):
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        n = seeds.size // 2
+        out = np.zeros((n, draws), dtype=np.uint32)
+        check(lib().hx_rng_streams(self.handle, kind, _ptr(seeds), n, draws, _ptr(out)))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().hx_context_destroy(self.handle)
+            self.handle = None
+
+
+class Event:
+    """Device timestamp recorded on a context's stream."""
+
+    def __init__(self, ctx):
+        h = C.c_void_p()
+        check(lib().hx_event_create(ctx.handle, C.byref(h)))
+        self.handle = h
+
+    def record(self):
+        check(lib().hx_event_record(self.handle))
+
+    def elapsed_ms(self, end):
+        ms = C.c_float()
+        check(lib().hx_event_elapsed(self.handle, end.handle, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if self.handle:
+            lib().hx_event_destroy(self.handle)
+            self.handle = None
+
+
+class PinnedBuffer:
+    """Page-locked host memory viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        h = C.c_void_p()
+        check(lib().hx_pinned_alloc(nbytes, C.byref(h)))
+        self.handle = h
+        buf = (C.c_uint8 * nbytes).from_address(h.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def close(self):
+        if self.handle:
+            self.array = None
+            lib().hx_pinned_free(self.handle)
+            self.handle = None
+
+
+class Scene:
+    """Device-resident scene: flattened triangles, BVH8, lights, environment
+    (replaces Scene::create_gpu_resources and the BLAS/TLAS builds)."""
+
+    def __init__(self, ctx, desc):
+        self.ctx = ctx
+        self._src = desc  # keeps a HostScene alive during the copy
+        if hasattr(desc, "desc"):
+            desc = desc.desc
+        h = C.c_void_p()
+        d = desc if isinstance(desc, SceneDesc) else desc.contents
+        check(lib().hx_scene_upload(ctx.handle, C.byref(d), C.byref(h)))
+        self.handle = h
+
+    def info(self):
+        i = SceneInfo()
+        check(lib().hx_scene_info_get(self.handle, C.byref(i)))
+        return i
+
+    def lights(self):
+        n = C.c_uint32()
+        check(lib().hx_scene_lights(self.handle, None, 0, C.byref(n)))
+        arr = (Light * max(1, n.value))()
+        check(lib().hx_scene_lights(self.handle, arr, n.value, C.byref(n)))
+        return [arr[i] for i in range(n.value)]
+
+    def export_bvh(self):
+        info = self.info()
+        n = info.num_triangles
+        morton = np.zeros(n, np.uint32)
+        sorted_ = np.zeros(n, np.uint32)
+        children = np.zeros(max(0, 2 * (n - 1)), np.uint32)
+        nodes = np.zeros(info.num_bvh8_nodes, BVH8_DTYPE)
+        leaf = np.zeros(n, np.uint32)
+        check(lib().hx_scene_export_bvh(self.handle, _ptr(morton), _ptr(sorted_),
+                                        _ptr(children) if children.size else None, _ptr(nodes), _ptr(leaf)))
+        return dict(morton=morton, sorted=sorted_, children=children, nodes=nodes, leaf_prims=leaf)
+
+    def export_env(self, width, height):
+        out = np.zeros((height, width, 3), np.float32)
+        check(lib().hx_scene_export_env(self.handle, _ptr(out)))
+        return out
+
+    def trace(self, rays, any_hit=False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        check(lib().hx_scene_trace(self.handle, _ptr(rays), rays.shape[0], 1 if any_hit else 0, _ptr(hits)))
+        return hits
+
+    def close(self):
+        if self.handle:
+            lib().hx_scene_destroy(self.handle)
+            self.handle = None
+
+
+class PathIntegrator:
+    """Mirror of helios::PathIntegrator (include/gfx/path_integrator.h:9-62)."""
+
+    def __init__(self, ctx, scene, width, height, max_ray_bounces=7, max_samples=5000, shadow_ray_bias=0.0,
+                 tiled=False, policy=None, max_paths_in_flight=0):
+        d = IntegratorDesc()
+        d.width, d.height = width, height
+        d.max_ray_bounces, d.max_samples = max_ray_bounces, max_samples
+        d.shadow_ray_bias = shadow_ray_bias
+        d.tiled = 1 if tiled else 0
+        d.max_paths_in_flight = max_paths_in_flight
+        d.policy = policy if policy is not None else policy_reference()
+        self.desc = d
+        self.width, self.height = width, height
+        h = C.c_void_p()
+        check(lib().hx_integrator_create(ctx.handle, scene.handle, C.byref(d), C.byref(h)))
+        self.handle = h
+        self.ctx, self.scene = ctx, scene
+
+    def render(self, frame, num_frames=1):
+        check(lib().hx_integrator_render_frames(self.handle, C.byref(frame), num_frames))
+
+    def restart_bake(self):
+        check(lib().hx_integrator_restart_bake(self.handle))
+
+    def set_max_ray_bounces(self, n):
+        check(lib().hx_integrator_set_max_ray_bounces(self.handle, n))
+
+    def set_max_samples(self, n):
+        check(lib().hx_integrator_set_max_samples(self.handle, n))
+
+    def set_shadow_ray_bias(self, b):
+        check(lib().hx_integrator_set_shadow_ray_bias(self.handle, b))
+
+    def set_tiled(self, tiled):
+        check(lib().hx_integrator_set_tiled(self.handle, 1 if tiled else 0))
+
+    def set_policy(self, policy):
+        check(lib().hx_integrator_set_policy(self.handle, C.byref(policy)))
+
+    def progress(self):
+        a, t, g = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib().hx_integrator_progress(self.handle, C.byref(a), C.byref(t), C.byref(g)))
+        return a.value, t.value, g.value
+
+    def num_accumulated_samples(self):
+        return self.progress()[0]
+
+    def tile_idx(self):
+        return self.progress()[1]
+
+    def num_target_samples(self):
+        return self.progress()[2]
+
+    def read_accumulation(self):
+        out = np.zeros((self.height, self.width, 4), np.float32)
+        check(lib().hx_integrator_read_accumulation(self.handle, _ptr(out)))
+        return out
+
+    def tonemap(self, op=TONEMAP_ACES, exposure=1.0, to_host=True):
+        out = np.zeros((self.height, self.width, 4), np.uint8) if to_host else None
+        check(lib().hx_integrator_tonemap(self.handle, op, exposure, _ptr(out)))
+        return out
+
+    def set_timing(self, on=True):
+        check(lib().hx_integrator_set_timing(self.handle, 1 if on else 0))
+
+    def set_counting(self, on=True):
+        check(lib().hx_integrator_set_counting(self.handle, 1 if on else 0))
+
+    def stats(self):
+        s = Stats()
+        check(lib().hx_integrator_stats(self.handle, C.byref(s)))
+        return s
+
+    def primary_hits(self, frame, frame_index=0):
+        out = np.zeros(self.width * self.height, HIT_DTYPE)
+        check(lib().hx_integrator_primary_hits(self.handle, C.byref(frame), frame_index, _ptr(out)))
+        return out
+
+    def sample_radiance(self, frame, frame_index=0):
+        out = np.zeros((self.width * self.height, 3), np.float32)
+        check(lib().hx_integrator_sample_radiance(self.handle, C.byref(frame), frame_index, _ptr(out)))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().hx_integrator_destroy(self.handle)
+            self.handle = None
+
+
+class Renderer:
+    """Mirror of the helios::Renderer surface this path owns
+    (include/gfx/renderer.h:83-97): render, tone-map operator, exposure,
+    save image."""
+
+    def __init__(self, integrator, tone_map_operator=TONEMAP_ACES, exposure=1.0):
+        self.integrator = integrator
+        self.tone_map_operator = tone_map_operator
+        self.exposure = exposure
+
+    def set_tone_map_operator(self, op):
+        self.tone_map_operator = op
+
+    def set_exposure(self, e):
+        self.exposure = e
+
+    def render(self, frame):
+        self.integrator.render(frame)
+        return self.integrator.tonemap(self.tone_map_operator, self.exposure, to_host=False)
+
+    def save_image_to_disk(self, path):
+        """Writes the tone-mapped RGBA8 image as binary PPM (no image
+        library dependency)."""
+        img = self.integrator.tonemap(self.tone_map_operator, self.exposure)
+        h, w = img.shape[:2]
+        with open(path, "wb") as f:
+            f.write(b"P6\n%d %d\n255\n" % (w, h))
+            f.write(np.ascontiguousarray(img[:, :, :3]).tobytes())
+        return img

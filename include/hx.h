@@ -1,0 +1,460 @@
+/*
+ * hx.h — C-ABI of the helios-gb300 path-tracing core (sm_103a).
+ *
+ * This is the drop-in boundary that replaces the Vulkan ray-tracing path of
+ * helios (diharaw/helios): the ray-gen / closest-hit / any-hit / miss / shadow
+ * shaders, the progressive accumulation and the tone-map pass.  The engine's
+ * C++ surface (helios::PathIntegrator, helios::Renderer, the packed scene
+ * buffers of helios::Scene) maps one-to-one onto the calls below; each
+ * declaration names the reference interface it replaces (path within the
+ * reference project, file:line).
+ *
+ * Rules of the ABI:
+ *   - plain C types, plain pointers and sizes; no C++ or framework types;
+ *   - every call returns hx_status; hx_last_error_string() gives the reason
+ *     of the last failure on the calling thread (no exceptions cross the ABI;
+ *     the reference logged and threw std::runtime_error, src/engine/gfx/vk.cpp:2306-2310);
+ *   - caller-owned host arrays are copied during the call; device memory is
+ *     owned by the library and charged to the context's HBM budget;
+ *   - all work of a context is ordered on that context's CUDA stream; one
+ *     context per host thread.
+ *
+ * Struct layouts marked "reference layout" keep the byte layout and field
+ * meaning of the reference's GPU buffers (std430), so a maintainer can pass
+ * the engine's packed arrays through unchanged.
+ */
+#ifndef HX_H
+#define HX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define HX_API __attribute__((visibility("default")))
+#else
+#define HX_API
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                              */
+/* ------------------------------------------------------------------------ */
+
+typedef enum hx_status {
+    HX_OK                = 0,
+    HX_ERR_INVALID_ARG   = 1,  /* bad pointer, size or enum value            */
+    HX_ERR_OOM_BUDGET    = 2,  /* allocation would exceed the HBM budget     */
+    HX_ERR_TIMEOUT       = 3,  /* a bounded device wait gave up              */
+    HX_ERR_DEVICE        = 4,  /* CUDA runtime error                         */
+    HX_ERR_NOT_READY     = 5,  /* result not available yet                   */
+    HX_ERR_UNSUPPORTED   = 6,  /* feature not built / not available          */
+    HX_ERR_CANCELLED     = 7   /* request cancelled before completion        */
+} hx_status;
+
+typedef struct hx_context    hx_context;
+typedef struct hx_scene      hx_scene;
+typedef struct hx_integrator hx_integrator;
+typedef struct hx_host_scene hx_host_scene;
+
+/* ------------------------------------------------------------------------ */
+/* Scene input — reference layouts                                           */
+/* ------------------------------------------------------------------------ */
+
+/* Vertex — reference layout include/resource/mesh.h:10-17 (5 x vec4 = 80 B).
+ * position.w carries the submesh index as written by the resource loader
+ * (src/engine/core/resource_manager.cpp:471-472). */
+typedef struct hx_vertex {
+    float position[4];
+    float tex_coord[4];
+    float normal[4];
+    float tangent[4];
+    float bitangent[4];
+} hx_vertex;
+
+/* Submesh flags. */
+#define HX_SUBMESH_NON_OPAQUE 1u  /* alpha-tested or non-opaque material:
+                                     the BLAS geometry lacks the OPAQUE bit
+                                     (src/engine/resource/mesh.cpp:75-76), so
+                                     any-hit alpha testing runs on it */
+
+/* SubMesh — include/resource/mesh.h:20-29 (the fields the path uses). */
+typedef struct hx_submesh {
+    uint32_t base_index;   /* first index (multiple of 3)                    */
+    uint32_t index_count;  /* number of indices (multiple of 3)              */
+    uint32_t material;     /* index into hx_scene_desc.materials             */
+    uint32_t flags;        /* HX_SUBMESH_*                                   */
+} hx_submesh;
+
+typedef struct hx_mesh_desc {
+    const hx_vertex*  vertices;
+    uint32_t          num_vertices;
+    const uint32_t*   indices;       /* absolute vertex indices              */
+    uint32_t          num_indices;
+    const hx_submesh* submeshes;
+    uint32_t          num_submeshes;
+} hx_mesh_desc;
+
+/* MaterialData — reference layout src/engine/resource/scene.cpp:25-32 and
+ * common.glsl:80-87 (80 B).  texture_indices0 = (albedo, normal, roughness,
+ * metallic), texture_indices1 = (emissive, -, roughness channel, metallic
+ * channel); -1 = no texture.  albedo is linear (the host already applied the
+ * sRGB->linear pow(2.2), scene.cpp:1017). */
+typedef struct hx_material {
+    int32_t texture_indices0[4];
+    int32_t texture_indices1[4];
+    float   albedo[4];
+    float   emissive[4];
+    float   roughness_metallic[4];
+} hx_material;
+
+/* Light types — src/engine/shader/common.glsl:12-16. */
+#define HX_LIGHT_DIRECTIONAL 0
+#define HX_LIGHT_SPOT        1
+#define HX_LIGHT_POINT       2
+#define HX_LIGHT_ENVIRONMENT 3
+#define HX_LIGHT_AREA        4
+
+/* LightData — reference layout src/engine/resource/scene.cpp:36-42,
+ * common.glsl:89-95 (64 B).  Only DIRECTIONAL / POINT / SPOT entries are
+ * passed in; the library derives the AREA and ENVIRONMENT entries and the
+ * list order itself (scene.cpp:1111-1119,1269-1309). */
+typedef struct hx_light {
+    float data0[4];  /* x: type, yzw: colour | area: x type, y instance, z material, w primitive offset */
+    float data1[4];  /* xyz: direction, w: intensity | area: x primitive count */
+    float data2[4];  /* xyz: position, w: radius */
+    float data3[4];  /* x: cos inner, y: cos outer */
+} hx_light;
+
+/* InstanceData — reference layout src/engine/resource/scene.cpp:46-52
+ * (144 B).  Matrices are column-major (GLM).  material_override replaces
+ * the submesh materials of this instance (-1 = none), the per-node
+ * override of scene.cpp:1125-1127. */
+typedef struct hx_instance {
+    float    model_matrix[16];
+    float    normal_matrix[16];
+    uint32_t mesh_index;
+    int32_t  material_override;
+    float    padding[2];
+} hx_instance;
+
+/* RGBA8 texture, linear UNORM, sampled bilinearly with REPEAT addressing at
+ * level 0 (textureLod(...,0) with the trilinear sampler, vk.cpp:3559-3580). */
+typedef struct hx_texture_desc {
+    const uint8_t* rgba8;
+    uint32_t       width;
+    uint32_t       height;
+} hx_texture_desc;
+
+#define HX_ENV_NONE          0u  /* black environment                        */
+#define HX_ENV_EQUIRECT      1u  /* caller-supplied RGBA32F lat-long map     */
+#define HX_ENV_HOSEK_WILKIE  2u  /* sky baked on the device from the model   */
+
+/* Environment.  The reference binds a 512^2 RGBA32F cubemap rendered by the
+ * Hosek-Wilkie raster pass (src/engine/gfx/hosek_wilkie_sky_model.cpp:658-764)
+ * or an IBL map.  Here the environment is a lat-long map (FP16 on the
+ * device) with a marginal/conditional CDF for importance sampling. */
+typedef struct hx_environment_desc {
+    uint32_t     kind;            /* HX_ENV_*                                   */
+    uint32_t     width, height;   /* lat-long resolution (e.g. 2048 x 1024)     */
+    const float* rgba32f;         /* HX_ENV_EQUIRECT: width*height*4 floats      */
+    float        sun_direction[4];/* HX_ENV_HOSEK_WILKIE: direction TO the sun  */
+    float        coeffs[40];      /* HX_ENV_HOSEK_WILKIE: A..I,Z as 10 x vec4
+                                     (the UBO of procedural_sky.frag:11-23)    */
+} hx_environment_desc;
+
+typedef struct hx_scene_desc {
+    const hx_mesh_desc*    meshes;          uint32_t num_meshes;
+    const hx_instance*     instances;       uint32_t num_instances;
+    const hx_material*     materials;       uint32_t num_materials;
+    const hx_texture_desc* textures;        uint32_t num_textures;
+    const hx_light*        punctual_lights; uint32_t num_punctual_lights;
+    hx_environment_desc    environment;
+} hx_scene_desc;
+
+/* ------------------------------------------------------------------------ */
+/* Integrator policy — reference-faithful vs benchmark-spec behaviour        */
+/* ------------------------------------------------------------------------ */
+
+#define HX_RNG_XOROSHIRO64STAR 0u /* Wang-hash seeded xoroshiro64*, random.glsl:17-50 */
+#define HX_RNG_PCG             1u /* PCG hash seeded per (pixel, sample)             */
+
+#define HX_ACCUM_RUNNING_MEAN  0u /* prev + (c - prev)/num_frames, path_trace_rgen.glsl:221-247 */
+#define HX_ACCUM_KAHAN         1u /* Kahan-compensated FP32 sum / n (precision form)            */
+
+#define HX_ENV_SAMPLE_COSINE     0u /* cosine-lobe env NEE, path_trace_rchit.glsl:366-372 */
+#define HX_ENV_SAMPLE_IMPORTANCE 1u /* lat-long CDF importance sampling                   */
+
+#define HX_PAYLOAD_FP32 0u
+#define HX_PAYLOAD_FP16 1u          /* FP16 ray / hit payloads (precision form)  */
+
+typedef struct hx_policy {
+    uint32_t rng;                 /* HX_RNG_*                                              */
+    uint32_t rr_start_depth;      /* RR at hits with depth >= this (0 = every depth)        */
+    uint32_t rr_clamp;            /* 1: RR probability clamped to <= 1                      */
+    float    radiance_clamp;      /* per-sample clamp (1.0 = RADIANCE_CLAMP_COLOR); <=0 off */
+    uint32_t accumulation;        /* HX_ACCUM_*                                            */
+    uint32_t area_count_from_x;   /* 1: read the area-light triangle count from data1.x     */
+    uint32_t area_w_one;          /* 1: transform area-light vertices with w = 1            */
+    uint32_t env_sampling;        /* HX_ENV_SAMPLE_*                                       */
+    uint32_t payload;             /* HX_PAYLOAD_*                                          */
+    uint32_t reserved[3];
+} hx_policy;
+
+/* Reference-faithful policy (every reference quirk reproduced). */
+HX_API void hx_policy_reference(hx_policy* out);
+/* Benchmark-spec policy (PCG RNG, RR after depth 3 with p <= 1, area-light
+ * count from .x, w = 1, importance-sampled environment). */
+HX_API void hx_policy_spec(hx_policy* out);
+
+/* ------------------------------------------------------------------------ */
+/* Integrator (replaces helios::PathIntegrator, include/gfx/path_integrator.h:9-62) */
+/* ------------------------------------------------------------------------ */
+
+typedef struct hx_integrator_desc {
+    uint32_t  width, height;       /* output extents (swap_chain_extents)          */
+    uint32_t  max_ray_bounces;     /* default 7, path_integrator.h:47               */
+    uint32_t  max_samples;         /* default 5000, path_integrator.h:48            */
+    float     shadow_ray_bias;     /* default 0, path_integrator.h:51               */
+    uint32_t  tiled;               /* 128x128 tiles, path_integrator.cpp:7,312-336  */
+    uint32_t  max_paths_in_flight; /* wavefront capacity (0 = width*height)         */
+    uint32_t  reserved;
+    hx_policy policy;
+} hx_integrator_desc;
+
+/* Per-frame constants: the push-constant block of path_integrator.cpp:11-28
+ * that launch_rays fills (path_integrator.cpp:136-161). */
+typedef struct hx_frame_desc {
+    float view_proj_inverse[16];  /* inverse(projection * view), column-major */
+    float camera_pos[4];
+    float up_direction[4];
+    float right_direction[4];
+    float focal_plane[4];
+    float focal_length;
+    float aperture_radius;
+    float reserved[2];
+} hx_frame_desc;
+
+/* Camera description used to fill hx_frame_desc the way CameraNode::update
+ * (src/engine/resource/scene.cpp:632-646) and launch_rays do: GLM
+ * perspective (right-handed, depth -1..1) and lookAt. */
+typedef struct hx_camera {
+    float position[3];
+    float target[3];
+    float up[3];
+    float fov_y_degrees;   /* default 60 (scene.h:258)            */
+    float near_plane;      /* default 1 (scene.h:256)             */
+    float far_plane;       /* default 1000 (scene.h:257)          */
+    float focal_length;    /* default 8 (scene.h:259)             */
+    float aperture_radius; /* default 0.1 (scene.h:260); 0 = pinhole */
+} hx_camera;
+
+HX_API hx_status hx_camera_to_frame_desc(const hx_camera* camera, uint32_t width,
+                                         uint32_t height, hx_frame_desc* out);
+
+#define HX_TONEMAP_ACES     0u  /* tone_map.frag:8-15 (Narkowicz fit) */
+#define HX_TONEMAP_REINHARD 1u  /* tone_map.frag:17-20                */
+#define HX_TONEMAP_NONE     2u  /* exposure + gamma only              */
+
+/* Hit record of a closest-hit query: prim = index into the scene's flattened
+ * triangle list (instance-major, submesh order), 0xFFFFFFFF on a miss. */
+typedef struct hx_hit {
+    float    t;
+    uint32_t prim;
+    float    u, v;   /* barycentric weights of vertex 1 and vertex 2 (b_HitAttribs) */
+} hx_hit;
+
+/* Compressed 8-wide BVH node (80 B).  Child boxes are stored as 8-bit
+ * offsets on a per-node grid: lo = origin + q * 2^exponent (exact products,
+ * one rounded add), quantised outward so every decoded child box contains
+ * the exact one.  meta[i]: 0 = empty slot; 0x80 | k = internal child
+ * (node child_base + k); (n << 5) | off = leaf with n (1..3) triangles at
+ * leaf-triangle index prim_base + off. */
+typedef struct hx_bvh8_node {
+    float    origin[3];
+    int8_t   exponent[3];
+    uint8_t  internal_mask;
+    uint32_t child_base;
+    uint32_t prim_base;
+    uint8_t  meta[8];
+    uint8_t  qlo[3][8];
+    uint8_t  qhi[3][8];
+} hx_bvh8_node;
+
+typedef struct hx_stats {
+    uint64_t paths;            /* camera samples traced                      */
+    uint64_t extension_rays;   /* closest-hit queries                        */
+    uint64_t shadow_rays;      /* any-hit visibility queries                 */
+    double   ms_total;         /* device time of the last render call        */
+    double   ms_raygen, ms_trace, ms_shade, ms_shadow, ms_accumulate;
+    uint32_t trace_launches;   /* closest-hit launches in the last call      */
+    uint32_t kernel_launches;  /* all kernel launches in the last call       */
+    uint64_t node_visits;      /* BVH8 nodes fetched by closest-hit traversal (counting mode) */
+    uint64_t tri_tests;        /* triangles tested by closest-hit traversal (counting mode)   */
+} hx_stats;
+
+/* Context: one CUDA device + stream + HBM budget (the role of vk::Backend). */
+HX_API hx_status   hx_context_create(int device, uint64_t hbm_budget_bytes, hx_context** out);
+HX_API hx_status   hx_context_destroy(hx_context* ctx);
+HX_API hx_status   hx_context_synchronize(hx_context* ctx);
+HX_API hx_status   hx_context_memory(hx_context* ctx, uint64_t* used_bytes, uint64_t* budget_bytes);
+HX_API const char* hx_last_error_string(void);
+HX_API const char* hx_version(void);
+
+/* Device timestamps on the context stream (the GPU half of the reference
+ * profiler's timestamp queries, src/engine/utility/profiler.cpp:84-140). */
+typedef struct hx_event hx_event;
+HX_API hx_status hx_event_create(hx_context* ctx, hx_event** out);
+HX_API hx_status hx_event_record(hx_event* ev);
+/* Waits for `end` and returns the device time between the two records. */
+HX_API hx_status hx_event_elapsed(hx_event* begin, hx_event* end, float* ms);
+HX_API hx_status hx_event_destroy(hx_event* ev);
+
+/* Page-locked host staging memory for fast host<->device copies. */
+HX_API hx_status hx_pinned_alloc(size_t bytes, void** out);
+HX_API hx_status hx_pinned_free(void* ptr);
+
+/* Scene upload (replaces Scene::create_gpu_resources, scene.cpp:915-1311, and
+ * the BLAS/TLAS builds of mesh.cpp:61-117 and renderer.cpp:113-181): copies
+ * the host arrays, flattens instances, builds the LBVH -> BVH8 on the device,
+ * derives the light list, bakes the environment. */
+HX_API hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc, hx_scene** out);
+HX_API hx_status hx_scene_destroy(hx_scene* scene);
+
+typedef struct hx_scene_info {
+    uint32_t num_triangles;    /* flattened triangles                       */
+    uint32_t num_bvh8_nodes;
+    uint32_t num_binary_nodes; /* internal nodes of the Karras tree (n-1)    */
+    uint32_t num_lights;       /* light list length (render_state.num_lights) */
+    uint64_t device_bytes;
+    double   build_ms;         /* device time of the BVH build               */
+    float    scene_min[3], scene_max[3];
+} hx_scene_info;
+HX_API hx_status hx_scene_info_get(const hx_scene* scene, hx_scene_info* out);
+
+/* Copies the light list the library derived (reference order, scene.cpp
+ * 1111-1119,1269-1309) into out[0..capacity). */
+HX_API hx_status hx_scene_lights(const hx_scene* scene, hx_light* out, uint32_t capacity,
+                                 uint32_t* count);
+
+/* Copies device BVH data for parity checks (any pointer may be NULL):
+ * morton[n] (30-bit codes in input order), sorted_prims[n] (stable sort
+ * order), binary nodes as (left,right) child pairs with leaf flag in bit 31
+ * [2*(n-1)], BVH8 nodes (80 B each) [num_bvh8_nodes*80 bytes], BVH8 leaf
+ * triangle order [n]. */
+HX_API hx_status hx_scene_export_bvh(const hx_scene* scene, uint32_t* morton,
+                                     uint32_t* sorted_prims, uint32_t* binary_children,
+                                     void* bvh8_nodes, uint32_t* bvh8_prims);
+
+/* PathIntegrator::PathIntegrator (path_integrator.cpp:32-38). */
+HX_API hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene,
+                                      const hx_integrator_desc* desc, hx_integrator** out);
+HX_API hx_status hx_integrator_destroy(hx_integrator* integ);
+
+/* PathIntegrator::render (path_integrator.cpp:48-84) + the accumulation of
+ * Renderer::render (renderer.cpp:183-227): traces one progressive frame
+ * (1 sample per pixel of the current tile) and accumulates it. */
+HX_API hx_status hx_integrator_render(hx_integrator* integ, const hx_frame_desc* frame);
+
+/* n consecutive render() calls with the same frame constants, batched into
+ * one wavefront.  Results are identical to n render() calls. */
+HX_API hx_status hx_integrator_render_frames(hx_integrator* integ, const hx_frame_desc* frame,
+                                             uint32_t num_frames);
+
+/* PathIntegrator::restart_bake (path_integrator.h:25-29) + the image clear of
+ * renderer.cpp:212-223. */
+HX_API hx_status hx_integrator_restart_bake(hx_integrator* integ);
+HX_API hx_status hx_integrator_set_max_ray_bounces(hx_integrator* integ, uint32_t n);
+HX_API hx_status hx_integrator_set_max_samples(hx_integrator* integ, uint32_t n);
+HX_API hx_status hx_integrator_set_shadow_ray_bias(hx_integrator* integ, float bias);
+HX_API hx_status hx_integrator_set_tiled(hx_integrator* integ, uint32_t tiled);
+HX_API hx_status hx_integrator_set_policy(hx_integrator* integ, const hx_policy* policy);
+/* num_accumulated_samples / tile_idx / num_target_samples (path_integrator.h:20-22). */
+HX_API hx_status hx_integrator_progress(const hx_integrator* integ, uint32_t* accumulated_samples,
+                                        uint32_t* tile_idx, uint32_t* target_samples);
+
+/* Renderer::tone_map (renderer.cpp:369-426) + tone_map.frag:22-51: exposure,
+ * ACES/Reinhard, gamma 1/2.2, RGBA8, vertically flipped like the
+ * negative-height viewport (renderer.cpp:394-399).  host_rgba8 may be NULL
+ * (result stays on the device). */
+HX_API hx_status hx_integrator_tonemap(hx_integrator* integ, uint32_t op, float exposure,
+                                       uint8_t* host_rgba8);
+
+/* Reads the RGBA32F accumulation image (the ping-pong output image of
+ * renderer.cpp:1483-1506) into width*height*4 floats. */
+HX_API hx_status hx_integrator_read_accumulation(hx_integrator* integ, float* host_rgba32f);
+
+/* Device-timed statistics of the last render call (CUDA events on the
+ * context stream when timing is on). */
+HX_API hx_status hx_integrator_set_timing(hx_integrator* integ, uint32_t enabled);
+/* Counting mode: closest-hit launches also count node fetches and triangle
+ * tests (into hx_stats.node_visits / tri_tests); used to derive the
+ * algorithmic bytes of the traversal, never in a timed run. */
+HX_API hx_status hx_integrator_set_counting(hx_integrator* integ, uint32_t enabled);
+HX_API hx_status hx_integrator_stats(const hx_integrator* integ, hx_stats* out);
+
+/* Parity hook: primary-ray closest hits (with the any-hit alpha test) for
+ * every pixel of frame `frame_index`, in pixel order (y*width + x). */
+HX_API hx_status hx_integrator_primary_hits(hx_integrator* integ, const hx_frame_desc* frame,
+                                            uint32_t frame_index, hx_hit* host_hits);
+
+/* Parity hook: per-sample radiance (before clamping) of frame `frame_index`
+ * for every pixel, RGB, in pixel order. */
+HX_API hx_status hx_integrator_sample_radiance(hx_integrator* integ, const hx_frame_desc* frame,
+                                               uint32_t frame_index, float* host_rgb);
+
+/* Parity hook: closest-hit queries for caller rays (origin xyz, tmin,
+ * direction xyz, tmax) x n, alpha testing when any_hit != 0. */
+HX_API hx_status hx_scene_trace(const hx_scene* scene, const float* host_rays, uint32_t n,
+                                uint32_t any_hit, hx_hit* host_hits);
+
+/* Parity hook: the baked environment as RGB floats (width*height*3), the
+ * FP16 texels widened. */
+HX_API hx_status hx_scene_export_env(const hx_scene* scene, float* host_rgb);
+
+/* Parity hook: RNG streams on the device.  For stream i the seed pair is
+ * (seeds[2i], seeds[2i+1]) = (pixel id, frame/sample index); writes
+ * draws_per_stream raw 32-bit outputs per stream. */
+HX_API hx_status hx_rng_streams(hx_context* ctx, uint32_t rng_kind, const uint32_t* seeds,
+                                uint32_t num_streams, uint32_t draws_per_stream,
+                                uint32_t* host_out);
+
+/* ------------------------------------------------------------------------ */
+/* Procedural scenes for the benchmark configurations (host side)            */
+/* ------------------------------------------------------------------------ */
+
+#define HX_SCENE_BOX          0u  /* 5-wall box + 2 boxes + quad light (36 tris)         */
+#define HX_SCENE_ICOSPHERES   1u  /* 12 icospheres + ground + alpha quads + sky + lights */
+
+typedef struct hx_procedural_params {
+    uint32_t kind;           /* HX_SCENE_*                                   */
+    uint64_t seed;
+    uint32_t num_alpha_quads;/* HX_SCENE_ICOSPHERES: default 100000          */
+    uint32_t mask_pool;      /* distinct 512^2 masks (default 64)            */
+    uint32_t mask_size;      /* default 512                                  */
+    uint32_t icosphere_level;/* default 6 (81,920 triangles)                 */
+    uint32_t env_width, env_height; /* default 2048 x 1024                   */
+    float    sun_elevation_deg;     /* default 30                             */
+    float    turbidity;             /* default 3                              */
+} hx_procedural_params;
+
+HX_API void      hx_procedural_defaults(uint32_t kind, hx_procedural_params* out);
+HX_API hx_status hx_procedural_scene_create(const hx_procedural_params* params, hx_host_scene** out);
+HX_API const hx_scene_desc* hx_host_scene_desc(const hx_host_scene* scene);
+HX_API hx_status hx_host_scene_camera(const hx_host_scene* scene, hx_camera* out);
+HX_API hx_status hx_host_scene_destroy(hx_host_scene* scene);
+
+/* Hosek-Wilkie RGB coefficients (A..I, Z; 10 x vec4) for the given sun
+ * direction, turbidity 3 or 4 and ground albedo 0.1, normalised so the
+ * luminance toward the sun is normalized_sun_y
+ * (hosek_wilkie_sky_model.cpp:658-686). */
+HX_API hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], float turbidity,
+                                              float normalized_sun_y, float out[40]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HX_H */

@@ -1,0 +1,1208 @@
+// oracle.cpp — CPU oracle for the helios-gb300 path-tracing core
+// (TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and
+// bench.py's CPU-baseline leg; never linked into the product library).
+//
+// A scalar restatement of the reference's path-tracing shaders, templated on
+// FP32 (bit-exact integer parity, CPU baseline) and FP64 (radiance oracle):
+//   random.glsl, sampling.glsl (RNG)               -> oracle_core.h
+//   brdf.glsl :6-167                               -> evaluate_uber / pdf_uber / sample_uber
+//   path_trace_rgen.glsl generate_ray :132-174     -> generate_ray
+//   path_trace_rgen.glsl main :180-250             -> trace_path + accumulate
+//   path_trace_rchit.glsl :143-280                 -> populate
+//   path_trace_rchit.glsl sample_light :284-451    -> sample_light
+//   path_trace_rchit.glsl direct :455-483, indirect :487-536, main :542-580 -> trace_path
+//   path_trace_rahit.glsl :162-188                 -> alpha_pass
+//   path_trace_rmiss.glsl :38-67, path_trace_shadow.rchit/.rmiss -> env_lookup, any-hit visibility
+//   tone_map.frag :8-51                            -> oracle_tonemap
+//   procedural_sky.frag :48-75                     -> sky_radiance
+//   scene.cpp :915-1311 (flattening, light order)  -> flatten / build_lights
+// plus an independent LBVH -> BVH8 builder (Karras 2012 hierarchy, greedy
+// 8-wide collapse, 8-bit conservative child boxes) whose integer outputs are
+// compared bit for bit with the device builder.
+//
+// Parity status: unpinned against reference outputs (the reference has no
+// tests and its Vulkan ray-tracing path cannot run without a graphics
+// stack); see oracle_core.h for the floating-point contract.
+#include "oracle_core.h"
+#include "../include/hx.h"
+
+#include <omp.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <numeric>
+#include <vector>
+
+namespace oracle {
+
+template <typename R> static inline R kpi() { return R(3.14159265359); }  // M_PI, common.glsl:18
+static const float kEpsilon = 0.0001f;                                    // EPSILON, common.glsl:19
+static const float kMinRoughness = 0.1f;                                  // MIN_ROUGHNESS, common.glsl:21
+static const uint32_t kNoHit = 0xffffffffu;
+
+struct PrimInfo {
+    uint32_t instance, mesh_prim, material, submesh;
+};
+struct Tex {
+    std::vector<uint8_t> rgba;
+    uint32_t w = 0, h = 0;
+};
+
+struct Bvh {
+    std::vector<uint32_t> morton, sorted;            // per input prim / sorted order
+    std::vector<uint32_t> children;                  // 2*(n-1), bit31 = leaf
+    std::vector<float> lo, hi;                       // internal boxes 3*(n-1)
+    std::vector<uint32_t> first, count;              // internal node ranges
+    std::vector<hx_bvh8_node> nodes;
+    std::vector<uint32_t> leaf_prims;                // flattened prim ids in leaf order
+};
+
+struct Scene {
+    std::vector<std::vector<hx_vertex>> vertices;
+    std::vector<std::vector<uint32_t>> indices;
+    std::vector<std::vector<hx_submesh>> submeshes;
+    std::vector<hx_instance> instances;
+    std::vector<hx_material> materials;
+    std::vector<Tex> textures;
+    std::vector<hx_light> punctual;
+    std::vector<hx_light> lights;
+    std::vector<PrimInfo> prims;
+    std::vector<float> wpos;     // 9 floats per prim, world space, FP32
+    std::vector<double> wpos64;  // same, FP64
+    std::vector<uint8_t> nonopaque;
+    Bvh bvh;
+    uint32_t env_kind = HX_ENV_NONE, env_w = 0, env_h = 0;
+    std::vector<float> env;  // rgb per texel, FP16-rounded
+    std::vector<double> env_marg, env_cond;
+    double env_total = 0;
+    float sun[3] = {0, 1, 0};
+    float coeffs[40] = {0};
+};
+
+// ---------------------------------------------------------------------------
+// Hosek-Wilkie sky radiance, procedural_sky.frag:48-75.
+// ---------------------------------------------------------------------------
+template <typename R> static V3<R> sky_radiance(const float* c, V3<R> v, V3<R> sun) {
+    R cos_theta = gclamp(v.y, R(0), R(1));
+    R cos_gamma = gclamp(dot(v, sun), R(0), R(1));
+    R gamma = std::acos(cos_gamma);
+    V3<R> out;
+    for (int k = 0; k < 3; ++k) {
+        R A = c[0 + k], B = c[4 + k], C = c[8 + k], D = c[12 + k], E = c[16 + k], F = c[20 + k], G = c[24 + k],
+          H = c[28 + k], I = c[32 + k], Z = c[36 + k];
+        R chi = (R(1) + cos_gamma * cos_gamma) / std::pow(R(1) + H * H - R(2) * cos_gamma * H, R(1.5));
+        R hw = (R(1) + A * std::exp(B / (cos_theta + R(0.01)))) *
+               (C + D * std::exp(E * gamma) + F * (cos_gamma * cos_gamma) + G * chi + I * std::sqrt(cos_theta));
+        out[k] = Z * hw;
+    }
+    return out;
+}
+
+// Lat-long mapping (texel centre): phi = 2pi(u - 0.5), theta = pi v,
+// d = (sin(theta) sin(phi), cos(theta), -sin(theta) cos(phi)).
+static V3<double> latlong_dir(double u, double v) {
+    double phi = 2.0 * 3.14159265358979323846 * (u - 0.5);
+    double theta = 3.14159265358979323846 * v;
+    double st = std::sin(theta);
+    return V3<double>(st * std::sin(phi), std::cos(theta), -st * std::cos(phi));
+}
+
+static float env_luminance(const float* e) { return 0.2126f * e[0] + 0.7152f * e[1] + 0.0722f * e[2]; }
+
+// Importance-sampling table: weight(i,j) = (lum + floor) * sin(theta_j).
+static void build_env_cdf(Scene& s) {
+    uint32_t w = s.env_w, h = s.env_h;
+    double mean = 0;
+    for (size_t i = 0; i < (size_t)w * h; ++i) mean += env_luminance(&s.env[i * 3]);
+    mean /= (double)w * h;
+    double floor_w = 1e-3 * mean + 1e-12;
+    s.env_cond.assign((size_t)h * (w + 1), 0.0);
+    s.env_marg.assign(h + 1, 0.0);
+    for (uint32_t j = 0; j < h; ++j) {
+        double st = std::sin(3.14159265358979323846 * (j + 0.5) / h);
+        double* row = &s.env_cond[(size_t)j * (w + 1)];
+        for (uint32_t i = 0; i < w; ++i) row[i + 1] = row[i] + ((double)env_luminance(&s.env[((size_t)j * w + i) * 3]) + floor_w) * st;
+        s.env_marg[j + 1] = s.env_marg[j] + row[w];
+    }
+    s.env_total = s.env_marg[h];
+}
+
+template <typename R> static V3<R> env_lookup(const Scene& s, V3<R> d) {
+    if (s.env_kind == HX_ENV_NONE) return V3<R>(R(0));
+    R theta = std::acos(gclamp(d.y, R(-1), R(1)));
+    R phi = std::atan2(d.x, -d.z);
+    R u = phi / (R(2) * R(3.14159265358979323846)) + R(0.5);
+    R v = theta / R(3.14159265358979323846);
+    R x = u * R(s.env_w) - R(0.5), y = v * R(s.env_h) - R(0.5);
+    R x0 = std::floor(x), y0 = std::floor(y);
+    R fx = x - x0, fy = y - y0;
+    long ix = (long)x0, iy = (long)y0;
+    long W = s.env_w, H = s.env_h;
+    long ix0 = ((ix % W) + W) % W, ix1 = (ix0 + 1) % W;
+    long iy0 = iy < 0 ? 0 : (iy >= H ? H - 1 : iy);
+    long iy1 = iy + 1 < 0 ? 0 : (iy + 1 >= H ? H - 1 : iy + 1);
+    V3<R> out;
+    for (int c = 0; c < 3; ++c) {
+        R a00 = s.env[((size_t)iy0 * W + ix0) * 3 + c], a10 = s.env[((size_t)iy0 * W + ix1) * 3 + c];
+        R a01 = s.env[((size_t)iy1 * W + ix0) * 3 + c], a11 = s.env[((size_t)iy1 * W + ix1) * 3 + c];
+        R top = a00 + (a10 - a00) * fx;
+        R bot = a01 + (a11 - a01) * fx;
+        out[c] = top + (bot - top) * fy;
+    }
+    return out;
+}
+
+// Samples a direction from the lat-long CDF with two uniforms; returns the
+// solid-angle pdf.
+template <typename R> static V3<R> env_sample(const Scene& s, R r0, R r1, R& pdf) {
+    uint32_t w = s.env_w, h = s.env_h;
+    double target = (double)r1 * s.env_total;
+    uint32_t j = (uint32_t)(std::upper_bound(s.env_marg.begin() + 1, s.env_marg.end(), target) - (s.env_marg.begin() + 1));
+    if (j >= h) j = h - 1;
+    const double* row = &s.env_cond[(size_t)j * (w + 1)];
+    double rt = (double)r0 * row[w];
+    uint32_t i = (uint32_t)(std::upper_bound(row + 1, row + w + 1, rt) - (row + 1));
+    if (i >= w) i = w - 1;
+    double fu = row[i + 1] > row[i] ? (rt - row[i]) / (row[i + 1] - row[i]) : 0.5;
+    double rm = s.env_marg[j + 1] - s.env_marg[j];
+    double fv = rm > 0 ? (target - s.env_marg[j]) / rm : 0.5;
+    fu = std::min(std::max(fu, 0.0), 1.0);
+    fv = std::min(std::max(fv, 0.0), 1.0);
+    double u = (i + fu) / w, v = (j + fv) / h;
+    V3<double> d = latlong_dir(u, v);
+    double theta = 3.14159265358979323846 * v;
+    double st = std::sin(theta);
+    double p_img = (row[i + 1] - row[i]) / s.env_total * (double)w * h;  // density over [0,1]^2
+    pdf = st > 0 ? R(p_img / (2.0 * 3.14159265358979323846 * 3.14159265358979323846 * st)) : R(0);
+    return V3<R>(R(d.x), R(d.y), R(d.z));
+}
+
+// ---------------------------------------------------------------------------
+// Scene construction.
+// ---------------------------------------------------------------------------
+static void flatten(Scene& s) {
+    for (uint32_t ii = 0; ii < s.instances.size(); ++ii) {
+        const hx_instance& inst = s.instances[ii];
+        uint32_t m = inst.mesh_index;
+        const auto& vs = s.vertices[m];
+        const auto& ix = s.indices[m];
+        double md[16];
+        for (int k = 0; k < 16; ++k) md[k] = inst.model_matrix[k];
+        for (uint32_t si = 0; si < s.submeshes[m].size(); ++si) {
+            const hx_submesh& sm = s.submeshes[m][si];
+            uint32_t mat = inst.material_override >= 0 ? (uint32_t)inst.material_override : sm.material;
+            for (uint32_t p = 0; p < sm.index_count / 3; ++p) {
+                uint32_t mp = sm.base_index / 3 + p;
+                s.prims.push_back({ii, mp, mat, si});
+                s.nonopaque.push_back((sm.flags & HX_SUBMESH_NON_OPAQUE) ? 1 : 0);
+                for (int c = 0; c < 3; ++c) {
+                    const hx_vertex& v = vs[ix[3 * mp + c]];
+                    float o[4];
+                    mat4_mul(inst.model_matrix, v.position[0], v.position[1], v.position[2], 1.0f, o);
+                    double od[4];
+                    mat4_mul(md, (double)v.position[0], (double)v.position[1], (double)v.position[2], 1.0, od);
+                    for (int a = 0; a < 3; ++a) {
+                        s.wpos.push_back(o[a]);
+                        s.wpos64.push_back(od[a]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+static bool material_emissive(const hx_material& m) {  // Material::is_emissive, material.cpp:71-77
+    if (m.texture_indices1[0] != -1) return true;
+    return m.emissive[0] > 0.0f || m.emissive[1] > 0.0f || m.emissive[2] > 0.0f;
+}
+
+static void build_lights(Scene& s) {
+    std::vector<uint8_t> seen(s.vertices.size(), 0);
+    for (uint32_t ii = 0; ii < s.instances.size(); ++ii) {
+        uint32_t m = s.instances[ii].mesh_index;
+        if (seen[m]) continue;
+        seen[m] = 1;
+        for (const hx_submesh& sm : s.submeshes[m]) {
+            uint32_t mat = s.instances[ii].material_override >= 0 ? (uint32_t)s.instances[ii].material_override : sm.material;
+            if (!material_emissive(s.materials[mat])) continue;
+            hx_light l{};
+            l.data0[0] = (float)HX_LIGHT_AREA;
+            l.data0[1] = (float)ii;
+            l.data0[2] = (float)mat;
+            l.data0[3] = (float)(sm.base_index / 3);
+            l.data1[0] = (float)(sm.index_count / 3);
+            s.lights.push_back(l);
+        }
+    }
+    bool has_dir = false;
+    for (const hx_light& l : s.punctual) has_dir |= (uint32_t)l.data0[0] == HX_LIGHT_DIRECTIONAL;
+    if (s.env_kind != HX_ENV_NONE || has_dir) {
+        hx_light l{};
+        l.data0[0] = (float)HX_LIGHT_ENVIRONMENT;
+        s.lights.push_back(l);
+    }
+    for (uint32_t type : {HX_LIGHT_DIRECTIONAL, HX_LIGHT_POINT, HX_LIGHT_SPOT})
+        for (const hx_light& l : s.punctual)
+            if ((uint32_t)l.data0[0] == type) s.lights.push_back(l);
+}
+
+// ---------------------------------------------------------------------------
+// LBVH: Morton codes, stable sort, Karras hierarchy, boxes, BVH8 collapse.
+// ---------------------------------------------------------------------------
+static uint32_t expand_bits(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+static int clz32(uint32_t x) { return x == 0 ? 32 : __builtin_clz(x); }
+
+static int karras_delta(const std::vector<uint32_t>& keys, int n, int i, int j) {
+    if (j < 0 || j > n - 1) return -1;
+    uint32_t a = keys[i], b = keys[j];
+    if (a == b) return 32 + clz32((uint32_t)i ^ (uint32_t)j);
+    return clz32(a ^ b);
+}
+
+static float f32_bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+static uint32_t bits_f32(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+
+// Smallest e with 2^e >= x (x > 0), e >= -126.
+static int ceil_log2f(float x) {
+    uint32_t b = bits_f32(x);
+    int ex = (int)((b >> 23) & 0xff);
+    if (ex == 0) return -126;
+    int e = ex - 127 + ((b & 0x7fffff) != 0 ? 1 : 0);
+    return e < -126 ? -126 : e;
+}
+static float pow2f(int e) { return f32_bits((uint32_t)(e + 127) << 23); }
+
+static float half_area(const float* lo, const float* hi) {
+    float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+static void quantise_node(hx_bvh8_node& node, int nslots, const float (*clo)[3], const float (*chi)[3]) {
+    float plo[3], phi[3];
+    for (int a = 0; a < 3; ++a) {
+        plo[a] = clo[0][a];
+        phi[a] = chi[0][a];
+        for (int k = 1; k < nslots; ++k) {
+            plo[a] = clo[k][a] < plo[a] ? clo[k][a] : plo[a];
+            phi[a] = chi[k][a] > phi[a] ? chi[k][a] : phi[a];
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        node.origin[a] = plo[a];
+        float ext = phi[a] - plo[a];
+        int e = ext > 0.0f ? ceil_log2f(ext / 255.0f) : -126;
+        while (e < 127 && plo[a] + 255.0f * pow2f(e) < phi[a]) ++e;
+        node.exponent[a] = (int8_t)e;
+        float scale = pow2f(e);
+        float inv = pow2f(-e > 126 ? 126 : (-e < -126 ? -126 : -e));
+        for (int k = 0; k < 8; ++k) {
+            if (k >= nslots) { node.qlo[a][k] = 0; node.qhi[a][k] = 0; continue; }
+            float fl = std::floor((clo[k][a] - plo[a]) * inv);
+            int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
+            while (ql > 0 && plo[a] + (float)ql * scale > clo[k][a]) --ql;
+            float fh = std::ceil((chi[k][a] - plo[a]) * inv);
+            int qh = fh < 0.0f ? 0 : (fh > 255.0f ? 255 : (int)fh);
+            while (qh < 255 && plo[a] + (float)qh * scale < chi[k][a]) ++qh;
+            node.qlo[a][k] = (uint8_t)ql;
+            node.qhi[a][k] = (uint8_t)qh;
+        }
+    }
+}
+
+static void build_bvh(Scene& s) {
+    Bvh& b = s.bvh;
+    int n = (int)s.prims.size();
+    b.morton.assign(n, 0);
+    b.sorted.resize(n);
+    if (n == 0) return;
+    // centroids and their bounds
+    std::vector<float> cen(3 * (size_t)n);
+    float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = 0; i < n; ++i) {
+        const float* p = &s.wpos[9 * (size_t)i];
+        for (int a = 0; a < 3; ++a) {
+            float c = (p[a] + p[3 + a] + p[6 + a]) / 3.0f;
+            cen[3 * (size_t)i + a] = c;
+            cmin[a] = c < cmin[a] ? c : cmin[a];
+            cmax[a] = c > cmax[a] ? c : cmax[a];
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        uint32_t q[3];
+        for (int a = 0; a < 3; ++a) {
+            float ext = cmax[a] - cmin[a];
+            float f = ext > 0.0f ? (cen[3 * (size_t)i + a] - cmin[a]) / ext : 0.0f;
+            float sc = f * 1024.0f;
+            sc = sc < 0.0f ? 0.0f : (sc > 1023.0f ? 1023.0f : sc);
+            q[a] = (uint32_t)sc;
+        }
+        b.morton[i] = (expand_bits(q[0]) << 2) | (expand_bits(q[1]) << 1) | expand_bits(q[2]);
+    }
+    std::iota(b.sorted.begin(), b.sorted.end(), 0u);
+    std::stable_sort(b.sorted.begin(), b.sorted.end(), [&](uint32_t x, uint32_t y) { return b.morton[x] < b.morton[y]; });
+    std::vector<uint32_t> keys(n);
+    for (int i = 0; i < n; ++i) keys[i] = b.morton[b.sorted[i]];
+
+    // leaf boxes in sorted order
+    std::vector<float> llo(3 * (size_t)n), lhi(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const float* p = &s.wpos[9 * (size_t)b.sorted[i]];
+        for (int a = 0; a < 3; ++a) {
+            float lo = p[a], hi = p[a];
+            lo = p[3 + a] < lo ? p[3 + a] : lo; hi = p[3 + a] > hi ? p[3 + a] : hi;
+            lo = p[6 + a] < lo ? p[6 + a] : lo; hi = p[6 + a] > hi ? p[6 + a] : hi;
+            llo[3 * (size_t)i + a] = lo;
+            lhi[3 * (size_t)i + a] = hi;
+        }
+    }
+
+    int ni = n - 1;
+    b.children.assign(2 * (size_t)ni, 0);
+    b.first.assign(ni, 0);
+    b.count.assign(ni, 0);
+    b.lo.assign(3 * (size_t)ni, 0.0f);
+    b.hi.assign(3 * (size_t)ni, 0.0f);
+    std::vector<int> parent_int(ni, -1), parent_leaf(n, -1);
+    for (int i = 0; i < ni; ++i) {
+        int d = karras_delta(keys, n, i, i + 1) - karras_delta(keys, n, i, i - 1) >= 0 ? 1 : -1;
+        int dmin = karras_delta(keys, n, i, i - d);
+        int lmax = 2;
+        while (karras_delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+        int l = 0;
+        for (int t = lmax / 2; t >= 1; t /= 2)
+            if (karras_delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+        int j = i + l * d;
+        int dnode = karras_delta(keys, n, i, j);
+        int sidx = 0;
+        int t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (karras_delta(keys, n, i, i + (sidx + t) * d) > dnode) sidx += t;
+        } while (t > 1);
+        int gamma = i + sidx * d + (d < 0 ? d : 0);
+        int lo = i < j ? i : j, hi = i < j ? j : i;
+        uint32_t left = (lo == gamma) ? (0x80000000u | (uint32_t)gamma) : (uint32_t)gamma;
+        uint32_t right = (hi == gamma + 1) ? (0x80000000u | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+        b.children[2 * (size_t)i] = left;
+        b.children[2 * (size_t)i + 1] = right;
+        b.first[i] = lo;
+        b.count[i] = hi - lo + 1;
+    }
+    // boxes bottom-up: children of an internal node always cover a sub-range,
+    // so processing nodes by increasing range size is a valid topological order.
+    std::vector<int> order(ni);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b.count[x] < b.count[y]; });
+    auto child_box = [&](uint32_t c, const float*& lo, const float*& hi) {
+        if (c & 0x80000000u) { lo = &llo[3 * (size_t)(c & 0x7fffffffu)]; hi = &lhi[3 * (size_t)(c & 0x7fffffffu)]; }
+        else { lo = &b.lo[3 * (size_t)c]; hi = &b.hi[3 * (size_t)c]; }
+    };
+    for (int i : order) {
+        const float *al, *ah, *bl, *bh;
+        child_box(b.children[2 * (size_t)i], al, ah);
+        child_box(b.children[2 * (size_t)i + 1], bl, bh);
+        for (int a = 0; a < 3; ++a) {
+            b.lo[3 * (size_t)i + a] = al[a] < bl[a] ? al[a] : bl[a];
+            b.hi[3 * (size_t)i + a] = ah[a] > bh[a] ? ah[a] : bh[a];
+        }
+    }
+
+    // BVH8 collapse, breadth-first.
+    b.nodes.clear();
+    b.leaf_prims.clear();
+    auto item_count = [&](uint32_t c) -> uint32_t { return (c & 0x80000000u) ? 1u : b.count[c]; };
+    auto item_first = [&](uint32_t c) -> uint32_t { return (c & 0x80000000u) ? (c & 0x7fffffffu) : b.first[c]; };
+    std::vector<uint32_t> queue;
+    if (n == 1) queue.push_back(0x80000000u);  // single leaf root
+    else queue.push_back(0u);
+    for (size_t k = 0; k < queue.size(); ++k) {
+        uint32_t src = queue[k];
+        uint32_t kids[8];
+        int nk = 0;
+        if (src & 0x80000000u) kids[nk++] = src;
+        else {
+            kids[nk++] = b.children[2 * (size_t)src];
+            kids[nk++] = b.children[2 * (size_t)src + 1];
+            while (nk < 8) {
+                int best = -1;
+                float best_area = -1.0f;
+                for (int c = 0; c < nk; ++c) {
+                    uint32_t it = kids[c];
+                    if ((it & 0x80000000u) || b.count[it] <= 3) continue;
+                    float a = half_area(&b.lo[3 * (size_t)it], &b.hi[3 * (size_t)it]);
+                    if (best < 0 || a > best_area || (a == best_area && it < kids[best])) { best = c; best_area = a; }
+                }
+                if (best < 0) break;
+                uint32_t it = kids[best];
+                for (int c = nk; c > best + 1; --c) kids[c] = kids[c - 1];
+                kids[best] = b.children[2 * (size_t)it];
+                kids[best + 1] = b.children[2 * (size_t)it + 1];
+                ++nk;
+            }
+        }
+        hx_bvh8_node node;
+        std::memset(&node, 0, sizeof(node));
+        node.child_base = (uint32_t)queue.size();
+        node.prim_base = (uint32_t)b.leaf_prims.size();
+        float clo[8][3], chi[8][3];
+        int rank = 0;
+        for (int c = 0; c < nk; ++c) {
+            uint32_t it = kids[c];
+            const float *lo, *hi;
+            child_box(it, lo, hi);
+            for (int a = 0; a < 3; ++a) { clo[c][a] = lo[a]; chi[c][a] = hi[a]; }
+            if (!(it & 0x80000000u) && b.count[it] > 3) {
+                node.meta[c] = (uint8_t)(0x80u | rank);
+                node.internal_mask |= (uint8_t)(1u << c);
+                ++rank;
+                queue.push_back(it);
+            } else {
+                uint32_t cnt = item_count(it), f = item_first(it);
+                uint32_t off = (uint32_t)b.leaf_prims.size() - node.prim_base;
+                node.meta[c] = (uint8_t)((cnt << 5) | off);
+                for (uint32_t q = 0; q < cnt; ++q) b.leaf_prims.push_back(b.sorted[f + q]);
+            }
+        }
+        quantise_node(node, nk, clo, chi);
+        b.nodes.push_back(node);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Traversal over the binary tree (independent of the BVH8 the device walks).
+// ---------------------------------------------------------------------------
+static inline uint8_t tex_fetch(const Tex& t, long x, long y, int c) { return t.rgba[((size_t)y * t.w + x) * 4 + c]; }
+
+// Software bilinear filter, REPEAT addressing, level 0.
+template <typename R> static R tex_bilinear(const Tex& t, R u, R v, int c) {
+    R x = u * R(t.w) - R(0.5), y = v * R(t.h) - R(0.5);
+    R x0 = std::floor(x), y0 = std::floor(y);
+    R fx = x - x0, fy = y - y0;
+    long W = t.w, H = t.h;
+    long ix0 = (((long)x0 % W) + W) % W, iy0 = (((long)y0 % H) + H) % H;
+    long ix1 = (ix0 + 1) % W, iy1 = (iy0 + 1) % H;
+    R a00 = R(tex_fetch(t, ix0, iy0, c)) / R(255), a10 = R(tex_fetch(t, ix1, iy0, c)) / R(255);
+    R a01 = R(tex_fetch(t, ix0, iy1, c)) / R(255), a11 = R(tex_fetch(t, ix1, iy1, c)) / R(255);
+    R top = a00 + (a10 - a00) * fx;
+    R bot = a01 + (a11 - a01) * fx;
+    return top + (bot - top) * fy;
+}
+
+// Any-hit alpha test (path_trace_rahit.glsl:174-188): interpolated UV,
+// albedo alpha, reject below 0.1.  Always evaluated in FP32.
+static bool alpha_pass(const Scene& s, uint32_t prim, float u, float v) {
+    const PrimInfo& pi = s.prims[prim];
+    const hx_material& m = s.materials[pi.material];
+    float alpha;
+    if (m.texture_indices0[0] == -1) alpha = m.albedo[3];
+    else {
+        uint32_t mesh = s.instances[pi.instance].mesh_index;
+        const auto& ix = s.indices[mesh];
+        const hx_vertex& a = s.vertices[mesh][ix[3 * pi.mesh_prim]];
+        const hx_vertex& b = s.vertices[mesh][ix[3 * pi.mesh_prim + 1]];
+        const hx_vertex& c = s.vertices[mesh][ix[3 * pi.mesh_prim + 2]];
+        float b0 = 1.0f - u - v;
+        float tu = a.tex_coord[0] * b0 + b.tex_coord[0] * u + c.tex_coord[0] * v;
+        float tv = a.tex_coord[1] * b0 + b.tex_coord[1] * u + c.tex_coord[1] * v;
+        alpha = tex_bilinear<float>(s.textures[m.texture_indices0[0]], tu, tv, 3);
+    }
+    return !(alpha < 0.1f);
+}
+
+template <typename R> static V3<R> prim_vertex(const Scene& s, uint32_t p, int c);
+template <> V3<float> prim_vertex<float>(const Scene& s, uint32_t p, int c) {
+    const float* q = &s.wpos[9 * (size_t)p + 3 * c];
+    return V3<float>(q[0], q[1], q[2]);
+}
+template <> V3<double> prim_vertex<double>(const Scene& s, uint32_t p, int c) {
+    const double* q = &s.wpos64[9 * (size_t)p + 3 * c];
+    return V3<double>(q[0], q[1], q[2]);
+}
+
+struct HitF {
+    float t, u, v;
+    uint32_t prim;
+};
+
+// Closest hit (any_hit = run the alpha test on non-opaque triangles) or, with
+// shadow = true, first accepted hit.  Triangle test in Real, boxes in FP32.
+template <typename R>
+static bool trace(const Scene& s, V3<R> o, V3<R> d, R tmin, R tmax, bool any_hit, bool shadow, bool brute, R& t_out,
+                  R& u_out, R& v_out, uint32_t& prim_out) {
+    const Bvh& b = s.bvh;
+    uint32_t n = (uint32_t)s.prims.size();
+    prim_out = kNoHit;
+    if (n == 0) return false;
+    RayPre<R> rp = ray_prepare(o, d);
+    R best_t = tmax, bu = 0, bv = 0;
+    uint32_t best = kNoHit;
+    float org[3] = {(float)o.x, (float)o.y, (float)o.z};
+    float inv[3] = {safe_inv((float)d.x), safe_inv((float)d.y), safe_inv((float)d.z)};
+    auto test = [&](uint32_t p) -> bool {
+        R t, u, v;
+        if (!intersect_triangle(rp, prim_vertex<R>(s, p, 0), prim_vertex<R>(s, p, 1), prim_vertex<R>(s, p, 2), tmin, best_t, t, u, v))
+            return false;
+        if (!(t < best_t || (t == best_t && p < best))) return false;
+        if (any_hit && s.nonopaque[p] && !alpha_pass(s, p, (float)u, (float)v)) return false;
+        best_t = t; bu = u; bv = v; best = p;
+        return true;
+    };
+    if (brute) {
+        for (uint32_t p = 0; p < n; ++p)
+            if (test(p) && shadow) break;
+    } else if (n == 1) {
+        test(b.sorted[0]);
+    } else {
+        uint32_t stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            uint32_t c = stack[--sp];
+            if (c & 0x80000000u) {
+                if (test(b.sorted[c & 0x7fffffffu]) && shadow) break;
+                continue;
+            }
+            float tn;
+            float lim = (float)best_t * 1.000001f;
+            if (!slab_test(inv, org, &b.lo[3 * (size_t)c], &b.hi[3 * (size_t)c], (float)tmin, lim, tn)) continue;
+            stack[sp++] = b.children[2 * (size_t)c + 1];
+            stack[sp++] = b.children[2 * (size_t)c];
+        }
+    }
+    if (best == kNoHit) return false;
+    t_out = best_t; u_out = bu; v_out = bv; prim_out = best;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Shading (brdf.glsl, path_trace_rchit.glsl) in Real precision.
+// ---------------------------------------------------------------------------
+template <typename R> struct Surface {
+    V3<R> position, normal, F0, albedo, emissive;
+    R albedo_a, metallic, roughness, alpha, alpha2;
+};
+
+template <typename R> static V3<R> rot_mul(V3<R> z, V3<R> t) {  // make_rotation_matrix(z) * t, sampling.glsl:28-36
+    V3<R> ref = std::fabs(z.x * R(0) + z.y * R(1) + z.z * R(0)) > R(0.99f) ? V3<R>(0, 0, 1) : V3<R>(0, 1, 0);
+    V3<R> x = normalize(cross(ref, z));
+    V3<R> y = cross(z, x);
+    return x * t.x + y * t.y + z * t.z;
+}
+template <typename R> static V3<R> sample_cosine_lobe(V3<R> n, R r0, R r1) {  // brdf.glsl:6-18
+    R rx = gmax(R(0.00001f), r0), ry = gmax(R(0.00001f), r1);
+    R phi = R(2) * kpi<R>() * ry;
+    R cos_theta = std::sqrt(rx);
+    R sin_theta = std::sqrt(R(1) - rx);
+    V3<R> t(sin_theta * std::cos(phi), sin_theta * std::sin(phi), cos_theta);
+    return normalize(rot_mul(n, t));
+}
+template <typename R> static R D_ggx(R ndoth, R alpha) {  // brdf.glsl:58-64
+    R a2 = alpha * alpha;
+    R denom = (ndoth * ndoth) * (a2 - R(1)) + R(1);
+    return a2 / gmax(R(kEpsilon), (kpi<R>() * denom * denom));
+}
+template <typename R> static R G1_schlick_ggx(R roughness, R ndotv) {  // brdf.glsl:66-71
+    R k = ((roughness + R(1)) * (roughness + R(1))) / R(8);
+    return ndotv / gmax(R(kEpsilon), (ndotv * (R(1) - k) + k));
+}
+template <typename R> static V3<R> evaluate_uber(const Surface<R>& p, V3<R> Wo, V3<R> Wh, V3<R> Wi) {  // brdf.glsl:109-121
+    R NdotL = gmax(dot(p.normal, Wi), R(0));
+    R NdotV = gmax(dot(p.normal, Wo), R(0));
+    R NdotH = gmax(dot(p.normal, Wh), R(0));
+    R VdotH = gmax(dot(Wi, Wh), R(0));
+    R f5 = std::pow(R(1) - VdotH, R(5));
+    V3<R> F = p.F0 + (V3<R>(R(1)) - p.F0) * f5;
+    R D = D_ggx(NdotH, p.roughness * p.roughness);
+    R G = G1_schlick_ggx(p.roughness, NdotL) * G1_schlick_ggx(p.roughness, NdotV);
+    V3<R> specular = ((F * D) * G) / gmax(R(kEpsilon), (R(4) * NdotL * NdotV));
+    V3<R> diffuse = p.albedo / kpi<R>();
+    return (V3<R>(R(1)) - F) * diffuse + specular;
+}
+template <typename R> static R pdf_uber(const Surface<R>& p, V3<R> Wo, V3<R> Wh, V3<R> Wi) {  // brdf.glsl:123-134
+    R NdotL = gmax(dot(p.normal, Wi), R(0));
+    R NdotH = gmax(dot(p.normal, Wh), R(0));
+    R VdotH = gmax(dot(Wi, Wh), R(0));
+    (void)Wo;
+    R pd = NdotL / kpi<R>();
+    R ps = D_ggx(NdotH, p.roughness * p.roughness) * NdotH / gmax(R(kEpsilon), (R(4) * VdotH));
+    return pd * (R(1) - R(0.5)) + ps * R(0.5);
+}
+template <typename R> static V3<R> sample_uber(const Surface<R>& p, V3<R> Wo, RNG rng, V3<R>& Wi, R& pdf) {  // brdf.glsl:136-167
+    R alpha = p.roughness * p.roughness;
+    R rx = next_float(rng), ry = next_float(rng), rz = next_float(rng);
+    V3<R> Wh;
+    bool is_specular = false;
+    if (rx < R(0.5)) {
+        R phi = R(2) * kpi<R>() * ry;  // sample_ggx, brdf.glsl:83-96
+        R cos_theta = std::sqrt((R(1) - rz) / (R(1) + (alpha * alpha - R(1)) * rz));
+        R sin_theta = std::sqrt(R(1) - cos_theta * cos_theta);
+        V3<R> dl(sin_theta * std::cos(phi), sin_theta * std::sin(phi), cos_theta);
+        Wh = normalize(rot_mul(p.normal, dl));
+        Wi = reflect(-Wo, Wh);
+        R NdotL = gmax(dot(p.normal, Wi), R(0));
+        R NdotV = gmax(dot(p.normal, Wo), R(0));
+        if (NdotL > R(0) && NdotV > R(0)) is_specular = true;
+    }
+    if (!is_specular) {
+        Wi = sample_cosine_lobe(p.normal, ry, rz);
+        Wh = normalize(Wo + Wi);
+    }
+    pdf = pdf_uber(p, Wo, Wh, Wi);
+    return evaluate_uber(p, Wo, Wh, Wi);
+}
+
+template <typename R> static const hx_vertex& mesh_vertex(const Scene& s, uint32_t mesh, uint32_t mp, int c) {
+    return s.vertices[mesh][s.indices[mesh][3 * mp + c]];
+}
+
+template <typename R> static Surface<R> populate(const Scene& s, uint32_t prim, float hu, float hv) {  // rchit.glsl:256-280
+    const PrimInfo& pi = s.prims[prim];
+    const hx_instance& inst = s.instances[pi.instance];
+    uint32_t mesh = inst.mesh_index;
+    const hx_vertex& a = mesh_vertex<R>(s, mesh, pi.mesh_prim, 0);
+    const hx_vertex& b = mesh_vertex<R>(s, mesh, pi.mesh_prim, 1);
+    const hx_vertex& c = mesh_vertex<R>(s, mesh, pi.mesh_prim, 2);
+    R u = hu, v = hv;
+    R b0 = R(1) - u - v, b1 = u, b2 = v;
+    auto lerp3 = [&](const float* x, const float* y, const float* z) {
+        return V3<R>(R(x[0]) * b0 + R(y[0]) * b1 + R(z[0]) * b2, R(x[1]) * b0 + R(y[1]) * b1 + R(z[1]) * b2,
+                     R(x[2]) * b0 + R(y[2]) * b1 + R(z[2]) * b2);
+    };
+    V3<R> pos = lerp3(a.position, b.position, c.position);
+    R tu = R(a.tex_coord[0]) * b0 + R(b.tex_coord[0]) * b1 + R(c.tex_coord[0]) * b2;
+    R tv = R(a.tex_coord[1]) * b0 + R(b.tex_coord[1]) * b1 + R(c.tex_coord[1]) * b2;
+    V3<R> nrm = normalize(lerp3(a.normal, b.normal, c.normal));
+    R M[16], N[16];
+    for (int k = 0; k < 16; ++k) { M[k] = inst.model_matrix[k]; N[k] = inst.normal_matrix[k]; }
+    R wp[4];
+    mat4_mul(M, pos.x, pos.y, pos.z, R(1), wp);
+    Surface<R> p;
+    p.position = V3<R>(wp[0], wp[1], wp[2]);
+    p.normal = mat3_mul(N, nrm);
+    const hx_material& m = s.materials[pi.material];
+    if (m.texture_indices0[0] == -1) {
+        p.albedo = V3<R>(R(m.albedo[0]), R(m.albedo[1]), R(m.albedo[2]));
+        p.albedo_a = R(m.albedo[3]);
+    } else {
+        const Tex& t = s.textures[m.texture_indices0[0]];
+        p.albedo = V3<R>(tex_bilinear<R>(t, tu, tv, 0), tex_bilinear<R>(t, tu, tv, 1), tex_bilinear<R>(t, tu, tv, 2));
+        p.albedo_a = tex_bilinear<R>(t, tu, tv, 3);
+    }
+    p.roughness = m.texture_indices0[2] == -1 ? R(m.roughness_metallic[0])
+                                               : tex_bilinear<R>(s.textures[m.texture_indices0[2]], tu, tv, m.texture_indices1[2]);
+    p.metallic = m.texture_indices0[3] == -1 ? R(m.roughness_metallic[1])
+                                              : tex_bilinear<R>(s.textures[m.texture_indices0[3]], tu, tv, m.texture_indices1[3]);
+    if (m.texture_indices1[0] == -1) p.emissive = V3<R>(R(m.emissive[0]), R(m.emissive[1]), R(m.emissive[2]));
+    else {
+        const Tex& t = s.textures[m.texture_indices1[0]];
+        p.emissive = V3<R>(tex_bilinear<R>(t, tu, tv, 0), tex_bilinear<R>(t, tu, tv, 1), tex_bilinear<R>(t, tu, tv, 2));
+    }
+    p.roughness = gmax(p.roughness, R(kMinRoughness));
+    p.F0 = V3<R>(R(0.03f)) * (R(1) - p.metallic) + p.albedo * p.metallic;  // mix(x, y, a) = x(1-a) + ya
+    p.alpha = p.roughness * p.roughness;
+    p.alpha2 = p.alpha * p.alpha;
+    return p;
+}
+
+struct Params {
+    uint32_t width, height, max_bounces;
+    float shadow_bias;
+    hx_policy pol;
+};
+
+struct Counters {
+    uint64_t paths = 0, ext = 0, shadow = 0;
+};
+
+template <typename R> static V3<R> fv3(const float* f) { return V3<R>(R(f[0]), R(f[1]), R(f[2])); }
+
+// sample_light (path_trace_rchit.glsl:284-451).  Returns Li (before
+// visibility); sets Wi, pdf, the shadow-ray tmax and whether to trace.
+template <typename R>
+static V3<R> sample_light(const Scene& s, const Params& P, const Surface<R>& p, const hx_light& light, RNG& rng, V3<R>& Wi,
+                          R& pdf, R& tmax, bool& trace_it) {
+    tmax = R(10000.0f);
+    trace_it = true;
+    uint32_t type = (uint32_t)light.data0[0];
+    V3<R> Li(R(0));
+    Wi = V3<R>(R(0));
+    pdf = R(0);
+    if (type == HX_LIGHT_DIRECTIONAL || type == HX_LIGHT_SPOT || type == HX_LIGHT_POINT) {
+        R r0 = next_float(rng), r1 = next_float(rng);
+        V3<R> light_dir, to_light;
+        R light_distance = 0, light_radius;
+        if (type == HX_LIGHT_DIRECTIONAL) {
+            light_dir = -fv3<R>(light.data1);
+            light_radius = R(light.data2[3]);
+        } else {
+            to_light = fv3<R>(light.data2) - p.position;
+            light_dir = normalize(to_light);
+            light_distance = length(to_light);
+            light_radius = R(light.data2[3]) / light_distance;
+        }
+        V3<R> lt = normalize(cross(light_dir, V3<R>(0, 1, 0)));
+        V3<R> lb = normalize(cross(lt, light_dir));
+        R point_radius = light_radius * std::sqrt(r0);
+        R point_angle = r1 * R(2) * kpi<R>();
+        R dx = point_radius * std::cos(point_angle), dy = point_radius * std::sin(point_angle);
+        Wi = normalize(light_dir + lt * dx + lb * dy);
+        V3<R> col = V3<R>(R(light.data0[1]), R(light.data0[2]), R(light.data0[3]));
+        R intensity = R(light.data1[3]);
+        if (type == HX_LIGHT_DIRECTIONAL) Li = col * intensity;
+        else if (type == HX_LIGHT_POINT) Li = col * intensity / (light_distance * light_distance);
+        else {
+            R att = dot(light_dir, -fv3<R>(light.data1));
+            R e0 = R(light.data3[1]), e1 = R(light.data3[0]);
+            // smoothstep(outer, inner, x); equal edges (resource_manager.cpp:592) act as a step
+            if (e1 == e0) att = att < e0 ? R(0) : R(1);
+            else {
+                R tt = gclamp((att - e0) / (e1 - e0), R(0), R(1));
+                att = tt * tt * (R(3) - R(2) * tt);
+            }
+            Li = col * intensity * att / (light_distance * light_distance);
+        }
+        pdf = R(0);
+        if (type != HX_LIGHT_DIRECTIONAL) tmax = light_distance;
+    } else if (type == HX_LIGHT_ENVIRONMENT) {
+        R r0 = next_float(rng), r1 = next_float(rng);
+        if (P.pol.env_sampling == HX_ENV_SAMPLE_IMPORTANCE && s.env_kind != HX_ENV_NONE) {
+            Wi = env_sample<R>(s, r0, r1, pdf);
+            Li = env_lookup(s, Wi);
+            if (!(pdf > R(0))) { Li = V3<R>(R(0)); trace_it = false; }
+        } else {
+            Wi = sample_cosine_lobe(p.normal, r0, r1);
+            Li = env_lookup(s, Wi);
+            pdf = dot(p.normal, Wi) / kpi<R>();
+        }
+    } else if (type == HX_LIGHT_AREA) {
+        uint32_t inst_id = (uint32_t)light.data0[1];
+        uint32_t num_tris = P.pol.area_count_from_x ? (uint32_t)light.data1[0] : (uint32_t)light.data1[2];
+        uint32_t prim_id = next_uint(rng, num_tris);
+        uint32_t mat = (uint32_t)light.data0[2];
+        uint32_t mp = prim_id + (uint32_t)light.data0[3];
+        const hx_instance& inst = s.instances[inst_id];
+        uint32_t mesh = inst.mesh_index;
+        R r0 = next_float(rng), r1 = next_float(rng);
+        R su0 = std::sqrt(r0);  // uniform_sample_triangle, brdf.glsl:40-44
+        R bx = R(1) - su0, by = r1 * su0;
+        R M[16], N[16];
+        for (int k = 0; k < 16; ++k) { M[k] = inst.model_matrix[k]; N[k] = inst.normal_matrix[k]; }
+        V3<R> P3[3], N3[3];
+        for (int c = 0; c < 3; ++c) {
+            const hx_vertex& v = mesh_vertex<R>(s, mesh, mp, c);
+            R w = P.pol.area_w_one ? R(1) : R(v.position[3]);
+            R o[4];
+            mat4_mul(M, R(v.position[0]), R(v.position[1]), R(v.position[2]), w, o);
+            P3[c] = V3<R>(o[0], o[1], o[2]);
+            N3[c] = fv3<R>(v.normal);
+        }
+        R c0 = R(1) - bx - by;  // barycentric_interpolate, brdf.glsl:46-51
+        V3<R> light_pos = P3[0] * c0 + P3[1] * bx + P3[2] * by;
+        V3<R> light_normal = normalize(mat3_mul(N, N3[0] * c0 + N3[1] * bx + N3[2] * by));
+        V3<R> light_dir = p.position - light_pos;
+        R dist_sqr = dot(light_dir, light_dir);
+        R area = R(0.5) * length(cross(P3[1] - P3[0], P3[2] - P3[0]));
+        if (area == R(0) || dist_sqr == R(0)) { trace_it = false; return V3<R>(R(0)); }
+        R dist = std::sqrt(dist_sqr);
+        light_dir = light_dir / dist;
+        tmax = gmax(R(0), dist - R(kEpsilon));
+        R cos_theta = dot(light_normal, light_dir);
+        if (cos_theta == R(0)) { trace_it = false; return V3<R>(R(0)); }
+        const hx_material& m = s.materials[mat];
+        Li = V3<R>(R(m.emissive[0]), R(m.emissive[1]), R(m.emissive[2]));
+        Wi = -light_dir;
+        pdf = dist_sqr / gmax(R(kEpsilon), cos_theta * area);  // pdf_triangle
+    }
+    return Li;
+}
+
+template <typename R>
+static void generate_ray(const hx_frame_desc& f, uint32_t x, uint32_t y, uint32_t W, uint32_t H, RNG& rng, V3<R>& org,
+                         V3<R>& dir) {  // path_trace_rgen.glsl:132-174
+    R px = R((float)x) + R(0.5), py = R((float)y) + R(0.5);
+    R jx = next_float(rng), jy = next_float(rng);
+    R tx = (px + jx) / R((float)W), ty = (py + jy) / R((float)H);
+    R nx = tx * R(2) - R(1), ny = ty * R(2) - R(1);
+    R m[16];
+    for (int k = 0; k < 16; ++k) m[k] = f.view_proj_inverse[k];
+    R tg[4];
+    mat4_mul(m, nx, ny, R(0), R(1), tg);
+    R tw = tg[3];
+    V3<R> target(tg[0] / tw, tg[1] / tw, tg[2] / tw);
+    V3<R> cam = fv3<R>(f.camera_pos);
+    R angle = R(next_float(rng)) * R(2) * kpi<R>();
+    R radius = std::sqrt(R(next_float(rng)));
+    R ap = R(f.aperture_radius);
+    R ox = std::cos(angle) * radius * ap, oy = std::sin(angle) * radius * ap;
+    V3<R> aperture_pos = cam + fv3<R>(f.right_direction) * ox + fv3<R>(f.up_direction) * oy;
+    V3<R> rdir = -normalize(target - cam);
+    V3<R> fp = fv3<R>(f.focal_plane);
+    R t = -(dot(cam, fp) + R(f.focal_plane[3])) / dot(rdir, fp);
+    V3<R> focus = cam + rdir * t;
+    org = aperture_pos;
+    dir = normalize(focus - aperture_pos);
+}
+
+// One camera sample: ray-gen + the closest-hit recursion unrolled into a
+// loop (the payload recursion of path_trace_rchit.glsl:487-536 sums L in the
+// same order: emission, direct light, then the deeper bounces).
+template <typename R>
+static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f, uint32_t x, uint32_t y, uint32_t frame,
+                        Counters& cnt, hx_hit* primary) {
+    RNG rng = rng_init(P.pol.rng, x, y, P.width, frame);
+    V3<R> L(R(0)), T(R(1));
+    uint32_t depth = 0;
+    V3<R> o, d;
+    generate_ray<R>(f, x, y, P.width, P.height, rng, o, d);
+    R tmin = R(0.001f), tmax = R(10000.0f);
+    bool any_hit = true;
+    uint32_t num_lights = (uint32_t)s.lights.size();
+    cnt.paths++;
+    for (;;) {
+        R t, hu, hv;
+        uint32_t prim;
+        cnt.ext++;
+        bool hit = trace<R>(s, o, d, tmin, tmax, any_hit, false, false, t, hu, hv, prim);
+        if (depth == 0 && primary) {
+            primary->t = hit ? (float)t : 0.0f;
+            primary->prim = hit ? prim : kNoHit;
+            primary->u = hit ? (float)hu : 0.0f;
+            primary->v = hit ? (float)hv : 0.0f;
+        }
+        if (!hit) {  // path_trace_rmiss.glsl:60-65
+            V3<R> e = env_lookup(s, d);
+            L = L + (depth == 0 ? e : T * e);
+            break;
+        }
+        Surface<R> p = populate<R>(s, prim, (float)hu, (float)hv);
+        if (depth == 0 && !is_black(p.emissive)) L = L + p.emissive;
+        V3<R> Wo = -d;
+        if (num_lights > 0) {  // direct_lighting, rchit.glsl:455-483
+            uint32_t li = next_uint(rng, num_lights);
+            V3<R> Wi;
+            R pdf, stmax;
+            bool trace_it;
+            V3<R> Li = sample_light<R>(s, P, p, s.lights[li], rng, Wi, pdf, stmax, trace_it);
+            if (trace_it && !is_black(Li)) {
+                V3<R> Wh = normalize(Wo + Wi);
+                V3<R> brdf = evaluate_uber(p, Wo, Wh, Wi);
+                R cos_theta = gclamp(dot(p.normal, Wi), R(0), R(1));
+                V3<R> so = p.position + p.normal * R(P.shadow_bias);
+                R st, su, sv;
+                uint32_t sp;
+                cnt.shadow++;
+                bool occluded = trace<R>(s, so, Wi, R(0.0001f), stmax, depth == 0, true, false, st, su, sv, sp);
+                if (!occluded) {
+                    V3<R> c = ((T * brdf) * cos_theta) * Li;
+                    if (pdf != R(0)) c = c / pdf;
+                    L = L + c * R((float)num_lights);
+                }
+            }
+        }
+        if (!((depth + 1) < P.max_bounces)) break;
+        // indirect_lighting, rchit.glsl:487-536
+        V3<R> Wi;
+        R pdf;
+        V3<R> brdf = sample_uber(p, Wo, rng, Wi, pdf);
+        R cos_theta = gclamp(dot(p.normal, Wi), R(0), R(1));
+        V3<R> Tn = (T * (brdf * cos_theta)) / pdf;
+        if (depth >= P.pol.rr_start_depth) {
+            R prob = gmax(Tn.x, gmax(Tn.y, Tn.z));
+            if (P.pol.rr_clamp) prob = gmin(prob, R(1));
+            if (R(next_float(rng)) > prob) break;
+            Tn = Tn * (R(1) / prob);
+        }
+        T = Tn;
+        depth++;
+        o = p.position;
+        d = Wi;
+        tmin = R(0.0001f);
+        tmax = R(10000.0f);
+        any_hit = false;
+    }
+    return L;
+}
+
+static Params make_params(const hx_integrator_desc& d, uint32_t num_lights) {
+    (void)num_lights;
+    Params P;
+    P.width = d.width;
+    P.height = d.height;
+    P.max_bounces = d.max_ray_bounces;
+    P.shadow_bias = d.shadow_ray_bias;
+    P.pol = d.policy;
+    return P;
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+// ---------------------------------------------------------------------------
+// C ABI for the tests (ctypes).
+// ---------------------------------------------------------------------------
+extern "C" {
+
+struct oracle_counters {
+    uint64_t paths, extension_rays, shadow_rays;
+    double seconds;
+    int threads;
+};
+
+void* oracle_scene_create(const hx_scene_desc* d) {
+    Scene* s = new Scene();
+    for (uint32_t m = 0; m < d->num_meshes; ++m) {
+        const hx_mesh_desc& md = d->meshes[m];
+        s->vertices.emplace_back(md.vertices, md.vertices + md.num_vertices);
+        s->indices.emplace_back(md.indices, md.indices + md.num_indices);
+        s->submeshes.emplace_back(md.submeshes, md.submeshes + md.num_submeshes);
+    }
+    s->instances.assign(d->instances, d->instances + d->num_instances);
+    s->materials.assign(d->materials, d->materials + d->num_materials);
+    for (uint32_t t = 0; t < d->num_textures; ++t) {
+        Tex tx;
+        tx.w = d->textures[t].width;
+        tx.h = d->textures[t].height;
+        tx.rgba.assign(d->textures[t].rgba8, d->textures[t].rgba8 + (size_t)tx.w * tx.h * 4);
+        s->textures.push_back(std::move(tx));
+    }
+    s->punctual.assign(d->punctual_lights, d->punctual_lights + d->num_punctual_lights);
+    const hx_environment_desc& e = d->environment;
+    s->env_kind = e.kind;
+    if (e.kind != HX_ENV_NONE) {
+        s->env_w = e.width;
+        s->env_h = e.height;
+        s->env.resize((size_t)e.width * e.height * 3);
+        std::memcpy(s->coeffs, e.coeffs, sizeof(s->coeffs));
+        for (int a = 0; a < 3; ++a) s->sun[a] = e.sun_direction[a];
+        for (uint32_t j = 0; j < e.height; ++j)
+            for (uint32_t i = 0; i < e.width; ++i) {
+                size_t k = (size_t)j * e.width + i;
+                float rgb[3];
+                if (e.kind == HX_ENV_EQUIRECT) {
+                    for (int c = 0; c < 3; ++c) rgb[c] = e.rgba32f[k * 4 + c];
+                } else {
+                    V3<double> dir = latlong_dir((i + 0.5) / e.width, (j + 0.5) / e.height);
+                    V3<double> sun((double)e.sun_direction[0], (double)e.sun_direction[1], (double)e.sun_direction[2]);
+                    V3<double> r = sky_radiance<double>(e.coeffs, dir, sun);
+                    for (int c = 0; c < 3; ++c) rgb[c] = (float)r[c];
+                }
+                for (int c = 0; c < 3; ++c) s->env[k * 3 + c] = half_to_float(float_to_half(rgb[c]));
+            }
+        build_env_cdf(*s);
+    }
+    flatten(*s);
+    build_lights(*s);
+    build_bvh(*s);
+    return s;
+}
+
+void oracle_scene_destroy(void* h) { delete (Scene*)h; }
+
+uint32_t oracle_scene_num_prims(void* h) { return (uint32_t)((Scene*)h)->prims.size(); }
+uint32_t oracle_scene_num_bvh8_nodes(void* h) { return (uint32_t)((Scene*)h)->bvh.nodes.size(); }
+uint32_t oracle_scene_num_lights(void* h) { return (uint32_t)((Scene*)h)->lights.size(); }
+
+void oracle_scene_lights(void* h, hx_light* out) {
+    Scene* s = (Scene*)h;
+    std::memcpy(out, s->lights.data(), s->lights.size() * sizeof(hx_light));
+}
+
+void oracle_scene_env(void* h, float* out_rgb) {
+    Scene* s = (Scene*)h;
+    std::memcpy(out_rgb, s->env.data(), s->env.size() * sizeof(float));
+}
+
+void oracle_bvh_export(void* h, uint32_t* morton, uint32_t* sorted, uint32_t* children, void* nodes, uint32_t* leaf_prims) {
+    Scene* s = (Scene*)h;
+    const Bvh& b = s->bvh;
+    if (morton) std::memcpy(morton, b.morton.data(), b.morton.size() * 4);
+    if (sorted) std::memcpy(sorted, b.sorted.data(), b.sorted.size() * 4);
+    if (children) std::memcpy(children, b.children.data(), b.children.size() * 4);
+    if (nodes) std::memcpy(nodes, b.nodes.data(), b.nodes.size() * sizeof(hx_bvh8_node));
+    if (leaf_prims) std::memcpy(leaf_prims, b.leaf_prims.data(), b.leaf_prims.size() * 4);
+}
+
+void oracle_trace(void* h, const float* rays, uint32_t n, uint32_t any_hit, uint32_t brute, hx_hit* out) {
+    Scene* s = (Scene*)h;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long i = 0; i < (long)n; ++i) {
+        const float* r = &rays[8 * (size_t)i];
+        float t, u, v;
+        uint32_t p;
+        bool hit = trace<float>(*s, V3<float>(r[0], r[1], r[2]), V3<float>(r[4], r[5], r[6]), r[3], r[7], any_hit != 0, false,
+                                brute != 0, t, u, v, p);
+        out[i].t = hit ? t : 0.0f;
+        out[i].prim = hit ? p : kNoHit;
+        out[i].u = hit ? u : 0.0f;
+        out[i].v = hit ? v : 0.0f;
+    }
+}
+
+void oracle_primary_rays(const hx_integrator_desc* d, const hx_frame_desc* f, uint32_t frame, float* out) {
+    Params P = make_params(*d, 0);
+    for (uint32_t y = 0; y < d->height; ++y)
+        for (uint32_t x = 0; x < d->width; ++x) {
+            RNG rng = rng_init(P.pol.rng, x, y, P.width, frame);
+            V3<float> o, dir;
+            generate_ray<float>(*f, x, y, P.width, P.height, rng, o, dir);
+            float* r = &out[8 * ((size_t)y * d->width + x)];
+            r[0] = o.x; r[1] = o.y; r[2] = o.z; r[3] = 0.001f;
+            r[4] = dir.x; r[5] = dir.y; r[6] = dir.z; r[7] = 10000.0f;
+        }
+}
+
+// Per-sample radiance L (before the clamp) of frame `frame` for the listed
+// pixels (pixel = y*width + x; NULL = all), precision 32 or 64.
+void oracle_sample_radiance(void* h, const hx_integrator_desc* d, const hx_frame_desc* f, uint32_t frame, uint32_t precision,
+                            const uint32_t* pixels, uint32_t n_pixels, float* out_rgb, hx_hit* primary) {
+    Scene* s = (Scene*)h;
+    Params P = make_params(*d, (uint32_t)s->lights.size());
+    uint32_t n = pixels ? n_pixels : d->width * d->height;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long i = 0; i < (long)n; ++i) {
+        uint32_t pix = pixels ? pixels[i] : (uint32_t)i;
+        uint32_t x = pix % d->width, y = pix / d->width;
+        Counters c;
+        hx_hit* ph = primary ? &primary[i] : nullptr;
+        if (precision == 64) {
+            V3<double> L = trace_path<double>(*s, P, *f, x, y, frame, c, ph);
+            out_rgb[3 * i] = (float)L.x; out_rgb[3 * i + 1] = (float)L.y; out_rgb[3 * i + 2] = (float)L.z;
+        } else {
+            V3<float> L = trace_path<float>(*s, P, *f, x, y, frame, c, ph);
+            out_rgb[3 * i] = L.x; out_rgb[3 * i + 1] = L.y; out_rgb[3 * i + 2] = L.z;
+        }
+    }
+}
+
+// Progressive accumulation of frames [0, num_frames) for the listed pixels
+// (NULL = all, in 16x16 tiles), with the policy's accumulation rule
+// (running mean of path_trace_rgen.glsl:217-248, or Kahan sum / n).
+// out_rgb holds 3 doubles per listed pixel.  threads <= 0: all cores.
+void oracle_render(void* h, const hx_integrator_desc* d, const hx_frame_desc* f, uint32_t num_frames, uint32_t precision,
+                   const uint32_t* pixels, uint32_t n_pixels, double* out_rgb, int threads, oracle_counters* counters) {
+    Scene* s = (Scene*)h;
+    Params P = make_params(*d, (uint32_t)s->lights.size());
+    uint32_t n = pixels ? n_pixels : d->width * d->height;
+    int nt = threads > 0 ? threads : omp_get_max_threads();
+    uint64_t tp = 0, te = 0, ts = 0;
+    float clampv = d->policy.radiance_clamp;
+    auto t0 = std::chrono::steady_clock::now();
+    // work items: 16x16 pixel tiles for full frames, chunks of 256 listed pixels otherwise
+    uint32_t tiles_x = (d->width + 15) / 16, tiles_y = (d->height + 15) / 16;
+    long items = pixels ? (long)((n + 255) / 256) : (long)tiles_x * tiles_y;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt) reduction(+ : tp, te, ts)
+    for (long it = 0; it < items; ++it) {
+        std::vector<uint32_t> list;
+        if (pixels) {
+            for (uint32_t k = (uint32_t)it * 256; k < n && k < (uint32_t)it * 256 + 256; ++k) list.push_back(k);
+        } else {
+            uint32_t tx = (uint32_t)(it % tiles_x), ty = (uint32_t)(it / tiles_x);
+            for (uint32_t y = ty * 16; y < ty * 16 + 16 && y < d->height; ++y)
+                for (uint32_t x = tx * 16; x < tx * 16 + 16 && x < d->width; ++x) list.push_back(y * d->width + x);
+        }
+        Counters c;
+        for (uint32_t k : list) {
+            uint32_t pix = pixels ? pixels[k] : k;
+            uint32_t x = pix % d->width, y = pix / d->width;
+            double acc[3] = {0, 0, 0}, comp[3] = {0, 0, 0};
+            float accf[3] = {0, 0, 0}, compf[3] = {0, 0, 0};
+            for (uint32_t fr = 0; fr < num_frames; ++fr) {
+                if (precision == 64) {
+                    V3<double> L = trace_path<double>(*s, P, *f, x, y, fr, c, nullptr);
+                    for (int ch = 0; ch < 3; ++ch) {
+                        double v = clampv > 0 ? gmin(L[ch], (double)clampv) : L[ch];
+                        if (d->policy.accumulation == HX_ACCUM_KAHAN) {
+                            double yk = v - comp[ch];
+                            double tk = acc[ch] + yk;
+                            comp[ch] = (tk - acc[ch]) - yk;
+                            acc[ch] = tk;
+                        } else acc[ch] = fr == 0 ? v : acc[ch] + (v - acc[ch]) / (double)fr;
+                    }
+                } else {
+                    V3<float> L = trace_path<float>(*s, P, *f, x, y, fr, c, nullptr);
+                    for (int ch = 0; ch < 3; ++ch) {
+                        float v = clampv > 0 ? gmin(L[ch], clampv) : L[ch];
+                        if (d->policy.accumulation == HX_ACCUM_KAHAN) {
+                            float yk = v - compf[ch];
+                            float tk = accf[ch] + yk;
+                            compf[ch] = (tk - accf[ch]) - yk;
+                            accf[ch] = tk;
+                        } else accf[ch] = fr == 0 ? v : accf[ch] + (v - accf[ch]) / (float)fr;
+                    }
+                }
+            }
+            uint32_t slot = pixels ? k : pix;
+            for (int ch = 0; ch < 3; ++ch) {
+                double v = precision == 64 ? acc[ch] : (double)accf[ch];
+                if (d->policy.accumulation == HX_ACCUM_KAHAN)
+                    v = precision == 64 ? acc[ch] / (double)num_frames : (double)(accf[ch] / (float)num_frames);
+                out_rgb[3 * (size_t)slot + ch] = v;
+            }
+        }
+        tp += c.paths; te += c.ext; ts += c.shadow;
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    if (counters) {
+        counters->paths = tp;
+        counters->extension_rays = te;
+        counters->shadow_rays = ts;
+        counters->seconds = std::chrono::duration<double>(t1 - t0).count();
+        counters->threads = nt;
+    }
+}
+
+// tone_map.frag:22-51 + R8G8B8A8_UNORM store, vertically flipped
+// (renderer.cpp:394-399 negative-height viewport).
+void oracle_tonemap(const float* accum_rgba, uint32_t w, uint32_t h, uint32_t op, float exposure, uint8_t* out) {
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            const float* c = &accum_rgba[4 * ((size_t)(h - 1 - y) * w + x)];
+            uint8_t* o = &out[4 * ((size_t)y * w + x)];
+            for (int ch = 0; ch < 3; ++ch) {
+                float v = c[ch] * exposure;
+                if (op == HX_TONEMAP_ACES) {
+                    float a = 2.51f, b = 0.03f, cc = 2.43f, dd = 0.59f, e = 0.14f;
+                    v = gclamp((v * (a * v + b)) / (v * (cc * v + dd) + e), 0.0f, 1.0f);
+                } else if (op == HX_TONEMAP_REINHARD) {
+                    v = v / (1.0f + v);
+                }
+                v = std::pow(v, 1.0f / 2.2f);
+                float q = gclamp(v, 0.0f, 1.0f) * 255.0f + 0.5f;
+                o[ch] = (uint8_t)q;
+            }
+            o[3] = 255;
+        }
+}
+
+void oracle_rng_streams(uint32_t kind, const uint32_t* seeds, uint32_t n, uint32_t draws, uint32_t* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        RNG r;
+        r.kind = kind;
+        if (kind == 0) {
+            r.s0 = wang_hash(seeds[2 * i]);
+            r.s1 = wang_hash(seeds[2 * i + 1]);
+            rng_next(r);
+        } else {
+            r.s0 = pcg_hash(pcg_hash(seeds[2 * i]) + seeds[2 * i + 1]);
+            r.s1 = 0;
+        }
+        for (uint32_t k = 0; k < draws; ++k) out[(size_t)i * draws + k] = rng_next(r);
+    }
+}
+
+uint32_t oracle_wang_hash(uint32_t v) { return wang_hash(v); }
+uint32_t oracle_pcg_hash(uint32_t v) { return pcg_hash(v); }
+uint16_t oracle_float_to_half(float f) { return float_to_half(f); }
+float oracle_half_to_float(uint16_t h) { return half_to_float(h); }
+int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+}  // extern "C"

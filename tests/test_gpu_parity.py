@@ -1,0 +1,205 @@
+"""GPU parity tests: the CUDA path (through the C-ABI) against the oracle.
+
+Integer outputs (RNG draws, Morton codes, BVH topology and node order,
+hit triangle IDs) must be bit-exact; radiance is compared by relative RMSE
+with the tolerance stated in each test.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import helios_gb300 as hx
+from oracle import binding as ob
+from tests.helpers import integrator_desc, random_rays, rel_rmse, small_icosphere_scene
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def box(gpu_ctx):
+    hs = hx.HostScene(hx.SCENE_BOX)
+    sc = hx.Scene(gpu_ctx, hs)
+    yield hs, sc, ob.OracleScene(hs)
+    sc.close()
+
+
+@pytest.fixture(scope="module")
+def ico(gpu_ctx):
+    hs = small_icosphere_scene(level=4, quads=5000, pool=8, mask=128, env=(256, 128))
+    sc = hx.Scene(gpu_ctx, hs)
+    yield hs, sc, ob.OracleScene(hs)
+    sc.close()
+
+
+def test_rng_streams_bit_exact(gpu_ctx):
+    kat = json.load(open(os.path.join(GOLDEN, "rng_kat.json")))
+    rng = np.random.default_rng(5)
+    seeds = np.concatenate([np.array([c["seed"] for c in kat["streams"]], np.uint32).ravel(),
+                            rng.integers(0, 2**32, size=2 * 4096, dtype=np.uint64).astype(np.uint32)])
+    for kind in (hx.RNG_XOROSHIRO64STAR, hx.RNG_PCG):
+        g = gpu_ctx.rng_streams(kind, seeds, 64)
+        o = ob.rng_streams(kind, seeds, 64)
+        assert np.array_equal(g, o)
+    g = gpu_ctx.rng_streams(0, seeds[:16], kat["draws"])
+    for i, c in enumerate(kat["streams"]):
+        assert g[i].tolist() == c["xoroshiro64star"]
+
+
+@pytest.mark.parametrize("which", ["box", "ico"])
+def test_bvh_bit_exact(which, box, ico):
+    hs, sc, osc = box if which == "box" else ico
+    g, o = sc.export_bvh(), osc.export_bvh()
+    assert np.array_equal(g["morton"], o["morton"])
+    assert np.array_equal(g["sorted"], o["sorted"])
+    assert np.array_equal(g["children"], o["children"])
+    assert g["nodes"].shape == o["nodes"].shape
+    assert g["nodes"].tobytes() == o["nodes"].tobytes()
+    assert np.array_equal(g["leaf_prims"], o["leaf_prims"])
+
+
+@pytest.mark.parametrize("which", ["box", "ico"])
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_trace_hits_bit_exact(which, any_hit, box, ico):
+    hs, sc, osc = box if which == "box" else ico
+    lo, hi = (0.05, 0.95) if which == "box" else (-25, 25)
+    rays = random_rays(20000, lo, hi, seed=11)
+    g = sc.trace(rays, any_hit=any_hit)
+    o = osc.trace(rays, any_hit=any_hit)
+    assert np.array_equal(g["prim"], o["prim"])
+    hit = o["prim"] != hx.NO_HIT
+    assert np.array_equal(g["t"][hit], o["t"][hit])
+    assert np.array_equal(g["u"][hit], o["u"][hit]) and np.array_equal(g["v"][hit], o["v"][hit])
+
+
+@pytest.mark.parametrize("which,policy", [("box", "spec"), ("box", "reference"), ("ico", "reference")])
+def test_primary_hit_ids_bit_exact(which, policy, gpu_ctx, box, ico):
+    hs, sc, osc = box if which == "box" else ico
+    W, H = (256, 256) if which == "box" else (320, 180)
+    d = integrator_desc(W, H, policy=policy)
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, policy=d.policy)
+    for frame in (0, 7):
+        g = it.primary_hits(f, frame)
+        o = osc.trace(ob.primary_rays(d, f, frame), any_hit=True)
+        assert np.array_equal(g["prim"], o["prim"])
+        assert np.array_equal(g["t"], o["t"])
+    it.close()
+
+
+@pytest.mark.parametrize("which,policy", [("box", "spec"), ("box", "reference"), ("ico", "reference"), ("ico", "spec")])
+def test_sample_radiance_matches_oracle(which, policy, gpu_ctx, box, ico):
+    """Per-sample radiance of one frame, FP32 device vs FP32 oracle: the same
+    paths; differences come only from transcendental rounding (relative RMSE
+    tolerance 1e-3 over the frame)."""
+    hs, sc, osc = box if which == "box" else ico
+    W, H = (64, 64) if which == "box" else (96, 54)
+    bounces = 5 if which == "box" else 8
+    d = integrator_desc(W, H, bounces=bounces, policy=policy)
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=bounces, policy=d.policy)
+    for frame in (0, 3):
+        g = it.sample_radiance(f, frame)
+        o, _ = osc.sample_radiance(d, f, frame, precision=32)
+        assert rel_rmse(g, o) < 1e-3, (frame, rel_rmse(g, o))
+        # most samples agree to float rounding
+        close = np.all(np.abs(g - o) <= 1e-4 * (1 + np.abs(o)), axis=1)
+        assert close.mean() > 0.97
+    it.close()
+
+
+def test_accumulation_and_tonemap_match_oracle(gpu_ctx, box):
+    hs, sc, osc = box
+    W = H = 64
+    d = integrator_desc(W, H, policy="spec")
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=5, policy=d.policy)
+    it.render(f, 32)
+    acc = it.read_accumulation()
+    o, _ = osc.render(d, f, 32, precision=32)
+    assert rel_rmse(acc[:, :, :3].reshape(-1, 3), o) < 1e-3
+    ldr = it.tonemap(hx.TONEMAP_ACES, 1.0)
+    ref = ob.tonemap(acc, hx.TONEMAP_ACES, 1.0)
+    assert np.abs(ldr.astype(int) - ref.astype(int)).max() <= 1
+    ldr = it.tonemap(hx.TONEMAP_REINHARD, 2.0)
+    ref = ob.tonemap(acc, hx.TONEMAP_REINHARD, 2.0)
+    assert np.abs(ldr.astype(int) - ref.astype(int)).max() <= 1
+    it.close()
+
+
+def test_batched_frames_equal_sequential(gpu_ctx, box):
+    hs, sc, _ = box
+    W = H = 48
+    f = hx.frame_desc(hs.camera(), W, H)
+    a = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=5)
+    b = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=5)
+    a.render(f, 12)
+    for _ in range(12):
+        b.render(f, 1)
+    assert np.array_equal(a.read_accumulation(), b.read_accumulation())
+    assert a.num_accumulated_samples() == b.num_accumulated_samples() == 12
+    a.close()
+    b.close()
+
+
+def test_progressive_and_tiled_schedule(gpu_ctx, box):
+    hs, sc, _ = box
+    W, H = 200, 150  # 2 x 2 tiles of 128
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=3, max_samples=4, tiled=True)
+    assert it.num_target_samples() == 16
+    it.render(f, 5)
+    acc, tile, _ = it.progress()
+    assert (acc, tile) == (5, 1)
+    img = it.read_accumulation()
+    assert np.all(img[:128, :128, 3] == 1.0) and np.all(img[:, 128:, 3] == 0.0)
+    it.render(f, 100)
+    assert it.progress()[:2] == (16, 4)
+    before = it.read_accumulation()
+    it.render(f, 3)  # bake finished: nothing more is traced
+    assert np.array_equal(before, it.read_accumulation())
+    it.restart_bake()
+    assert it.progress()[:2] == (0, 0)
+    it.close()
+
+
+def test_converged_radiance_vs_fp64_oracle(gpu_ctx, box):
+    """Box scene, spec policy, 16384 samples per pixel: relative RMSE of the
+    device image against the FP64 oracle at the same seeds <= 1e-3 on a seeded
+    subset of 256 pixels."""
+    hs, sc, osc = box
+    W = H = 256
+    spp = 16384
+    d = integrator_desc(W, H, policy="spec", max_samples=spp)
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=5, max_samples=spp, policy=d.policy)
+    it.render(f, spp)
+    img = it.read_accumulation()[:, :, :3].reshape(-1, 3)
+    pix = np.random.default_rng(3).choice(W * H, size=256, replace=False).astype(np.uint32)
+    o, _ = osc.render(d, f, spp, precision=64, pixels=pix)
+    err = rel_rmse(img[pix], o)
+    assert err <= 1e-3, err
+    it.close()
+
+
+def test_environment_bake_matches_oracle(ico, gpu_ctx):
+    hs, sc, osc = ico
+    w, h = hs.params.env_width, hs.params.env_height
+    g = sc.export_env(w, h)
+    o = osc.env(w, h)
+    # FP16 texels from FP32 device math vs FP64 host math: within 2 half ulps
+    assert np.allclose(g, o, rtol=2e-3, atol=1e-6)
+
+
+def test_errors_are_reported_not_raised_on_device(gpu_ctx, box):
+    hs, sc, _ = box
+    with pytest.raises(hx.HxError) as e:
+        hx.PathIntegrator(gpu_ctx, sc, 0, 10)
+    assert e.value.status == hx.HX_ERR_INVALID_ARG
+    small = hx.Context(0, hbm_budget_bytes=1 << 20)
+    with pytest.raises(hx.HxError) as e:
+        hx.PathIntegrator(small, hx.Scene(small, hs) if False else sc, 512, 512)
+    assert e.value.status == hx.HX_ERR_OOM_BUDGET
+    small.close()

@@ -1,0 +1,82 @@
+"""CPU tests of the product library's host side: the C-ABI loads and exports
+every declared symbol; host-only entry points (policies, camera, procedural
+scenes, Hosek-Wilkie coefficients) behave; no device call is made."""
+import ctypes as C
+import json
+import os
+import re
+
+import numpy as np
+
+import helios_gb300 as hx
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    src = open(os.path.join(ROOT, "include", "hx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"HX_API\s+[^;(]*?\b(hx_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    names = _declared_symbols()
+    assert len(names) > 30
+    lib = hx.lib()
+    for n in names:
+        assert hasattr(lib, n), n
+    # the binding covers every declared entry point
+    assert set(names) <= set(hx.exported_symbols()) | {"hx_scene_export_env"}
+
+
+def test_policies():
+    r, s = hx.policy_reference(), hx.policy_spec()
+    assert (r.rng, r.rr_start_depth, r.rr_clamp, r.area_count_from_x, r.area_w_one) == (0, 0, 0, 0, 0)
+    assert r.radiance_clamp == 1.0 and r.accumulation == hx.ACCUM_RUNNING_MEAN
+    assert (s.rng, s.rr_start_depth, s.rr_clamp, s.area_count_from_x, s.area_w_one) == (1, 3, 1, 1, 1)
+    assert s.env_sampling == hx.ENV_SAMPLE_IMPORTANCE
+
+
+def test_camera_frame_desc():
+    cam = hx.Camera((0.5, 0.5, 2.5), (0.5, 0.5, 0.0), (0, 1, 0), 40.0, 1.0, 1000.0, 8.0, 0.0)
+    f = hx.frame_desc(cam, 256, 256)
+    assert list(f.camera_pos)[:3] == [0.5, 0.5, 2.5]
+    # focal plane: normal = -forward = +z, through z = 2.5 - 8
+    assert np.allclose(list(f.focal_plane), [0, 0, 1, 5.5], atol=1e-5)
+    # unproject the image centre: lies on the view axis
+    M = np.array(f.view_proj_inverse[:], np.float64).reshape(4, 4).T
+    p = M @ np.array([0, 0, 0, 1.0])
+    p = p[:3] / p[3]
+    d = p - np.array([0.5, 0.5, 2.5])
+    assert np.allclose(d / np.linalg.norm(d), [0, 0, -1], atol=1e-5)
+
+
+def test_procedural_scene_sizes():
+    hs = hx.HostScene(hx.SCENE_BOX)
+    d = hs.desc.contents
+    tris = sum(d.meshes[d.instances[i].mesh_index].num_indices // 3 for i in range(d.num_instances))
+    assert tris == 36
+    ico = hx.HostScene(hx.SCENE_ICOSPHERES, icosphere_level=6, num_alpha_quads=100000, mask_pool=2, mask_size=32,
+                       env_width=64, env_height=32)
+    d = ico.desc.contents
+    tris = sum(d.meshes[d.instances[i].mesh_index].num_indices // 3 for i in range(d.num_instances))
+    assert tris == 12 * 81920 + 2 + 200000
+    assert d.num_punctual_lights == 4 and d.environment.kind == hx.ENV_HOSEK_WILKIE
+
+
+def test_alpha_masks_are_half_cut_out():
+    ico = hx.HostScene(hx.SCENE_ICOSPHERES, icosphere_level=1, num_alpha_quads=10, mask_pool=3, mask_size=128,
+                       env_width=16, env_height=8)
+    d = ico.desc.contents
+    for t in range(d.num_textures):
+        tx = d.textures[t]
+        a = np.ctypeslib.as_array(tx.rgba8, shape=(tx.width * tx.height * 4,))[3::4]
+        assert abs((a >= 26).mean() - 0.5) < 0.01
+
+
+def test_hosek_coefficients_match_reference_golden():
+    g = json.load(open(os.path.join(ROOT, "tests", "golden", "hosek_coeffs.json")))
+    for case in g["cases"]:
+        k = hx.hosek_wilkie_coefficients(case["sun_direction"], case["turbidity"], 1.15)
+        ref = np.array(case["coeffs"], np.float32).reshape(10, 3)
+        assert np.allclose(k, ref, rtol=2e-5, atol=1e-7), case

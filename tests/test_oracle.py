@@ -1,0 +1,143 @@
+"""CPU tests: the oracle against the golden vectors and its own invariants."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import helios_gb300 as hx
+from oracle import binding as ob
+from tests.helpers import integrator_desc, random_rays, rel_rmse, small_icosphere_scene
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_rng_known_answers():
+    kat = json.load(open(os.path.join(GOLDEN, "rng_kat.json")))
+    seeds = np.array([c["seed"] for c in kat["streams"]], np.uint32)
+    xo = ob.rng_streams(0, seeds, kat["draws"])
+    pc = ob.rng_streams(1, seeds, kat["draws"])
+    for i, c in enumerate(kat["streams"]):
+        assert xo[i].tolist() == c["xoroshiro64star"]
+        assert pc[i].tolist() == c["pcg"]
+    for v, h in kat["hashes"]["wang"]:
+        assert ob.lib().oracle_wang_hash(v) == h
+    for v, h in kat["hashes"]["pcg"]:
+        assert ob.lib().oracle_pcg_hash(v) == h
+
+
+def test_half_conversion_round_trip():
+    vals = np.array([0.0, 1.0, -2.5, 65504.0, 1e-5, 3.14159, 0.1, 6.1e-5, 5.96e-8, 70000.0], np.float32)
+    for v in vals:
+        h = ob.lib().oracle_float_to_half(float(v))
+        assert np.float16(v).view(np.uint16) == h, v
+        assert ob.lib().oracle_half_to_float(h) == np.float32(np.float16(v))
+
+
+def _scene(kind):
+    if kind == "box":
+        return hx.HostScene(hx.SCENE_BOX)
+    return small_icosphere_scene()
+
+
+@pytest.mark.parametrize("kind", ["box", "ico"])
+def test_bvh_traversal_matches_brute_force(kind):
+    hs = _scene(kind)
+    osc = ob.OracleScene(hs)
+    lo, hi = (0.05, 0.95) if kind == "box" else (-25, 25)
+    rays = random_rays(4000, lo, hi, seed=3)
+    for any_hit in (False, True):
+        a = osc.trace(rays, any_hit=any_hit)
+        b = osc.trace(rays, any_hit=any_hit, brute=True)
+        assert np.array_equal(a["prim"], b["prim"])
+        assert np.array_equal(a["t"], b["t"])
+
+
+@pytest.mark.parametrize("kind", ["box", "ico"])
+def test_bvh8_structure(kind):
+    hs = _scene(kind)
+    osc = ob.OracleScene(hs)
+    b = osc.export_bvh()
+    n = osc.num_prims
+    # every triangle lands in exactly one leaf slot
+    assert np.array_equal(np.sort(b["leaf_prims"]), np.arange(n, dtype=np.uint32))
+    assert np.array_equal(np.sort(b["sorted"]), np.arange(n, dtype=np.uint32))
+    # Morton codes sorted along the stable order
+    m = b["morton"][b["sorted"]]
+    assert np.all(m[1:] >= m[:-1])
+    # conservative quantisation: decoded child boxes contain their triangles
+    nodes = b["nodes"]
+    from tests.test_oracle import _world_tris
+    tris = _world_tris(hs)
+    for node in nodes:
+        scale = np.ldexp(np.float32(1.0), node["exponent"].astype(np.int32)).astype(np.float32)
+        for c in range(8):
+            meta = int(node["meta"][c])
+            if meta == 0 or meta & 0x80:
+                continue
+            cnt, off = meta >> 5, meta & 31
+            lo = (node["origin"] + node["qlo"][:, c].astype(np.float32) * scale).astype(np.float32)
+            hi = (node["origin"] + node["qhi"][:, c].astype(np.float32) * scale).astype(np.float32)
+            for q in range(cnt):
+                p = b["leaf_prims"][node["prim_base"] + off + q]
+                v = tris[p]
+                assert np.all(v >= lo - 0.0) and np.all(v <= hi + 0.0)
+
+
+def _world_tris(hs):
+    """World-space triangles in flattened order, computed like the oracle."""
+    d = hs.desc.contents
+    out = []
+    for ii in range(d.num_instances):
+        inst = d.instances[ii]
+        M = np.array(inst.model_matrix[:], np.float32).reshape(4, 4)  # column-major: M[col][row]
+        mesh = d.meshes[inst.mesh_index]
+        for si in range(mesh.num_submeshes):
+            sm = mesh.submeshes[si]
+            for t in range(sm.index_count // 3):
+                tri = []
+                for c in range(3):
+                    v = mesh.vertices[mesh.indices[sm.base_index + 3 * t + c]]
+                    p = [np.float32(v.position[0]), np.float32(v.position[1]), np.float32(v.position[2])]
+                    row = []
+                    for r in range(3):
+                        acc = np.float32(M[0][r] * p[0])
+                        acc = np.float32(acc + np.float32(M[1][r] * p[1]))
+                        acc = np.float32(acc + np.float32(M[2][r] * p[2]))
+                        acc = np.float32(acc + np.float32(M[3][r] * np.float32(1.0)))
+                        row.append(acc)
+                    tri.append(row)
+                out.append(tri)
+    return np.array(out, np.float32)
+
+
+def test_fp32_matches_fp64_oracle():
+    hs = hx.HostScene(hx.SCENE_BOX)
+    osc = ob.OracleScene(hs)
+    d = integrator_desc(48, 48)
+    f = hx.frame_desc(hs.camera(), 48, 48)
+    a, _ = osc.render(d, f, 32, precision=32)
+    b, _ = osc.render(d, f, 32, precision=64)
+    assert rel_rmse(a, b) < 1e-4
+
+
+def test_light_list_reference_order():
+    hs = small_icosphere_scene()
+    osc = ob.OracleScene(hs)
+    L = osc.lights()
+    types = L[:, 0].astype(int).tolist()
+    # no emissive materials: environment first, then the 4 point lights
+    assert types == [hx.LIGHT_ENVIRONMENT] + [hx.LIGHT_POINT] * 4
+    box = ob.OracleScene(hx.HostScene(hx.SCENE_BOX)).lights()
+    assert box.shape[0] == 1 and int(box[0, 0]) == hx.LIGHT_AREA
+    assert box[0, 1] == 3 and box[0, 2] == 3 and box[0, 4] == 2  # instance 3, material 3, 2 triangles
+
+
+def test_policy_differences_change_the_image():
+    hs = hx.HostScene(hx.SCENE_BOX)
+    osc = ob.OracleScene(hs)
+    f = hx.frame_desc(hs.camera(), 32, 32)
+    a, _ = osc.render(integrator_desc(32, 32, policy="spec"), f, 16)
+    b, _ = osc.render(integrator_desc(32, 32, policy="reference"), f, 16)
+    # the reference samples only triangle 0 of the quad light (light_data1.z is never written)
+    assert a.mean() > b.mean()
