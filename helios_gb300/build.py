@@ -68,6 +68,17 @@ def build_library(force=False, verbose=False):
     return LIB
 
 
+def build_driver():
+    """Builds the headless C++ driver (helios_gb300/cpp/hx_render) against libhx.so."""
+    src = os.path.join(HERE, "cpp", "hx_render.cpp")
+    out = os.path.join(HERE, "cpp", "hx_render")
+    deps = [src, os.path.join(ROOT, "include", "hx.h"), os.path.join(ROOT, "include", "helios_gb300.hpp"), LIB]
+    if _stale(out, deps):
+        _run([CXX, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", out, "-L", HERE, "-lhx",
+              "-Wl,-rpath,$ORIGIN/.."])
+    return out
+
+
 def build_oracle():
     d = os.path.join(ROOT, "oracle")
     _run(["make", "-s", "-C", d])
@@ -88,5 +99,6 @@ def build_reference_checks():
 
 if __name__ == "__main__":
     build_library(force="--force" in sys.argv, verbose=True)
+    build_driver()
     build_oracle()
     print(LIB)

@@ -263,6 +263,45 @@ __global__ void k_collapse_plan(const uint32_t* __restrict__ queue, uint32_t lev
     n_leaf[k] = nl;
 }
 
+// Octant slot assignment (same rule as the oracle): slot bit k set = child
+// centre on the positive side of the node centre along axis k; greedy over
+// (child, slot) pairs by decreasing alignment score, ties to the lower child
+// position then the lower slot.
+__device__ void assign_octant_slots(uint32_t nk, const float (*klo)[3], const float (*khi)[3], uint32_t slot_kid[8]) {
+    float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t c = 0; c < nk; ++c)
+        for (int a = 0; a < 3; ++a) {
+            nlo[a] = klo[c][a] < nlo[a] ? klo[c][a] : nlo[a];
+            nhi[a] = khi[c][a] > nhi[a] ? khi[c][a] : nhi[a];
+        }
+    float score[8][8];
+    for (uint32_t c = 0; c < nk; ++c) {
+        float dv[3];
+        for (int a = 0; a < 3; ++a) dv[a] = (klo[c][a] + khi[c][a]) * 0.5f - (nlo[a] + nhi[a]) * 0.5f;
+        for (int sl = 0; sl < 8; ++sl) {
+            float x = (sl & 1) ? dv[0] : -dv[0];
+            float y = (sl & 2) ? dv[1] : -dv[1];
+            float z = (sl & 4) ? dv[2] : -dv[2];
+            score[c][sl] = x + y + z;
+        }
+    }
+    for (int sl = 0; sl < 8; ++sl) slot_kid[sl] = 0xffffffffu;
+    uint32_t done = 0;
+    for (uint32_t round = 0; round < nk; ++round) {
+        int bc = -1, bs = -1;
+        float best = 0.0f;
+        for (uint32_t c = 0; c < nk; ++c) {
+            if (done & (1u << c)) continue;
+            for (int sl = 0; sl < 8; ++sl) {
+                if (slot_kid[sl] != 0xffffffffu) continue;
+                if (bc < 0 || score[c][sl] > best) { bc = (int)c; bs = sl; best = score[c][sl]; }
+            }
+        }
+        done |= 1u << bc;
+        slot_kid[bs] = (uint32_t)bc;
+    }
+}
+
 __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_begin, uint32_t level_count,
                                 uint32_t level_end, uint32_t leaf_base, const Plan* __restrict__ plans,
                                 const uint32_t* __restrict__ scan_int, const uint32_t* __restrict__ scan_leaf,
@@ -274,6 +313,14 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= level_count) return;
     const Plan pl = plans[k];
+    float klo[8][3], khi[8][3];
+    for (uint32_t c = 0; c < pl.nk; ++c) {
+        const float *lo, *hi;
+        child_box(pl.kids[c], llo, lhi, blo, bhi, lo, hi);
+        for (int a = 0; a < 3; ++a) { klo[c][a] = lo[a]; khi[c][a] = hi[a]; }
+    }
+    uint32_t slot_kid[8];
+    assign_octant_slots(pl.nk, klo, khi, slot_kid);
     hx_bvh8_node node;
     uint8_t* raw = (uint8_t*)&node;
     for (int b = 0; b < (int)sizeof(node); ++b) raw[b] = 0;
@@ -281,11 +328,13 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
     node.prim_base = leaf_base + scan_leaf[k];
     float clo[8][3], chi[8][3];
     uint32_t rank = 0, off = 0;
-    for (uint32_t c = 0; c < pl.nk; ++c) {
-        uint32_t it = pl.kids[c];
-        const float *lo, *hi;
-        child_box(it, llo, lhi, blo, bhi, lo, hi);
-        for (int a = 0; a < 3; ++a) { clo[c][a] = lo[a]; chi[c][a] = hi[a]; }
+    for (uint32_t c = 0; c < 8; ++c) {
+        if (slot_kid[c] == 0xffffffffu) {
+            for (int a = 0; a < 3; ++a) { clo[c][a] = 0.0f; chi[c][a] = 0.0f; }
+            continue;
+        }
+        uint32_t it = pl.kids[slot_kid[c]];
+        for (int a = 0; a < 3; ++a) { clo[c][a] = klo[slot_kid[c]][a]; chi[c][a] = khi[slot_kid[c]][a]; }
         if (!(it & 0x80000000u) && count[it] > kLeafMax) {
             node.meta[c] = (uint8_t)(0x80u | rank);
             node.internal_mask |= (uint8_t)(1u << c);
@@ -299,12 +348,11 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
             off += cnt;
         }
     }
-    // quantise child boxes on the node grid (conservative, exact decode)
-    float plo[3], phi[3];
-    for (int a = 0; a < 3; ++a) {
-        plo[a] = clo[0][a];
-        phi[a] = chi[0][a];
-        for (uint32_t c = 1; c < pl.nk; ++c) {
+    // quantise the occupied slots on the node grid (conservative, exact decode)
+    float plo[3] = {INFINITY, INFINITY, INFINITY}, phi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t c = 0; c < 8; ++c) {
+        if (node.meta[c] == 0) continue;
+        for (int a = 0; a < 3; ++a) {
             plo[a] = clo[c][a] < plo[a] ? clo[c][a] : plo[a];
             phi[a] = chi[c][a] > phi[a] ? chi[c][a] : phi[a];
         }
@@ -318,7 +366,7 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
         float scale = pow2f(e);
         float inv = pow2f(-e > 126 ? 126 : (-e < -126 ? -126 : -e));
         for (uint32_t c = 0; c < 8; ++c) {
-            if (c >= pl.nk) continue;
+            if (node.meta[c] == 0) continue;
             float fl = floorf((clo[c][a] - plo[a]) * inv);
             int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
             while (ql > 0 && plo[a] + (float)ql * scale > clo[c][a]) --ql;

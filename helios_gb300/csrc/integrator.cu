@@ -38,7 +38,7 @@ struct Queues {
     float4* T;          // throughput + depth bits
     float4* L;          // radiance
     uint2* rng;
-    uint32_t* counters; // [0],[1] ray queues, [2] shadow queue
+    uint32_t* counters; // [0],[1] ray queues, [2] shadow queue, [4],[5] trace / shadow fetch cursors
     unsigned long long* stats;  // [0] extension rays, [1] shadow rays
     uint32_t* status;   // bit 0: traversal stack overflow
 };
@@ -84,21 +84,49 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
     }
 }
 
+// Persistent-warp closest-hit kernel: lanes pull rays from the queue with
+// warp-aggregated atomics (counter at fetch[0]) and refill as soon as their
+// ray finishes.
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(DevScene s, const float4* __restrict__ qo,
                                                          const float4* __restrict__ qd, const uint32_t* __restrict__ qp,
                                                          const uint32_t* __restrict__ count, float4* __restrict__ hits,
-                                                         unsigned long long* stats, uint32_t* status) {
-    uint32_t n = *count;
+                                                         unsigned long long* stats, uint32_t* status, uint32_t* fetch) {
+    const uint32_t n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)n);
+    const uint32_t lane = threadIdx.x & 31u;
     bool overflow = false;
     TraverseCount cnt;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 o = qo[i], d = qd[i];
-        bool any = (qp[i] & kAnyHitFlag) != 0;
-        HitRec h;
-        bool hit = trace_bvh8<COUNT>(s, v3(o), v3(d), o.w, d.w, any, false, h, overflow, &cnt);
-        hits[i] = hit ? make_float4(h.t, __uint_as_float(h.prim), h.u, h.v) : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+    uint2 stack[kStackSize];
+    TravState st;
+    uint32_t ray = kNoHit;  // kNoHit: lane needs a ray
+    bool done = false;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xffffffffu, ray == kNoHit && !done);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need & (1u << lane)) {
+                const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+                if (i < n) {
+                    ray = i;
+                    const float4 o = qo[i], d = qd[i];
+                    trav_init(st, s, v3(o), v3(d), o.w, d.w, (qp[i] & kAnyHitFlag) != 0);
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray != kNoHit) == 0) break;
+        if (ray != kNoHit) {
+            if (trav_step<false, COUNT>(st, stack, s, overflow, &cnt)) {
+                hits[ray] = st.best != kNoHit ? make_float4(st.best_t, __uint_as_float(st.best), st.bu, st.bv)
+                                              : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                ray = kNoHit;
+            }
+        }
     }
     if (COUNT) {
         atomicAdd(&stats[2], (unsigned long long)cnt.nodes);
@@ -202,20 +230,46 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, u
     }
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene s, Queues q) {
-    uint32_t n = q.counters[2];
+// Persistent-warp any-hit kernel for the shadow queue (fetch counter at
+// fetch[1]); an unoccluded entry adds its NEE contribution to its path.
+__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene s, Queues q, uint32_t* fetch) {
+    const uint32_t n = q.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+    const uint32_t lane = threadIdx.x & 31u;
     bool overflow = false;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 o = q.so[i], d = q.sd[i];
-        bool any = __float_as_uint(d.w) != 0u;
-        HitRec h;
-        bool occluded = trace_bvh8(s, v3(o), v3(d), 0.0001f, o.w, any, true, h, overflow);
-        if (!occluded) {
-            float4 c = q.sc[i];
-            uint32_t path = __float_as_uint(c.w);
-            float4 L = q.L[path];
-            q.L[path] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+    uint2 stack[kStackSize];
+    TravState st;
+    uint32_t ray = kNoHit;
+    bool done = false;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xffffffffu, ray == kNoHit && !done);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need & (1u << lane)) {
+                const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+                if (i < n) {
+                    ray = i;
+                    const float4 o = q.so[i], d = q.sd[i];
+                    trav_init(st, s, v3(o), v3(d), 0.0001f, o.w, __float_as_uint(d.w) != 0u);
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray != kNoHit) == 0) break;
+        if (ray != kNoHit) {
+            if (trav_step<true, false>(st, stack, s, overflow, nullptr)) {
+                if (st.best == kNoHit) {
+                    const float4 c = q.sc[ray];
+                    const uint32_t path = __float_as_uint(c.w);
+                    const float4 L = q.L[path];
+                    q.L[path] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+                }
+                ray = kNoHit;
+            }
         }
     }
     if (overflow) atomicOr(q.status, 1u);
@@ -392,7 +446,7 @@ struct hx_integrator {
     bool timing = false;
     bool counting = false;
     hx_stats stats{};
-    int grid_trace = 0, grid_shade = 0, grid_gen = 0;
+    int grid_trace = 0, grid_shadow = 0, grid_shade = 0, grid_gen = 0;
 };
 
 static void compute_tiles(hx_integrator* it) {  // path_integrator.cpp:312-336
@@ -466,6 +520,8 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     int per_sm = 0;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false>, kTraceThreads, 0));
     it->grid_trace = std::max(1, per_sm) * ctx->num_sms;
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow, kTraceThreads, 0));
+    it->grid_shadow = std::max(1, per_sm) * ctx->num_sms;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade, kShadeThreads, 0));
     it->grid_shade = std::max(1, per_sm) * ctx->num_sms;
     it->grid_gen = ctx->num_sms * 8;
@@ -538,12 +594,15 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
         int cur = b & 1;
         {
             StageTimer t(it, &it->stats.ms_trace);
+            HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 8, st));
             if (it->counting)
                 k_trace<true><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q.o[cur], it->q.d[cur], it->q.p[cur],
-                                                                       it->q.counters + cur, it->q.hit, it->q.stats, it->q.status);
+                                                                       it->q.counters + cur, it->q.hit, it->q.stats, it->q.status,
+                                                                       it->q.counters + 4);
             else
                 k_trace<false><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q.o[cur], it->q.d[cur], it->q.p[cur],
-                                                                        it->q.counters + cur, it->q.hit, it->q.stats, it->q.status);
+                                                                        it->q.counters + cur, it->q.hit, it->q.stats, it->q.status,
+                                                                        it->q.counters + 4);
             it->stats.trace_launches++;
             it->stats.kernel_launches++;
         }
@@ -556,7 +615,7 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
         }
         {
             StageTimer t(it, &it->stats.ms_shadow);
-            k_shadow<<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q);
+            k_shadow<<<it->grid_shadow, kTraceThreads, 0, st>>>(s, it->q, it->q.counters + 5);
             it->stats.kernel_launches++;
         }
     }
@@ -731,8 +790,9 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
     k_raygen<<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
+    HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
     k_trace<false><<<it->grid_trace, kTraceThreads, 0, st>>>(it->scene->d, it->q.o[0], it->q.d[0], it->q.p[0], it->q.counters,
-                                                             it->q.hit, it->q.stats, it->q.status);
+                                                             it->q.hit, it->q.stats, it->q.status, it->q.counters + 4);
     uint32_t n = W * H;
     k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(it->q.hit, n, it->hits_host_layout);
     HX_CUDA(cudaGetLastError());

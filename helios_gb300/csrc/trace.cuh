@@ -112,128 +112,230 @@ struct HitRec {
     uint32_t prim;
 };
 
-constexpr int kStackSize = 64;
+constexpr int kStackSize = 32;
 
-// Node child-box decode + slab test for all 8 slots; returns a hit mask
-// and the entry distances.
-HXD uint32_t node_intersect(const hx_bvh8_node& n, const RayPre& r, float tmin, float lim, float* tn_out) {
-    uint32_t mask = 0;
-    float sx = __uint_as_float((uint32_t)((int)n.exponent[0] + 127) << 23);
-    float sy = __uint_as_float((uint32_t)((int)n.exponent[1] + 127) << 23);
-    float sz = __uint_as_float((uint32_t)((int)n.exponent[2] + 127) << 23);
+HXD uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
+
+// Intersects the ray with the (up to) 8 children of a node held in five
+// 16-byte words and returns the hit mask in node-group form: bit
+// 24 + (slot ^ oct_inv) for a hit internal child, bits off..off+cnt-1 for the
+// triangles of a hit leaf.  Child planes are decoded exactly like the
+// builder checked them (L = origin + q * 2^e: exact product, one rounding),
+// then t = (L - o) * inv; the far distance is widened by 1 + 2^-21.
+HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, const uint4 w3, const uint4 w4,
+                                const RayPre& r, uint32_t oct_inv, float tmin, float lim) {
+    const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y), oz = __uint_as_float(w0.z);
+    const float sx = __uint_as_float((uint32_t)((int)(int8_t)(w0.w & 0xffu) + 127) << 23);
+    const float sy = __uint_as_float((uint32_t)((int)(int8_t)((w0.w >> 8) & 0xffu) + 127) << 23);
+    const float sz = __uint_as_float((uint32_t)((int)(int8_t)((w0.w >> 16) & 0xffu) + 127) << 23);
+    // near/far byte planes per axis chosen by the direction sign
+    const bool nx = r.ix < 0.0f, ny = r.iy < 0.0f, nz = r.iz < 0.0f;
+    const uint32_t lox0 = w2.x, lox1 = w2.y, loy0 = w2.z, loy1 = w2.w, loz0 = w3.x, loz1 = w3.y;
+    const uint32_t hix0 = w3.z, hix1 = w3.w, hiy0 = w4.x, hiy1 = w4.y, hiz0 = w4.z, hiz1 = w4.w;
+    const uint32_t nx0 = nx ? hix0 : lox0, nx1 = nx ? hix1 : lox1, fx0 = nx ? lox0 : hix0, fx1 = nx ? lox1 : hix1;
+    const uint32_t ny0 = ny ? hiy0 : loy0, ny1 = ny ? hiy1 : loy1, fy0 = ny ? loy0 : hiy0, fy1 = ny ? loy1 : hiy1;
+    const uint32_t nz0 = nz ? hiz0 : loz0, nz1 = nz ? hiz1 : loz1, fz0 = nz ? loz0 : hiz0, fz1 = nz ? loz1 : hiz1;
+    uint32_t hits = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-        if (n.meta[c] == 0) continue;
-        float lx = n.origin[0] + (float)n.qlo[0][c] * sx, hx = n.origin[0] + (float)n.qhi[0][c] * sx;
-        float ly = n.origin[1] + (float)n.qlo[1][c] * sy, hy = n.origin[1] + (float)n.qhi[1][c] * sy;
-        float lz = n.origin[2] + (float)n.qlo[2][c] * sz, hz = n.origin[2] + (float)n.qhi[2][c] * sz;
-        float t0x = (lx - r.o.x) * r.ix, t1x = (hx - r.o.x) * r.ix;
-        float t0y = (ly - r.o.y) * r.iy, t1y = (hy - r.o.y) * r.iy;
-        float t0z = (lz - r.o.z) * r.iz, t1z = (hz - r.o.z) * r.iz;
-        float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-        float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), lim));
-        if (tn <= tf * 1.000000477f) {
-            mask |= 1u << c;
-            tn_out[c] = tn;
+        const uint32_t m = byte_of(c < 4 ? w1.z : w1.w, c & 3);
+        const int k = c & 3;
+        const float Lnx = __fmaf_rn((float)byte_of(c < 4 ? nx0 : nx1, k), sx, ox);
+        const float Lfx = __fmaf_rn((float)byte_of(c < 4 ? fx0 : fx1, k), sx, ox);
+        const float Lny = __fmaf_rn((float)byte_of(c < 4 ? ny0 : ny1, k), sy, oy);
+        const float Lfy = __fmaf_rn((float)byte_of(c < 4 ? fy0 : fy1, k), sy, oy);
+        const float Lnz = __fmaf_rn((float)byte_of(c < 4 ? nz0 : nz1, k), sz, oz);
+        const float Lfz = __fmaf_rn((float)byte_of(c < 4 ? fz0 : fz1, k), sz, oz);
+        const float tnx = (Lnx - r.o.x) * r.ix, tfx = (Lfx - r.o.x) * r.ix;
+        const float tny = (Lny - r.o.y) * r.iy, tfy = (Lfy - r.o.y) * r.iy;
+        const float tnz = (Lnz - r.o.z) * r.iz, tfz = (Lfz - r.o.z) * r.iz;
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, lim));
+        const bool hit = m != 0u && tn <= tf * 1.000000477f;
+        if (hit) {
+            if (m & 0x80u) hits |= 1u << (24 + (c ^ oct_inv));
+            else hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
         }
     }
-    return mask;
+    return hits;
 }
 
-HXD void load_node(const hx_bvh8_node* nodes, uint32_t idx, hx_bvh8_node& n) {
-    const uint4* src = reinterpret_cast<const uint4*>(nodes + idx);
-    uint4* dst = reinterpret_cast<uint4*>(&n);
-#pragma unroll
-    for (int k = 0; k < 5; ++k) dst[k] = __ldg(src + k);
-}
-
-// Closest hit (shadow = false) or first accepted hit (shadow = true).
-// Sets overflow when the traversal stack overflowed or the node-visit cap
-// was hit (results then incomplete; the host reports HX_ERR_DEVICE).
 struct TraverseCount {
     uint32_t nodes = 0, tris = 0;
 };
 
+// Closest hit (shadow = false) or first accepted hit (shadow = true) over the
+// compressed 8-wide BVH.  Children are visited near-to-far by the octant
+// order of their slots (slot ^ ray octant), no per-ray sorting; the stack
+// holds node groups (first child index, remaining child bits | internal
+// mask).  Sets overflow when the stack or the node-visit cap overflowed or
+// an index was out of range (the host reports HX_ERR_DEVICE).
 template <bool COUNT = false>
 HXD bool trace_bvh8(const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool any_hit, bool shadow, HitRec& hit,
                     bool& overflow, TraverseCount* tc = nullptr) {
     if (s.num_nodes == 0) return false;
-    RayPre r = ray_prepare(o, d);
+    const RayPre r = ray_prepare(o, d);
+    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    const uint32_t oct_inv = 7u - oct;
     float best_t = tmax, bu = 0.0f, bv = 0.0f;
     uint32_t best = kNoHit;
-    uint32_t stack[kStackSize];
+    uint2 stack[kStackSize];
     int sp = 0;
-    uint32_t node_idx = 0;
-    // A valid traversal visits each node at most once; the cap turns a
-    // malformed tree into a reported error instead of an endless loop.
+    // the root is slot 0 of a virtual parent whose only child is internal
+    uint32_t g_base = 0, g_mask = (1u << (24 + oct_inv)) | 1u;
+    uint32_t t_base = 0, t_mask = 0;
     uint32_t visits_left = s.num_nodes + 16;
     for (;;) {
-        if (visits_left-- == 0 || node_idx >= s.num_nodes) {
-            overflow = true;
-            break;
-        }
-        hx_bvh8_node n;
-        load_node(s.nodes, node_idx, n);
-        if (COUNT) tc->nodes++;
-        float tn[8];
-        uint32_t mask = node_intersect(n, r, tmin, best_t * 1.000001f, tn);
-        // leaves first (slot order), then push internal children far-to-near
-        uint32_t leaf_mask = mask & ~(uint32_t)n.internal_mask;
-        while (leaf_mask) {
-            int c = __ffs(leaf_mask) - 1;
-            leaf_mask &= leaf_mask - 1;
-            uint32_t m = n.meta[c];
-            uint32_t cnt = m >> 5, off = m & 31u;
-            for (uint32_t q = 0; q < cnt; ++q) {
-                uint32_t k = n.prim_base + off + q;
-                if (k >= s.num_prims) {
-                    overflow = true;
-                    break;
-                }
-                if (COUNT) tc->tris++;
-                float4 a = __ldg(&s.tri[3 * (size_t)k]);
-                float4 b = __ldg(&s.tri[3 * (size_t)k + 1]);
-                float4 cc = __ldg(&s.tri[3 * (size_t)k + 2]);
-                float t, u, v;
-                if (!intersect_tri(r, v3(a), v3(b), v3(cc), tmin, best_t, t, u, v)) continue;
-                uint32_t prim = __float_as_uint(a.w);
-                if (!(t < best_t || (t == best_t && prim < best))) continue;
-                if (any_hit && (__float_as_uint(b.w) & HX_TRI_NONOPAQUE) && !alpha_pass(s, prim, u, v)) continue;
-                best_t = t; bu = u; bv = v; best = prim;
-                if (shadow) {
-                    hit.t = t; hit.u = u; hit.v = v; hit.prim = prim;
-                    return true;
-                }
-            }
-        }
-        uint32_t int_mask = mask & (uint32_t)n.internal_mask;
-        // order internal hits by entry distance (insertion sort, <= 8)
-        uint32_t ids[8];
-        float ds[8];
-        int nh = 0;
-        while (int_mask) {
-            int c = __ffs(int_mask) - 1;
-            int_mask &= int_mask - 1;
-            float dist = tn[c];
-            uint32_t child = n.child_base + (n.meta[c] & 7u);
-            int j = nh++;
-            while (j > 0 && ds[j - 1] < dist) { ds[j] = ds[j - 1]; ids[j] = ids[j - 1]; --j; }
-            ds[j] = dist;
-            ids[j] = child;
-        }
-        // ds is sorted descending: push far first, the nearest is visited next
-        if (nh > 0) {
-            for (int j = 0; j < nh - 1; ++j) {
-                if (sp < kStackSize) stack[sp++] = ids[j];
+        if (g_mask > 0x00ffffffu) {
+            const uint32_t bit = 31u - __clz(g_mask);
+            g_mask &= ~(1u << bit);
+            const uint32_t slot = (bit - 24u) ^ oct_inv;
+            const uint32_t child = g_base + __popc(g_mask & 0xffu & ((1u << slot) - 1u));
+            if (g_mask > 0x00ffffffu) {
+                if (sp < kStackSize) stack[sp++] = make_uint2(g_base, g_mask);
                 else overflow = true;
             }
-            node_idx = ids[nh - 1];
-            continue;
+            if (visits_left-- == 0 || child >= s.num_nodes) {
+                overflow = true;
+                break;
+            }
+            const uint4* np = reinterpret_cast<const uint4*>(s.nodes + child);
+            const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+            if (COUNT) tc->nodes++;
+            const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, r, oct_inv, tmin, best_t * 1.000001f);
+            g_base = w1.x;
+            g_mask = (hm & 0xff000000u) | (w0.w >> 24);
+            t_base = w1.y;
+            t_mask = hm & 0x00ffffffu;
+        } else {
+            t_base = g_base;  // a postponed triangle group popped from the stack
+            t_mask = g_mask;
+            g_mask = 0;
         }
-        if (sp == 0) break;
-        node_idx = stack[--sp];
+        while (t_mask) {
+            const uint32_t b = __ffs(t_mask) - 1u;
+            t_mask &= t_mask - 1u;
+            const uint32_t k = t_base + b;
+            if (k >= s.num_prims) {
+                overflow = true;
+                break;
+            }
+            if (COUNT) tc->tris++;
+            const float4 a = __ldg(&s.tri[3 * (size_t)k]);
+            const float4 bb = __ldg(&s.tri[3 * (size_t)k + 1]);
+            const float4 cc = __ldg(&s.tri[3 * (size_t)k + 2]);
+            float t, u, v;
+            if (!intersect_tri(r, v3(a), v3(bb), v3(cc), tmin, best_t, t, u, v)) continue;
+            const uint32_t prim = __float_as_uint(a.w);
+            if (!(t < best_t || (t == best_t && prim < best))) continue;
+            if (any_hit && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE) && !alpha_pass(s, prim, u, v)) continue;
+            best_t = t; bu = u; bv = v; best = prim;
+            if (shadow) {
+                hit.t = t; hit.u = u; hit.v = v; hit.prim = prim;
+                return true;
+            }
+        }
+        if (g_mask <= 0x00ffffffu) {
+            if (sp == 0) break;
+            const uint2 e = stack[--sp];
+            g_base = e.x;
+            g_mask = e.y;
+        }
     }
     if (best == kNoHit) return false;
     hit.t = best_t; hit.u = bu; hit.v = bv; hit.prim = best;
     return true;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent-warp traversal: per-lane state machine.  One call of step()
+// intersects at most one node and then tests the triangles it exposed; a
+// lane whose ray finished refills itself with the next ray of the queue, so
+// long rays never hold their warp-mates idle.
+// ---------------------------------------------------------------------------
+struct TravState {
+    RayPre r;
+    uint32_t oct_inv;
+    float tmin, best_t, bu, bv;
+    uint32_t best;
+    uint32_t g_base, g_mask, t_base, t_mask;
+    int sp;
+    uint32_t visits_left;
+    bool any_hit;
+};
+
+HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool any_hit) {
+    st.r = ray_prepare(o, d);
+    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    st.oct_inv = 7u - oct;
+    st.tmin = tmin;
+    st.best_t = tmax;
+    st.bu = st.bv = 0.0f;
+    st.best = kNoHit;
+    st.g_base = 0;
+    st.g_mask = s.num_nodes ? ((1u << (24 + st.oct_inv)) | 1u) : 0u;
+    st.t_base = 0;
+    st.t_mask = 0;
+    st.sp = 0;
+    st.visits_left = s.num_nodes + 16;
+    st.any_hit = any_hit;
+}
+
+// Returns true when the ray is finished (traversal exhausted, or the first
+// accepted hit of a shadow ray).
+template <bool SHADOW, bool COUNT>
+HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflow, TraverseCount* tc) {
+    if (st.g_mask > 0x00ffffffu) {
+        const uint32_t bit = 31u - __clz(st.g_mask);
+        st.g_mask &= ~(1u << bit);
+        const uint32_t slot = (bit - 24u) ^ st.oct_inv;
+        const uint32_t child = st.g_base + __popc(st.g_mask & 0xffu & ((1u << slot) - 1u));
+        if (st.g_mask > 0x00ffffffu) {
+            if (st.sp < kStackSize) stack[st.sp++] = make_uint2(st.g_base, st.g_mask);
+            else overflow = true;
+        }
+        if (st.visits_left-- == 0 || child >= s.num_nodes) {
+            overflow = true;
+            return true;
+        }
+        const uint4* np = reinterpret_cast<const uint4*>(s.nodes + child);
+        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+        if (COUNT) tc->nodes++;
+        const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.oct_inv, st.tmin, st.best_t * 1.000001f);
+        st.g_base = w1.x;
+        st.g_mask = (hm & 0xff000000u) | (w0.w >> 24);
+        st.t_base = w1.y;
+        st.t_mask = hm & 0x00ffffffu;
+    } else {
+        st.t_base = st.g_base;
+        st.t_mask = st.g_mask;
+        st.g_mask = 0;
+    }
+    while (st.t_mask) {
+        const uint32_t b = __ffs(st.t_mask) - 1u;
+        st.t_mask &= st.t_mask - 1u;
+        const uint32_t k = st.t_base + b;
+        if (k >= s.num_prims) {
+            overflow = true;
+            return true;
+        }
+        if (COUNT) tc->tris++;
+        const float4 a = __ldg(&s.tri[3 * (size_t)k]);
+        const float4 bb = __ldg(&s.tri[3 * (size_t)k + 1]);
+        const float4 cc = __ldg(&s.tri[3 * (size_t)k + 2]);
+        float t, u, v;
+        if (!intersect_tri(st.r, v3(a), v3(bb), v3(cc), st.tmin, st.best_t, t, u, v)) continue;
+        const uint32_t prim = __float_as_uint(a.w);
+        if (!(t < st.best_t || (t == st.best_t && prim < st.best))) continue;
+        if (st.any_hit && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE) && !alpha_pass(s, prim, u, v)) continue;
+        st.best_t = t; st.bu = u; st.bv = v; st.best = prim;
+        if (SHADOW) return true;
+    }
+    if (st.g_mask <= 0x00ffffffu) {
+        if (st.sp == 0) return true;
+        const uint2 e = stack[--st.sp];
+        st.g_base = e.x;
+        st.g_mask = e.y;
+    }
+    return false;
 }

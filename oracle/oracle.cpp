@@ -74,8 +74,7 @@ struct Scene {
     Bvh bvh;
     uint32_t env_kind = HX_ENV_NONE, env_w = 0, env_h = 0;
     std::vector<float> env;  // rgb per texel, FP16-rounded
-    std::vector<double> env_marg, env_cond;
-    double env_total = 0;
+    std::vector<float> env_margf, env_condf;
     float sun[3] = {0, 1, 0};
     float coeffs[40] = {0};
 };
@@ -108,24 +107,67 @@ static V3<double> latlong_dir(double u, double v) {
     return V3<double>(st * std::sin(phi), std::cos(theta), -st * std::cos(phi));
 }
 
-static float env_luminance(const float* e) { return 0.2126f * e[0] + 0.7152f * e[1] + 0.0722f * e[2]; }
 
-// Importance-sampling table: weight(i,j) = (lum + floor) * sin(theta_j).
+// Importance-sampling table (the device construction, restated in FP32
+// with the same summation order): weight(i,j) = (lum + floor) * sin(theta_j),
+// floor = 1e-3 * mean luminance; rows prefix-summed in 256 contiguous chunks,
+// each row normalised to 1, then a normalised marginal over the row totals.
+static float texel_lum(const float* e) { return 0.2126f * e[0] + 0.7152f * e[1] + 0.0722f * e[2]; }
+
 static void build_env_cdf(Scene& s) {
-    uint32_t w = s.env_w, h = s.env_h;
-    double mean = 0;
-    for (size_t i = 0; i < (size_t)w * h; ++i) mean += env_luminance(&s.env[i * 3]);
-    mean /= (double)w * h;
-    double floor_w = 1e-3 * mean + 1e-12;
-    s.env_cond.assign((size_t)h * (w + 1), 0.0);
-    s.env_marg.assign(h + 1, 0.0);
+    const uint32_t w = s.env_w, h = s.env_h, T = 256;
+    std::vector<float> rowlum(h), rowsum(h);
     for (uint32_t j = 0; j < h; ++j) {
-        double st = std::sin(3.14159265358979323846 * (j + 0.5) / h);
-        double* row = &s.env_cond[(size_t)j * (w + 1)];
-        for (uint32_t i = 0; i < w; ++i) row[i + 1] = row[i] + ((double)env_luminance(&s.env[((size_t)j * w + i) * 3]) + floor_w) * st;
-        s.env_marg[j + 1] = s.env_marg[j] + row[w];
+        float part[256];
+        for (uint32_t t = 0; t < T; ++t) {
+            float acc = 0.0f;
+            for (uint32_t i = t; i < w; i += T) acc += texel_lum(&s.env[((size_t)j * w + i) * 3]);
+            part[t] = acc;
+        }
+        for (uint32_t o = T / 2; o > 0; o >>= 1)
+            for (uint32_t t = 0; t < o; ++t) part[t] += part[t + o];
+        rowlum[j] = part[0];
     }
-    s.env_total = s.env_marg[h];
+    float tot = 0.0f;
+    for (uint32_t j = 0; j < h; ++j) tot += rowlum[j];
+    const float floor_w = 1e-3f * tot / ((float)w * (float)h) + 1e-12f;
+    const float kPiF32 = 3.14159265358979323846f;
+    s.env_condf.assign((size_t)h * (w + 1), 0.0f);
+    s.env_margf.assign(h + 1, 0.0f);
+    const uint32_t chunk = (w + T - 1) / T;
+    for (uint32_t j = 0; j < h; ++j) {
+        float st = std::sin(kPiF32 * ((float)j + 0.5f) / (float)h);
+        float part[256];
+        for (uint32_t t = 0; t < T; ++t) {
+            uint32_t i0 = t * chunk, i1 = std::min(w, i0 + chunk);
+            float local = 0.0f;
+            for (uint32_t i = i0; i < i1; ++i) local += (texel_lum(&s.env[((size_t)j * w + i) * 3]) + floor_w) * st;
+            part[t] = local;
+        }
+        float run = 0.0f;
+        for (uint32_t t = 0; t < T; ++t) { float x = part[t]; part[t] = run; run += x; }
+        rowsum[j] = run;
+        float* row = &s.env_condf[(size_t)j * (w + 1)];
+        row[0] = 0.0f;
+        for (uint32_t t = 0; t < T; ++t) {
+            uint32_t i0 = t * chunk, i1 = std::min(w, i0 + chunk);
+            float r = part[t];
+            for (uint32_t i = i0; i < i1; ++i) {
+                r += (texel_lum(&s.env[((size_t)j * w + i) * 3]) + floor_w) * st;
+                row[i + 1] = run > 0.0f ? r / run : (float)(i + 1) / (float)w;
+            }
+        }
+        row[w] = 1.0f;
+    }
+    float mt = 0.0f;
+    for (uint32_t j = 0; j < h; ++j) mt += rowsum[j];
+    float run = 0.0f;
+    s.env_margf[0] = 0.0f;
+    for (uint32_t j = 0; j < h; ++j) {
+        run += rowsum[j];
+        s.env_margf[j + 1] = mt > 0.0f ? run / mt : (float)(j + 1) / (float)h;
+    }
+    s.env_margf[h] = 1.0f;
 }
 
 template <typename R> static V3<R> env_lookup(const Scene& s, V3<R> d) {
@@ -153,29 +195,39 @@ template <typename R> static V3<R> env_lookup(const Scene& s, V3<R> d) {
     return out;
 }
 
-// Samples a direction from the lat-long CDF with two uniforms; returns the
-// solid-angle pdf.
-template <typename R> static V3<R> env_sample(const Scene& s, R r0, R r1, R& pdf) {
-    uint32_t w = s.env_w, h = s.env_h;
-    double target = (double)r1 * s.env_total;
-    uint32_t j = (uint32_t)(std::upper_bound(s.env_marg.begin() + 1, s.env_marg.end(), target) - (s.env_marg.begin() + 1));
-    if (j >= h) j = h - 1;
-    const double* row = &s.env_cond[(size_t)j * (w + 1)];
-    double rt = (double)r0 * row[w];
-    uint32_t i = (uint32_t)(std::upper_bound(row + 1, row + w + 1, rt) - (row + 1));
-    if (i >= w) i = w - 1;
-    double fu = row[i + 1] > row[i] ? (rt - row[i]) / (row[i + 1] - row[i]) : 0.5;
-    double rm = s.env_marg[j + 1] - s.env_marg[j];
-    double fv = rm > 0 ? (target - s.env_marg[j]) / rm : 0.5;
-    fu = std::min(std::max(fu, 0.0), 1.0);
-    fv = std::min(std::max(fv, 0.0), 1.0);
-    double u = (i + fu) / w, v = (j + fv) / h;
-    V3<double> d = latlong_dir(u, v);
-    double theta = 3.14159265358979323846 * v;
-    double st = std::sin(theta);
-    double p_img = (row[i + 1] - row[i]) / s.env_total * (double)w * h;  // density over [0,1]^2
-    pdf = st > 0 ? R(p_img / (2.0 * 3.14159265358979323846 * 3.14159265358979323846 * st)) : R(0);
-    return V3<R>(R(d.x), R(d.y), R(d.z));
+// Samples a direction from the lat-long CDF with two uniforms (binary
+// searches over the normalised FP32 tables, continuous within the texel);
+// returns the solid-angle pdf.
+static int upper_bound_f(const float* a, int lo, int hi, float x) {
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] > x) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+template <typename R> static V3<R> env_sample(const Scene& s, float r0, float r1, R& pdf) {
+    int W = (int)s.env_w, H = (int)s.env_h;
+    int j = upper_bound_f(s.env_margf.data(), 1, H + 1, r1) - 1;
+    j = j < 0 ? 0 : (j >= H ? H - 1 : j);
+    const float* row = &s.env_condf[(size_t)j * (W + 1)];
+    int i = upper_bound_f(row, 1, W + 1, r0) - 1;
+    i = i < 0 ? 0 : (i >= W ? W - 1 : i);
+    float m0 = s.env_margf[j], m1 = s.env_margf[j + 1], c0 = row[i], c1 = row[i + 1];
+    R fv = m1 > m0 ? (R(r1) - R(m0)) / (R(m1) - R(m0)) : R(0.5);
+    R fu = c1 > c0 ? (R(r0) - R(c0)) / (R(c1) - R(c0)) : R(0.5);
+    fv = gclamp(fv, R(0), R(1));
+    fu = gclamp(fu, R(0), R(1));
+    R u = (R(i) + fu) / R(W), v = (R(j) + fv) / R(H);
+    const R pi = R(3.14159265358979323846);
+    R phi = R(2) * pi * (u - R(0.5));
+    R theta = pi * v;
+    R st = std::sin(theta);
+    V3<R> d(st * std::sin(phi), std::cos(theta), -st * std::cos(phi));
+    R pmf = (R(c1) - R(c0)) * (R(m1) - R(m0));
+    pdf = st > R(0) ? pmf * R(W) * R(H) / (R(2) * pi * pi * st) : R(0);
+    return d;
 }
 
 // ---------------------------------------------------------------------------
@@ -285,12 +337,12 @@ static float half_area(const float* lo, const float* hi) {
     return dx * dy + dy * dz + dz * dx;
 }
 
-static void quantise_node(hx_bvh8_node& node, int nslots, const float (*clo)[3], const float (*chi)[3]) {
-    float plo[3], phi[3];
-    for (int a = 0; a < 3; ++a) {
-        plo[a] = clo[0][a];
-        phi[a] = chi[0][a];
-        for (int k = 1; k < nslots; ++k) {
+// Quantises the occupied slots (meta != 0) of a node on its own grid.
+static void quantise_node(hx_bvh8_node& node, const float (*clo)[3], const float (*chi)[3]) {
+    float plo[3] = {INFINITY, INFINITY, INFINITY}, phi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < 8; ++k) {
+        if (node.meta[k] == 0) continue;
+        for (int a = 0; a < 3; ++a) {
             plo[a] = clo[k][a] < plo[a] ? clo[k][a] : plo[a];
             phi[a] = chi[k][a] > phi[a] ? chi[k][a] : phi[a];
         }
@@ -304,7 +356,7 @@ static void quantise_node(hx_bvh8_node& node, int nslots, const float (*clo)[3],
         float scale = pow2f(e);
         float inv = pow2f(-e > 126 ? 126 : (-e < -126 ? -126 : -e));
         for (int k = 0; k < 8; ++k) {
-            if (k >= nslots) { node.qlo[a][k] = 0; node.qhi[a][k] = 0; continue; }
+            if (node.meta[k] == 0) { node.qlo[a][k] = 0; node.qhi[a][k] = 0; continue; }
             float fl = std::floor((clo[k][a] - plo[a]) * inv);
             int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
             while (ql > 0 && plo[a] + (float)ql * scale > clo[k][a]) --ql;
@@ -314,6 +366,45 @@ static void quantise_node(hx_bvh8_node& node, int nslots, const float (*clo)[3],
             node.qlo[a][k] = (uint8_t)ql;
             node.qhi[a][k] = (uint8_t)qh;
         }
+    }
+}
+
+// Octant slot assignment of up to 8 children (boxes klo/khi): the score of
+// child i in slot s is the sum over axes of +-(c_i - c_node), + where bit k
+// of s is set; greedy over (child, slot) pairs by decreasing score, ties to
+// the lower child position then the lower slot.  slot_kid[s] = child or ~0.
+static void assign_octant_slots(int nk, const float (*klo)[3], const float (*khi)[3], uint32_t slot_kid[8]) {
+    float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < nk; ++c)
+        for (int a = 0; a < 3; ++a) {
+            nlo[a] = klo[c][a] < nlo[a] ? klo[c][a] : nlo[a];
+            nhi[a] = khi[c][a] > nhi[a] ? khi[c][a] : nhi[a];
+        }
+    float score[8][8];
+    for (int c = 0; c < nk; ++c) {
+        float dv[3];
+        for (int a = 0; a < 3; ++a) dv[a] = (klo[c][a] + khi[c][a]) * 0.5f - (nlo[a] + nhi[a]) * 0.5f;
+        for (int sl = 0; sl < 8; ++sl) {
+            float x = (sl & 1) ? dv[0] : -dv[0];
+            float y = (sl & 2) ? dv[1] : -dv[1];
+            float z = (sl & 4) ? dv[2] : -dv[2];
+            score[c][sl] = x + y + z;
+        }
+    }
+    for (int sl = 0; sl < 8; ++sl) slot_kid[sl] = 0xffffffffu;
+    bool kid_done[8] = {false, false, false, false, false, false, false, false};
+    for (int round = 0; round < nk; ++round) {
+        int bc = -1, bs = -1;
+        float best = 0.0f;
+        for (int c = 0; c < nk; ++c) {
+            if (kid_done[c]) continue;
+            for (int sl = 0; sl < 8; ++sl) {
+                if (slot_kid[sl] != 0xffffffffu) continue;
+                if (bc < 0 || score[c][sl] > best) { bc = c; bs = sl; best = score[c][sl]; }
+            }
+        }
+        kid_done[bc] = true;
+        slot_kid[bs] = (uint32_t)bc;
     }
 }
 
@@ -448,17 +539,30 @@ static void build_bvh(Scene& s) {
                 ++nk;
             }
         }
+        // octant slot assignment: slot bit k set = child centre on the
+        // positive side of the node centre along axis k; greedy on the
+        // alignment score (ties: lower child position, then lower slot)
+        float klo[8][3], khi[8][3];
+        for (int c = 0; c < nk; ++c) {
+            const float *lo, *hi;
+            child_box(kids[c], lo, hi);
+            for (int a = 0; a < 3; ++a) { klo[c][a] = lo[a]; khi[c][a] = hi[a]; }
+        }
+        uint32_t slot_kid[8];
+        assign_octant_slots(nk, klo, khi, slot_kid);
         hx_bvh8_node node;
         std::memset(&node, 0, sizeof(node));
         node.child_base = (uint32_t)queue.size();
         node.prim_base = (uint32_t)b.leaf_prims.size();
         float clo[8][3], chi[8][3];
         int rank = 0;
-        for (int c = 0; c < nk; ++c) {
-            uint32_t it = kids[c];
-            const float *lo, *hi;
-            child_box(it, lo, hi);
-            for (int a = 0; a < 3; ++a) { clo[c][a] = lo[a]; chi[c][a] = hi[a]; }
+        for (int c = 0; c < 8; ++c) {
+            if (slot_kid[c] == 0xffffffffu) {
+                for (int a = 0; a < 3; ++a) { clo[c][a] = 0.0f; chi[c][a] = 0.0f; }
+                continue;
+            }
+            uint32_t it = kids[slot_kid[c]];
+            for (int a = 0; a < 3; ++a) { clo[c][a] = klo[slot_kid[c]][a]; chi[c][a] = khi[slot_kid[c]][a]; }
             if (!(it & 0x80000000u) && b.count[it] > 3) {
                 node.meta[c] = (uint8_t)(0x80u | rank);
                 node.internal_mask |= (uint8_t)(1u << c);
@@ -471,7 +575,7 @@ static void build_bvh(Scene& s) {
                 for (uint32_t q = 0; q < cnt; ++q) b.leaf_prims.push_back(b.sorted[f + q]);
             }
         }
-        quantise_node(node, nk, clo, chi);
+        quantise_node(node, clo, chi);
         b.nodes.push_back(node);
     }
 }
@@ -774,7 +878,7 @@ static V3<R> sample_light(const Scene& s, const Params& P, const Surface<R>& p, 
     } else if (type == HX_LIGHT_ENVIRONMENT) {
         R r0 = next_float(rng), r1 = next_float(rng);
         if (P.pol.env_sampling == HX_ENV_SAMPLE_IMPORTANCE && s.env_kind != HX_ENV_NONE) {
-            Wi = env_sample<R>(s, r0, r1, pdf);
+            Wi = env_sample<R>(s, (float)r0, (float)r1, pdf);
             Li = env_lookup(s, Wi);
             if (!(pdf > R(0))) { Li = V3<R>(R(0)); trace_it = false; }
         } else {
@@ -1084,7 +1188,8 @@ void oracle_sample_radiance(void* h, const hx_integrator_desc* d, const hx_frame
 }
 
 // Progressive accumulation of frames [0, num_frames) for the listed pixels
-// (NULL = all, in 16x16 tiles), with the policy's accumulation rule
+// (NULL = all, in 16x16 tiles; listed pixels in chunks sized to keep every
+// thread busy), with the policy's accumulation rule
 // (running mean of path_trace_rgen.glsl:217-248, or Kahan sum / n).
 // out_rgb holds 3 doubles per listed pixel.  threads <= 0: all cores.
 void oracle_render(void* h, const hx_integrator_desc* d, const hx_frame_desc* f, uint32_t num_frames, uint32_t precision,
@@ -1098,12 +1203,13 @@ void oracle_render(void* h, const hx_integrator_desc* d, const hx_frame_desc* f,
     auto t0 = std::chrono::steady_clock::now();
     // work items: 16x16 pixel tiles for full frames, chunks of 256 listed pixels otherwise
     uint32_t tiles_x = (d->width + 15) / 16, tiles_y = (d->height + 15) / 16;
-    long items = pixels ? (long)((n + 255) / 256) : (long)tiles_x * tiles_y;
+    uint32_t chunk = pixels ? std::max<uint32_t>(1, std::min<uint32_t>(256, n / (4u * (uint32_t)nt))) : 0;
+    long items = pixels ? (long)((n + chunk - 1) / chunk) : (long)tiles_x * tiles_y;
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nt) reduction(+ : tp, te, ts)
     for (long it = 0; it < items; ++it) {
         std::vector<uint32_t> list;
         if (pixels) {
-            for (uint32_t k = (uint32_t)it * 256; k < n && k < (uint32_t)it * 256 + 256; ++k) list.push_back(k);
+            for (uint32_t k = (uint32_t)it * chunk; k < n && k < (uint32_t)it * chunk + chunk; ++k) list.push_back(k);
         } else {
             uint32_t tx = (uint32_t)(it % tiles_x), ty = (uint32_t)(it / tiles_x);
             for (uint32_t y = ty * 16; y < ty * 16 + 16 && y < d->height; ++y)

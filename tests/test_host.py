@@ -80,3 +80,13 @@ def test_hosek_coefficients_match_reference_golden():
         k = hx.hosek_wilkie_coefficients(case["sun_direction"], case["turbidity"], 1.15)
         ref = np.array(case["coeffs"], np.float32).reshape(10, 3)
         assert np.allclose(k, ref, rtol=2e-5, atol=1e-7), case
+
+
+def test_cpp_driver_builds_and_links():
+    """The C++ engine surface (include/helios_gb300.hpp) compiles and links
+    against the C-ABI; without arguments the driver prints its usage."""
+    import subprocess
+    from helios_gb300 import build as b
+    exe = b.build_driver()
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
