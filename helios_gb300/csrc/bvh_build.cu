@@ -199,13 +199,26 @@ __global__ void k_fit(uint32_t n, const uint32_t* __restrict__ children, const i
     }
 }
 
-__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(e + 127) << 23); }
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(e < -126 ? 1 : e + 127) << 23); }
 __device__ __forceinline__ int ceil_log2f(float x) {
     uint32_t b = __float_as_uint(x);
     int ex = (int)((b >> 23) & 0xff);
     if (ex == 0) return -126;
     int e = ex - 127 + ((b & 0x7fffff) != 0 ? 1 : 0);
     return e < -126 ? -126 : e;
+}
+// Grid exponent of one node axis (see the oracle's grid_exponent): 254
+// steps cover [lo, hi] (the snapped origin adds at most one) and 2^e >= 2 ulp(max |coordinate|), so every decoded
+// plane is exactly representable.
+__device__ __forceinline__ int grid_exponent(float lo, float hi) {
+    float ext = hi - lo;
+    int e = ext > 0.0f ? ceil_log2f(ext / 254.0f) : -126;
+    float m = fabsf(lo) > fabsf(hi) ? fabsf(lo) : fabsf(hi);
+    uint32_t mb = __float_as_uint(m);
+    int mexp = (int)((mb >> 23) & 0xff);
+    int e_min = mexp == 0 ? -126 : mexp - 127 - 23 + 1;
+    e = e > e_min ? e : e_min;
+    return e < -126 ? -126 : (e > 119 ? 119 : e);
 }
 __device__ __forceinline__ float half_area(const float* lo, const float* hi) {
     float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
@@ -358,21 +371,25 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
         }
     }
     for (int a = 0; a < 3; ++a) {
-        node.origin[a] = plo[a];
-        float ext = phi[a] - plo[a];
-        int e = ext > 0.0f ? ceil_log2f(ext / 255.0f) : -126;
-        while (e < 127 && plo[a] + 255.0f * pow2f(e) < phi[a]) ++e;
-        node.exponent[a] = (int8_t)e;
+        int e = grid_exponent(plo[a], phi[a]);
         float scale = pow2f(e);
-        float inv = pow2f(-e > 126 ? 126 : (-e < -126 ? -126 : -e));
+        float origin = floorf(plo[a] * pow2f(-e)) * scale;
+        while (e < 119 && origin + 255.0f * scale < phi[a]) {
+            ++e;
+            scale = pow2f(e);
+            origin = floorf(plo[a] * pow2f(-e)) * scale;
+        }
+        node.origin[a] = origin;
+        node.exponent[a] = (int8_t)e;
+        float inv = pow2f(-e);
         for (uint32_t c = 0; c < 8; ++c) {
             if (node.meta[c] == 0) continue;
-            float fl = floorf((clo[c][a] - plo[a]) * inv);
+            float fl = floorf((clo[c][a] - origin) * inv);
             int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
-            while (ql > 0 && plo[a] + (float)ql * scale > clo[c][a]) --ql;
-            float fh = ceilf((chi[c][a] - plo[a]) * inv);
+            while (ql > 0 && origin + (float)ql * scale > clo[c][a]) --ql;
+            float fh = ceilf((chi[c][a] - origin) * inv);
             int qh = fh < 0.0f ? 0 : (fh > 255.0f ? 255 : (int)fh);
-            while (qh < 255 && plo[a] + (float)qh * scale < chi[c][a]) ++qh;
+            while (qh < 255 && origin + (float)qh * scale < chi[c][a]) ++qh;
             node.qlo[a][c] = (uint8_t)ql;
             node.qhi[a][c] = (uint8_t)qh;
         }

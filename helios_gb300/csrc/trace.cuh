@@ -116,18 +116,26 @@ constexpr int kStackSize = 32;
 
 HXD uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
+// 2^23 + q for byte k of w, built with one byte permute (bits 0x4B000000 | q:
+// the byte fills the low mantissa byte of 2^23).
+HXD float byte_biased(uint32_t w, int k) { return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k)); }
+
 // Intersects the ray with the (up to) 8 children of a node held in five
 // 16-byte words and returns the hit mask in node-group form: bit
 // 24 + (slot ^ oct_inv) for a hit internal child, bits off..off+cnt-1 for the
-// triangles of a hit leaf.  Child planes are decoded exactly like the
-// builder checked them (L = origin + q * 2^e: exact product, one rounding),
-// then t = (L - o) * inv; the far distance is widened by 1 + 2^-21.
+// triangles of a hit leaf.  Planes decode exactly (the builder snaps each
+// node grid so origin + q 2^e is representable and |origin| < 2^23 2^e):
+// L = (2^23 + q) * 2^e + (origin - 2^23 2^e), one rounding-free FMA; then
+// t = (L - o) * inv, with the far planes multiplied by the slack-widened
+// reciprocal (1 + 2^-21).
 HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, const uint4 w3, const uint4 w4,
-                                const RayPre& r, uint32_t oct_inv, float tmin, float lim) {
-    const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y), oz = __uint_as_float(w0.z);
-    const float sx = __uint_as_float((uint32_t)((int)(int8_t)(w0.w & 0xffu) + 127) << 23);
-    const float sy = __uint_as_float((uint32_t)((int)(int8_t)((w0.w >> 8) & 0xffu) + 127) << 23);
-    const float sz = __uint_as_float((uint32_t)((int)(int8_t)((w0.w >> 16) & 0xffu) + 127) << 23);
+                                const RayPre& r, float fix, float fiy, float fiz, uint32_t oct_inv, float tmin,
+                                float lim) {
+    const int ex = (int)(int8_t)(w0.w & 0xffu), ey = (int)(int8_t)((w0.w >> 8) & 0xffu), ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
+    const float Sx = __uint_as_float((uint32_t)(ex + 127) << 23), Sy = __uint_as_float((uint32_t)(ey + 127) << 23),
+                Sz = __uint_as_float((uint32_t)(ez + 127) << 23);
+    const float Ox = __fmaf_rn(-8388608.0f, Sx, __uint_as_float(w0.x)), Oy = __fmaf_rn(-8388608.0f, Sy, __uint_as_float(w0.y)),
+                Oz = __fmaf_rn(-8388608.0f, Sz, __uint_as_float(w0.z));
     // near/far byte planes per axis chosen by the direction sign
     const bool nx = r.ix < 0.0f, ny = r.iy < 0.0f, nz = r.iz < 0.0f;
     const uint32_t lox0 = w2.x, lox1 = w2.y, loy0 = w2.z, loy1 = w2.w, loz0 = w3.x, loz1 = w3.y;
@@ -140,19 +148,18 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
     for (int c = 0; c < 8; ++c) {
         const uint32_t m = byte_of(c < 4 ? w1.z : w1.w, c & 3);
         const int k = c & 3;
-        const float Lnx = __fmaf_rn((float)byte_of(c < 4 ? nx0 : nx1, k), sx, ox);
-        const float Lfx = __fmaf_rn((float)byte_of(c < 4 ? fx0 : fx1, k), sx, ox);
-        const float Lny = __fmaf_rn((float)byte_of(c < 4 ? ny0 : ny1, k), sy, oy);
-        const float Lfy = __fmaf_rn((float)byte_of(c < 4 ? fy0 : fy1, k), sy, oy);
-        const float Lnz = __fmaf_rn((float)byte_of(c < 4 ? nz0 : nz1, k), sz, oz);
-        const float Lfz = __fmaf_rn((float)byte_of(c < 4 ? fz0 : fz1, k), sz, oz);
-        const float tnx = (Lnx - r.o.x) * r.ix, tfx = (Lfx - r.o.x) * r.ix;
-        const float tny = (Lny - r.o.y) * r.iy, tfy = (Lfy - r.o.y) * r.iy;
-        const float tnz = (Lnz - r.o.z) * r.iz, tfz = (Lfz - r.o.z) * r.iz;
+        const float Lnx = __fmaf_rn(byte_biased(c < 4 ? nx0 : nx1, k), Sx, Ox);
+        const float Lfx = __fmaf_rn(byte_biased(c < 4 ? fx0 : fx1, k), Sx, Ox);
+        const float Lny = __fmaf_rn(byte_biased(c < 4 ? ny0 : ny1, k), Sy, Oy);
+        const float Lfy = __fmaf_rn(byte_biased(c < 4 ? fy0 : fy1, k), Sy, Oy);
+        const float Lnz = __fmaf_rn(byte_biased(c < 4 ? nz0 : nz1, k), Sz, Oz);
+        const float Lfz = __fmaf_rn(byte_biased(c < 4 ? fz0 : fz1, k), Sz, Oz);
+        const float tnx = (Lnx - r.o.x) * r.ix, tfx = (Lfx - r.o.x) * fix;
+        const float tny = (Lny - r.o.y) * r.iy, tfy = (Lfy - r.o.y) * fiy;
+        const float tnz = (Lnz - r.o.z) * r.iz, tfz = (Lfz - r.o.z) * fiz;
         const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
         const float tf = fminf(fminf(tfx, tfy), fminf(tfz, lim));
-        const bool hit = m != 0u && tn <= tf * 1.000000477f;
-        if (hit) {
+        if (m != 0u && tn <= tf) {
             if (m & 0x80u) hits |= 1u << (24 + (c ^ oct_inv));
             else hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
         }
@@ -202,7 +209,8 @@ HXD bool trace_bvh8(const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool 
             const uint4* np = reinterpret_cast<const uint4*>(s.nodes + child);
             const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
             if (COUNT) tc->nodes++;
-            const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, r, oct_inv, tmin, best_t * 1.000001f);
+            const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, r, r.ix * 1.000000477f, r.iy * 1.000000477f,
+                                                   r.iz * 1.000000477f, oct_inv, tmin, best_t * 1.000001f);
             g_base = w1.x;
             g_mask = (hm & 0xff000000u) | (w0.w >> 24);
             t_base = w1.y;
@@ -255,6 +263,7 @@ HXD bool trace_bvh8(const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool 
 // ---------------------------------------------------------------------------
 struct TravState {
     RayPre r;
+    float fix, fiy, fiz;  // far-plane reciprocals widened by 1 + 2^-21
     uint32_t oct_inv;
     float tmin, best_t, bu, bv;
     uint32_t best;
@@ -266,6 +275,9 @@ struct TravState {
 
 HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool any_hit) {
     st.r = ray_prepare(o, d);
+    st.fix = st.r.ix * 1.000000477f;
+    st.fiy = st.r.iy * 1.000000477f;
+    st.fiz = st.r.iz * 1.000000477f;
     const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
     st.oct_inv = 7u - oct;
     st.tmin = tmin;
@@ -301,7 +313,8 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         const uint4* np = reinterpret_cast<const uint4*>(s.nodes + child);
         const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
         if (COUNT) tc->nodes++;
-        const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.oct_inv, st.tmin, st.best_t * 1.000001f);
+        const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.fix, st.fiy, st.fiz, st.oct_inv, st.tmin,
+                                               st.best_t * 1.000001f);
         st.g_base = w1.x;
         st.g_mask = (hm & 0xff000000u) | (w0.w >> 24);
         st.t_base = w1.y;

@@ -31,6 +31,7 @@ _SIGS = {
     "oracle_bvh_export": (None, [_P, _P, _P, _P, _P, _P]),
     "oracle_trace": (None, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
     "oracle_primary_rays": (None, [_P, _P, C.c_uint32, _P]),
+    "oracle_trace_bvh8": (None, [_P, _P, C.c_uint32, C.c_uint32, _P, C.POINTER(C.c_uint64)]),
     "oracle_sample_radiance": (None, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P, _P]),
     "oracle_render": (None, [_P, _P, _P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P, C.c_int, C.POINTER(Counters)]),
     "oracle_tonemap": (None, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, _P]),
@@ -110,6 +111,14 @@ class OracleScene:
         hits = np.zeros(rays.shape[0], HIT_DTYPE)
         lib().oracle_trace(self.handle, _ptr(rays), rays.shape[0], 1 if any_hit else 0, 1 if brute else 0, _ptr(hits))
         return hits
+
+    def trace_bvh8(self, rays, any_hit=False):
+        """Closest hits through the 8-wide tree in the device arithmetic."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        nv = C.c_uint64()
+        lib().oracle_trace_bvh8(self.handle, _ptr(rays), rays.shape[0], 1 if any_hit else 0, _ptr(hits), C.byref(nv))
+        return hits, nv.value
 
     def sample_radiance(self, idesc, frame, frame_index=0, precision=32, pixels=None):
         pix = None if pixels is None else np.ascontiguousarray(pixels, dtype=np.uint32)

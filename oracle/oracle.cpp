@@ -330,7 +330,24 @@ static int ceil_log2f(float x) {
     int e = ex - 127 + ((b & 0x7fffff) != 0 ? 1 : 0);
     return e < -126 ? -126 : e;
 }
-static float pow2f(int e) { return f32_bits((uint32_t)(e + 127) << 23); }
+static float pow2f(int e) { return f32_bits((uint32_t)(e < -126 ? 1 : e + 127) << 23); }
+
+// Grid exponent of one node axis: 254 steps of 2^e cover [lo, hi] (the
+// snapped origin takes at most one more step of the 255), and 2^e is at
+// least twice the ulp of the largest coordinate, so with the origin snapped
+// to a multiple of 2^e, |origin| < 2^23 2^e and every decoded plane
+// origin + q 2^e (and origin - 2^23 2^e) is exactly representable: any
+// decode formula that rounds once gives the same plane.
+static int grid_exponent(float lo, float hi) {
+    float ext = hi - lo;
+    int e = ext > 0.0f ? ceil_log2f(ext / 254.0f) : -126;
+    float m = std::fabs(lo) > std::fabs(hi) ? std::fabs(lo) : std::fabs(hi);
+    uint32_t mb = bits_f32(m);
+    int mexp = (int)((mb >> 23) & 0xff);
+    int e_min = mexp == 0 ? -126 : mexp - 127 - 23 + 1;
+    e = e > e_min ? e : e_min;
+    return e < -126 ? -126 : (e > 119 ? 119 : e);
+}
 
 static float half_area(const float* lo, const float* hi) {
     float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
@@ -348,21 +365,25 @@ static void quantise_node(hx_bvh8_node& node, const float (*clo)[3], const float
         }
     }
     for (int a = 0; a < 3; ++a) {
-        node.origin[a] = plo[a];
-        float ext = phi[a] - plo[a];
-        int e = ext > 0.0f ? ceil_log2f(ext / 255.0f) : -126;
-        while (e < 127 && plo[a] + 255.0f * pow2f(e) < phi[a]) ++e;
-        node.exponent[a] = (int8_t)e;
+        int e = grid_exponent(plo[a], phi[a]);
         float scale = pow2f(e);
-        float inv = pow2f(-e > 126 ? 126 : (-e < -126 ? -126 : -e));
+        float origin = std::floor(plo[a] * pow2f(-e)) * scale;
+        while (e < 119 && origin + 255.0f * scale < phi[a]) {
+            ++e;
+            scale = pow2f(e);
+            origin = std::floor(plo[a] * pow2f(-e)) * scale;
+        }
+        node.origin[a] = origin;
+        node.exponent[a] = (int8_t)e;
+        float inv = pow2f(-e);
         for (int k = 0; k < 8; ++k) {
             if (node.meta[k] == 0) { node.qlo[a][k] = 0; node.qhi[a][k] = 0; continue; }
-            float fl = std::floor((clo[k][a] - plo[a]) * inv);
+            float fl = std::floor((clo[k][a] - origin) * inv);
             int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
-            while (ql > 0 && plo[a] + (float)ql * scale > clo[k][a]) --ql;
-            float fh = std::ceil((chi[k][a] - plo[a]) * inv);
+            while (ql > 0 && origin + (float)ql * scale > clo[k][a]) --ql;
+            float fh = std::ceil((chi[k][a] - origin) * inv);
             int qh = fh < 0.0f ? 0 : (fh > 255.0f ? 255 : (int)fh);
-            while (qh < 255 && plo[a] + (float)qh * scale < chi[k][a]) ++qh;
+            while (qh < 255 && origin + (float)qh * scale < chi[k][a]) ++qh;
             node.qlo[a][k] = (uint8_t)ql;
             node.qhi[a][k] = (uint8_t)qh;
         }
@@ -683,6 +704,93 @@ static bool trace(const Scene& s, V3<R> o, V3<R> d, R tmin, R tmax, bool any_hit
     }
     if (best == kNoHit) return false;
     t_out = best_t; u_out = bu; v_out = bv; prim_out = best;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// BVH8 traversal in the device's arithmetic (exact plane decode, far planes
+// widened by 1 + 2^-21, octant-ordered node groups).  Checks on the CPU that
+// the quantised 8-wide tree never loses a hit; not used by the radiance path.
+// ---------------------------------------------------------------------------
+static bool trace_bvh8_cpu(const Scene& s, V3<float> o, V3<float> d, float tmin, float tmax, bool any_hit, float& t_out,
+                           uint32_t& prim_out, uint32_t* node_visits) {
+    const Bvh& b = s.bvh;
+    prim_out = kNoHit;
+    if (b.nodes.empty()) return false;
+    RayPre<float> r = ray_prepare(o, d);
+    float ix = safe_inv(d.x), iy = safe_inv(d.y), iz = safe_inv(d.z);
+    float fix = ix * 1.000000477f, fiy = iy * 1.000000477f, fiz = iz * 1.000000477f;
+    uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    uint32_t oct_inv = 7u - oct;
+    float best_t = tmax;
+    uint32_t best = kNoHit;
+    std::vector<std::pair<uint32_t, uint32_t>> stack;
+    uint32_t g_base = 0, g_mask = (1u << (24 + oct_inv)) | 1u;
+    for (;;) {
+        uint32_t t_base = 0, t_mask = 0;
+        if (g_mask > 0x00ffffffu) {
+            uint32_t bit = 31u - (uint32_t)__builtin_clz(g_mask);
+            g_mask &= ~(1u << bit);
+            uint32_t slot = (bit - 24u) ^ oct_inv;
+            uint32_t child = g_base + (uint32_t)__builtin_popcount(g_mask & 0xffu & ((1u << slot) - 1u));
+            if (g_mask > 0x00ffffffu) stack.push_back({g_base, g_mask});
+            const hx_bvh8_node& n = b.nodes[child];
+            if (node_visits) ++*node_visits;
+            uint32_t hits = 0;
+            float S[3], O[3];
+            for (int a = 0; a < 3; ++a) {
+                S[a] = pow2f(n.exponent[a]);
+                O[a] = std::fma(-8388608.0f, S[a], n.origin[a]);
+            }
+            const float inv[3] = {ix, iy, iz}, finv[3] = {fix, fiy, fiz}, org[3] = {o.x, o.y, o.z};
+            float lim = best_t * 1.000001f;
+            for (int c = 0; c < 8; ++c) {
+                uint32_t m = n.meta[c];
+                float tn = tmin, tf = lim;
+                float tna[3], tfa[3];
+                for (int a = 0; a < 3; ++a) {
+                    bool neg = inv[a] < 0.0f;
+                    uint32_t qn = neg ? n.qhi[a][c] : n.qlo[a][c], qf = neg ? n.qlo[a][c] : n.qhi[a][c];
+                    float un = f32_bits(0x4B000000u | qn), uf = f32_bits(0x4B000000u | qf);
+                    float Ln = std::fma(un, S[a], O[a]), Lf = std::fma(uf, S[a], O[a]);
+                    tna[a] = (Ln - org[a]) * inv[a];
+                    tfa[a] = (Lf - org[a]) * finv[a];
+                }
+                tn = std::fmax(std::fmax(tna[0], tna[1]), std::fmax(tna[2], tmin));
+                tf = std::fmin(std::fmin(tfa[0], tfa[1]), std::fmin(tfa[2], lim));
+                if (m != 0u && tn <= tf) {
+                    if (m & 0x80u) hits |= 1u << (24 + (c ^ oct_inv));
+                    else hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+                }
+            }
+            g_base = n.child_base;
+            g_mask = (hits & 0xff000000u) | n.internal_mask;
+            t_base = n.prim_base;
+            t_mask = hits & 0x00ffffffu;
+        }
+        while (t_mask) {
+            uint32_t bt = (uint32_t)__builtin_ctz(t_mask);
+            t_mask &= t_mask - 1u;
+            uint32_t p = b.leaf_prims[t_base + bt];
+            float t, u, v;
+            if (!intersect_triangle(r, prim_vertex<float>(s, p, 0), prim_vertex<float>(s, p, 1), prim_vertex<float>(s, p, 2),
+                                    tmin, best_t, t, u, v))
+                continue;
+            if (!(t < best_t || (t == best_t && p < best))) continue;
+            if (any_hit && s.nonopaque[p] && !alpha_pass(s, p, u, v)) continue;
+            best_t = t;
+            best = p;
+        }
+        if (g_mask <= 0x00ffffffu) {
+            if (stack.empty()) break;
+            g_base = stack.back().first;
+            g_mask = stack.back().second;
+            stack.pop_back();
+        }
+    }
+    if (best == kNoHit) return false;
+    t_out = best_t;
+    prim_out = best;
     return true;
 }
 
@@ -1149,6 +1257,26 @@ void oracle_trace(void* h, const float* rays, uint32_t n, uint32_t any_hit, uint
         out[i].u = hit ? u : 0.0f;
         out[i].v = hit ? v : 0.0f;
     }
+}
+
+// Closest hits through the BVH8 in the device arithmetic (CPU check of the
+// quantised tree); node_visits (optional) accumulates node fetches.
+void oracle_trace_bvh8(void* h, const float* rays, uint32_t n, uint32_t any_hit, hx_hit* out, uint64_t* node_visits) {
+    Scene* s = (Scene*)h;
+    uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (long i = 0; i < (long)n; ++i) {
+        const float* r = &rays[8 * (size_t)i];
+        float t = 0.0f;
+        uint32_t p, nv = 0;
+        bool hit = trace_bvh8_cpu(*s, V3<float>(r[0], r[1], r[2]), V3<float>(r[4], r[5], r[6]), r[3], r[7], any_hit != 0, t, p, &nv);
+        out[i].t = hit ? t : 0.0f;
+        out[i].prim = hit ? p : kNoHit;
+        out[i].u = 0.0f;
+        out[i].v = 0.0f;
+        total += nv;
+    }
+    if (node_visits) *node_visits = total;
 }
 
 void oracle_primary_rays(const hx_integrator_desc* d, const hx_frame_desc* f, uint32_t frame, float* out) {

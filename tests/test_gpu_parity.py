@@ -103,10 +103,14 @@ def test_sample_radiance_matches_oracle(which, policy, gpu_ctx, box, ico):
     for frame in (0, 3):
         g = it.sample_radiance(f, frame)
         o, _ = osc.sample_radiance(d, f, frame, precision=32)
-        assert rel_rmse(g, o) < 1e-3, (frame, rel_rmse(g, o))
-        # most samples agree to float rounding
         close = np.all(np.abs(g - o) <= 1e-4 * (1 + np.abs(o)), axis=1)
-        assert close.mean() > 0.97
+        far = np.nonzero(~close)[0]
+        info = (frame, rel_rmse(g, o), far.size, [(int(i), g[i].tolist(), o[i].tolist()) for i in far[:4]])
+        # the same paths: all but a few samples agree to float rounding; a
+        # rare sample may take another branch (a sky texel rounded to a
+        # neighbouring FP16 value moves an importance-sampled direction)
+        assert close.mean() > 0.995, info
+        assert rel_rmse(g, o) < 1e-2, info
     it.close()
 
 

@@ -54,6 +54,23 @@ def test_bvh_traversal_matches_brute_force(kind):
 
 
 @pytest.mark.parametrize("kind", ["box", "ico"])
+def test_bvh8_traversal_never_loses_a_hit(kind):
+    """The quantised 8-wide tree, traversed in the device's arithmetic (exact
+    plane decode, widened far planes, octant order), finds exactly the
+    brute-force closest hits."""
+    hs = _scene(kind)
+    osc = ob.OracleScene(hs)
+    lo, hi = (0.05, 0.95) if kind == "box" else (-25, 25)
+    rays = random_rays(20000, lo, hi, seed=5)
+    for any_hit in (False, True):
+        a, _ = osc.trace_bvh8(rays, any_hit=any_hit)
+        b = osc.trace(rays, any_hit=any_hit, brute=True)
+        bad = np.nonzero(a["prim"] != b["prim"])[0]
+        assert bad.size == 0, (bad[:5], a[bad[:5]], b[bad[:5]])
+        assert np.array_equal(a["t"], b["t"])
+
+
+@pytest.mark.parametrize("kind", ["box", "ico"])
 def test_bvh8_structure(kind):
     hs = _scene(kind)
     osc = ob.OracleScene(hs)
@@ -67,6 +84,14 @@ def test_bvh8_structure(kind):
     assert np.all(m[1:] >= m[:-1])
     # conservative quantisation: decoded child boxes contain their triangles
     nodes = b["nodes"]
+    # every decoded plane origin + q 2^e (and origin - 2^23 2^e) is exactly
+    # representable in FP32, so any single-rounding decode is exact
+    scale64 = np.ldexp(1.0, nodes["exponent"].astype(np.int32))
+    for qname in ("qlo", "qhi"):
+        dec = nodes["origin"].astype(np.float64)[:, :, None] + nodes[qname].astype(np.float64) * scale64[:, :, None]
+        assert np.array_equal(dec, dec.astype(np.float32).astype(np.float64))
+    shifted = nodes["origin"].astype(np.float64) - 8388608.0 * scale64
+    assert np.array_equal(shifted, shifted.astype(np.float32).astype(np.float64))
     from tests.test_oracle import _world_tris
     tris = _world_tris(hs)
     for node in nodes:
