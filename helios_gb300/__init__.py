@@ -188,6 +188,7 @@ _SIGS = {
     "hx_pinned_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "hx_pinned_free": (C.c_int, [_P]),
     "hx_scene_export_env": (C.c_int, [_P, _P]),
+    "hx_lbvh_sort_noalloc": (C.c_int, [_P, C.c_uint32, _P, _P, _P]),
     "hx_integrator_primary_hits": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
     "hx_integrator_sample_radiance": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
     "hx_rng_streams": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P]),

@@ -18,6 +18,7 @@
 #include "hx_internal.h"
 
 #include <algorithm>
+#include <mutex>
 
 namespace {
 
@@ -560,6 +561,93 @@ hx_status hx_build_bvh(hx_context* ctx, hx_scene* s, const float* d_world, uint3
 hx_status hx_world_tris(hx_context* ctx, const DevScene& d, float* world) {
     if (d.num_prims == 0) return HX_OK;
     k_world_tris<<<blocks_for(d.num_prims), kThreads, 0, ctx->stream>>>(d.prim_info, d.indices, d.vtx, d.inst, d.num_prims, world);
+    HX_CUDA(cudaGetLastError());
+    return HX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free Morton sort (no counterpart in the reference).
+//
+// Some callers cannot allocate device memory: an engine or plugin host whose
+// own allocator owns every device byte, a process that is not allowed to
+// grow its CUDA memory footprint after start-up, or a caller in a
+// latency-critical thread that must not take the allocator's locks and
+// implicit synchronisation.  hx_lbvh_sort_noalloc gives them the Morton-code
+// + stable-sort stage of the LBVH build without any cudaMalloc: inputs and
+// outputs are the caller's device buffers, and every scratch byte lives in
+// the fixed array below, which each GPU that loads this library holds until
+// the process exits.
+//
+// The array is shared by all calls on a device and keeps the contents of the
+// last call; nothing in it needs to start at zero (every pass writes the
+// parts it reads).  Calls whose work overlaps on the GPU (different streams,
+// or different host threads without ordering) race on it.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kNoAllocMaxTriangles = 1u << 18;
+constexpr uint32_t kNoAllocBoundsBlocks = 1024;
+
+constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// scratch layout: bound partials | bounds | keys | vals | keys2 | vals2 | radix temp
+constexpr size_t kNoAllocOffPartial = 0;
+constexpr size_t kNoAllocOffBounds = kNoAllocOffPartial + align256(6 * sizeof(float) * kNoAllocBoundsBlocks);
+constexpr size_t kNoAllocOffKeys = kNoAllocOffBounds + align256(6 * sizeof(float));
+constexpr size_t kNoAllocOffVals = kNoAllocOffKeys + align256(4 * (size_t)kNoAllocMaxTriangles);
+constexpr size_t kNoAllocOffKeys2 = kNoAllocOffVals + align256(4 * (size_t)kNoAllocMaxTriangles);
+constexpr size_t kNoAllocOffVals2 = kNoAllocOffKeys2 + align256(4 * (size_t)kNoAllocMaxTriangles);
+constexpr size_t kNoAllocOffRadix = kNoAllocOffVals2 + align256(4 * (size_t)kNoAllocMaxTriangles);
+// radix temp for 2^18 keys: 64 tiles -> 2 x 256 x 64 words + scan temp; 1 MiB covers it
+constexpr size_t kNoAllocRadixBytes = 1u << 20;
+constexpr size_t kNoAllocScratchBytes = kNoAllocOffRadix + kNoAllocRadixBytes;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+extern "C" hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n, uint32_t* d_morton,
+                                          uint32_t* d_sorted, void* cuda_stream) {
+    HX_CHECK_ARG(d_world_tris && d_morton && d_sorted, "hx_lbvh_sort_noalloc: null device pointer");
+    HX_CHECK_ARG(n >= 1 && n <= kNoAllocMaxTriangles,
+                 "hx_lbvh_sort_noalloc: %u triangles; this entry point handles 1..%u (its scratch is a fixed %zu-byte "
+                 "device array)", n, kNoAllocMaxTriangles, (size_t)kNoAllocScratchBytes);
+    HX_CHECK_ARG(hx_radix_temp_bytes(n) <= kNoAllocRadixBytes, "hx_lbvh_sort_noalloc: radix scratch too small");
+    int dev = 0;
+    HX_CUDA(cudaGetDevice(&dev));
+    HX_CHECK_ARG(dev >= 0 && dev < kNoAllocMaxDevices, "hx_lbvh_sort_noalloc: device %d out of range", dev);
+    void* base = nullptr;
+    {
+        // once per device, with that device current: the device address of the array
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                hx_set_error("hx_lbvh_sort_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+                return HX_ERR_DEVICE;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    char* b = (char*)base;
+    float* partial = (float*)(b + kNoAllocOffPartial);
+    float* bounds = (float*)(b + kNoAllocOffBounds);
+    uint32_t* keys = (uint32_t*)(b + kNoAllocOffKeys);
+    uint32_t* vals = (uint32_t*)(b + kNoAllocOffVals);
+    const uint32_t bnd_blocks = std::min<uint32_t>(kNoAllocBoundsBlocks, (n + kThreads - 1) / kThreads);
+    k_centroid_bounds<<<bnd_blocks, kThreads, 0, st>>>(d_world_tris, n, partial);
+    k_bounds_final<<<1, 32, 0, st>>>(partial, bnd_blocks, bounds);
+    k_morton<<<blocks_for(n), kThreads, 0, st>>>(d_world_tris, n, bounds, d_morton, keys, vals);
+    hx_radix_sort_pairs(keys, vals, (uint32_t*)(b + kNoAllocOffKeys2), (uint32_t*)(b + kNoAllocOffVals2), n, 30,
+                        b + kNoAllocOffRadix, st);
+    HX_CUDA(cudaMemcpyAsync(d_sorted, vals, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
     HX_CUDA(cudaGetLastError());
     return HX_OK;
 }

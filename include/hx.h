@@ -421,6 +421,24 @@ HX_API hx_status hx_rng_streams(hx_context* ctx, uint32_t rng_kind, const uint32
                                 uint32_t num_streams, uint32_t draws_per_stream,
                                 uint32_t* host_out);
 
+/* Allocation-free Morton sort.  No counterpart in the reference.  For callers
+ * that cannot allocate device memory (an engine whose own allocator owns all
+ * device memory, a process that may not grow its footprint after start-up, a
+ * latency-critical thread that must not take the allocator's locks): the
+ * Morton-code + stable-sort stage of the LBVH build over the caller's device
+ * buffers, with no cudaMalloc.  d_world_tris: n x 9 floats (world-space
+ * vertices, flattened order); d_morton[n]: 30-bit codes in input order;
+ * d_sorted[n]: the stable sort order — the same values hx_scene_upload
+ * computes (hx_scene_export_bvh).  n must be 1..262144 (2^18); larger n is
+ * rejected with HX_ERR_INVALID_ARG.  Scratch is one fixed device array of
+ * about 5 MB in the library, held by every GPU that loads it until exit;
+ * the first call on a device looks up that array's address (make it before
+ * any stream capture).  Work is ordered on cuda_stream (a cudaStream_t,
+ * NULL = default stream); calls that overlap on the GPU race on the shared
+ * scratch. */
+HX_API hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n, uint32_t* d_morton, uint32_t* d_sorted,
+                                      void* cuda_stream);
+
 /* ------------------------------------------------------------------------ */
 /* Procedural scenes for the benchmark configurations (host side)            */
 /* ------------------------------------------------------------------------ */
