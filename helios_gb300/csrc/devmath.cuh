@@ -115,3 +115,35 @@ constexpr float kPiF = 3.14159265359f;  // M_PI of common.glsl:18 as a float lit
 constexpr float kEpsilonF = 0.0001f;    // EPSILON, common.glsl:19
 constexpr float kMinRoughnessF = 0.1f;  // MIN_ROUGHNESS, common.glsl:21
 constexpr uint32_t kNoHit = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): each lane rounds
+// exactly like the scalar instruction, so results equal the scalar forms.
+// ---------------------------------------------------------------------------
+HXD unsigned long long f2_bits(float2 a) { return ((unsigned long long)__float_as_uint(a.y) << 32) | __float_as_uint(a.x); }
+HXD float2 bits_f2(unsigned long long r) { return make_float2(__uint_as_float((uint32_t)r), __uint_as_float((uint32_t)(r >> 32))); }
+HXD float2 fma2_rn(float2 a, float2 b, float2 c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
+    return bits_f2(r);
+}
+HXD float2 sub2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(r);
+}
+HXD float2 mul2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(r);
+}
+HXD float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+HXD float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}

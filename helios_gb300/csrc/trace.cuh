@@ -143,22 +143,24 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
     const uint32_t nx0 = nx ? hix0 : lox0, nx1 = nx ? hix1 : lox1, fx0 = nx ? lox0 : hix0, fx1 = nx ? lox1 : hix1;
     const uint32_t ny0 = ny ? hiy0 : loy0, ny1 = ny ? hiy1 : loy1, fy0 = ny ? loy0 : hiy0, fy1 = ny ? loy1 : hiy1;
     const uint32_t nz0 = nz ? hiz0 : loz0, nz1 = nz ? hiz1 : loz1, fz0 = nz ? loz0 : hiz0, fz1 = nz ? loz1 : hiz1;
+    const float2 Sx2 = make_float2(Sx, Sx), Sy2 = make_float2(Sy, Sy), Sz2 = make_float2(Sz, Sz);
+    const float2 Ox2 = make_float2(Ox, Ox), Oy2 = make_float2(Oy, Oy), Oz2 = make_float2(Oz, Oz);
+    const float2 ox2 = make_float2(r.o.x, r.o.x), oy2 = make_float2(r.o.y, r.o.y), oz2 = make_float2(r.o.z, r.o.z);
+    const float2 ix2 = make_float2(r.ix, fix), iy2 = make_float2(r.iy, fiy), iz2 = make_float2(r.iz, fiz);
     uint32_t hits = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const uint32_t m = byte_of(c < 4 ? w1.z : w1.w, c & 3);
         const int k = c & 3;
-        const float Lnx = __fmaf_rn(byte_biased(c < 4 ? nx0 : nx1, k), Sx, Ox);
-        const float Lfx = __fmaf_rn(byte_biased(c < 4 ? fx0 : fx1, k), Sx, Ox);
-        const float Lny = __fmaf_rn(byte_biased(c < 4 ? ny0 : ny1, k), Sy, Oy);
-        const float Lfy = __fmaf_rn(byte_biased(c < 4 ? fy0 : fy1, k), Sy, Oy);
-        const float Lnz = __fmaf_rn(byte_biased(c < 4 ? nz0 : nz1, k), Sz, Oz);
-        const float Lfz = __fmaf_rn(byte_biased(c < 4 ? fz0 : fz1, k), Sz, Oz);
-        const float tnx = (Lnx - r.o.x) * r.ix, tfx = (Lfx - r.o.x) * fix;
-        const float tny = (Lny - r.o.y) * r.iy, tfy = (Lfy - r.o.y) * fiy;
-        const float tnz = (Lnz - r.o.z) * r.iz, tfz = (Lfz - r.o.z) * fiz;
-        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, lim));
+        // (near, far) pairs per axis in packed FP32x2: L = q' S + O, t = (L - o) inv
+        const float2 Lx = fma2_rn(make_float2(byte_biased(c < 4 ? nx0 : nx1, k), byte_biased(c < 4 ? fx0 : fx1, k)), Sx2, Ox2);
+        const float2 Ly = fma2_rn(make_float2(byte_biased(c < 4 ? ny0 : ny1, k), byte_biased(c < 4 ? fy0 : fy1, k)), Sy2, Oy2);
+        const float2 Lz = fma2_rn(make_float2(byte_biased(c < 4 ? nz0 : nz1, k), byte_biased(c < 4 ? fz0 : fz1, k)), Sz2, Oz2);
+        const float2 tx = mul2_rn(sub2_rn(Lx, ox2), ix2);
+        const float2 ty = mul2_rn(sub2_rn(Ly, oy2), iy2);
+        const float2 tz = mul2_rn(sub2_rn(Lz, oz2), iz2);
+        const float tn = fmaxf(max3f(tx.x, ty.x, tz.x), tmin);
+        const float tf = fminf(min3f(tx.y, ty.y, tz.y), lim);
         if (m != 0u && tn <= tf) {
             if (m & 0x80u) hits |= 1u << (24 + (c ^ oct_inv));
             else hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
@@ -295,7 +297,9 @@ HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, flo
 
 // Returns true when the ray is finished (traversal exhausted, or the first
 // accepted hit of a shadow ray).
-template <bool SHADOW, bool COUNT>
+constexpr int kPostponeLanes = 8;  // postpone triangle tests below this many lanes
+
+template <bool SHADOW, bool COUNT, bool POSTPONE = false>
 HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflow, TraverseCount* tc) {
     if (st.g_mask > 0x00ffffffu) {
         const uint32_t bit = 31u - __clz(st.g_mask);
@@ -325,6 +329,15 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         st.g_mask = 0;
     }
     while (st.t_mask) {
+        // Postpone the triangles when few lanes of the warp test triangles
+        // now and this lane still has nodes to visit: push the group and
+        // keep the warp on node steps (Ylitie et al. 2017).  A pushed group
+        // has no bit >= 24, so it is popped as a triangle group.
+        if (POSTPONE && st.g_mask > 0x00ffffffu && __popc(__activemask()) < kPostponeLanes && st.sp + 1 < kStackSize) {
+            stack[st.sp++] = make_uint2(st.t_base, st.t_mask);
+            st.t_mask = 0;
+            break;
+        }
         const uint32_t b = __ffs(st.t_mask) - 1u;
         st.t_mask &= st.t_mask - 1u;
         const uint32_t k = st.t_base + b;
