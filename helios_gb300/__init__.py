@@ -141,6 +141,28 @@ class ProceduralParams(C.Structure):
                 ("turbidity", C.c_float)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("request_arena_bytes", C.c_uint64), ("max_paths_per_tick", C.c_uint32),
+                ("max_ray_bounces", C.c_uint32), ("policy", Policy)]
+
+
+class RequestDesc(C.Structure):
+    _fields_ = [("scene_id", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("denoise", C.c_uint32), ("tonemap_op", C.c_uint32), ("exposure", C.c_float),
+                ("reserved", C.c_uint32), ("frame", FrameDesc), ("user_tag", C.c_uint64)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("request_id", C.c_uint64), ("user_tag", C.c_uint64), ("paths", C.c_uint64),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double), ("status", C.c_int), ("reserved", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("ticks", C.c_uint64), ("requests_done", C.c_uint64),
+                ("requests_pending", C.c_uint64), ("requests_active", C.c_uint64), ("arena_bytes", C.c_uint64),
+                ("arena_used", C.c_uint64), ("seconds", C.c_double)]
+
+
 BVH8_NODE_BYTES = 80
 BVH8_DTYPE = np.dtype([("origin", np.float32, 3), ("exponent", np.int8, 3), ("internal_mask", np.uint8),
                        ("child_base", np.uint32), ("prim_base", np.uint32), ("meta", np.uint8, 8),
@@ -189,6 +211,14 @@ _SIGS = {
     "hx_pinned_free": (C.c_int, [_P]),
     "hx_scene_export_env": (C.c_int, [_P, _P]),
     "hx_lbvh_sort_noalloc": (C.c_int, [_P, C.c_uint32, _P, _P, _P]),
+    "hx_server_create": (C.c_int, [_P, C.POINTER(ServerDesc), C.POINTER(_P)]),
+    "hx_server_add_scene": (C.c_int, [_P, _P, C.POINTER(C.c_uint32)]),
+    "hx_server_start": (C.c_int, [_P]),
+    "hx_server_submit": (C.c_int, [_P, C.POINTER(RequestDesc), C.POINTER(C.c_uint64)]),
+    "hx_server_poll": (C.c_int, [_P, C.POINTER(RequestResult), C.c_uint32, C.POINTER(C.c_uint32), C.c_double]),
+    "hx_server_fetch": (C.c_int, [_P, C.c_uint64, _P]),
+    "hx_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "hx_server_destroy": (C.c_int, [_P]),
     "hx_integrator_primary_hits": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
     "hx_integrator_sample_radiance": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
     "hx_rng_streams": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P]),
@@ -504,6 +534,63 @@ class PathIntegrator:
     def close(self):
         if self.handle:
             lib().hx_integrator_destroy(self.handle)
+            self.handle = None
+
+
+class Server:
+    """Resident render-serving loop (hx_server_*): scenes stay on the device,
+    requests are admitted by HBM budget and batched into CUDA-graph ticks."""
+
+    def __init__(self, ctx, arena_bytes=4 << 30, max_paths_per_tick=4 << 20, max_ray_bounces=8, policy=None):
+        d = ServerDesc()
+        d.request_arena_bytes = arena_bytes
+        d.max_paths_per_tick = max_paths_per_tick
+        d.max_ray_bounces = max_ray_bounces
+        d.policy = policy if policy is not None else policy_reference()
+        h = C.c_void_p()
+        check(lib().hx_server_create(ctx.handle, C.byref(d), C.byref(h)))
+        self.handle = h
+        self.ctx = ctx
+        self.sizes = {}
+
+    def add_scene(self, scene):
+        sid = C.c_uint32()
+        check(lib().hx_server_add_scene(self.handle, scene.handle, C.byref(sid)))
+        return sid.value
+
+    def start(self):
+        check(lib().hx_server_start(self.handle))
+
+    def submit(self, scene_id, frame, width, height, spp, tonemap_op=TONEMAP_ACES, exposure=1.0, user_tag=0):
+        r = RequestDesc()
+        r.scene_id, r.width, r.height, r.spp = scene_id, width, height, spp
+        r.tonemap_op, r.exposure, r.user_tag = tonemap_op, exposure, user_tag
+        r.frame = frame
+        rid = C.c_uint64()
+        check(lib().hx_server_submit(self.handle, C.byref(r), C.byref(rid)))
+        self.sizes[rid.value] = (width, height)
+        return rid.value
+
+    def poll(self, wait_seconds=0.0, capacity=256):
+        arr = (RequestResult * capacity)()
+        n = C.c_uint32()
+        check(lib().hx_server_poll(self.handle, arr, capacity, C.byref(n), wait_seconds))
+        return [arr[i] for i in range(n.value)]
+
+    def fetch(self, request_id):
+        w, h = self.sizes.pop(request_id)
+        out = np.zeros((h, w, 4), np.uint8)
+        check(lib().hx_server_fetch(self.handle, request_id, _ptr(out)))
+        return out
+
+    def stats(self):
+        s = ServerStats()
+        check(lib().hx_server_stats_get(self.handle, C.byref(s)))
+        return s
+
+    def close(self):
+        if self.handle:
+            lib().hx_server_destroy(self.handle)
             self.handle = None
 
 

@@ -1,0 +1,646 @@
+// server.cu — resident render-serving loop (spec serving form; the
+// nearest reference hook is the per-frame Renderer::render,
+// src/engine/gfx/renderer.cpp:107, driven once per window frame by the
+// application loop, src/engine/core/application.cpp:38-54).
+//
+// Scenes, BVHs and per-request accumulation images stay on the device.  A
+// worker thread admits requests into a pre-allocated HBM arena (first fit,
+// so a large request waiting for memory does not block smaller ones), and
+// runs ticks: each tick of a scene batches chunks of several requests —
+// different resolutions and sample counts — into one wavefront, shortest
+// remaining work first, and replays a CUDA graph captured once per scene
+// (every launch parameter lives in a device-side request table, so the same
+// graph serves any batch).  Different scenes tick on their own streams and
+// overlap on the device.  Per-pixel accumulation runs in sample order, so a
+// request's image is identical whether it ran alone or in a mix.
+#include "wavefront.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct Chunk {              // device request-table entry: samples x pixels of one request
+    uint32_t slot;          // request slot (index into the slot table)
+    uint32_t sample_begin;  // first sample (progressive frame index)
+    uint32_t nsamples;
+    uint32_t pixel_begin;   // first pixel, row-major
+    uint32_t npix;
+    uint32_t path_begin;    // first path of the chunk in the wavefront (sample-major)
+    uint32_t acc_begin;     // prefix of npix over chunks (accumulation threads)
+    uint32_t pad;
+};
+
+struct SlotDev {            // per admitted request, device side
+    hx_frame_desc frame;
+    float4* acc;
+    uint32_t width, height, pad[2];
+};
+
+struct TableHeader {
+    uint32_t num_chunks, total_paths, total_acc, pad;
+};
+
+constexpr uint32_t kMaxChunks = 1024;
+constexpr uint32_t kMaxSlots = 4096;
+
+__device__ __forceinline__ uint32_t find_chunk(const Chunk* c, uint32_t n, uint32_t key, bool by_acc) {
+    uint32_t lo = 0, hi = n;  // last chunk with begin <= key
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        uint32_t b = by_acc ? c[mid].acc_begin : c[mid].path_begin;
+        if (b <= key) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_raygen_multi(const TableHeader* hdr, const Chunk* chunks, const SlotDev* slots, uint32_t kind, Queues q) {
+    const uint32_t total = hdr->total_paths, nc = hdr->num_chunks;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        const Chunk c = chunks[find_chunk(chunks, nc, p, false)];
+        const SlotDev& sd = slots[c.slot];
+        uint32_t local = p - c.path_begin;
+        uint32_t s = local / c.npix, pix = c.pixel_begin + (local - s * c.npix);
+        uint32_t x = pix % sd.width, y = pix / sd.width;
+        Rng rng = rng_init(kind, x, y, sd.width, c.sample_begin + s);
+        V3 o, d;
+        generate_ray(sd.frame, kind, x, y, sd.width, sd.height, rng, o, d);
+        q.T[p] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+        q.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        q.rng[p] = make_uint2(rng.s0, rng.s1);
+        q.o[0][p] = make_float4(o.x, o.y, o.z, 0.001f);
+        q.d[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+        q.p[0][p] = p | kAnyHitFlag;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        q.counters[0] = total;
+        q.counters[1] = 0;
+        q.counters[2] = 0;
+    }
+}
+
+// Running-mean accumulation (path_trace_rgen.glsl:217-248) per request pixel,
+// samples of the chunk in order.
+__global__ void k_accumulate_multi(const TableHeader* hdr, const Chunk* chunks, const SlotDev* slots, float clampv,
+                                   const float4* __restrict__ L) {
+    const uint32_t total = hdr->total_acc, nc = hdr->num_chunks;
+    for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < total; a += gridDim.x * blockDim.x) {
+        const Chunk c = chunks[find_chunk(chunks, nc, a, true)];
+        const SlotDev& sd = slots[c.slot];
+        uint32_t i = a - c.acc_begin;
+        float4* dst = sd.acc + c.pixel_begin + i;
+        float4 v = *dst;
+        for (uint32_t s = 0; s < c.nsamples; ++s) {
+            float4 l = L[(size_t)c.path_begin + (size_t)s * c.npix + i];
+            float cc[3] = {l.x, l.y, l.z};
+            if (clampv > 0.0f)
+                for (int k = 0; k < 3; ++k) cc[k] = gmin(cc[k], clampv);
+            uint32_t frame = c.sample_begin + s;
+            float* av = &v.x;
+            for (int k = 0; k < 3; ++k) av[k] = frame == 0 ? cc[k] : av[k] + (cc[k] - av[k]) / (float)frame;
+            v.w = 1.0f;
+        }
+        *dst = v;
+    }
+}
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct ServerRequest {
+    uint64_t id = 0;
+    hx_request_desc desc{};
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int slot = -1;
+    size_t arena_off = 0, arena_bytes = 0;
+    float4* acc = nullptr;
+    uchar4* ldr = nullptr;
+    uint8_t* host_ldr = nullptr;  // pinned
+    uint32_t samples_done = 0, pixel_cursor = 0;
+    bool in_flight = false, finishing = false, done = false;
+    hx_status status = HX_OK;
+    uint64_t paths_traced = 0;
+};
+
+struct PendingChunk {
+    ServerRequest* r;
+    uint32_t nsamples, npix;
+};
+
+struct SceneBatch {
+    const hx_scene* scene = nullptr;
+    cudaStream_t stream = nullptr;
+    Queues q{};
+    std::vector<void*> allocs;
+    TableHeader* d_hdr = nullptr;
+    Chunk* d_chunks = nullptr;
+    char* h_table = nullptr;  // pinned: header + chunks
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    std::vector<PendingChunk> running;
+    std::vector<ServerRequest*> finishing;
+    cudaEvent_t finish_ev = nullptr;
+    bool finish_busy = false;
+    uint64_t ticks = 0;
+};
+
+struct hx_server {
+    hx_context* ctx = nullptr;
+    hx_server_desc desc{};
+    std::vector<SceneBatch*> batches;
+    // request slots (device table) and the HBM arena for per-request images
+    SlotDev* d_slots = nullptr;
+    std::vector<int> free_slots;
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    std::map<size_t, size_t> arena_free;  // offset -> size
+    // queues
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<ServerRequest*> pending;
+    std::vector<ServerRequest*> admitted;
+    std::map<uint64_t, ServerRequest*> all;
+    std::vector<hx_request_result> completed;
+    uint64_t next_id = 1;
+    std::thread worker;
+    std::atomic<bool> running{false};
+    std::atomic<int> worker_error{0};
+    char worker_msg[512] = "";
+    // stats
+    uint64_t paths_total = 0, ticks_total = 0, requests_done = 0;
+    double t_start = 0, busy_first = 0, busy_last = 0;
+};
+
+static size_t request_bytes(const hx_request_desc& d) {
+    size_t npix = (size_t)d.width * d.height;
+    return ((16 * npix + 255) & ~(size_t)255) + ((4 * npix + 255) & ~(size_t)255);
+}
+
+static bool arena_alloc(hx_server* s, size_t bytes, size_t* off) {
+    for (auto it = s->arena_free.begin(); it != s->arena_free.end(); ++it) {
+        if (it->second >= bytes) {
+            *off = it->first;
+            size_t rest = it->second - bytes;
+            size_t noff = it->first + bytes;
+            s->arena_free.erase(it);
+            if (rest) s->arena_free[noff] = rest;
+            return true;
+        }
+    }
+    return false;
+}
+
+static void arena_release(hx_server* s, size_t off, size_t bytes) {
+    auto it = s->arena_free.emplace(off, bytes).first;
+    auto next = std::next(it);
+    if (next != s->arena_free.end() && it->first + it->second == next->first) {
+        it->second += next->second;
+        s->arena_free.erase(next);
+    }
+    if (it != s->arena_free.begin()) {
+        auto prev = std::prev(it);
+        if (prev->first + prev->second == it->first) {
+            prev->second += it->second;
+            s->arena_free.erase(it);
+        }
+    }
+}
+
+static hx_status batch_init(hx_server* s, SceneBatch* b) {
+    hx_context* ctx = s->ctx;
+    const uint32_t cap = s->desc.max_paths_per_tick;
+    auto A = [&](void** p, size_t bytes) -> hx_status {
+        hx_status st = hx_alloc(ctx, p, bytes);
+        if (st == HX_OK) b->allocs.push_back(*p);
+        return st;
+    };
+    for (int k = 0; k < 2; ++k) {
+        HX_TRY(A((void**)&b->q.o[k], 16ull * cap));
+        HX_TRY(A((void**)&b->q.d[k], 16ull * cap));
+        HX_TRY(A((void**)&b->q.p[k], 4ull * cap));
+    }
+    HX_TRY(A((void**)&b->q.hit, 16ull * cap));
+    HX_TRY(A((void**)&b->q.so, 16ull * cap));
+    HX_TRY(A((void**)&b->q.sd, 16ull * cap));
+    HX_TRY(A((void**)&b->q.sc, 16ull * cap));
+    HX_TRY(A((void**)&b->q.T, 16ull * cap));
+    HX_TRY(A((void**)&b->q.L, 16ull * cap));
+    HX_TRY(A((void**)&b->q.rng, 8ull * cap));
+    HX_TRY(A((void**)&b->q.counters, 64));
+    HX_TRY(A((void**)&b->q.stats, 64));
+    HX_TRY(A((void**)&b->q.status, 64));
+    HX_TRY(A((void**)&b->d_hdr, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks));
+    b->d_chunks = (Chunk*)(b->d_hdr + 1);
+    HX_CUDA(cudaMallocHost(&b->h_table, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks));
+    HX_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    HX_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    HX_CUDA(cudaEventCreateWithFlags(&b->finish_ev, cudaEventDisableTiming));
+    HX_CUDA(cudaMemsetAsync(b->q.stats, 0, 64, b->stream));
+    HX_CUDA(cudaMemsetAsync(b->q.status, 0, 64, b->stream));
+    // capture the tick: table upload, ray generation, bounces, accumulation
+    const DevScene& sc = b->scene->d;
+    Policy P = make_policy(s->desc.policy);
+    int per_sm = 0;
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false>, kTraceThreads, 0));
+    const int grid_trace = std::max(1, per_sm) * ctx->num_sms;
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade, kShadeThreads, 0));
+    const int grid_shade = std::max(1, per_sm) * ctx->num_sms;
+    const int grid_gen = ctx->num_sms * 8;
+    cudaStream_t st = b->stream;
+    cudaGraph_t g;
+    HX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaMemcpyAsync(b->d_hdr, b->h_table, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks, cudaMemcpyHostToDevice, st);
+    k_raygen_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, P.rng, b->q);
+    for (uint32_t bo = 0; bo < s->desc.max_ray_bounces; ++bo) {
+        int cur = bo & 1;
+        cudaMemsetAsync(b->q.counters + 4, 0, 8, st);
+        k_trace<false><<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q.o[cur], b->q.d[cur], b->q.p[cur], b->q.counters + cur,
+                                                             b->q.hit, b->q.stats, b->q.status, b->q.counters + 4);
+        cudaMemsetAsync(b->q.counters + (cur ^ 1), 0, 4, st);
+        cudaMemsetAsync(b->q.counters + 2, 0, 4, st);
+        k_shade<<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
+        k_shadow<<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q, b->q.counters + 5);
+    }
+    k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp, b->q.L);
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (ce != cudaSuccess) {
+        hx_set_error("server: graph capture failed: %s", cudaGetErrorString(ce));
+        return HX_ERR_DEVICE;
+    }
+    HX_CUDA(cudaGraphInstantiate(&b->graph, g, 0));
+    cudaGraphDestroy(g);
+    return HX_OK;
+}
+
+static void batch_free(hx_server* s, SceneBatch* b) {
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (void* p : b->allocs) hx_free(s->ctx, p);
+    if (b->h_table) cudaFreeHost(b->h_table);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->finish_ev) cudaEventDestroy(b->finish_ev);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+// Admit pending requests whose images fit the arena (first fit, in arrival order).
+static void admit(hx_server* s) {
+    for (auto it = s->pending.begin(); it != s->pending.end();) {
+        ServerRequest* r = *it;
+        if (s->free_slots.empty()) break;
+        size_t off;
+        if (!arena_alloc(s, r->arena_bytes, &off)) {
+            ++it;
+            continue;
+        }
+        r->arena_off = off;
+        r->slot = s->free_slots.back();
+        s->free_slots.pop_back();
+        size_t npix = (size_t)r->desc.width * r->desc.height;
+        r->acc = (float4*)(s->arena + off);
+        r->ldr = (uchar4*)(s->arena + off + ((16 * npix + 255) & ~(size_t)255));
+        r->t_admit = now_s();
+        s->admitted.push_back(r);
+        it = s->pending.erase(it);
+    }
+}
+
+static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
+    // requests of this scene with work left and nothing in flight, shortest remaining work first
+    std::vector<ServerRequest*> cand;
+    for (ServerRequest* r : s->admitted)
+        if (r->desc.scene_id == scene_id && !r->in_flight && !r->finishing && r->samples_done < r->desc.spp) cand.push_back(r);
+    if (cand.empty()) return HX_OK;
+    auto remaining = [](const ServerRequest* r) {
+        return (uint64_t)(r->desc.spp - r->samples_done) * r->desc.width * r->desc.height - r->pixel_cursor;
+    };
+    std::stable_sort(cand.begin(), cand.end(), [&](ServerRequest* a, ServerRequest* c) { return remaining(a) < remaining(c); });
+    TableHeader* hdr = (TableHeader*)b->h_table;
+    Chunk* ch = (Chunk*)(hdr + 1);
+    uint32_t nc = 0, paths = 0, accs = 0;
+    const uint32_t cap = s->desc.max_paths_per_tick;
+    b->running.clear();
+    // slot table updates for newly admitted requests happen before the tick
+    for (ServerRequest* r : cand) {
+        if (nc >= kMaxChunks || paths >= cap) break;
+        uint32_t npix_img = r->desc.width * r->desc.height;
+        uint32_t left = cap - paths;
+        Chunk c{};
+        c.slot = (uint32_t)r->slot;
+        c.sample_begin = r->samples_done;
+        if (r->pixel_cursor == 0 && left >= npix_img) {
+            c.nsamples = std::min<uint32_t>(r->desc.spp - r->samples_done, left / npix_img);
+            c.pixel_begin = 0;
+            c.npix = npix_img;
+        } else {
+            c.nsamples = 1;
+            c.pixel_begin = r->pixel_cursor;
+            c.npix = std::min<uint32_t>(npix_img - r->pixel_cursor, left);
+        }
+        c.path_begin = paths;
+        c.acc_begin = accs;
+        ch[nc++] = c;
+        paths += c.nsamples * c.npix;
+        accs += c.npix;
+        r->in_flight = true;
+        b->running.push_back({r, c.nsamples, c.npix});
+    }
+    hdr->num_chunks = nc;
+    hdr->total_paths = paths;
+    hdr->total_acc = accs;
+    HX_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    HX_CUDA(cudaEventRecord(b->done, b->stream));
+    b->busy = true;
+    b->ticks++;
+    s->ticks_total++;
+    s->paths_total += paths;
+    return HX_OK;
+}
+
+static hx_status retire_tick(hx_server* s, SceneBatch* b) {
+    for (const PendingChunk& pc : b->running) {
+        ServerRequest* r = pc.r;
+        r->in_flight = false;
+        r->paths_traced += (uint64_t)pc.nsamples * pc.npix;
+        uint32_t npix_img = r->desc.width * r->desc.height;
+        if (pc.npix == npix_img && r->pixel_cursor == 0) r->samples_done += pc.nsamples;
+        else {
+            r->pixel_cursor += pc.npix;
+            if (r->pixel_cursor >= npix_img) {
+                r->pixel_cursor = 0;
+                r->samples_done += 1;
+            }
+        }
+        if (r->samples_done >= r->desc.spp) {
+            // tone map to RGBA8 and copy to the request's pinned host buffer
+            r->finishing = true;
+            k_tonemap<<<s->ctx->num_sms * 4, kGenThreads, 0, b->stream>>>(r->acc, nullptr, r->desc.width, r->desc.height,
+                                                                           r->desc.tonemap_op, r->desc.exposure, r->ldr);
+            HX_CUDA(cudaMemcpyAsync(r->host_ldr, r->ldr, 4ull * npix_img, cudaMemcpyDeviceToHost, b->stream));
+            b->finishing.push_back(r);
+        }
+    }
+    b->running.clear();
+    if (!b->finishing.empty()) {
+        HX_CUDA(cudaEventRecord(b->finish_ev, b->stream));
+        b->finish_busy = true;
+    }
+    b->busy = false;
+    return HX_OK;
+}
+
+static void complete_finished(hx_server* s, SceneBatch* b) {
+    double t = now_s();
+    for (ServerRequest* r : b->finishing) {
+        r->finishing = false;
+        r->done = true;
+        r->t_done = t;
+        hx_request_result res{};
+        res.request_id = r->id;
+        res.status = r->status;
+        res.queue_ms = (r->t_admit - r->t_submit) * 1000.0;
+        res.latency_ms = (r->t_done - r->t_submit) * 1000.0;
+        res.paths = r->paths_traced;
+        res.user_tag = r->desc.user_tag;
+        s->completed.push_back(res);
+        s->requests_done++;
+        // release the device slot and arena space; the pinned LDR copy stays until fetch
+        s->free_slots.push_back(r->slot);
+        arena_release(s, r->arena_off, r->arena_bytes);
+        r->slot = -1;
+        s->admitted.erase(std::find(s->admitted.begin(), s->admitted.end(), r));
+    }
+    b->finishing.clear();
+    b->finish_busy = false;
+}
+
+static hx_status upload_new_slots(hx_server* s, cudaStream_t st, const std::vector<ServerRequest*>& fresh) {
+    for (ServerRequest* r : fresh) {
+        SlotDev sd;
+        std::memset(&sd, 0, sizeof(sd));
+        sd.frame = r->desc.frame;
+        sd.acc = r->acc;
+        sd.width = r->desc.width;
+        sd.height = r->desc.height;
+        HX_CUDA(cudaMemcpyAsync(s->d_slots + r->slot, &sd, sizeof(sd), cudaMemcpyHostToDevice, st));
+        HX_CUDA(cudaMemsetAsync(r->acc, 0, 16ull * r->desc.width * r->desc.height, st));
+    }
+    if (!fresh.empty()) HX_CUDA(cudaStreamSynchronize(st));
+    return HX_OK;
+}
+
+static void worker_main(hx_server* s) {
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t setup;
+    cudaStreamCreateWithFlags(&setup, cudaStreamNonBlocking);
+    while (s->running.load()) {
+        std::vector<ServerRequest*> fresh;
+        bool idle = true;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            size_t before = s->admitted.size();
+            admit(s);
+            fresh.assign(s->admitted.begin() + before, s->admitted.end());
+        }
+        hx_status st = upload_new_slots(s, setup, fresh);
+        if (st == HX_OK) {
+            std::unique_lock<std::mutex> lk(s->mu);
+            for (uint32_t k = 0; k < s->batches.size() && st == HX_OK; ++k) {
+                SceneBatch* b = s->batches[k];
+                if (b->finish_busy && cudaEventQuery(b->finish_ev) == cudaSuccess) complete_finished(s, b);
+                if (b->busy && cudaEventQuery(b->done) == cudaSuccess) st = retire_tick(s, b);
+                if (st == HX_OK && !b->busy && !b->finish_busy) st = launch_tick(s, b, k);
+                if (b->busy || b->finish_busy) idle = false;
+            }
+            if (!s->completed.empty()) s->cv.notify_all();
+        }
+        if (st != HX_OK) {
+            std::snprintf(s->worker_msg, sizeof(s->worker_msg), "%s", hx_last_error_string());
+            s->worker_error.store((int)st);
+            s->cv.notify_all();
+            break;
+        }
+        if (idle) {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->pending.empty()) s->cv.wait_for(lk, std::chrono::microseconds(500));
+        } else {
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+    cudaStreamDestroy(setup);
+}
+
+extern "C" hx_status hx_server_create(hx_context* ctx, const hx_server_desc* desc, hx_server** out) {
+    HX_CHECK_ARG(ctx && desc && out, "hx_server_create: null argument");
+    HX_CHECK_ARG(desc->max_paths_per_tick >= 1024 && desc->max_ray_bounces >= 1 && desc->max_ray_bounces <= 64,
+                 "hx_server_create: bad parameters");
+    HX_CHECK_ARG(desc->request_arena_bytes >= (1u << 20), "hx_server_create: request arena too small");
+    HX_CUDA(cudaSetDevice(ctx->device));
+    hx_server* s = new hx_server();
+    s->ctx = ctx;
+    s->desc = *desc;
+    hx_status st = hx_alloc(ctx, (void**)&s->arena, desc->request_arena_bytes);
+    if (st != HX_OK) {
+        delete s;
+        return st;
+    }
+    s->arena_bytes = desc->request_arena_bytes;
+    s->arena_free[0] = s->arena_bytes;
+    st = hx_alloc(ctx, (void**)&s->d_slots, sizeof(SlotDev) * kMaxSlots);
+    if (st != HX_OK) {
+        hx_free(ctx, s->arena);
+        delete s;
+        return st;
+    }
+    for (int k = (int)kMaxSlots - 1; k >= 0; --k) s->free_slots.push_back(k);
+    s->t_start = now_s();
+    *out = s;
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_add_scene(hx_server* s, const hx_scene* scene, uint32_t* scene_id) {
+    HX_CHECK_ARG(s && scene && scene_id, "hx_server_add_scene: null argument");
+    HX_CHECK_ARG(!s->running.load(), "hx_server_add_scene: add scenes before hx_server_start");
+    SceneBatch* b = new SceneBatch();
+    b->scene = scene;
+    hx_status st = batch_init(s, b);
+    if (st != HX_OK) {
+        batch_free(s, b);
+        return st;
+    }
+    *scene_id = (uint32_t)s->batches.size();
+    s->batches.push_back(b);
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_start(hx_server* s) {
+    HX_CHECK_ARG(s && !s->running.load(), "hx_server_start: already running");
+    s->running.store(true);
+    s->worker = std::thread(worker_main, s);
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_submit(hx_server* s, const hx_request_desc* d, uint64_t* request_id) {
+    HX_CHECK_ARG(s && d && request_id, "hx_server_submit: null argument");
+    HX_CHECK_ARG(d->scene_id < s->batches.size(), "hx_server_submit: unknown scene %u", d->scene_id);
+    HX_CHECK_ARG(d->width > 0 && d->height > 0 && (uint64_t)d->width * d->height <= 64ull << 20 && d->spp >= 1,
+                 "hx_server_submit: bad request size");
+    HX_CHECK_ARG(d->tonemap_op <= 2, "hx_server_submit: bad tone-map operator");
+    if (s->worker_error.load()) {
+        hx_set_error("server worker failed: %s", s->worker_msg);
+        return (hx_status)s->worker_error.load();
+    }
+    ServerRequest* r = new ServerRequest();
+    r->desc = *d;
+    r->arena_bytes = request_bytes(*d);
+    if (r->arena_bytes > s->arena_bytes) {
+        delete r;
+        hx_set_error("hx_server_submit: request needs %zu bytes, the arena holds %zu", request_bytes(*d), s->arena_bytes);
+        return HX_ERR_OOM_BUDGET;
+    }
+    cudaError_t e = cudaMallocHost(&r->host_ldr, 4ull * d->width * d->height);
+    if (e != cudaSuccess) {
+        delete r;
+        hx_set_error("hx_server_submit: pinned result buffer: %s", cudaGetErrorString(e));
+        return HX_ERR_DEVICE;
+    }
+    r->t_submit = now_s();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->id = s->next_id++;
+        s->all[r->id] = r;
+        s->pending.push_back(r);
+    }
+    s->cv.notify_all();
+    *request_id = r->id;
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_poll(hx_server* s, hx_request_result* out, uint32_t capacity, uint32_t* count,
+                                    double wait_seconds) {
+    HX_CHECK_ARG(s && count, "hx_server_poll: null argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (s->completed.empty() && wait_seconds > 0)
+        s->cv.wait_for(lk, std::chrono::duration<double>(wait_seconds),
+                       [&] { return !s->completed.empty() || s->worker_error.load() != 0; });
+    if (s->worker_error.load()) {
+        hx_set_error("server worker failed: %s", s->worker_msg);
+        return (hx_status)s->worker_error.load();
+    }
+    uint32_t n = (uint32_t)std::min<size_t>(capacity, s->completed.size());
+    if (out) std::copy(s->completed.begin(), s->completed.begin() + n, out);
+    s->completed.erase(s->completed.begin(), s->completed.begin() + n);
+    *count = n;
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_fetch(hx_server* s, uint64_t request_id, uint8_t* host_rgba8) {
+    HX_CHECK_ARG(s, "hx_server_fetch: null server");
+    ServerRequest* r = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->all.find(request_id);
+        HX_CHECK_ARG(it != s->all.end(), "hx_server_fetch: unknown request %llu", (unsigned long long)request_id);
+        r = it->second;
+        if (!r->done) {
+            hx_set_error("hx_server_fetch: request %llu not finished", (unsigned long long)request_id);
+            return HX_ERR_NOT_READY;
+        }
+        s->all.erase(it);
+    }
+    if (host_rgba8) std::memcpy(host_rgba8, r->host_ldr, 4ull * r->desc.width * r->desc.height);
+    cudaFreeHost(r->host_ldr);
+    delete r;
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_stats_get(hx_server* s, hx_server_stats* out) {
+    HX_CHECK_ARG(s && out, "hx_server_stats_get: null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->paths = s->paths_total;
+    out->ticks = s->ticks_total;
+    out->requests_done = s->requests_done;
+    out->requests_pending = s->pending.size();
+    out->requests_active = s->admitted.size();
+    size_t free_b = 0;
+    for (auto& kv : s->arena_free) free_b += kv.second;
+    out->arena_bytes = s->arena_bytes;
+    out->arena_used = s->arena_bytes - free_b;
+    out->seconds = now_s() - s->t_start;
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_destroy(hx_server* s) {
+    if (!s) return HX_OK;
+    if (s->running.load()) {
+        s->running.store(false);
+        s->cv.notify_all();
+        if (s->worker.joinable()) s->worker.join();
+    }
+    for (SceneBatch* b : s->batches) batch_free(s, b);
+    for (auto& kv : s->all) {
+        if (kv.second->host_ldr) cudaFreeHost(kv.second->host_ldr);
+        delete kv.second;
+    }
+    if (s->arena) hx_free(s->ctx, s->arena);
+    if (s->d_slots) hx_free(s->ctx, s->d_slots);
+    delete s;
+    return HX_OK;
+}

@@ -1,0 +1,363 @@
+// wavefront.cuh — the wavefront stages shared by the progressive integrator
+// (integrator.cu) and the serving loop (server.cu): path-state queues, ray
+// generation, closest-hit / shade / shadow kernels, accumulation and tone
+// map.  Kernels live in an anonymous namespace (one copy per translation
+// unit).
+#pragma once
+
+#include "shade.cuh"
+
+namespace {
+
+
+constexpr uint32_t kAnyHitFlag = 0x80000000u;
+constexpr int kTraceThreads = 128;
+constexpr int kShadeThreads = 128;
+constexpr int kGenThreads = 256;
+
+struct Queues {
+    float4* o[2];       // (origin, tmin)
+    float4* d[2];       // (direction, tmax)
+    uint32_t* p[2];     // path id | any-hit flag
+    float4* hit;        // (t, prim bits, u, v)
+    float4* so;         // shadow (origin, tmax)
+    float4* sd;         // shadow (direction, any-hit flag bits)
+    float4* sc;         // shadow (contribution, path id bits)
+    float4* T;          // throughput + depth bits
+    float4* L;          // radiance
+    uint2* rng;
+    uint32_t* counters; // [0],[1] ray queues, [2] shadow queue, [4],[5] trace / shadow fetch cursors
+    unsigned long long* stats;  // [0] extension rays, [1] shadow rays
+    uint32_t* status;   // bit 0: traversal stack overflow
+};
+
+struct Rect {
+    uint32_t x0, y0, w, h;
+};
+
+// Warp-aggregated queue append: one atomic per warp, slots in lane order.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    const uint32_t active = __activemask();
+    const uint32_t mask = __ballot_sync(active, pred);
+    if (mask == 0) return 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(active, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uint32_t frame0, uint32_t nframes,
+                         uint32_t kind, Queues q) {
+    uint32_t npix = rect.w * rect.h;
+    uint32_t total = npix * nframes;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        uint32_t fr = p / npix, pix = p - fr * npix;
+        uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        Rng rng = rng_init(kind, x, y, W, frame0 + fr);
+        V3 o, d;
+        generate_ray(f, kind, x, y, W, H, rng, o, d);
+        q.T[p] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+        q.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        q.rng[p] = make_uint2(rng.s0, rng.s1);
+        q.o[0][p] = make_float4(o.x, o.y, o.z, 0.001f);
+        q.d[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+        q.p[0][p] = p | kAnyHitFlag;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        q.counters[0] = total;
+        q.counters[1] = 0;
+        q.counters[2] = 0;
+    }
+}
+
+// Persistent-warp closest-hit kernel: lanes pull rays from the queue with
+// warp-aggregated atomics (counter at fetch[0]) and refill as soon as their
+// ray finishes.
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads) k_trace(DevScene s, const float4* __restrict__ qo,
+                                                         const float4* __restrict__ qd, const uint32_t* __restrict__ qp,
+                                                         const uint32_t* __restrict__ count, float4* __restrict__ hits,
+                                                         unsigned long long* stats, uint32_t* status, uint32_t* fetch) {
+    const uint32_t n = *count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)n);
+    const uint32_t lane = threadIdx.x & 31u;
+    bool overflow = false;
+    TraverseCount cnt;
+    uint2 stack[kStackSize];
+    TravState st;
+    uint32_t ray = kNoHit;  // kNoHit: lane needs a ray
+    bool done = false;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xffffffffu, ray == kNoHit && !done);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need & (1u << lane)) {
+                const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+                if (i < n) {
+                    ray = i;
+                    const float4 o = qo[i], d = qd[i];
+                    trav_init(st, s, v3(o), v3(d), o.w, d.w, (qp[i] & kAnyHitFlag) != 0);
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray != kNoHit) == 0) break;
+        if (ray != kNoHit) {
+            if (trav_step<false, COUNT>(st, stack, s, overflow, &cnt)) {
+                hits[ray] = st.best != kNoHit ? make_float4(st.best_t, __uint_as_float(st.best), st.bu, st.bv)
+                                              : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                ray = kNoHit;
+            }
+        }
+    }
+    if (COUNT) {
+        atomicAdd(&stats[2], (unsigned long long)cnt.nodes);
+        atomicAdd(&stats[3], (unsigned long long)cnt.tris);
+    }
+    if (overflow) atomicOr(status, 1u);
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, uint32_t max_bounces, float bias, int cur,
+                                                         Queues q) {
+    const uint32_t n = q.counters[cur];
+    const int nxt = cur ^ 1;
+    const uint32_t num_lights = s.num_lights;
+    // grid-stride with warp-uniform trip count so the append ballots see whole warps
+    uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t start = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t iters = (n + stride - 1) / stride;
+    for (uint32_t it = 0; it < iters; ++it) {
+        uint32_t i = start + it * stride;
+        bool active = i < n;
+        bool emit_shadow = false, emit_ray = false;
+        float4 so = make_float4(0, 0, 0, 0), sd = make_float4(0, 0, 0, 0), sc = make_float4(0, 0, 0, 0);
+        float4 no = make_float4(0, 0, 0, 0), nd = make_float4(0, 0, 0, 0);
+        uint32_t path = 0;
+        if (active) {
+            path = q.p[cur][i] & ~kAnyHitFlag;
+            float4 Tw = q.T[path];
+            float4 Lw = q.L[path];
+            uint2 rs = q.rng[path];
+            Rng rng{rs.x, rs.y};
+            V3 T = v3(Tw), L = v3(Lw);
+            uint32_t depth = __float_as_uint(Tw.w);
+            float4 rd = q.d[cur][i];
+            V3 d = v3(rd);
+            float4 h = q.hit[i];
+            uint32_t prim = __float_as_uint(h.y);
+            if (prim == kNoHit) {
+                V3 e = env_lookup(s.env, d);
+                L = L + (depth == 0 ? e : T * e);
+                q.L[path] = make_float4(L.x, L.y, L.z, 0.0f);
+            } else {
+                Surface p = populate(s, prim, h.z, h.w);
+                if (depth == 0 && !is_black(p.emissive)) L = L + p.emissive;
+                V3 Wo = -d;
+                if (num_lights > 0) {
+                    uint32_t li = next_uint(P.rng, rng, num_lights);
+                    V3 Wi;
+                    float pdf, stmax;
+                    bool trace_it;
+                    V3 Li = sample_light(s, P, p, li, rng, Wi, pdf, stmax, trace_it);
+                    if (trace_it && !is_black(Li)) {
+                        V3 Wh = normalize(Wo + Wi);
+                        V3 brdf = evaluate_uber(p, Wo, Wh, Wi);
+                        float cos_theta = gclamp(dot(p.normal, Wi), 0.0f, 1.0f);
+                        V3 c = ((T * brdf) * cos_theta) * Li;
+                        if (pdf != 0.0f) c = c / pdf;
+                        c = c * (float)num_lights;
+                        V3 o = p.position + p.normal * bias;
+                        so = make_float4(o.x, o.y, o.z, stmax);
+                        sd = make_float4(Wi.x, Wi.y, Wi.z, __uint_as_float(depth == 0 ? 1u : 0u));
+                        sc = make_float4(c.x, c.y, c.z, __uint_as_float(path));
+                        emit_shadow = true;
+                    }
+                }
+                if ((depth + 1) < max_bounces) {
+                    V3 Wi;
+                    float pdf;
+                    V3 brdf = sample_uber(P.rng, p, Wo, rng, Wi, pdf);
+                    float cos_theta = gclamp(dot(p.normal, Wi), 0.0f, 1.0f);
+                    V3 Tn = (T * (brdf * cos_theta)) / pdf;
+                    bool alive = true;
+                    if (depth >= P.rr_start) {
+                        float prob = gmax(Tn.x, gmax(Tn.y, Tn.z));
+                        if (P.rr_clamp) prob = gmin(prob, 1.0f);
+                        if (next_float(P.rng, rng) > prob) alive = false;
+                        else Tn = Tn * (1.0f / prob);
+                    }
+                    if (alive) {
+                        q.T[path] = make_float4(Tn.x, Tn.y, Tn.z, __uint_as_float(depth + 1));
+                        no = make_float4(p.position.x, p.position.y, p.position.z, 0.0001f);
+                        nd = make_float4(Wi.x, Wi.y, Wi.z, 10000.0f);
+                        emit_ray = true;
+                    }
+                }
+                q.L[path] = make_float4(L.x, L.y, L.z, 0.0f);
+                q.rng[path] = make_uint2(rng.s0, rng.s1);
+            }
+        }
+        uint32_t sslot = warp_append(&q.counters[2], emit_shadow);
+        if (emit_shadow) {
+            q.so[sslot] = so;
+            q.sd[sslot] = sd;
+            q.sc[sslot] = sc;
+        }
+        uint32_t rslot = warp_append(&q.counters[nxt], emit_ray);
+        if (emit_ray) {
+            q.o[nxt][rslot] = no;
+            q.d[nxt][rslot] = nd;
+            q.p[nxt][rslot] = path;
+        }
+    }
+}
+
+// Persistent-warp any-hit kernel for the shadow queue (fetch counter at
+// fetch[1]); an unoccluded entry adds its NEE contribution to its path.
+__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene s, Queues q, uint32_t* fetch) {
+    const uint32_t n = q.counters[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+    const uint32_t lane = threadIdx.x & 31u;
+    bool overflow = false;
+    uint2 stack[kStackSize];
+    TravState st;
+    uint32_t ray = kNoHit;
+    bool done = false;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xffffffffu, ray == kNoHit && !done);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need & (1u << lane)) {
+                const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+                if (i < n) {
+                    ray = i;
+                    const float4 o = q.so[i], d = q.sd[i];
+                    trav_init(st, s, v3(o), v3(d), 0.0001f, o.w, __float_as_uint(d.w) != 0u);
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray != kNoHit) == 0) break;
+        if (ray != kNoHit) {
+            if (trav_step<true, false>(st, stack, s, overflow, nullptr)) {
+                if (st.best == kNoHit) {
+                    const float4 c = q.sc[ray];
+                    const uint32_t path = __float_as_uint(c.w);
+                    const float4 L = q.L[path];
+                    q.L[path] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+                }
+                ray = kNoHit;
+            }
+        }
+    }
+    if (overflow) atomicOr(q.status, 1u);
+}
+
+// Accumulation (path_trace_rgen.glsl:217-248): clamp, then running mean
+// prev + (c - prev) / num_frames with frame 0 stored raw; or Kahan sum.
+__global__ void k_accumulate(Rect rect, uint32_t W, uint32_t frame0, uint32_t nframes, float clampv, uint32_t kahan,
+                             const float4* __restrict__ L, float4* __restrict__ acc, float4* __restrict__ comp) {
+    uint32_t npix = rect.w * rect.h;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
+        uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        size_t idx = (size_t)y * W + x;
+        float4 a = acc[idx];
+        float4 cp = kahan ? comp[idx] : make_float4(0, 0, 0, 0);
+        for (uint32_t f = 0; f < nframes; ++f) {
+            float4 l = L[(size_t)f * npix + pix];
+            float c[3] = {l.x, l.y, l.z};
+            if (clampv > 0.0f)
+                for (int k = 0; k < 3; ++k) c[k] = gmin(c[k], clampv);
+            uint32_t frame = frame0 + f;
+            float* av = &a.x;
+            float* cv = &cp.x;
+            for (int k = 0; k < 3; ++k) {
+                if (kahan) {
+                    float yk = c[k] - cv[k];
+                    float tk = av[k] + yk;
+                    cv[k] = (tk - av[k]) - yk;
+                    av[k] = tk;
+                } else {
+                    av[k] = frame == 0 ? c[k] : av[k] + (c[k] - av[k]) / (float)frame;
+                }
+            }
+            a.w = 1.0f;
+        }
+        acc[idx] = a;
+        if (kahan) comp[idx] = cp;
+    }
+}
+
+// tone_map.frag:22-51, R8G8B8A8_UNORM, vertical flip.
+__global__ void k_tonemap(const float4* __restrict__ acc, const float* __restrict__ inv_count, uint32_t W, uint32_t H,
+                          uint32_t op, float exposure, uchar4* __restrict__ out) {
+    uint32_t n = W * H;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t x = i % W, y = i / W;
+        size_t src = (size_t)(H - 1 - y) * W + x;
+        float4 c = acc[src];
+        float sc = inv_count ? inv_count[src] : 1.0f;
+        float v[3] = {c.x * sc, c.y * sc, c.z * sc};
+        unsigned char o[3];
+        for (int k = 0; k < 3; ++k) {
+            float t = v[k] * exposure;
+            if (op == HX_TONEMAP_ACES) {
+                const float a = 2.51f, b = 0.03f, cc = 2.43f, d = 0.59f, e = 0.14f;
+                t = gclamp((t * (a * t + b)) / (t * (cc * t + d) + e), 0.0f, 1.0f);
+            } else if (op == HX_TONEMAP_REINHARD) {
+                t = t / (1.0f + t);
+            }
+            t = powf(t, 1.0f / 2.2f);
+            o[k] = (unsigned char)(gclamp(t, 0.0f, 1.0f) * 255.0f + 0.5f);
+        }
+        out[i] = make_uchar4(o[0], o[1], o[2], 255);
+    }
+}
+
+// Resolved image: running mean as is; Kahan sum divided by the per-pixel
+// sample count.
+__global__ void k_resolve(const float4* __restrict__ acc, const uint32_t* __restrict__ count_map, uint32_t n, uint32_t kahan,
+                          float4* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 a = acc[i];
+        if (kahan) {
+            uint32_t c = count_map[i];
+            float s = c ? 1.0f / (float)c : 0.0f;
+            a = make_float4(a.x * s, a.y * s, a.z * s, 1.0f);
+        }
+        out[i] = a;
+    }
+}
+
+__global__ void k_count_add(Rect rect, uint32_t W, uint32_t add, uint32_t* __restrict__ count_map) {
+    uint32_t npix = rect.w * rect.h;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
+        uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        count_map[(size_t)y * W + x] += add;
+    }
+}
+
+Policy make_policy(const hx_policy& p) {
+    Policy P;
+    P.rng = p.rng;
+    P.rr_start = p.rr_start_depth;
+    P.rr_clamp = p.rr_clamp;
+    P.area_count_x = p.area_count_from_x;
+    P.area_w_one = p.area_w_one;
+    P.env_importance = p.env_sampling == HX_ENV_SAMPLE_IMPORTANCE;
+    P.clampv = p.radiance_clamp;
+    return P;
+}
+
+
+}  // namespace

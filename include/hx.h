@@ -421,6 +421,64 @@ HX_API hx_status hx_rng_streams(hx_context* ctx, uint32_t rng_kind, const uint32
                                 uint32_t num_streams, uint32_t draws_per_stream,
                                 uint32_t* host_out);
 
+/* ------------------------------------------------------------------------ */
+/* Serving loop (no reference counterpart; the nearest hook is the per-frame   */
+/* Renderer::render, src/engine/gfx/renderer.cpp:107, that the application    */
+/* loop calls once per window frame, application.cpp:38-54)                   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct hx_server hx_server;
+
+typedef struct hx_server_desc {
+    uint64_t  request_arena_bytes;  /* HBM for per-request images: the admission budget */
+    uint32_t  max_paths_per_tick;   /* wavefront capacity of one scene tick             */
+    uint32_t  max_ray_bounces;
+    hx_policy policy;
+} hx_server_desc;
+
+typedef struct hx_request_desc {
+    uint32_t      scene_id;          /* from hx_server_add_scene                  */
+    uint32_t      width, height;
+    uint32_t      spp;               /* progressive samples per pixel             */
+    uint32_t      denoise;           /* reserved (0)                              */
+    uint32_t      tonemap_op;        /* HX_TONEMAP_*                              */
+    float         exposure;
+    uint32_t      reserved;
+    hx_frame_desc frame;             /* camera constants of the view              */
+    uint64_t      user_tag;
+} hx_request_desc;
+
+typedef struct hx_request_result {
+    uint64_t  request_id, user_tag;
+    uint64_t  paths;                 /* camera samples traced for the request     */
+    double    queue_ms;              /* submit -> admitted                        */
+    double    latency_ms;            /* submit -> tone-mapped image in host memory */
+    hx_status status;
+    uint32_t  reserved;
+} hx_request_result;
+
+typedef struct hx_server_stats {
+    uint64_t paths, ticks, requests_done, requests_pending, requests_active;
+    uint64_t arena_bytes, arena_used;
+    double   seconds;
+} hx_server_stats;
+
+HX_API hx_status hx_server_create(hx_context* ctx, const hx_server_desc* desc, hx_server** out);
+/* Makes a resident scene servable (captures its tick as a CUDA graph). */
+HX_API hx_status hx_server_add_scene(hx_server* server, const hx_scene* scene, uint32_t* scene_id);
+/* Starts the worker thread (admission, batching, launches). */
+HX_API hx_status hx_server_start(hx_server* server);
+/* Thread-safe, non-blocking. */
+HX_API hx_status hx_server_submit(hx_server* server, const hx_request_desc* request, uint64_t* request_id);
+/* Completed requests since the last poll; waits up to wait_seconds for one. */
+HX_API hx_status hx_server_poll(hx_server* server, hx_request_result* out, uint32_t capacity, uint32_t* count,
+                                double wait_seconds);
+/* Copies a finished request's RGBA8 image (width*height*4, may be NULL) and
+ * releases it. */
+HX_API hx_status hx_server_fetch(hx_server* server, uint64_t request_id, uint8_t* host_rgba8);
+HX_API hx_status hx_server_stats_get(hx_server* server, hx_server_stats* out);
+HX_API hx_status hx_server_destroy(hx_server* server);
+
 /* Allocation-free Morton sort.  No counterpart in the reference.  For callers
  * that cannot allocate device memory (an engine whose own allocator owns all
  * device memory, a process that may not grow its footprint after start-up, a

@@ -1,0 +1,100 @@
+"""GPU tests of the serving loop (hx_server_*): continuous batching of
+requests of different scenes, resolutions and sample counts; each result is
+the same alone and in the mix (bit-exact RGBA8, the same as the progressive
+integrator's image); admission by the HBM arena budget."""
+import numpy as np
+import pytest
+
+import helios_gb300 as hx
+from tests.helpers import small_icosphere_scene
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scenes(gpu_ctx):
+    box = hx.HostScene(hx.SCENE_BOX)
+    ico = small_icosphere_scene(level=3, quads=3000, pool=4, mask=64, env=(256, 128))
+    s_box, s_ico = hx.Scene(gpu_ctx, box), hx.Scene(gpu_ctx, ico)
+    yield (box, s_box), (ico, s_ico)
+    s_box.close()
+    s_ico.close()
+
+
+def _wait_all(srv, ids, timeout=120.0):
+    import time
+    done = {}
+    t0 = time.time()
+    while len(done) < len(ids):
+        for r in srv.poll(wait_seconds=0.5):
+            done[r.request_id] = r
+        assert time.time() - t0 < timeout, "requests did not finish"
+    return done
+
+
+def _reference_image(ctx, scene, hs, w, h, spp, pol, bounces):
+    it = hx.PathIntegrator(ctx, scene, w, h, max_ray_bounces=bounces, max_samples=spp, policy=pol)
+    it.render(hx.frame_desc(hs.camera(), w, h), spp)
+    img = it.tonemap(hx.TONEMAP_ACES, 1.0)
+    it.close()
+    return img
+
+
+def test_results_identical_alone_and_in_the_mix(gpu_ctx, scenes):
+    (box, s_box), (ico, s_ico) = scenes
+    pol = hx.policy_reference()
+    pol.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
+    srv = hx.Server(gpu_ctx, arena_bytes=1 << 30, max_paths_per_tick=1 << 20, max_ray_bounces=6, policy=pol)
+    ib, ii = srv.add_scene(s_box), srv.add_scene(s_ico)
+    srv.start()
+    reqs = [  # (scene id, host scene, device scene, w, h, spp)
+        (ib, box, s_box, 256, 256, 16),
+        (ii, ico, s_ico, 320, 180, 4),
+        (ib, box, s_box, 640, 360, 2),
+        (ii, ico, s_ico, 1280, 720, 2),   # one sample per tick (921,600 px)
+        (ib, box, s_box, 1920, 1080, 1),  # larger than a tick: split into pixel chunks
+        (ii, ico, s_ico, 96, 54, 64),
+    ]
+    # alone: one request in the server at a time
+    alone = []
+    for sid, hs, sc, w, h, spp in reqs:
+        rid = srv.submit(sid, hx.frame_desc(hs.camera(), w, h), w, h, spp)
+        _wait_all(srv, [rid])
+        alone.append(srv.fetch(rid))
+    # the mix: all at once
+    ids = [srv.submit(sid, hx.frame_desc(hs.camera(), w, h), w, h, spp) for sid, hs, sc, w, h, spp in reqs]
+    res = _wait_all(srv, ids)
+    mixed = [srv.fetch(i) for i in ids]
+    for k, (a, m) in enumerate(zip(alone, mixed)):
+        assert np.array_equal(a, m), k
+        assert res[ids[k]].paths == reqs[k][3] * reqs[k][4] * reqs[k][5]
+    st = srv.stats()
+    srv.close()
+    assert st.requests_done == 2 * len(reqs)
+    # and identical to the progressive integrator's image for the same view
+    for k in (0, 1, 4):
+        sid, hs, sc, w, h, spp = reqs[k]
+        ref = _reference_image(gpu_ctx, sc, hs, w, h, spp, pol, 6)
+        assert np.array_equal(ref, alone[k]), k
+
+
+def test_admission_by_hbm_budget(gpu_ctx, scenes):
+    (box, s_box), _ = scenes
+    # arena for about two 512x512 requests (20 B per pixel each)
+    srv = hx.Server(gpu_ctx, arena_bytes=11 << 20, max_paths_per_tick=1 << 18, max_ray_bounces=4)
+    sid = srv.add_scene(s_box)
+    srv.start()
+    with pytest.raises(hx.HxError) as e:
+        srv.submit(sid, hx.frame_desc(box.camera(), 1024, 1024), 1024, 1024, 1)
+    assert e.value.status == hx.HX_ERR_OOM_BUDGET
+    ids = [srv.submit(sid, hx.frame_desc(box.camera(), 512, 512), 512, 512, 8) for _ in range(6)]
+    res = _wait_all(srv, ids)
+    queued = sorted(res[i].queue_ms for i in ids)
+    # at most two fit at a time: later requests waited for memory to free up
+    assert queued[-1] > queued[0]
+    imgs = [srv.fetch(i) for i in ids]
+    for im in imgs[1:]:
+        assert np.array_equal(im, imgs[0])
+    st = srv.stats()
+    assert st.arena_used == 0
+    srv.close()
