@@ -46,6 +46,12 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--serving", action="store_true", help="serving workload (Poisson request stream)")
+    p.add_argument("--rate", type=float, default=200.0)
+    p.add_argument("--duration", type=float, default=8.0)
+    p.add_argument("--scenes", type=int, default=8)
+    p.add_argument("--tick-paths", type=int, default=4 << 20)
+    p.add_argument("--arena-gb", type=float, default=64.0)
     return p.parse_args()
 
 
@@ -346,11 +352,99 @@ def run_ours(args, dist):
         print(json.dumps(line), flush=True)
 
 
+RESOLUTIONS = [(256, 256), (1280, 720), (1920, 1080), (3840, 2160)]
+SPPS = [1, 4, 16, 64]
+
+
+def run_serving(args, dist):
+    """Serving workload: Poisson arrivals at args.rate req/s for args.duration
+    seconds over a pool of resident procedural scenes; each request draws a
+    random camera, a resolution from RESOLUTIONS, spp from SPPS and a denoise
+    flag.  Reports throughput and p50/p99 latency (submit -> tone-mapped image
+    in host memory) of the completed requests, overall and per class."""
+    import numpy as np
+    import helios_gb300 as hx
+    ctx = hx.Context(dist.local)
+    rng = np.random.default_rng(1234)
+    pol = make_policy(hx)
+    srv = hx.Server(ctx, arena_bytes=int(args.arena_gb * (1 << 30)), max_paths_per_tick=args.tick_paths,
+                    max_ray_bounces=DEPTH, policy=pol)
+    pool = []
+    t0 = time.time()
+    for k in range(args.scenes):
+        if k < 2:
+            hs = hx.HostScene(hx.SCENE_BOX)
+        else:
+            hs = hx.HostScene(hx.SCENE_ICOSPHERES, seed=1000 + k)
+        sc = hx.Scene(ctx, hs)
+        pool.append((hs, sc, srv.add_scene(sc)))
+    build_s = time.time() - t0
+    srv.start()
+    # warm up every scene's graph once
+    for hs, sc, sid in pool:
+        rid = srv.submit(sid, hx.frame_desc(hs.camera(), 64, 64), 64, 64, 1)
+        while not [r for r in srv.poll(wait_seconds=1.0)]:
+            pass
+        srv.fetch(rid)
+    n_req = int(args.rate * args.duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n_req))
+    meta = {}
+    results = []
+    start = time.perf_counter()
+    s0 = srv.stats()
+    i = 0
+    while i < n_req:
+        now = time.perf_counter() - start
+        while i < n_req and arrivals[i] <= now:
+            hs, sc, sid = pool[int(rng.integers(len(pool)))]
+            w, h = RESOLUTIONS[int(rng.integers(4))]
+            spp = SPPS[int(rng.integers(4))]
+            cam = hs.camera()
+            for a in range(3):
+                cam.position[a] += float(rng.normal(0, 0.05 if sid < 2 else 1.0))
+            denoise = int(rng.random() < 0.5)
+            rid = srv.submit(sid, hx.frame_desc(cam, w, h), w, h, spp, user_tag=i)
+            meta[rid] = (w, h, spp, denoise, sid)
+            i += 1
+        for r in srv.poll(wait_seconds=0.0005):
+            results.append(r)
+            srv.fetch(r.request_id)
+    elapsed = time.perf_counter() - start
+    for r in srv.poll(wait_seconds=0.0):
+        results.append(r)
+        srv.fetch(r.request_id)
+    s1 = srv.stats()
+    paths = s1.paths - s0.paths
+    srv.close()
+
+    def pct(v, q):
+        return float(np.percentile(v, q)) if len(v) else None
+
+    lat = [r.latency_ms for r in results]
+    classes = {}
+    for r in results:
+        w, h, spp, dn, sid = meta[r.request_id]
+        classes.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.latency_ms)
+    offered = sum(w * h * spp for (w, h, spp, dn, sid) in meta.values())
+    line = {"metric": "serving latency p50/p99 (ms) and Mpaths/s", "mode": "serving", "n_gpus": 1,
+            "rate_req_per_s": args.rate, "duration_s": args.duration, "requests_submitted": n_req,
+            "requests_completed": len(results), "scenes": args.scenes, "scene_build_s": build_s,
+            "throughput_mpaths_per_s": paths / elapsed / 1e6, "offered_mpaths_per_s": offered / args.duration / 1e6,
+            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+            "per_class_latency_ms": {k: {"n": len(v), "p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(classes.items())},
+            "tick_paths": args.tick_paths, "arena_gb": args.arena_gb, "denoise": "flag recorded; no denoiser applied",
+            "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.serving:
+            if dist.rank == 0:
+                run_serving(args, dist)
+        elif args.impl == "reference":
             run_reference(args, dist)
         else:
             run_ours(args, dist)

@@ -309,6 +309,13 @@ static void admit(hx_server* s) {
             ++it;
             continue;
         }
+        // pinned host buffer for the result, held from admission to fetch
+        if (cudaMallocHost(&r->host_ldr, 4ull * r->desc.width * r->desc.height) != cudaSuccess) {
+            arena_release(s, off, r->arena_bytes);
+            r->host_ldr = nullptr;
+            ++it;
+            continue;
+        }
         r->arena_off = off;
         r->slot = s->free_slots.back();
         s->free_slots.pop_back();
@@ -553,12 +560,6 @@ extern "C" hx_status hx_server_submit(hx_server* s, const hx_request_desc* d, ui
         delete r;
         hx_set_error("hx_server_submit: request needs %zu bytes, the arena holds %zu", request_bytes(*d), s->arena_bytes);
         return HX_ERR_OOM_BUDGET;
-    }
-    cudaError_t e = cudaMallocHost(&r->host_ldr, 4ull * d->width * d->height);
-    if (e != cudaSuccess) {
-        delete r;
-        hx_set_error("hx_server_submit: pinned result buffer: %s", cudaGetErrorString(e));
-        return HX_ERR_DEVICE;
     }
     r->t_submit = now_s();
     {
