@@ -143,7 +143,8 @@ class ProceduralParams(C.Structure):
 
 class ServerDesc(C.Structure):
     _fields_ = [("request_arena_bytes", C.c_uint64), ("max_paths_per_tick", C.c_uint32),
-                ("max_ray_bounces", C.c_uint32), ("policy", Policy)]
+                ("max_ray_bounces", C.c_uint32), ("policy", Policy), ("result_arena_bytes", C.c_uint64),
+                ("admitted_work_paths", C.c_uint64), ("max_concurrent_ticks", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class RequestDesc(C.Structure):

@@ -128,6 +128,8 @@ struct ServerRequest {
     double t_submit = 0, t_admit = 0, t_done = 0;
     int slot = -1;
     size_t arena_off = 0, arena_bytes = 0;
+    size_t host_off = 0, host_bytes = 0;
+    uint64_t work = 0;  // camera samples of the whole request
     float4* acc = nullptr;
     uchar4* ldr = nullptr;
     uint8_t* host_ldr = nullptr;  // pinned
@@ -170,10 +172,14 @@ struct hx_server {
     char* arena = nullptr;
     size_t arena_bytes = 0;
     std::map<size_t, size_t> arena_free;  // offset -> size
+    char* harena = nullptr;               // pinned host arena for finished images
+    size_t harena_bytes = 0;
+    std::map<size_t, size_t> harena_free;
+    uint64_t admitted_work = 0;           // remaining camera samples of admitted requests
     // queues
     std::mutex mu;
     std::condition_variable cv;
-    std::deque<ServerRequest*> pending;
+    std::multimap<uint64_t, ServerRequest*> pending;  // by total work: smallest first
     std::vector<ServerRequest*> admitted;
     std::map<uint64_t, ServerRequest*> all;
     std::vector<hx_request_result> completed;
@@ -192,34 +198,39 @@ static size_t request_bytes(const hx_request_desc& d) {
     return ((16 * npix + 255) & ~(size_t)255) + ((4 * npix + 255) & ~(size_t)255);
 }
 
-static bool arena_alloc(hx_server* s, size_t bytes, size_t* off) {
-    for (auto it = s->arena_free.begin(); it != s->arena_free.end(); ++it) {
+// First-fit sub-allocation in an arena described by its free map (offset -> size).
+static bool arena_alloc(std::map<size_t, size_t>& fm, size_t bytes, size_t* off) {
+    for (auto it = fm.begin(); it != fm.end(); ++it) {
         if (it->second >= bytes) {
             *off = it->first;
             size_t rest = it->second - bytes;
             size_t noff = it->first + bytes;
-            s->arena_free.erase(it);
-            if (rest) s->arena_free[noff] = rest;
+            fm.erase(it);
+            if (rest) fm[noff] = rest;
             return true;
         }
     }
     return false;
 }
 
-static void arena_release(hx_server* s, size_t off, size_t bytes) {
-    auto it = s->arena_free.emplace(off, bytes).first;
+static void arena_release(std::map<size_t, size_t>& fm, size_t off, size_t bytes) {
+    auto it = fm.emplace(off, bytes).first;
     auto next = std::next(it);
-    if (next != s->arena_free.end() && it->first + it->second == next->first) {
+    if (next != fm.end() && it->first + it->second == next->first) {
         it->second += next->second;
-        s->arena_free.erase(next);
+        fm.erase(next);
     }
-    if (it != s->arena_free.begin()) {
+    if (it != fm.begin()) {
         auto prev = std::prev(it);
         if (prev->first + prev->second == it->first) {
             prev->second += it->second;
-            s->arena_free.erase(it);
+            fm.erase(it);
         }
     }
+}
+
+static uint64_t remaining_work(const ServerRequest* r) {
+    return (uint64_t)(r->desc.spp - r->samples_done) * r->desc.width * r->desc.height - r->pixel_cursor;
 }
 
 static hx_status batch_init(hx_server* s, SceneBatch* b) {
@@ -299,23 +310,28 @@ static void batch_free(hx_server* s, SceneBatch* b) {
     delete b;
 }
 
-// Admit pending requests whose images fit the arena (first fit, in arrival order).
+// Admit pending requests, smallest total work first, while the admitted
+// remaining work stays under the cap and both arenas (device image, pinned
+// host result) have room; a request that does not fit is skipped, not
+// blocking smaller ones behind it.
 static void admit(hx_server* s) {
     for (auto it = s->pending.begin(); it != s->pending.end();) {
-        ServerRequest* r = *it;
+        ServerRequest* r = it->second;
         if (s->free_slots.empty()) break;
-        size_t off;
-        if (!arena_alloc(s, r->arena_bytes, &off)) {
+        if (!s->admitted.empty() && s->admitted_work + r->work > s->desc.admitted_work_paths) break;
+        size_t off, hoff;
+        if (!arena_alloc(s->arena_free, r->arena_bytes, &off)) {
             ++it;
             continue;
         }
-        // pinned host buffer for the result, held from admission to fetch
-        if (cudaMallocHost(&r->host_ldr, 4ull * r->desc.width * r->desc.height) != cudaSuccess) {
-            arena_release(s, off, r->arena_bytes);
-            r->host_ldr = nullptr;
+        if (!arena_alloc(s->harena_free, r->host_bytes, &hoff)) {
+            arena_release(s->arena_free, off, r->arena_bytes);
             ++it;
             continue;
         }
+        r->host_off = hoff;
+        r->host_ldr = (uint8_t*)(s->harena + hoff);
+        s->admitted_work += r->work;
         r->arena_off = off;
         r->slot = s->free_slots.back();
         s->free_slots.pop_back();
@@ -385,6 +401,7 @@ static hx_status retire_tick(hx_server* s, SceneBatch* b) {
         ServerRequest* r = pc.r;
         r->in_flight = false;
         r->paths_traced += (uint64_t)pc.nsamples * pc.npix;
+        s->admitted_work -= std::min<uint64_t>(s->admitted_work, (uint64_t)pc.nsamples * pc.npix);
         uint32_t npix_img = r->desc.width * r->desc.height;
         if (pc.npix == npix_img && r->pixel_cursor == 0) r->samples_done += pc.nsamples;
         else {
@@ -429,7 +446,7 @@ static void complete_finished(hx_server* s, SceneBatch* b) {
         s->requests_done++;
         // release the device slot and arena space; the pinned LDR copy stays until fetch
         s->free_slots.push_back(r->slot);
-        arena_release(s, r->arena_off, r->arena_bytes);
+        arena_release(s->arena_free, r->arena_off, r->arena_bytes);
         r->slot = -1;
         s->admitted.erase(std::find(s->admitted.begin(), s->admitted.end(), r));
     }
@@ -468,13 +485,31 @@ static void worker_main(hx_server* s) {
         hx_status st = upload_new_slots(s, setup, fresh);
         if (st == HX_OK) {
             std::unique_lock<std::mutex> lk(s->mu);
+            uint32_t ticking = 0;
             for (uint32_t k = 0; k < s->batches.size() && st == HX_OK; ++k) {
                 SceneBatch* b = s->batches[k];
                 if (b->finish_busy && cudaEventQuery(b->finish_ev) == cudaSuccess) complete_finished(s, b);
                 if (b->busy && cudaEventQuery(b->done) == cudaSuccess) st = retire_tick(s, b);
-                if (st == HX_OK && !b->busy && !b->finish_busy) st = launch_tick(s, b, k);
-                if (b->busy || b->finish_busy) idle = false;
+                if (b->busy) ++ticking;
             }
+            // start ticks up to the concurrency limit, scene of the globally
+            // smallest remaining request first (shortest remaining work)
+            while (st == HX_OK && ticking < s->desc.max_concurrent_ticks) {
+                int best = -1;
+                uint64_t best_work = ~0ull;
+                for (ServerRequest* r : s->admitted) {
+                    if (r->in_flight || r->finishing || r->samples_done >= r->desc.spp) continue;
+                    SceneBatch* b = s->batches[r->desc.scene_id];
+                    if (b->busy || b->finish_busy) continue;
+                    uint64_t w = remaining_work(r);
+                    if (w < best_work) { best_work = w; best = (int)r->desc.scene_id; }
+                }
+                if (best < 0) break;
+                st = launch_tick(s, s->batches[best], (uint32_t)best);
+                ++ticking;
+            }
+            for (SceneBatch* b : s->batches)
+                if (b->busy || b->finish_busy) idle = false;
             if (!s->completed.empty()) s->cv.notify_all();
         }
         if (st != HX_OK) {
@@ -502,6 +537,9 @@ extern "C" hx_status hx_server_create(hx_context* ctx, const hx_server_desc* des
     hx_server* s = new hx_server();
     s->ctx = ctx;
     s->desc = *desc;
+    if (!s->desc.result_arena_bytes) s->desc.result_arena_bytes = std::max<uint64_t>(1u << 20, desc->request_arena_bytes / 4);
+    if (!s->desc.admitted_work_paths) s->desc.admitted_work_paths = 4ull * desc->max_paths_per_tick;
+    if (!s->desc.max_concurrent_ticks) s->desc.max_concurrent_ticks = 4;
     hx_status st = hx_alloc(ctx, (void**)&s->arena, desc->request_arena_bytes);
     if (st != HX_OK) {
         delete s;
@@ -509,6 +547,14 @@ extern "C" hx_status hx_server_create(hx_context* ctx, const hx_server_desc* des
     }
     s->arena_bytes = desc->request_arena_bytes;
     s->arena_free[0] = s->arena_bytes;
+    if (cudaMallocHost(&s->harena, s->desc.result_arena_bytes) != cudaSuccess) {
+        hx_free(ctx, s->arena);
+        delete s;
+        hx_set_error("hx_server_create: pinned result arena of %llu bytes", (unsigned long long)s->desc.result_arena_bytes);
+        return HX_ERR_OOM_BUDGET;
+    }
+    s->harena_bytes = s->desc.result_arena_bytes;
+    s->harena_free[0] = s->harena_bytes;
     st = hx_alloc(ctx, (void**)&s->d_slots, sizeof(SlotDev) * kMaxSlots);
     if (st != HX_OK) {
         hx_free(ctx, s->arena);
@@ -556,9 +602,12 @@ extern "C" hx_status hx_server_submit(hx_server* s, const hx_request_desc* d, ui
     ServerRequest* r = new ServerRequest();
     r->desc = *d;
     r->arena_bytes = request_bytes(*d);
-    if (r->arena_bytes > s->arena_bytes) {
+    r->host_bytes = (4ull * d->width * d->height + 255) & ~(size_t)255;
+    r->work = (uint64_t)d->width * d->height * d->spp;
+    if (r->arena_bytes > s->arena_bytes || r->host_bytes > s->harena_bytes) {
         delete r;
-        hx_set_error("hx_server_submit: request needs %zu bytes, the arena holds %zu", request_bytes(*d), s->arena_bytes);
+        hx_set_error("hx_server_submit: request needs %zu device / %zu host bytes, the arenas hold %zu / %zu",
+                     request_bytes(*d), (size_t)(4ull * d->width * d->height), s->arena_bytes, s->harena_bytes);
         return HX_ERR_OOM_BUDGET;
     }
     r->t_submit = now_s();
@@ -566,7 +615,7 @@ extern "C" hx_status hx_server_submit(hx_server* s, const hx_request_desc* d, ui
         std::lock_guard<std::mutex> lk(s->mu);
         r->id = s->next_id++;
         s->all[r->id] = r;
-        s->pending.push_back(r);
+        s->pending.emplace(r->work, r);
     }
     s->cv.notify_all();
     *request_id = r->id;
@@ -606,7 +655,11 @@ extern "C" hx_status hx_server_fetch(hx_server* s, uint64_t request_id, uint8_t*
         s->all.erase(it);
     }
     if (host_rgba8) std::memcpy(host_rgba8, r->host_ldr, 4ull * r->desc.width * r->desc.height);
-    cudaFreeHost(r->host_ldr);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        arena_release(s->harena_free, r->host_off, r->host_bytes);
+    }
+    s->cv.notify_all();
     delete r;
     return HX_OK;
 }
@@ -636,10 +689,8 @@ extern "C" hx_status hx_server_destroy(hx_server* s) {
         if (s->worker.joinable()) s->worker.join();
     }
     for (SceneBatch* b : s->batches) batch_free(s, b);
-    for (auto& kv : s->all) {
-        if (kv.second->host_ldr) cudaFreeHost(kv.second->host_ldr);
-        delete kv.second;
-    }
+    for (auto& kv : s->all) delete kv.second;
+    if (s->harena) cudaFreeHost(s->harena);
     if (s->arena) hx_free(s->ctx, s->arena);
     if (s->d_slots) hx_free(s->ctx, s->d_slots);
     delete s;

@@ -430,10 +430,14 @@ HX_API hx_status hx_rng_streams(hx_context* ctx, uint32_t rng_kind, const uint32
 typedef struct hx_server hx_server;
 
 typedef struct hx_server_desc {
-    uint64_t  request_arena_bytes;  /* HBM for per-request images: the admission budget */
-    uint32_t  max_paths_per_tick;   /* wavefront capacity of one scene tick             */
+    uint64_t  request_arena_bytes;  /* HBM for per-request images: the admission budget  */
+    uint32_t  max_paths_per_tick;   /* wavefront capacity of one scene tick              */
     uint32_t  max_ray_bounces;
     hx_policy policy;
+    uint64_t  result_arena_bytes;   /* pinned host memory for finished images (0: 1/4 of the HBM arena) */
+    uint64_t  admitted_work_paths;  /* admit while admitted remaining work <= this (0: 4 ticks) */
+    uint32_t  max_concurrent_ticks; /* scene ticks in flight at once (0: 4)                */
+    uint32_t  reserved;
 } hx_server_desc;
 
 typedef struct hx_request_desc {

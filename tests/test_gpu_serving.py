@@ -21,13 +21,18 @@ def scenes(gpu_ctx):
     s_ico.close()
 
 
-def _wait_all(srv, ids, timeout=120.0):
+def _wait_all(srv, ids, timeout=120.0, images=None):
+    """Waits for the requests; with images (a dict) fetches each result as
+    it arrives (finished images hold the pinned result arena until fetched,
+    so a client that never fetches stalls admission)."""
     import time
     done = {}
     t0 = time.time()
     while len(done) < len(ids):
         for r in srv.poll(wait_seconds=0.5):
             done[r.request_id] = r
+            if images is not None:
+                images[r.request_id] = srv.fetch(r.request_id)
         assert time.time() - t0 < timeout, "requests did not finish"
     return done
 
@@ -88,11 +93,12 @@ def test_admission_by_hbm_budget(gpu_ctx, scenes):
         srv.submit(sid, hx.frame_desc(box.camera(), 1024, 1024), 1024, 1024, 1)
     assert e.value.status == hx.HX_ERR_OOM_BUDGET
     ids = [srv.submit(sid, hx.frame_desc(box.camera(), 512, 512), 512, 512, 8) for _ in range(6)]
-    res = _wait_all(srv, ids)
+    got = {}
+    res = _wait_all(srv, ids, images=got)
     queued = sorted(res[i].queue_ms for i in ids)
     # at most two fit at a time: later requests waited for memory to free up
     assert queued[-1] > queued[0]
-    imgs = [srv.fetch(i) for i in ids]
+    imgs = [got[i] for i in ids]
     for im in imgs[1:]:
         assert np.array_equal(im, imgs[0])
     st = srv.stats()
