@@ -52,6 +52,11 @@ def parse():
     p.add_argument("--scenes", type=int, default=8)
     p.add_argument("--tick-paths", type=int, default=4 << 20)
     p.add_argument("--arena-gb", type=float, default=64.0)
+    p.add_argument("--precision", action="store_true", help="precision-form report (terrain scene)")
+    p.add_argument("--terrain-size", type=int, default=4096)
+    p.add_argument("--spp", type=int, default=256)
+    p.add_argument("--ref-spp", type=int, default=1024)
+    p.add_argument("--ref-pixels", type=int, default=64)
     return p.parse_args()
 
 
@@ -437,11 +442,84 @@ def run_serving(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args, dist):
+    """Precision form at scale: 200 spheres + a terrain_size^2 fBm heightfield,
+    1920x1080, FP16 ray/hit payloads, FP32 traversal, Kahan FP32 accumulation
+    to args.spp samples.  Reports throughput, the relative RMSE of the FP16
+    and FP32-payload images against the FP64 oracle (args.ref_spp samples, the
+    same seeds, on a seeded pixel subset), and the primary hit-ID agreement of
+    FP16-direction rays with FP32 rays; the quantised 8-bit BVH itself is
+    hit-exact against the unquantised binary tree (bit-exact tests)."""
+    import numpy as np
+    import helios_gb300 as hx
+    from oracle import binding as ob
+    ctx = hx.Context(dist.local)
+    t0 = time.time()
+    hs = hx.HostScene(hx.SCENE_TERRAIN, terrain_size=args.terrain_size)
+    scene = hx.Scene(ctx, hs)
+    info = scene.info()
+    t_scene = time.time() - t0
+    W, H = WIDTH, HEIGHT
+    f = hx.frame_desc(hs.camera(), W, H)
+    out = {"metric": "precision form: relative RMSE vs FP64 oracle", "mode": "precision", "n_gpus": 1,
+           "scene": {"triangles": info.num_triangles, "bvh8_nodes": info.num_bvh8_nodes, "build_ms": info.build_ms,
+                     "device_mb": info.device_bytes / 2**20, "setup_s": t_scene},
+           "width": W, "height": H, "spp": args.spp, "ref_spp": args.ref_spp, "data": "synthetic"}
+    imgs = {}
+    for name, fp16, kahan in (("fp16_kahan", True, True), ("fp32", False, False)):
+        pol = hx.policy_reference()
+        pol.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
+        pol.payload = hx.PAYLOAD_FP16 if fp16 else hx.PAYLOAD_FP32
+        pol.accumulation = hx.ACCUM_KAHAN if kahan else hx.ACCUM_RUNNING_MEAN
+        it = hx.PathIntegrator(ctx, scene, W, H, max_ray_bounces=DEPTH, max_samples=args.spp, policy=pol)
+        e0, e1 = hx.Event(ctx), hx.Event(ctx)
+        ctx.synchronize()
+        e0.record()
+        it.render(f, args.spp)
+        e1.record()
+        ms = e0.elapsed_ms(e1)
+        imgs[name] = it.read_accumulation()[:, :, :3].reshape(-1, 3).astype(np.float64)
+        out[name + "_mpaths_per_s"] = W * H * args.spp / (ms / 1000.0) / 1e6
+        it.close()
+    # FP64 oracle (FP32 payload semantics, reference policy) on a pixel subset
+    osc = ob.OracleScene(hs)
+    d = hx.IntegratorDesc()
+    d.width, d.height, d.max_ray_bounces, d.max_samples = W, H, DEPTH, 1 << 30
+    d.policy = hx.policy_reference()
+    d.policy.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
+    pix = np.random.default_rng(11).choice(W * H, size=args.ref_pixels, replace=False).astype(np.uint32)
+    t1 = time.time()
+    ref, cnt = osc.render(d, f, args.ref_spp, precision=64, pixels=pix)
+    out["oracle_s"] = time.time() - t1
+
+    def rr(a):
+        return float(np.linalg.norm(a - ref) / np.linalg.norm(ref))
+    out["rel_rmse_vs_fp64"] = {k: rr(v[pix]) for k, v in imgs.items()}
+    out["rel_rmse_fp16_vs_fp32_full_frame"] = float(np.linalg.norm(imgs["fp16_kahan"] - imgs["fp32"]) /
+                                                    np.linalg.norm(imgs["fp32"]))
+    # primary hit-ID agreement, FP16-direction vs FP32 rays (oracle's bit-exact traversal on a subset)
+    d16 = hx.IntegratorDesc()
+    d16.width, d16.height, d16.max_ray_bounces, d16.max_samples = W, H, 1, 1
+    d16.policy = hx.policy_reference()
+    d16.policy.payload = hx.PAYLOAD_FP16
+    sub = np.random.default_rng(12).choice(W * H, size=65536, replace=False).astype(np.uint32)
+    _, h16 = osc.sample_radiance(d16, f, 0, precision=32, pixels=sub)
+    r32 = ob.primary_rays(d16, f, 0)[sub]
+    gh = scene.trace(r32, any_hit=True)
+    out["primary_hit_agreement_fp16_vs_fp32"] = float((h16["prim"] == gh["prim"]).mean())
+    osc.close()
+    scene.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.serving:
+        if args.precision:
+            if dist.rank == 0:
+                run_precision(args, dist)
+        elif args.serving:
             if dist.rank == 0:
                 run_serving(args, dist)
         elif args.impl == "reference":

@@ -24,7 +24,7 @@ ACCUM_RUNNING_MEAN, ACCUM_KAHAN = 0, 1
 ENV_SAMPLE_COSINE, ENV_SAMPLE_IMPORTANCE = 0, 1
 PAYLOAD_FP32, PAYLOAD_FP16 = 0, 1
 TONEMAP_ACES, TONEMAP_REINHARD, TONEMAP_NONE = 0, 1, 2
-SCENE_BOX, SCENE_ICOSPHERES = 0, 1
+SCENE_BOX, SCENE_ICOSPHERES, SCENE_TERRAIN = 0, 1, 2
 SUBMESH_NON_OPAQUE = 1
 NO_HIT = 0xFFFFFFFF
 
@@ -138,7 +138,7 @@ class ProceduralParams(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("num_alpha_quads", C.c_uint32),
                 ("mask_pool", C.c_uint32), ("mask_size", C.c_uint32), ("icosphere_level", C.c_uint32),
                 ("env_width", C.c_uint32), ("env_height", C.c_uint32), ("sun_elevation_deg", C.c_float),
-                ("turbidity", C.c_float)]
+                ("turbidity", C.c_float), ("terrain_size", C.c_uint32), ("num_spheres", C.c_uint32)]
 
 
 class ServerDesc(C.Structure):

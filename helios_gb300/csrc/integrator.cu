@@ -173,7 +173,7 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     it->grid_trace = std::max(1, per_sm) * ctx->num_sms;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow, kTraceThreads, 0));
     it->grid_shadow = std::max(1, per_sm) * ctx->num_sms;
-    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade, kShadeThreads, 0));
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     it->grid_shade = std::max(1, per_sm) * ctx->num_sms;
     it->grid_gen = ctx->num_sms * 8;
     compute_tiles(it);
@@ -235,10 +235,14 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
     Policy P = make_policy(it->desc.policy);
     uint32_t npix = rect.w * rect.h;
     uint32_t total = npix * nframes;
+    const bool fp16 = it->desc.policy.payload == HX_PAYLOAD_FP16;
     it->stats.paths += total;
     {
         StageTimer t(it, &it->stats.ms_raygen);
-        k_raygen<<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, P.rng, it->q);
+        if (fp16)
+            k_raygen<true><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, P.rng, it->q);
+        else
+            k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, P.rng, it->q);
         it->stats.kernel_launches++;
     }
     for (uint32_t b = 0; b < it->desc.max_ray_bounces; ++b) {
@@ -246,14 +250,18 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
         {
             StageTimer t(it, &it->stats.ms_trace);
             HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 8, st));
-            if (it->counting)
-                k_trace<true><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q.o[cur], it->q.d[cur], it->q.p[cur],
-                                                                       it->q.counters + cur, it->q.hit, it->q.stats, it->q.status,
-                                                                       it->q.counters + 4);
-            else
-                k_trace<false><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q.o[cur], it->q.d[cur], it->q.p[cur],
-                                                                        it->q.counters + cur, it->q.hit, it->q.stats, it->q.status,
-                                                                        it->q.counters + 4);
+#define HX_TRACE(COUNT, FP16)                                                                                       \
+    k_trace<COUNT, FP16><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q.o[cur], it->q.d[cur], it->q.p[cur],     \
+                                                                   it->q.counters + cur, it->q.hit, it->q.stats,     \
+                                                                   it->q.status, it->q.counters + 4)
+            if (it->counting) {
+                if (fp16) HX_TRACE(true, true);
+                else HX_TRACE(true, false);
+            } else {
+                if (fp16) HX_TRACE(false, true);
+                else HX_TRACE(false, false);
+            }
+#undef HX_TRACE
             it->stats.trace_launches++;
             it->stats.kernel_launches++;
         }
@@ -261,7 +269,10 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
         HX_CUDA(cudaMemsetAsync(it->q.counters + 2, 0, 4, st));
         {
             StageTimer t(it, &it->stats.ms_shade);
-            k_shade<<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
+            if (fp16)
+                k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
+            else
+                k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
             it->stats.kernel_launches++;
         }
         {
@@ -440,7 +451,7 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     HX_CHECK_ARG((uint64_t)W * H <= it->capacity, "frame exceeds wavefront capacity");
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
-    k_raygen<<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
+    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
     k_trace<false><<<it->grid_trace, kTraceThreads, 0, st>>>(it->scene->d, it->q.o[0], it->q.d[0], it->q.p[0], it->q.counters,
                                                              it->q.hit, it->q.stats, it->q.status, it->q.counters + 4);

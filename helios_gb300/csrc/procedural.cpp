@@ -404,6 +404,113 @@ hx_status build_icospheres(hx_host_scene* s, const hx_procedural_params& P) {
     return HX_OK;
 }
 
+// Periodic value-noise fBm over [0,1)^2 (6 octaves), for terrain heights.
+float fbm(const std::vector<float>& lat, uint32_t g, float x, float y) {
+    float sum = 0.0f, amp = 0.5f, freq = 1.0f;
+    for (int o = 0; o < 6; ++o) {
+        float fx = x * g * freq, fy = y * g * freq;
+        float x0f = std::floor(fx), y0f = std::floor(fy);
+        float tx = fx - x0f, ty = fy - y0f;
+        tx = tx * tx * (3 - 2 * tx);
+        ty = ty * ty * (3 - 2 * ty);
+        uint32_t gs = g * (1u << o);
+        uint32_t x0 = (uint32_t)x0f % gs, y0 = (uint32_t)y0f % gs, x1 = (x0 + 1) % gs, y1 = (y0 + 1) % gs;
+        // lattice values hashed from the base lattice (one table for every octave)
+        auto L = [&](uint32_t i, uint32_t j) { return lat[((i * 73856093u) ^ (j * 19349663u) ^ (o * 83492791u)) % lat.size()]; };
+        float a = L(x0, y0), b = L(x1, y0), c = L(x0, y1), d = L(x1, y1);
+        float top = a + (b - a) * tx, bot = c + (d - c) * tx;
+        sum += amp * (top + (bot - top) * ty);
+        amp *= 0.5f;
+        freq *= 2.0f;
+    }
+    return sum;
+}
+
+// Terrain scene (precision form at scale): num_spheres seeded subdivided
+// spheres over an N x N-vertex fBm heightfield (2 (N-1)^2 triangles), sun and
+// Hosek-Wilkie sky.
+hx_status build_terrain(hx_host_scene* s, const hx_procedural_params& P) {
+    Rng64 rng(P.seed ^ 0x7e77a1ull);
+    const uint32_t N = std::max<uint32_t>(2, P.terrain_size);
+    const float extent = 4096.0f, hmax = 300.0f;
+    s->materials.push_back(make_material(0.35f, 0.30f, 0.22f, 0.9f, 0.0f));  // 0 terrain
+    for (uint32_t i = 0; i < 16; ++i) {
+        float r = (float)rng.uniform(), g = (float)rng.uniform(), b = (float)rng.uniform();
+        s->materials.push_back(make_material(r, g, b, (float)rng.uniform(0.05, 1.0), rng.uniform() < 0.3 ? 1.0f : 0.0f));
+    }
+    std::vector<float> lat(1 << 16);
+    for (auto& v : lat) v = (float)rng.uniform();
+    // mesh 0: heightfield
+    s->vertices.emplace_back(); s->indices.emplace_back(); s->submeshes.emplace_back();
+    {
+        auto& vs = s->vertices.back();
+        auto& ix = s->indices.back();
+        vs.resize((size_t)N * N);
+        std::vector<float> h((size_t)N * N);
+        for (uint32_t j = 0; j < N; ++j)
+            for (uint32_t i = 0; i < N; ++i) h[(size_t)j * N + i] = hmax * fbm(lat, 4, (float)i / N, (float)j / N);
+        const float step = extent / (float)(N - 1);
+        for (uint32_t j = 0; j < N; ++j)
+            for (uint32_t i = 0; i < N; ++i) {
+                uint32_t il = i ? i - 1 : i, ir = i + 1 < N ? i + 1 : i, jd = j ? j - 1 : j, ju = j + 1 < N ? j + 1 : j;
+                float dx = (h[(size_t)j * N + ir] - h[(size_t)j * N + il]) / ((ir - il) * step);
+                float dz = (h[(size_t)ju * N + i] - h[(size_t)jd * N + i]) / ((ju - jd) * step);
+                float nx = -dx, ny = 1.0f, nz = -dz;
+                float nl = std::sqrt(nx * nx + ny * ny + nz * nz);
+                vs[(size_t)j * N + i] = make_vertex(-extent * 0.5f + i * step, h[(size_t)j * N + i], -extent * 0.5f + j * step,
+                                                    0.0f, nx / nl, ny / nl, nz / nl, (float)i / (N - 1), (float)j / (N - 1));
+            }
+        ix.reserve((size_t)6 * (N - 1) * (N - 1));
+        for (uint32_t j = 0; j + 1 < N; ++j)
+            for (uint32_t i = 0; i + 1 < N; ++i) {
+                uint32_t a = j * N + i, b = a + 1, c = a + N, d = c + 1;
+                const uint32_t t[6] = {a, c, b, b, c, d};
+                ix.insert(ix.end(), t, t + 6);
+            }
+        s->submeshes.back() = {{0, (uint32_t)ix.size(), 0, 0}};
+    }
+    // mesh 1: sphere
+    s->vertices.emplace_back(); s->indices.emplace_back(); s->submeshes.emplace_back();
+    icosphere(P.icosphere_level, s->vertices.back(), s->indices.back());
+    s->submeshes.back() = {{0, (uint32_t)s->indices.back().size(), 1, 0}};
+    float I[16];
+    identity(I);
+    add_instance(s, 0, I, I, -1);
+    for (uint32_t k = 0; k < P.num_spheres; ++k) {
+        double u1 = rng.uniform(), u2 = rng.uniform(), u3 = rng.uniform();
+        double q[4] = {std::sqrt(1 - u1) * std::sin(2 * 3.14159265358979323846 * u2),
+                       std::sqrt(1 - u1) * std::cos(2 * 3.14159265358979323846 * u2),
+                       std::sqrt(u1) * std::sin(2 * 3.14159265358979323846 * u3),
+                       std::sqrt(u1) * std::cos(2 * 3.14159265358979323846 * u3)};
+        double scale = rng.uniform(5.0, 40.0);
+        double t[3] = {rng.uniform(-600, 600), rng.uniform(hmax, hmax + 200), rng.uniform(-600, 600)};
+        float model[16], normal[16];
+        trs(q, scale, t, model, normal);
+        add_instance(s, 1, model, normal, 1 + (int32_t)(k % 16));
+    }
+    // sun (directional) + sky
+    hx_environment_desc& e = s->desc.environment;
+    e.kind = HX_ENV_HOSEK_WILKIE;
+    e.width = P.env_width;
+    e.height = P.env_height;
+    double el = P.sun_elevation_deg * 3.14159265358979323846 / 180.0, az = 40.0 * 3.14159265358979323846 / 180.0;
+    e.sun_direction[0] = (float)(std::cos(el) * std::sin(az));
+    e.sun_direction[1] = (float)std::sin(el);
+    e.sun_direction[2] = (float)(std::cos(el) * std::cos(az));
+    hx_status st = hx_hosek_wilkie_coefficients(e.sun_direction, P.turbidity, 1.15f, e.coeffs);
+    if (st != HX_OK) return st;
+    hx_light sun;
+    std::memset(&sun, 0, sizeof(sun));
+    sun.data0[0] = (float)HX_LIGHT_DIRECTIONAL;
+    sun.data0[1] = 1.0f; sun.data0[2] = 0.95f; sun.data0[3] = 0.85f;
+    for (int a = 0; a < 3; ++a) sun.data1[a] = -e.sun_direction[a];  // light forward: from the sun
+    sun.data1[3] = 3.0f;
+    sun.data2[3] = 0.01f;
+    s->lights.push_back(sun);
+    s->camera = hx_camera{{0.0f, hmax + 350.0f, 1100.0f}, {0.0f, hmax * 0.5f, 0.0f}, {0.0f, 1.0f, 0.0f}, 50.0f, 1.0f, 10000.0f, 8.0f, 0.0f};
+    return HX_OK;
+}
+
 }  // namespace
 
 extern "C" void hx_procedural_defaults(uint32_t kind, hx_procedural_params* p) {
@@ -418,19 +525,22 @@ extern "C" void hx_procedural_defaults(uint32_t kind, hx_procedural_params* p) {
     p->env_height = 1024;
     p->sun_elevation_deg = 30.0f;
     p->turbidity = 3.0f;
+    p->terrain_size = 4096;
+    p->num_spheres = 200;
+    if (kind == HX_SCENE_TERRAIN) p->icosphere_level = 4;
 }
 
 extern "C" hx_status hx_procedural_scene_create(const hx_procedural_params* params, hx_host_scene** out) {
     if (!params || !out) { hx_set_error("hx_procedural_scene_create: null argument"); return HX_ERR_INVALID_ARG; }
-    if (params->kind > HX_SCENE_ICOSPHERES || params->icosphere_level > 8 || params->mask_size > 4096 ||
-        params->mask_size == 0 || params->env_width < 2 || params->env_height < 2) {
+    if (params->kind > HX_SCENE_TERRAIN || params->icosphere_level > 8 || params->mask_size > 4096 ||
+        params->mask_size == 0 || params->env_width < 2 || params->env_height < 2 || params->terrain_size > 8192) {
         hx_set_error("hx_procedural_scene_create: bad parameters");
         return HX_ERR_INVALID_ARG;
     }
     std::unique_ptr<hx_host_scene> s(new hx_host_scene());
     if (params->kind == HX_SCENE_BOX) build_box(s.get());
     else {
-        hx_status st = build_icospheres(s.get(), *params);
+        hx_status st = params->kind == HX_SCENE_ICOSPHERES ? build_icospheres(s.get(), *params) : build_terrain(s.get(), *params);
         if (st != HX_OK) return st;
     }
     hx_environment_desc env = s->desc.environment;

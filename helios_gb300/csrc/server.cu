@@ -270,7 +270,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     int per_sm = 0;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false>, kTraceThreads, 0));
     const int grid_trace = std::max(1, per_sm) * ctx->num_sms;
-    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade, kShadeThreads, 0));
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     const int grid_shade = std::max(1, per_sm) * ctx->num_sms;
     const int grid_gen = ctx->num_sms * 8;
     cudaStream_t st = b->stream;
@@ -285,7 +285,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
                                                              b->q.hit, b->q.stats, b->q.status, b->q.counters + 4);
         cudaMemsetAsync(b->q.counters + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(b->q.counters + 2, 0, 4, st);
-        k_shade<<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
+        k_shade<false><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
         k_shadow<<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q, b->q.counters + 5);
     }
     k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp, b->q.L);

@@ -48,6 +48,48 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// ---------------------------------------------------------------------------
+// 16-bit payloads (precision form): an extension ray is 16 B — origin FP32
+// and the direction as two 16-bit signed-normalised octahedral coordinates
+// (FP16 coordinates spend their precision near zero and left 19% of the
+// terrain's primary hits on a different triangle; snorm16 spacing is uniform,
+// 2/65534).  tmin/tmax follow from the ray kind (primary 0.001 / secondary
+// 0.0001, tmax 10000).  A hit record is 8 B — triangle id and FP16
+// barycentrics.  Traversal stays FP32.
+// ---------------------------------------------------------------------------
+HXD uint32_t snorm16(float x) {
+    float q = rintf(fminf(fmaxf(x, -1.0f), 1.0f) * 32767.0f);
+    return (uint32_t)(int32_t)q & 0xffffu;
+}
+HXD float unsnorm16(uint32_t b) { return (float)(int32_t)(int16_t)(uint16_t)b / 32767.0f; }
+HXD uint32_t oct_encode(V3 d) {
+    float l1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+    float u = d.x / l1, v = d.y / l1;
+    if (d.z < 0.0f) {
+        float nu = (1.0f - fabsf(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        float nv = (1.0f - fabsf(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+        u = nu;
+        v = nv;
+    }
+    return snorm16(u) | (snorm16(v) << 16);
+}
+HXD V3 oct_decode(uint32_t bits) {
+    float u = unsnorm16(bits & 0xffffu), v = unsnorm16(bits >> 16);
+    float z = 1.0f - fabsf(u) - fabsf(v);
+    if (z < 0.0f) {
+        float nu = (1.0f - fabsf(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        float nv = (1.0f - fabsf(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+        u = nu;
+        v = nv;
+    }
+    return normalize(v3(u, v, z));
+}
+HXD uint32_t half2_bits(float a, float b) {
+    __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+template <bool FP16>
 __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uint32_t frame0, uint32_t nframes,
                          uint32_t kind, Queues q) {
     uint32_t npix = rect.w * rect.h;
@@ -61,8 +103,12 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
         q.T[p] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
         q.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         q.rng[p] = make_uint2(rng.s0, rng.s1);
-        q.o[0][p] = make_float4(o.x, o.y, o.z, 0.001f);
-        q.d[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+        if (FP16) {
+            q.o[0][p] = make_float4(o.x, o.y, o.z, __uint_as_float(oct_encode(d)));
+        } else {
+            q.o[0][p] = make_float4(o.x, o.y, o.z, 0.001f);
+            q.d[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+        }
         q.p[0][p] = p | kAnyHitFlag;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -75,7 +121,7 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
 // Persistent-warp closest-hit kernel: lanes pull rays from the queue with
 // warp-aggregated atomics (counter at fetch[0]) and refill as soon as their
 // ray finishes.
-template <bool COUNT>
+template <bool COUNT, bool FP16 = false>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(DevScene s, const float4* __restrict__ qo,
                                                          const float4* __restrict__ qd, const uint32_t* __restrict__ qp,
                                                          const uint32_t* __restrict__ count, float4* __restrict__ hits,
@@ -100,8 +146,14 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(DevScene s, const float
                 const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
                 if (i < n) {
                     ray = i;
-                    const float4 o = qo[i], d = qd[i];
-                    trav_init(st, s, v3(o), v3(d), o.w, d.w, (qp[i] & kAnyHitFlag) != 0);
+                    const bool any = (qp[i] & kAnyHitFlag) != 0;
+                    const float4 o = qo[i];
+                    if (FP16) {
+                        trav_init(st, s, v3(o), oct_decode(__float_as_uint(o.w)), any ? 0.001f : 0.0001f, 10000.0f, any);
+                    } else {
+                        const float4 d = qd[i];
+                        trav_init(st, s, v3(o), v3(d), o.w, d.w, any);
+                    }
                 } else {
                     done = true;
                 }
@@ -110,8 +162,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(DevScene s, const float
         if (__ballot_sync(0xffffffffu, ray != kNoHit) == 0) break;
         if (ray != kNoHit) {
             if (trav_step<false, COUNT>(st, stack, s, overflow, &cnt)) {
-                hits[ray] = st.best != kNoHit ? make_float4(st.best_t, __uint_as_float(st.best), st.bu, st.bv)
-                                              : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                if (FP16)
+                    reinterpret_cast<uint2*>(hits)[ray] =
+                        make_uint2(st.best, st.best != kNoHit ? half2_bits(st.bu, st.bv) : 0u);
+                else
+                    hits[ray] = st.best != kNoHit ? make_float4(st.best_t, __uint_as_float(st.best), st.bu, st.bv)
+                                                  : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
                 ray = kNoHit;
             }
         }
@@ -123,6 +179,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(DevScene s, const float
     if (overflow) atomicOr(status, 1u);
 }
 
+template <bool FP16>
 __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, uint32_t max_bounces, float bias, int cur,
                                                          Queues q) {
     const uint32_t n = q.counters[cur];
@@ -147,10 +204,20 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, u
             Rng rng{rs.x, rs.y};
             V3 T = v3(Tw), L = v3(Lw);
             uint32_t depth = __float_as_uint(Tw.w);
-            float4 rd = q.d[cur][i];
-            V3 d = v3(rd);
-            float4 h = q.hit[i];
-            uint32_t prim = __float_as_uint(h.y);
+            V3 d;
+            float4 h;
+            uint32_t prim;
+            if (FP16) {
+                d = oct_decode(__float_as_uint(q.o[cur][i].w));
+                const uint2 hh = reinterpret_cast<const uint2*>(q.hit)[i];
+                prim = hh.x;
+                __half2 uv = *reinterpret_cast<const __half2*>(&hh.y);
+                h = make_float4(0.0f, 0.0f, __low2float(uv), __high2float(uv));
+            } else {
+                d = v3(q.d[cur][i]);
+                h = q.hit[i];
+                prim = __float_as_uint(h.y);
+            }
             if (prim == kNoHit) {
                 V3 e = env_lookup(s.env, d);
                 L = L + (depth == 0 ? e : T * e);
@@ -194,8 +261,12 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, u
                     }
                     if (alive) {
                         q.T[path] = make_float4(Tn.x, Tn.y, Tn.z, __uint_as_float(depth + 1));
-                        no = make_float4(p.position.x, p.position.y, p.position.z, 0.0001f);
-                        nd = make_float4(Wi.x, Wi.y, Wi.z, 10000.0f);
+                        if (FP16) {
+                            no = make_float4(p.position.x, p.position.y, p.position.z, __uint_as_float(oct_encode(Wi)));
+                        } else {
+                            no = make_float4(p.position.x, p.position.y, p.position.z, 0.0001f);
+                            nd = make_float4(Wi.x, Wi.y, Wi.z, 10000.0f);
+                        }
                         emit_ray = true;
                     }
                 }
@@ -212,7 +283,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, u
         uint32_t rslot = warp_append(&q.counters[nxt], emit_ray);
         if (emit_ray) {
             q.o[nxt][rslot] = no;
-            q.d[nxt][rslot] = nd;
+            if (!FP16) q.d[nxt][rslot] = nd;
             q.p[nxt][rslot] = path;
         }
     }

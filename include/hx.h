@@ -188,7 +188,9 @@ typedef struct hx_scene_desc {
 #define HX_ENV_SAMPLE_IMPORTANCE 1u /* lat-long CDF importance sampling                   */
 
 #define HX_PAYLOAD_FP32 0u
-#define HX_PAYLOAD_FP16 1u          /* FP16 ray / hit payloads (precision form)  */
+#define HX_PAYLOAD_FP16 1u          /* 16-bit ray / hit payloads (precision form):
+                                       direction = two snorm16 octahedral coords,
+                                       barycentrics = FP16; traversal stays FP32 */
 
 typedef struct hx_policy {
     uint32_t rng;                 /* HX_RNG_*                                              */
@@ -507,6 +509,7 @@ HX_API hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n, uin
 
 #define HX_SCENE_BOX          0u  /* 5-wall box + 2 boxes + quad light (36 tris)         */
 #define HX_SCENE_ICOSPHERES   1u  /* 12 icospheres + ground + alpha quads + sky + lights */
+#define HX_SCENE_TERRAIN      2u  /* spheres + fBm heightfield + sun and sky             */
 
 typedef struct hx_procedural_params {
     uint32_t kind;           /* HX_SCENE_*                                   */
@@ -518,6 +521,8 @@ typedef struct hx_procedural_params {
     uint32_t env_width, env_height; /* default 2048 x 1024                   */
     float    sun_elevation_deg;     /* default 30                             */
     float    turbidity;             /* default 3                              */
+    uint32_t terrain_size;          /* HX_SCENE_TERRAIN: grid vertices per side (default 4096) */
+    uint32_t num_spheres;           /* HX_SCENE_TERRAIN: sphere instances (default 200)        */
 } hx_procedural_params;
 
 HX_API void      hx_procedural_defaults(uint32_t kind, hx_procedural_params* out);

@@ -1063,6 +1063,42 @@ static void generate_ray(const hx_frame_desc& f, uint32_t x, uint32_t y, uint32_
     dir = normalize(focus - aperture_pos);
 }
 
+// 16-bit payload emulation (precision form): ray directions travel as two
+// 16-bit snorm octahedral coordinates and hit barycentrics as FP16, exactly
+// like the device queues; the arithmetic below matches the device codec.
+static uint32_t snorm16_f(float x) {
+    float q = std::rint(std::fmin(std::fmax(x, -1.0f), 1.0f) * 32767.0f);
+    return (uint32_t)(int32_t)q & 0xffffu;
+}
+static float unsnorm16_f(uint32_t b) { return (float)(int32_t)(int16_t)(uint16_t)b / 32767.0f; }
+static uint32_t oct_encode_f(V3<float> d) {
+    float l1 = std::fabs(d.x) + std::fabs(d.y) + std::fabs(d.z);
+    float u = d.x / l1, v = d.y / l1;
+    if (d.z < 0.0f) {
+        float nu = (1.0f - std::fabs(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        float nv = (1.0f - std::fabs(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+        u = nu;
+        v = nv;
+    }
+    return snorm16_f(u) | (snorm16_f(v) << 16);
+}
+static V3<float> oct_decode_f(uint32_t b) {
+    float u = unsnorm16_f(b & 0xffffu), v = unsnorm16_f(b >> 16);
+    float z = 1.0f - std::fabs(u) - std::fabs(v);
+    if (z < 0.0f) {
+        float nu = (1.0f - std::fabs(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        float nv = (1.0f - std::fabs(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+        u = nu;
+        v = nv;
+    }
+    return normalize(V3<float>(u, v, z));
+}
+template <typename R> static V3<R> payload_dir(V3<R> d) {
+    V3<float> f = oct_decode_f(oct_encode_f(V3<float>((float)d.x, (float)d.y, (float)d.z)));
+    return V3<R>(R(f.x), R(f.y), R(f.z));
+}
+static float payload_bary(float x) { return half_to_float(float_to_half(x)); }
+
 // One camera sample: ray-gen + the closest-hit recursion unrolled into a
 // loop (the payload recursion of path_trace_rchit.glsl:487-536 sums L in the
 // same order: emission, direct light, then the deeper bounces).
@@ -1074,6 +1110,8 @@ static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f,
     uint32_t depth = 0;
     V3<R> o, d;
     generate_ray<R>(f, x, y, P.width, P.height, rng, o, d);
+    const bool fp16 = P.pol.payload == HX_PAYLOAD_FP16;
+    if (fp16) d = payload_dir(d);
     R tmin = R(0.001f), tmax = R(10000.0f);
     bool any_hit = true;
     uint32_t num_lights = (uint32_t)s.lights.size();
@@ -1094,7 +1132,12 @@ static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f,
             L = L + (depth == 0 ? e : T * e);
             break;
         }
-        Surface<R> p = populate<R>(s, prim, (float)hu, (float)hv);
+        float su = (float)hu, sv = (float)hv;
+        if (fp16) {
+            su = payload_bary(su);
+            sv = payload_bary(sv);
+        }
+        Surface<R> p = populate<R>(s, prim, su, sv);
         if (depth == 0 && !is_black(p.emissive)) L = L + p.emissive;
         V3<R> Wo = -d;
         if (num_lights > 0) {  // direct_lighting, rchit.glsl:455-483
@@ -1135,7 +1178,7 @@ static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f,
         T = Tn;
         depth++;
         o = p.position;
-        d = Wi;
+        d = fp16 ? payload_dir(Wi) : Wi;
         tmin = R(0.0001f);
         tmax = R(10000.0f);
         any_hit = false;
