@@ -55,8 +55,13 @@ def parse():
     p.add_argument("--precision", action="store_true", help="precision-form report (terrain scene)")
     p.add_argument("--terrain-size", type=int, default=4096)
     p.add_argument("--spp", type=int, default=256)
-    p.add_argument("--ref-spp", type=int, default=1024)
-    p.add_argument("--ref-pixels", type=int, default=64)
+    p.add_argument("--ref-pixels", type=int, default=4096)
+    p.add_argument("--denoise", action="store_true", help="learned-denoiser training + time-to-RMSE report")
+    p.add_argument("--dn-variants", type=int, default=64)
+    p.add_argument("--dn-target-spp", type=int, default=4096)
+    p.add_argument("--dn-steps", type=int, default=3000)
+    p.add_argument("--dn-ref-spp", type=int, default=4096)
+    p.add_argument("--dn-eval-seeds", type=int, nargs="+", default=[5000, 5001])
     return p.parse_args()
 
 
@@ -464,7 +469,7 @@ def run_precision(args, dist):
     out = {"metric": "precision form: relative RMSE vs FP64 oracle", "mode": "precision", "n_gpus": 1,
            "scene": {"triangles": info.num_triangles, "bvh8_nodes": info.num_bvh8_nodes, "build_ms": info.build_ms,
                      "device_mb": info.device_bytes / 2**20, "setup_s": t_scene},
-           "width": W, "height": H, "spp": args.spp, "ref_spp": args.ref_spp, "data": "synthetic"}
+           "width": W, "height": H, "spp": args.spp, "data": "synthetic"}
     imgs = {}
     for name, fp16, kahan in (("fp16_kahan", True, True), ("fp32", False, False)):
         pol = hx.policy_reference()
@@ -481,7 +486,9 @@ def run_precision(args, dist):
         imgs[name] = it.read_accumulation()[:, :, :3].reshape(-1, 3).astype(np.float64)
         out[name + "_mpaths_per_s"] = W * H * args.spp / (ms / 1000.0) / 1e6
         it.close()
-    # FP64 oracle (FP32 payload semantics, reference policy) on a pixel subset
+    # FP64 oracle (FP32-payload semantics, reference policy, the same sample
+    # sequence: spp frames) on a seeded pixel subset, so the difference is
+    # the arithmetic and payload precision, not Monte Carlo noise
     osc = ob.OracleScene(hs)
     d = hx.IntegratorDesc()
     d.width, d.height, d.max_ray_bounces, d.max_samples = W, H, DEPTH, 1 << 30
@@ -489,8 +496,9 @@ def run_precision(args, dist):
     d.policy.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
     pix = np.random.default_rng(11).choice(W * H, size=args.ref_pixels, replace=False).astype(np.uint32)
     t1 = time.time()
-    ref, cnt = osc.render(d, f, args.ref_spp, precision=64, pixels=pix)
+    ref, cnt = osc.render(d, f, args.spp, precision=64, pixels=pix)
     out["oracle_s"] = time.time() - t1
+    out["oracle_pixels"] = int(pix.size)
 
     def rr(a):
         return float(np.linalg.norm(a - ref) / np.linalg.norm(ref))
@@ -512,11 +520,133 @@ def run_precision(args, dist):
     print(json.dumps(out), flush=True)
 
 
+def conv_flops_per_pixel():
+    """Forward FLOPs per full-resolution pixel of the denoiser network
+    (2 * 9 * cin * N per output pixel of each convolution, N = MMA width)."""
+    from oracle import denoiser_ref as dr
+    lev = {"x": 0, "a0": 0, "p0": 1, "p1": 2, "p2": 3, "p3": 4, "a4": 4, "u3": 3, "u2": 2, "u1": 1, "u0": 0,
+           "d0": 0, "d0b": 0}
+    tot = 0.0
+    for (_, srcs, cout, _), (ci, co) in zip(dr.LAYERS, dr.layer_shapes()):
+        n = (co + 15) // 16 * 16
+        tot += 2.0 * 9 * ci * n / 4 ** lev[srcs[0][0]]
+    return tot
+
+
+def run_denoise(args, dist):
+    """Learned denoiser: data from this tracer, training by the library's own
+    tensor-core kernels, then time-to-RMSE at 1920x1080 on held-out variants
+    against plain accumulation."""
+    import numpy as np
+    import helios_gb300 as hx
+    from helios_gb300 import denoise_train as T
+    from oracle import denoiser_ref as dr
+    ctx = hx.Context(dist.local)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    kw = dict(quads=100000, level=6, env=(1024, 512), mask_pool=16, mask_size=256)
+    out = {"mode": "denoise", "metric": "time-to-RMSE speed-up vs plain accumulation", "n_gpus": 1,
+           "data": "synthetic: seeded variants of the icosphere scene (transforms, materials, lights, masks, sun "
+                   "U(10,80) deg, orbit camera); 100k alpha quads, 16 masks 256^2, 1024x512 sky",
+           "network": "5-level U-Net, 3x3 convs 32->128 ch, skips; BF16 weights/activations, FP32 accumulate "
+                      "(tcgen05/TMEM); %d parameters" % dr.num_params()}
+    spp_in = [1, 2, 4, 8, 16, 32, 64]
+    seeds = list(range(1000, 1000 + args.dn_variants))
+    data = T.render_pairs(ctx, seeds, 256, 256, spp_in, args.dn_target_spp, bounces=DEPTH, scene_kw=kw)
+    out["train_data"] = {"variants": len(seeds), "pairs": data.count, "crop": [256, 256], "input_spp": spp_in,
+                         "target_spp": args.dn_target_spp, "render_s": round(data.render_s, 1)}
+    dn = hx.Denoiser(ctx)
+    dn.set_params(dr.init_params(0))
+    t0 = time.time()
+    e0, e1 = hx.Event(ctx), hx.Event(ctx)
+    e0.record()
+    hist = T.train(dn, data, args.dn_steps, batch=16, lr=1e-3, lr_final=1e-4, seed=1,
+                   log_every=max(1, args.dn_steps // 10))
+    e1.record()
+    ctx.synchronize()
+    train_ms = e0.elapsed_ms(e1)
+    step_flops = 3.0 * conv_flops_per_pixel() * 16 * 256 * 256
+    out["training"] = {"steps": args.dn_steps, "batch": 16, "adam_lr": [1e-3, 1e-4], "wall_s": round(time.time() - t0, 1),
+                       "ms_per_step": train_ms / args.dn_steps,
+                       "conv_tflops": step_flops / (train_ms / args.dn_steps * 1e-3) / 1e12,
+                       "loss": [(s, round(l, 5)) for s, l in hist]}
+    data.close()
+    # held-out evaluation at 1920x1080
+    W, H = WIDTH, HEIGHT
+    evals = []
+    feat = hx.DeviceBuffer(ctx, W * H * 48)
+    den = hx.DeviceBuffer(ctx, W * H * 16)
+    checkpoints = [1, 2, 4, 8, 16, 32, 64, 128, 256]
+    for seed in args.dn_eval_seeds:
+        hs, cam = T.variant_scene(seed, **kw)
+        sc = hx.Scene(ctx, hs)
+        f = hx.frame_desc(cam, W, H)
+        it = hx.PathIntegrator(ctx, sc, W, H, max_ray_bounces=DEPTH, max_samples=1 << 30, policy=hx.policy_reference())
+        it.render(f, args.dn_ref_spp)
+        ref = it.read_accumulation()[..., 0:3].astype(np.float64)
+        it.restart_bake()
+        plain, dnz, done, frame_ms = {}, {}, 0, 0.0
+        for c in checkpoints:
+            e0.record()
+            it.render(f, c - done)
+            e1.record()
+            ctx.synchronize()
+            frame_ms += e0.elapsed_ms(e1)
+            done = c
+            img = it.read_accumulation()[..., 0:3]
+            plain[c] = T.rel_rmse(img, ref)
+            if c <= 64:
+                e0.record()
+                it.features(f, feat)
+                dn.infer(feat, 1, H, W, den)
+                e1.record()
+                dn.check()
+                dn_ms = e0.elapsed_ms(e1)
+                dnz[c] = T.rel_rmse(den.download((H, W, 4))[..., 0:3], ref)
+        frame_ms /= checkpoints[-1]
+        # inference alone (features excluded), warm
+        for _ in range(3):
+            dn.infer(feat, 1, H, W, den)
+        e0.record()
+        for _ in range(10):
+            dn.infer(feat, 1, H, W, den)
+        e1.record()
+        ctx.synchronize()
+        infer_ms = e0.elapsed_ms(e1) / 10
+        e256 = plain[256]
+        ok = [c for c in sorted(dnz) if dnz[c] <= e256]
+        s_star = ok[0] if ok else None
+        t_plain = 256 * frame_ms
+        t_den = (s_star * frame_ms + dn_ms) if s_star else None
+        evals.append({"seed": seed, "ref_spp": args.dn_ref_spp, "frame_ms": frame_ms, "features_plus_infer_ms": dn_ms,
+                      "infer_ms": infer_ms, "rel_rmse_plain": plain, "rel_rmse_denoised": dnz,
+                      "denoised_spp_reaching_plain_256": s_star,
+                      "speedup_vs_plain_256": (t_plain / t_den) if t_den else None})
+        it.close()
+        sc.close()
+    flops = conv_flops_per_pixel() * W * ((H + 15) // 16 * 16)
+    infer_ms = statistics.median(e["infer_ms"] for e in evals)
+    out["eval"] = evals
+    out["roofline"] = {"bound": "tensor", "kernel": "k_conv (forward, all 13 layers)",
+                       "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                       "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
+                       "flops_per_1080p_inference": flops, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
+    speed = [e["speedup_vs_plain_256"] for e in evals if e["speedup_vs_plain_256"]]
+    out["value"] = min(speed) if len(speed) == len(evals) else None
+    out["unit"] = "x (plain 256-spp time / denoised time at equal or lower RMSE)"
+    feat.close()
+    den.close()
+    dn.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.precision:
+        if args.denoise:
+            if dist.rank == 0:
+                run_denoise(args, dist)
+        elif args.precision:
             if dist.rank == 0:
                 run_precision(args, dist)
         elif args.serving:

@@ -161,7 +161,7 @@ class RequestResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("ticks", C.c_uint64), ("requests_done", C.c_uint64),
                 ("requests_pending", C.c_uint64), ("requests_active", C.c_uint64), ("arena_bytes", C.c_uint64),
-                ("arena_used", C.c_uint64), ("seconds", C.c_double)]
+                ("arena_used", C.c_uint64), ("seconds", C.c_double), ("requests_denoised", C.c_uint64)]
 
 
 BVH8_NODE_BYTES = 80
@@ -229,6 +229,28 @@ _SIGS = {
     "hx_host_scene_camera": (C.c_int, [_P, C.POINTER(Camera)]),
     "hx_host_scene_destroy": (C.c_int, [_P]),
     "hx_hosek_wilkie_coefficients": (C.c_int, [C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_float)]),
+    "hx_device_alloc": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
+    "hx_device_free": (C.c_int, [_P, _P]),
+    "hx_device_copy": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_uint32]),
+    "hx_denoiser_create": (C.c_int, [_P, C.POINTER(_P)]),
+    "hx_denoiser_destroy": (C.c_int, [_P]),
+    "hx_denoiser_num_params": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "hx_denoiser_set_params": (C.c_int, [_P, _P, C.c_uint64]),
+    "hx_denoiser_get_params": (C.c_int, [_P, _P, C.c_uint64]),
+    "hx_denoiser_forward_backward": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32,
+                                               C.POINTER(C.c_float)]),
+    "hx_denoiser_get_gradients": (C.c_int, [_P, _P, C.c_uint64]),
+    "hx_denoiser_adam_step": (C.c_int, [_P, C.c_float]),
+    "hx_denoiser_train_step": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
+                                         C.POINTER(C.c_float)]),
+    "hx_denoiser_infer": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
+    "hx_denoiser_check": (C.c_int, [_P]),
+    "hx_denoiser_read_tensor": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, C.c_uint64]),
+    "hx_denoiser_read_output": (C.c_int, [_P, C.c_uint32, _P, C.c_uint64]),
+    "hx_integrator_features": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
+    "hx_integrator_resolve": (C.c_int, [_P, _P]),
+    "hx_integrator_denoise": (C.c_int, [_P, _P, C.POINTER(FrameDesc), C.c_uint32, C.c_float, _P, _P]),
+    "hx_server_set_denoiser": (C.c_int, [_P, _P]),
 }
 
 _lib_handle = None
@@ -532,9 +554,151 @@ class PathIntegrator:
         check(lib().hx_integrator_sample_radiance(self.handle, C.byref(frame), frame_index, _ptr(out)))
         return out
 
+    def features(self, frame, buf, offset=0, frame_index=0):
+        """Denoiser features (width*height*12 floats) into a DeviceBuffer at a byte offset."""
+        check(lib().hx_integrator_features(self.handle, C.byref(frame), frame_index, buf.at(offset)))
+
+    def resolve(self, buf, offset=0):
+        """The accumulated image (RGBA floats) into a DeviceBuffer at a byte offset."""
+        check(lib().hx_integrator_resolve(self.handle, buf.at(offset)))
+
+    def denoise(self, denoiser, frame, op=0, exposure=1.0, hdr=True, ldr=False):
+        """Denoise the accumulated image; returns (rgba8 or None, rgba32f or None)."""
+        o8 = np.zeros((self.height, self.width, 4), np.uint8) if ldr else None
+        o32 = np.zeros((self.height, self.width, 4), np.float32) if hdr else None
+        check(lib().hx_integrator_denoise(self.handle, denoiser.handle, C.byref(frame), op, exposure, _ptr(o8),
+                                          _ptr(o32)))
+        return o8, o32
+
     def close(self):
         if self.handle:
             lib().hx_integrator_destroy(self.handle)
+            self.handle = None
+
+
+class DeviceBuffer:
+    """Device memory from a context's budgeted allocator."""
+
+    def __init__(self, ctx, nbytes):
+        h = C.c_void_p()
+        check(lib().hx_device_alloc(ctx.handle, int(nbytes), C.byref(h)))
+        self.ctx, self.ptr, self.nbytes = ctx, h.value, int(nbytes)
+
+    def at(self, offset=0):
+        if offset < 0 or offset > self.nbytes:
+            raise ValueError("offset %d outside a %d-byte buffer" % (offset, self.nbytes))
+        return C.c_void_p(self.ptr + offset)
+
+    def upload(self, array, offset=0):
+        a = np.ascontiguousarray(array)
+        if offset + a.nbytes > self.nbytes:
+            raise ValueError("upload past the end of the buffer")
+        check(lib().hx_device_copy(self.ctx.handle, self.at(offset), _ptr(a), a.nbytes, 0))
+
+    def download(self, shape, dtype=np.float32, offset=0):
+        out = np.zeros(shape, dtype)
+        if offset + out.nbytes > self.nbytes:
+            raise ValueError("download past the end of the buffer")
+        check(lib().hx_device_copy(self.ctx.handle, _ptr(out), self.at(offset), out.nbytes, 1))
+        return out
+
+    def copy_from(self, src, nbytes, dst_offset=0, src_offset=0):
+        if dst_offset + nbytes > self.nbytes or src_offset + nbytes > src.nbytes:
+            raise ValueError("copy out of range")
+        check(lib().hx_device_copy(self.ctx.handle, self.at(dst_offset), src.at(src_offset), nbytes, 2))
+
+    def close(self):
+        if self.ptr:
+            lib().hx_device_free(self.ctx.handle, C.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# Denoiser tensors in network order: (name, channels, level)
+DENOISER_TENSORS = [("x", 32, 0), ("a0", 32, 0), ("a0b", 32, 0), ("p0", 32, 1), ("a1", 64, 1), ("p1", 64, 2),
+                    ("a2", 64, 2), ("p2", 64, 3), ("a3", 96, 3), ("p3", 96, 4), ("a4", 128, 4), ("a4b", 128, 4),
+                    ("u3", 128, 3), ("d3", 96, 3), ("u2", 96, 2), ("d2", 64, 2), ("u1", 64, 1), ("d1", 64, 1),
+                    ("u0", 64, 0), ("d0", 32, 0), ("d0b", 32, 0), ("gy", 32, 0)]
+FEATURE_CHANNELS = 12
+
+
+def _bf16_to_f32(u16):
+    return (u16.astype(np.uint32) << 16).view(np.float32)
+
+
+class Denoiser:
+    """The learned denoiser (tensor-core training and inference)."""
+
+    def __init__(self, ctx):
+        h = C.c_void_p()
+        check(lib().hx_denoiser_create(ctx.handle, C.byref(h)))
+        self.handle, self.ctx = h, ctx
+        n = C.c_uint64()
+        check(lib().hx_denoiser_num_params(h, C.byref(n)))
+        self.num_params = n.value
+        self._shape = {}
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        check(lib().hx_denoiser_set_params(self.handle, _ptr(p), p.size))
+
+    def get_params(self):
+        out = np.zeros(self.num_params, np.float32)
+        check(lib().hx_denoiser_get_params(self.handle, _ptr(out), out.size))
+        return out
+
+    def gradients(self):
+        out = np.zeros(self.num_params, np.float32)
+        check(lib().hx_denoiser_get_gradients(self.handle, _ptr(out), out.size))
+        return out
+
+    def forward_backward(self, features, targets, n, h, w, feat_offset=0, tgt_offset=0):
+        loss = C.c_float()
+        check(lib().hx_denoiser_forward_backward(self.handle, features.at(feat_offset), targets.at(tgt_offset), n, h,
+                                                 w, C.byref(loss)))
+        self._shape[1] = (n, h, w)
+        return loss.value
+
+    def adam_step(self, lr):
+        check(lib().hx_denoiser_adam_step(self.handle, lr))
+
+    def train_step(self, features, targets, n, h, w, lr, feat_offset=0, tgt_offset=0, want_loss=True):
+        loss = C.c_float()
+        check(lib().hx_denoiser_train_step(self.handle, features.at(feat_offset), targets.at(tgt_offset), n, h, w, lr,
+                                           C.byref(loss) if want_loss else None))
+        self._shape[1] = (n, h, w)
+        return loss.value if want_loss else None
+
+    def infer(self, features, n, h, w, out, feat_offset=0, out_offset=0):
+        check(lib().hx_denoiser_infer(self.handle, features.at(feat_offset), n, h, w, out.at(out_offset)))
+        self._shape[0] = (n, (h + 15) // 16 * 16, (w + 15) // 16 * 16)
+
+    def check(self):
+        check(lib().hx_denoiser_check(self.handle))
+
+    def read_tensor(self, name, training=True, gradient=False):
+        idx = [t[0] for t in DENOISER_TENSORS].index(name)
+        _, c, lev = DENOISER_TENSORS[idx]
+        n, h, w = self._shape[1 if training else 0]
+        raw = np.zeros((n, h >> lev, w >> lev, c), np.uint16)
+        check(lib().hx_denoiser_read_tensor(self.handle, 1 if training else 0, idx, 1 if gradient else 0, _ptr(raw),
+                                            raw.nbytes))
+        return _bf16_to_f32(raw)
+
+    def read_output(self, training=True):
+        n, h, w = self._shape[1 if training else 0]
+        out = np.zeros((n, h, w, 4), np.float32)
+        check(lib().hx_denoiser_read_output(self.handle, 1 if training else 0, _ptr(out), out.size))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().hx_denoiser_destroy(self.handle)
             self.handle = None
 
 
@@ -562,9 +726,14 @@ class Server:
     def start(self):
         check(lib().hx_server_start(self.handle))
 
-    def submit(self, scene_id, frame, width, height, spp, tonemap_op=TONEMAP_ACES, exposure=1.0, user_tag=0):
+    def set_denoiser(self, denoiser):
+        check(lib().hx_server_set_denoiser(self.handle, denoiser.handle if denoiser else None))
+
+    def submit(self, scene_id, frame, width, height, spp, tonemap_op=TONEMAP_ACES, exposure=1.0, user_tag=0,
+               denoise=False):
         r = RequestDesc()
         r.scene_id, r.width, r.height, r.spp = scene_id, width, height, spp
+        r.denoise = 1 if denoise else 0
         r.tonemap_op, r.exposure, r.user_tag = tonemap_op, exposure, user_tag
         r.frame = frame
         rid = C.c_uint64()

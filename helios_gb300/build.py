@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompil
 CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden", "-Wall"]
 
-CU_SOURCES = ["context.cu", "sort.cu", "bvh_build.cu", "scene.cu", "integrator.cu", "server.cu"]
+CU_SOURCES = ["context.cu", "sort.cu", "bvh_build.cu", "scene.cu", "integrator.cu", "server.cu", "denoise.cu"]
 CPP_SOURCES = ["procedural.cpp"]
 
 

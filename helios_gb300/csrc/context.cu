@@ -156,6 +156,33 @@ extern "C" hx_status hx_pinned_free(void* ptr) {
     return HX_OK;
 }
 
+extern "C" hx_status hx_device_alloc(hx_context* ctx, uint64_t bytes, void** out) {
+    HX_CHECK_ARG(ctx && out && bytes > 0, "hx_device_alloc: bad argument");
+    HX_CUDA(cudaSetDevice(ctx->device));
+    return hx_alloc(ctx, out, bytes);
+}
+
+extern "C" hx_status hx_device_free(hx_context* ctx, void* ptr) {
+    HX_CHECK_ARG(ctx, "hx_device_free: null context");
+    if (ptr) {
+        HX_CUDA(cudaStreamSynchronize(ctx->stream));
+        hx_free(ctx, ptr);
+    }
+    return HX_OK;
+}
+
+extern "C" hx_status hx_device_copy(hx_context* ctx, void* dst, const void* src, uint64_t bytes, uint32_t kind) {
+    HX_CHECK_ARG(ctx && dst && src && kind <= HX_COPY_DEVICE_TO_DEVICE, "hx_device_copy: bad argument");
+    if (bytes == 0) return HX_OK;
+    const cudaMemcpyKind k = kind == HX_COPY_HOST_TO_DEVICE   ? cudaMemcpyHostToDevice
+                             : kind == HX_COPY_DEVICE_TO_HOST ? cudaMemcpyDeviceToHost
+                                                              : cudaMemcpyDeviceToDevice;
+    HX_CUDA(cudaSetDevice(ctx->device));
+    HX_CUDA(cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
+    if (kind != HX_COPY_DEVICE_TO_DEVICE) HX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return HX_OK;
+}
+
 extern "C" void hx_policy_reference(hx_policy* p) {
     std::memset(p, 0, sizeof(*p));
     p->rng = HX_RNG_XOROSHIRO64STAR;

@@ -90,6 +90,8 @@ struct hx_integrator {
     uchar4* ldr = nullptr;
     hx_hit* hits_host_layout = nullptr;
     float* rgb_tmp = nullptr;
+    float* feat = nullptr;        // denoiser features (12 floats per pixel), on first use
+    float4* denoised = nullptr;
     // progressive state (path_integrator.h:46-53)
     uint32_t accumulated = 0, tile_idx = 0;
     std::vector<Rect> tiles;
@@ -460,6 +462,57 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     HX_CUDA(cudaGetLastError());
     HX_CUDA(cudaMemcpyAsync(host, it->hits_host_layout, sizeof(hx_hit) * n, cudaMemcpyDeviceToHost, st));
     HX_TRY(check_status(it));
+    return HX_OK;
+}
+
+extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_desc* f, uint32_t frame_index,
+                                            float* d_features) {
+    HX_CHECK_ARG(it && f && d_features, "hx_integrator_features: null argument");
+    cudaStream_t st = it->ctx->stream;
+    uint32_t W = it->desc.width, H = it->desc.height, n = W * H;
+    HX_CHECK_ARG((uint64_t)n <= it->capacity, "frame exceeds wavefront capacity");
+    bool kahan = it->desc.policy.accumulation == HX_ACCUM_KAHAN;
+    k_resolve<<<it->grid_gen, kGenThreads, 0, st>>>(it->acc, it->count_map, n, kahan ? 1u : 0u, it->resolved);
+    Rect r{0, 0, W, H};
+    Policy P = make_policy(it->desc.policy);
+    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
+    HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
+    k_trace<false><<<it->grid_trace, kTraceThreads, 0, st>>>(it->scene->d, it->q.o[0], it->q.d[0], it->q.p[0], it->q.counters,
+                                                             it->q.hit, it->q.stats, it->q.status, it->q.counters + 4);
+    k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, n, d_features);
+    HX_CUDA(cudaGetLastError());
+    HX_TRY(check_status(it));
+    return HX_OK;
+}
+
+extern "C" hx_status hx_integrator_resolve(hx_integrator* it, float* d_rgba) {
+    HX_CHECK_ARG(it && d_rgba, "hx_integrator_resolve: null argument");
+    uint32_t n = it->desc.width * it->desc.height;
+    bool kahan = it->desc.policy.accumulation == HX_ACCUM_KAHAN;
+    k_resolve<<<it->grid_gen, kGenThreads, 0, it->ctx->stream>>>(it->acc, it->count_map, n, kahan ? 1u : 0u,
+                                                                  reinterpret_cast<float4*>(d_rgba));
+    HX_CUDA(cudaGetLastError());
+    return HX_OK;
+}
+
+extern "C" hx_status hx_integrator_denoise(hx_integrator* it, hx_denoiser* dn, const hx_frame_desc* f, uint32_t op,
+                                           float exposure, uint8_t* host_rgba8, float* host_rgba32f) {
+    HX_CHECK_ARG(it && dn && f && op <= 2, "hx_integrator_denoise: bad argument");
+    cudaStream_t st = it->ctx->stream;
+    uint32_t W = it->desc.width, H = it->desc.height, n = W * H;
+    if (!it->feat) {
+        HX_TRY(hx_alloc_t(it->ctx, &it->feat, 12 * (size_t)it->capacity));
+        it->allocs.push_back(it->feat);
+        HX_TRY(hx_alloc_t(it->ctx, &it->denoised, (size_t)it->capacity));
+        it->allocs.push_back(it->denoised);
+    }
+    HX_TRY(hx_integrator_features(it, f, 0, it->feat));
+    HX_TRY(hx_denoiser_infer(dn, it->feat, 1, H, W, reinterpret_cast<float*>(it->denoised)));
+    k_tonemap<<<it->grid_gen, kGenThreads, 0, st>>>(it->denoised, nullptr, W, H, op, exposure, it->ldr);
+    HX_CUDA(cudaGetLastError());
+    if (host_rgba8) HX_CUDA(cudaMemcpyAsync(host_rgba8, it->ldr, 4 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (host_rgba32f) HX_CUDA(cudaMemcpyAsync(host_rgba32f, it->denoised, 16 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    HX_TRY(hx_denoiser_check(dn));
     return HX_OK;
 }
 

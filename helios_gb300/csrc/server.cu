@@ -132,6 +132,8 @@ struct ServerRequest {
     uint64_t work = 0;  // camera samples of the whole request
     float4* acc = nullptr;
     uchar4* ldr = nullptr;
+    float* feat = nullptr;        // denoise: features (12 floats per pixel)
+    float4* den = nullptr;        // denoise: denoised radiance
     uint8_t* host_ldr = nullptr;  // pinned
     uint32_t samples_done = 0, pixel_cursor = 0;
     bool in_flight = false, finishing = false, done = false;
@@ -160,6 +162,7 @@ struct SceneBatch {
     cudaEvent_t finish_ev = nullptr;
     bool finish_busy = false;
     uint64_t ticks = 0;
+    int grid_trace = 0, grid_gen = 0;
 };
 
 struct hx_server {
@@ -189,13 +192,22 @@ struct hx_server {
     std::atomic<int> worker_error{0};
     char worker_msg[512] = "";
     // stats
-    uint64_t paths_total = 0, ticks_total = 0, requests_done = 0;
+    uint64_t paths_total = 0, ticks_total = 0, requests_done = 0, denoised = 0;
     double t_start = 0, busy_first = 0, busy_last = 0;
+    // learned denoiser for requests with denoise set (runs on the context stream)
+    hx_denoiser* denoiser = nullptr;
+    cudaEvent_t dn_ready = nullptr, dn_done = nullptr;
 };
 
+static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Arena bytes of a request: accumulation (16 B/px) + RGBA8 (4 B/px), and
+// with denoise its features (48 B/px) and denoised image (16 B/px).
 static size_t request_bytes(const hx_request_desc& d) {
     size_t npix = (size_t)d.width * d.height;
-    return ((16 * npix + 255) & ~(size_t)255) + ((4 * npix + 255) & ~(size_t)255);
+    size_t b = round256(16 * npix) + round256(4 * npix);
+    if (d.denoise) b += round256(48 * npix) + round256(16 * npix);
+    return b;
 }
 
 // First-fit sub-allocation in an arena described by its free map (offset -> size).
@@ -273,6 +285,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     const int grid_shade = std::max(1, per_sm) * ctx->num_sms;
     const int grid_gen = ctx->num_sms * 8;
+    b->grid_trace = grid_trace;
+    b->grid_gen = grid_gen;
     cudaStream_t st = b->stream;
     cudaGraph_t g;
     HX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -337,7 +351,11 @@ static void admit(hx_server* s) {
         s->free_slots.pop_back();
         size_t npix = (size_t)r->desc.width * r->desc.height;
         r->acc = (float4*)(s->arena + off);
-        r->ldr = (uchar4*)(s->arena + off + ((16 * npix + 255) & ~(size_t)255));
+        r->ldr = (uchar4*)(s->arena + off + round256(16 * npix));
+        if (r->desc.denoise) {
+            r->feat = (float*)(s->arena + off + round256(16 * npix) + round256(4 * npix));
+            r->den = (float4*)((char*)r->feat + round256(48 * npix));
+        }
         r->t_admit = now_s();
         s->admitted.push_back(r);
         it = s->pending.erase(it);
@@ -396,6 +414,35 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
     return HX_OK;
 }
 
+// Denoise a finished request: features of its sample-0 primary hits (rays
+// generated and traced in row bands that fit the batch's queues, on the
+// batch stream), then the denoiser on the context stream; the batch stream
+// waits for the result before tone mapping.
+static hx_status denoise_request(hx_server* s, SceneBatch* b, ServerRequest* r) {
+    const uint32_t W = r->desc.width, H = r->desc.height;
+    const uint32_t rows = std::max<uint32_t>(1, std::min<uint32_t>(H, s->desc.max_paths_per_tick / W));
+    const DevScene& sc = b->scene->d;
+    Policy P = make_policy(s->desc.policy);
+    for (uint32_t y0 = 0; y0 < H; y0 += rows) {
+        Rect rc{0, y0, W, std::min(rows, H - y0)};
+        const uint32_t n = rc.w * rc.h;
+        k_raygen<false><<<b->grid_gen, kGenThreads, 0, b->stream>>>(r->desc.frame, rc, W, H, 0, 1, P.rng, b->q);
+        HX_CUDA(cudaMemsetAsync(b->q.counters + 4, 0, 4, b->stream));
+        k_trace<false><<<b->grid_trace, kTraceThreads, 0, b->stream>>>(sc, b->q.o[0], b->q.d[0], b->q.p[0], b->q.counters,
+                                                                      b->q.hit, b->q.stats, b->q.status, b->q.counters + 4);
+        k_features<<<b->grid_gen, kGenThreads, 0, b->stream>>>(sc, b->q.hit, r->acc + (size_t)y0 * W, n,
+                                                              r->feat + 12 * (size_t)y0 * W);
+    }
+    HX_CUDA(cudaGetLastError());
+    HX_CUDA(cudaEventRecord(s->dn_ready, b->stream));
+    HX_CUDA(cudaStreamWaitEvent(s->ctx->stream, s->dn_ready, 0));
+    HX_TRY(hx_denoiser_infer(s->denoiser, r->feat, 1, H, W, reinterpret_cast<float*>(r->den)));
+    HX_CUDA(cudaEventRecord(s->dn_done, s->ctx->stream));
+    HX_CUDA(cudaStreamWaitEvent(b->stream, s->dn_done, 0));
+    s->denoised++;
+    return HX_OK;
+}
+
 static hx_status retire_tick(hx_server* s, SceneBatch* b) {
     for (const PendingChunk& pc : b->running) {
         ServerRequest* r = pc.r;
@@ -412,9 +459,11 @@ static hx_status retire_tick(hx_server* s, SceneBatch* b) {
             }
         }
         if (r->samples_done >= r->desc.spp) {
-            // tone map to RGBA8 and copy to the request's pinned host buffer
+            // (denoise, then) tone map to RGBA8 and copy to the request's pinned host buffer
             r->finishing = true;
-            k_tonemap<<<s->ctx->num_sms * 4, kGenThreads, 0, b->stream>>>(r->acc, nullptr, r->desc.width, r->desc.height,
+            if (r->desc.denoise) HX_TRY(denoise_request(s, b, r));
+            k_tonemap<<<s->ctx->num_sms * 4, kGenThreads, 0, b->stream>>>(r->desc.denoise ? r->den : r->acc, nullptr,
+                                                                           r->desc.width, r->desc.height,
                                                                            r->desc.tonemap_op, r->desc.exposure, r->ldr);
             HX_CUDA(cudaMemcpyAsync(r->host_ldr, r->ldr, 4ull * npix_img, cudaMemcpyDeviceToHost, b->stream));
             b->finishing.push_back(r);
@@ -562,8 +611,24 @@ extern "C" hx_status hx_server_create(hx_context* ctx, const hx_server_desc* des
         return st;
     }
     for (int k = (int)kMaxSlots - 1; k >= 0; --k) s->free_slots.push_back(k);
+    if (cudaEventCreateWithFlags(&s->dn_ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->dn_done, cudaEventDisableTiming) != cudaSuccess) {
+        hx_free(ctx, s->arena);
+        hx_free(ctx, s->d_slots);
+        cudaFreeHost(s->harena);
+        delete s;
+        hx_set_error("hx_server_create: event creation failed");
+        return HX_ERR_DEVICE;
+    }
     s->t_start = now_s();
     *out = s;
+    return HX_OK;
+}
+
+extern "C" hx_status hx_server_set_denoiser(hx_server* s, hx_denoiser* dn) {
+    HX_CHECK_ARG(s, "hx_server_set_denoiser: null server");
+    HX_CHECK_ARG(!s->running.load(), "hx_server_set_denoiser: attach the denoiser before hx_server_start");
+    s->denoiser = dn;
     return HX_OK;
 }
 
@@ -595,6 +660,7 @@ extern "C" hx_status hx_server_submit(hx_server* s, const hx_request_desc* d, ui
     HX_CHECK_ARG(d->width > 0 && d->height > 0 && (uint64_t)d->width * d->height <= 64ull << 20 && d->spp >= 1,
                  "hx_server_submit: bad request size");
     HX_CHECK_ARG(d->tonemap_op <= 2, "hx_server_submit: bad tone-map operator");
+    HX_CHECK_ARG(!d->denoise || s->denoiser, "hx_server_submit: denoise requested but no denoiser is attached");
     if (s->worker_error.load()) {
         hx_set_error("server worker failed: %s", s->worker_msg);
         return (hx_status)s->worker_error.load();
@@ -678,6 +744,7 @@ extern "C" hx_status hx_server_stats_get(hx_server* s, hx_server_stats* out) {
     out->arena_bytes = s->arena_bytes;
     out->arena_used = s->arena_bytes - free_b;
     out->seconds = now_s() - s->t_start;
+    out->requests_denoised = s->denoised;
     return HX_OK;
 }
 
@@ -693,6 +760,8 @@ extern "C" hx_status hx_server_destroy(hx_server* s) {
     if (s->harena) cudaFreeHost(s->harena);
     if (s->arena) hx_free(s->ctx, s->arena);
     if (s->d_slots) hx_free(s->ctx, s->d_slots);
+    if (s->dn_ready) cudaEventDestroy(s->dn_ready);
+    if (s->dn_done) cudaEventDestroy(s->dn_done);
     delete s;
     return HX_OK;
 }

@@ -431,4 +431,28 @@ Policy make_policy(const hx_policy& p) {
 }
 
 
+// Denoiser features per pixel (12 floats): current image rgb, 0, albedo rgb,
+// depth feature log1p(t)/8, shading normal xyz, 0 — first-hit AOVs as the
+// reference's debug views define them (debug_visualization.frag:142-161:
+// base colour, shading normal); zeros on a miss.
+__global__ void k_features(DevScene s, const float4* __restrict__ hit, const float4* __restrict__ img, uint32_t n,
+                           float* __restrict__ feat) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 h = hit[i], r = img[i];
+        const uint32_t prim = __float_as_uint(h.y);
+        V3 alb = v3(0.0f), nrm = v3(0.0f);
+        float depth = 0.0f;
+        if (prim != kNoHit) {
+            Surface sf = populate(s, prim, h.z, h.w);
+            alb = sf.albedo;
+            nrm = normalize(sf.normal);
+            depth = log1pf(h.x) * 0.125f;
+        }
+        float4* o = reinterpret_cast<float4*>(feat + 12 * (size_t)i);
+        o[0] = make_float4(r.x, r.y, r.z, 0.0f);
+        o[1] = make_float4(alb.x, alb.y, alb.z, depth);
+        o[2] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+    }
+}
+
 }  // namespace

@@ -58,6 +58,7 @@ typedef struct hx_context    hx_context;
 typedef struct hx_scene      hx_scene;
 typedef struct hx_integrator hx_integrator;
 typedef struct hx_host_scene hx_host_scene;
+typedef struct hx_denoiser   hx_denoiser;
 
 /* ------------------------------------------------------------------------ */
 /* Scene input — reference layouts                                           */
@@ -318,6 +319,15 @@ HX_API hx_status hx_event_destroy(hx_event* ev);
 HX_API hx_status hx_pinned_alloc(size_t bytes, void** out);
 HX_API hx_status hx_pinned_free(void* ptr);
 
+/* Device buffers from the context's budgeted allocator, and copies ordered
+ * on the context stream (host copies return when complete). */
+#define HX_COPY_HOST_TO_DEVICE   0u
+#define HX_COPY_DEVICE_TO_HOST   1u
+#define HX_COPY_DEVICE_TO_DEVICE 2u
+HX_API hx_status hx_device_alloc(hx_context* ctx, uint64_t bytes, void** out);
+HX_API hx_status hx_device_free(hx_context* ctx, void* ptr);
+HX_API hx_status hx_device_copy(hx_context* ctx, void* dst, const void* src, uint64_t bytes, uint32_t kind);
+
 /* Scene upload (replaces Scene::create_gpu_resources, scene.cpp:915-1311, and
  * the BLAS/TLAS builds of mesh.cpp:61-117 and renderer.cpp:113-181): copies
  * the host arrays, flattens instances, builds the LBVH -> BVH8 on the device,
@@ -446,7 +456,7 @@ typedef struct hx_request_desc {
     uint32_t      scene_id;          /* from hx_server_add_scene                  */
     uint32_t      width, height;
     uint32_t      spp;               /* progressive samples per pixel             */
-    uint32_t      denoise;           /* reserved (0)                              */
+    uint32_t      denoise;           /* 1: denoise with the attached denoiser     */
     uint32_t      tonemap_op;        /* HX_TONEMAP_*                              */
     float         exposure;
     uint32_t      reserved;
@@ -467,11 +477,17 @@ typedef struct hx_server_stats {
     uint64_t paths, ticks, requests_done, requests_pending, requests_active;
     uint64_t arena_bytes, arena_used;
     double   seconds;
+    uint64_t requests_denoised;
 } hx_server_stats;
 
 HX_API hx_status hx_server_create(hx_context* ctx, const hx_server_desc* desc, hx_server** out);
 /* Makes a resident scene servable (captures its tick as a CUDA graph). */
 HX_API hx_status hx_server_add_scene(hx_server* server, const hx_scene* scene, uint32_t* scene_id);
+/* Attaches the learned denoiser used for requests with denoise set (same
+ * context; before hx_server_start).  A finished request then gets first-hit
+ * features traced on its scene's stream and is denoised on the context
+ * stream before tone mapping. */
+HX_API hx_status hx_server_set_denoiser(hx_server* server, hx_denoiser* denoiser);
 /* Starts the worker thread (admission, batching, launches). */
 HX_API hx_status hx_server_start(hx_server* server);
 /* Thread-safe, non-blocking. */
@@ -537,6 +553,63 @@ HX_API hx_status hx_host_scene_destroy(hx_host_scene* scene);
  * (hosek_wilkie_sky_model.cpp:658-686). */
 HX_API hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], float turbidity,
                                               float normalized_sun_y, float out[40]);
+
+/* ------------------------------------------------------------------------
+ * Learned denoiser (no counterpart in the reference engine; its auxiliary
+ * inputs follow the reference's AOV definitions, renderer.h:27-35 and
+ * debug_visualization.frag:142-161).  A 5-level convolutional
+ * encoder-decoder (3x3 convolutions, 32 -> 128 channels, skip connections),
+ * BF16 weights and activations with FP32 accumulation on the tensor cores,
+ * trained by its own forward/backward kernels and Adam.
+ *
+ * Features: per pixel 12 floats, NHWC — radiance rgb, 0, albedo rgb, depth
+ * feature log1p(t)/8 (0 on a miss), shading normal xyz, 0.  Targets: per
+ * pixel RGBA float radiance (alpha ignored).  The network predicts
+ * log1p(radiance); the loss is the mean |y - log1p(target)| over pixels and
+ * colour channels.  Parameters: one flat FP32 vector, per layer W[9][cout][cin]
+ * (tap = ky*3 + kx) then b[cout].
+ * ------------------------------------------------------------------------ */
+HX_API hx_status hx_denoiser_create(hx_context* ctx, hx_denoiser** out);
+HX_API hx_status hx_denoiser_destroy(hx_denoiser* dn);
+HX_API hx_status hx_denoiser_num_params(hx_denoiser* dn, uint64_t* n);
+/* Load parameters (host FP32) and reset the Adam state. */
+HX_API hx_status hx_denoiser_set_params(hx_denoiser* dn, const float* host, uint64_t n);
+HX_API hx_status hx_denoiser_get_params(hx_denoiser* dn, float* host, uint64_t n);
+/* Forward + backward over n crops of h x w (multiples of 16) held on the
+ * device; the parameter gradient stays on the device (get_gradients reads
+ * it); *loss (optional) receives the batch loss. */
+HX_API hx_status hx_denoiser_forward_backward(hx_denoiser* dn, const float* d_features, const float* d_targets,
+                                              uint32_t n, uint32_t h, uint32_t w, float* loss);
+HX_API hx_status hx_denoiser_get_gradients(hx_denoiser* dn, float* host, uint64_t n);
+HX_API hx_status hx_denoiser_adam_step(hx_denoiser* dn, float lr);
+HX_API hx_status hx_denoiser_train_step(hx_denoiser* dn, const float* d_features, const float* d_targets,
+                                        uint32_t n, uint32_t h, uint32_t w, float lr, float* loss);
+/* Inference over n images of h x w (any size; padded to 16 internally):
+ * d_out_rgba receives n*h*w RGBA floats of denoised radiance.  Ordered on
+ * the context stream; call hx_denoiser_check to collect pipeline errors. */
+HX_API hx_status hx_denoiser_infer(hx_denoiser* dn, const float* d_features, uint32_t n, uint32_t h, uint32_t w,
+                                   float* d_out_rgba);
+HX_API hx_status hx_denoiser_check(hx_denoiser* dn);
+/* Test access: a stored BF16 tensor (activation, or its gradient) of the
+ * last training (training = 1) or inference pass, by index in network order
+ * (x, a0, a0b, p0, a1, p1, a2, p2, a3, p3, a4, a4b, u3, d3, u2, d2, u1, d1,
+ * u0, d0, d0b, gy), and the FP32 network output (RGBA per padded pixel). */
+HX_API hx_status hx_denoiser_read_tensor(hx_denoiser* dn, uint32_t training, uint32_t index, uint32_t gradient,
+                                         void* host, uint64_t bytes);
+HX_API hx_status hx_denoiser_read_output(hx_denoiser* dn, uint32_t training, float* host, uint64_t count);
+
+/* Denoiser inputs from an integrator: the current accumulated image plus
+ * albedo / normal / depth of the primary hits of sample frame_index, into
+ * d_features (width*height*12 floats, device memory). */
+HX_API hx_status hx_integrator_features(hx_integrator* it, const hx_frame_desc* frame, uint32_t frame_index,
+                                        float* d_features);
+/* The accumulated image (resolved RGBA floats) into device memory. */
+HX_API hx_status hx_integrator_resolve(hx_integrator* it, float* d_rgba);
+/* Denoise the accumulated image (features of sample 0) and tone-map the
+ * result like hx_integrator_tonemap; host_rgba8 (optional) receives it, and
+ * host_rgba32f (optional) the denoised HDR radiance. */
+HX_API hx_status hx_integrator_denoise(hx_integrator* it, hx_denoiser* dn, const hx_frame_desc* frame, uint32_t op,
+                                       float exposure, uint8_t* host_rgba8, float* host_rgba32f);
 
 #ifdef __cplusplus
 }

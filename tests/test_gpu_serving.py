@@ -104,3 +104,36 @@ def test_admission_by_hbm_budget(gpu_ctx, scenes):
     st = srv.stats()
     assert st.arena_used == 0
     srv.close()
+
+
+def test_denoised_requests_identical_alone_in_the_mix_and_to_the_integrator(gpu_ctx, scenes):
+    """Requests with denoise set: the served RGBA8 equals the integrator's
+    denoise of the same view and sample count, alone and in a mix with plain
+    requests (the denoiser's kernels are deterministic)."""
+    from oracle import denoiser_ref as dr
+    (box, s_box), (ico, s_ico) = scenes
+    pol = hx.policy_reference()
+    dn = hx.Denoiser(gpu_ctx)
+    dn.set_params(dr.init_params(5))
+    srv = hx.Server(gpu_ctx, arena_bytes=1 << 30, max_paths_per_tick=1 << 18, max_ray_bounces=6, policy=pol)
+    ii = srv.add_scene(s_ico)
+    srv.set_denoiser(dn)
+    srv.start()
+    w, h, spp = 640, 360, 2  # 230,400 px: features traced in row bands of a 2^18-path tick
+    f = hx.frame_desc(ico.camera(), w, h)
+    rid = srv.submit(ii, f, w, h, spp, denoise=True)
+    _wait_all(srv, [rid])
+    alone = srv.fetch(rid)
+    ids = [srv.submit(ii, f, 256, 256, 8), srv.submit(ii, f, w, h, spp, denoise=True), srv.submit(ii, f, 96, 54, 4)]
+    imgs = {}
+    _wait_all(srv, ids, images=imgs)
+    st = srv.stats()
+    srv.close()
+    assert np.array_equal(alone, imgs[ids[1]])
+    assert st.requests_denoised == 2
+    it = hx.PathIntegrator(gpu_ctx, s_ico, w, h, max_ray_bounces=6, max_samples=spp, policy=pol)
+    it.render(f, spp)
+    ldr, _ = it.denoise(dn, f, op=hx.TONEMAP_ACES, exposure=1.0, hdr=False, ldr=True)
+    it.close()
+    dn.close()
+    assert np.array_equal(ldr, alone)
