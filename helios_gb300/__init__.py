@@ -251,6 +251,7 @@ _SIGS = {
     "hx_integrator_resolve": (C.c_int, [_P, _P]),
     "hx_integrator_denoise": (C.c_int, [_P, _P, C.POINTER(FrameDesc), C.c_uint32, C.c_float, _P, _P]),
     "hx_server_set_denoiser": (C.c_int, [_P, _P]),
+    "hx_denoiser_set_loss": (C.c_int, [_P, C.c_uint32]),
 }
 
 _lib_handle = None
@@ -625,6 +626,7 @@ DENOISER_TENSORS = [("x", 32, 0), ("a0", 32, 0), ("a0b", 32, 0), ("p0", 32, 1), 
                     ("u3", 128, 3), ("d3", 96, 3), ("u2", 96, 2), ("d2", 64, 2), ("u1", 64, 1), ("d1", 64, 1),
                     ("u0", 64, 0), ("d0", 32, 0), ("d0b", 32, 0), ("gy", 32, 0)]
 FEATURE_CHANNELS = 12
+DN_LOSS_L1_LOG, DN_LOSS_L2_LINEAR = 0, 1
 
 
 def _bf16_to_f32(u16):
@@ -666,6 +668,9 @@ class Denoiser:
 
     def adam_step(self, lr):
         check(lib().hx_denoiser_adam_step(self.handle, lr))
+
+    def set_loss(self, kind):
+        check(lib().hx_denoiser_set_loss(self.handle, kind))
 
     def train_step(self, features, targets, n, h, w, lr, feat_offset=0, tgt_offset=0, want_loss=True):
         loss = C.c_float()

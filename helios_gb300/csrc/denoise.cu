@@ -561,19 +561,33 @@ __global__ void k_unpack_output(const float4* __restrict__ y, int h, int w, int 
     }
 }
 
-// L1 loss in log1p space: g_y = sign(y - log1p(target)), per-block |diff| sums.
+// Loss and its gradient per pixel (3 colour channels), per-block sums:
+//   HX_DN_LOSS_L1_LOG:   |y - log1p(t)|,               g_y = sign(y - log1p(t))
+//   HX_DN_LOSS_L2_LINEAR: (expm1(y) - t)^2,            g_y = 2 (expm1(y) - t) exp(y)
+// (t = max(target, 0); the 1 / (3 P) mean factor is applied to the parameter
+// gradients).
 constexpr int kLossBlocks = 256;
-__global__ void k_loss(const float4* __restrict__ y, const float4* __restrict__ tgt, size_t P, bf16* __restrict__ gy,
-                       float* __restrict__ part) {
+__global__ void k_loss(const float4* __restrict__ y, const float4* __restrict__ tgt, size_t P, uint32_t kind,
+                       bf16* __restrict__ gy, float* __restrict__ part) {
     __shared__ float red[256];
     float s = 0.0f;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
         const float4 v = y[p], t = tgt[p];
-        const float d0 = v.x - log1pf(fmaxf(t.x, 0.0f)), d1 = v.y - log1pf(fmaxf(t.y, 0.0f)),
-                    d2 = v.z - log1pf(fmaxf(t.z, 0.0f));
-        s += fabsf(d0) + fabsf(d1) + fabsf(d2);
-        auto sg = [](float d) { return d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f); };
-        __nv_bfloat162 a = __floats2bfloat162_rn(sg(d0), sg(d1)), b = __floats2bfloat162_rn(sg(d2), 0.0f);
+        const float yv[3] = {v.x, v.y, v.z}, tv[3] = {fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f), fmaxf(t.z, 0.0f)};
+        float g[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (kind == HX_DN_LOSS_L2_LINEAR) {
+                const float e = expf(yv[c]), d = (e - 1.0f) - tv[c];
+                s += d * d;
+                g[c] = 2.0f * d * e;
+            } else {
+                const float d = yv[c] - log1pf(tv[c]);
+                s += fabsf(d);
+                g[c] = d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f);
+            }
+        }
+        __nv_bfloat162 a = __floats2bfloat162_rn(g[0], g[1]), b = __floats2bfloat162_rn(g[2], 0.0f);
         uint2 w = make_uint2(*reinterpret_cast<uint32_t*>(&a), *reinterpret_cast<uint32_t*>(&b));
         *reinterpret_cast<uint2*>(gy + p * 32) = w;
     }
@@ -746,6 +760,7 @@ struct hx_denoiser {
     float* adam_v = nullptr;
     uint32_t* err = nullptr;
     int step = 0;
+    uint32_t loss_kind = HX_DN_LOSS_L1_LOG;
     std::vector<void*> allocs;
     std::unique_ptr<Plan> train_plan;
     std::vector<std::unique_ptr<Plan>> infer_plans;  // most recently used first
@@ -1176,8 +1191,8 @@ hx_status hx_denoiser_forward_backward(hx_denoiser* dn, const float* d_features,
     k_pack_input<<<grid_for(P, 256, ctx->num_sms), 256, 0, ctx->stream>>>(d_features, h, w, h, w, n, p->t[X]);
     HX_CUDA(cudaGetLastError());
     HX_TRY(run_forward(dn, p));
-    k_loss<<<kLossBlocks, 256, 0, ctx->stream>>>(p->y, reinterpret_cast<const float4*>(d_targets), P, p->g[GYT],
-                                                  p->loss_part);
+    k_loss<<<kLossBlocks, 256, 0, ctx->stream>>>(p->y, reinterpret_cast<const float4*>(d_targets), P, dn->loss_kind,
+                                                  p->g[GYT], p->loss_part);
     HX_CUDA(cudaGetLastError());
     HX_TRY(run_backward(dn, p, (float)(1.0 / (3.0 * (double)P))));
     if (loss) {
@@ -1190,6 +1205,12 @@ hx_status hx_denoiser_forward_backward(hx_denoiser* dn, const float* d_features,
     } else {
         HX_TRY(check_err(dn));
     }
+    return HX_OK;
+}
+
+hx_status hx_denoiser_set_loss(hx_denoiser* dn, uint32_t kind) {
+    HX_CHECK_ARG(dn && kind <= HX_DN_LOSS_L2_LINEAR, "hx_denoiser_set_loss: bad argument");
+    dn->loss_kind = kind;
     return HX_OK;
 }
 

@@ -10,6 +10,7 @@ same view (the target), all kept on the device.  A training step takes
 `batch` images at random from the set and gathers them into the batch
 buffers with device-to-device copies.
 """
+import ctypes
 import time
 
 import numpy as np
@@ -36,6 +37,22 @@ def variant_scene(seed, quads=20000, level=4, env=(512, 256), mask_pool=8, mask_
     return hs, cam
 
 
+def crop_frame(frame, full_w, full_h, x0, y0, w, h):
+    """Frame constants of the w x h window at (x0, y0) of a full_w x full_h
+    view: the same rays as the full frame's pixels there (camera NDC of the
+    window mapped onto the full frame's NDC in view_proj_inverse)."""
+    f = hx.FrameDesc()
+    ctypes.memmove(ctypes.addressof(f), ctypes.addressof(frame), ctypes.sizeof(f))
+    m = list(frame.view_proj_inverse)
+    sx, sy = w / full_w, h / full_h
+    bx, by = (2.0 * x0 + w) / full_w - 1.0, (2.0 * y0 + h) / full_h - 1.0
+    for r in range(4):
+        f.view_proj_inverse[0 * 4 + r] = sx * m[0 * 4 + r]
+        f.view_proj_inverse[1 * 4 + r] = sy * m[1 * 4 + r]
+        f.view_proj_inverse[3 * 4 + r] = bx * m[0 * 4 + r] + by * m[1 * 4 + r] + m[3 * 4 + r]
+    return f
+
+
 class PairSet:
     """Device-resident (features, target) images, all width x height."""
 
@@ -57,12 +74,15 @@ class PairSet:
         self.targets.close()
 
 
-def render_pairs(ctx, seeds, width, height, spp_in, spp_target, bounces=8, policy=None, scene_kw=None):
+def render_pairs(ctx, seeds, width, height, spp_in, spp_target, bounces=8, policy=None, scene_kw=None,
+                 full_res=None):
     """One pair per (seed, input spp): the target is the seed's image at
     spp_target; the inputs are the features of the progressive image after
     each count in spp_in (ascending; an int means one count).  The input
     samples are the first frames of the same sample sequence as the target,
-    a shared fraction of spp_in / spp_target."""
+    a shared fraction of spp_in / spp_target.  With full_res = (W, H) each
+    image is a seeded width x height window of the W x H view (the pixel
+    scale of full-resolution renders), else the whole view at width x height."""
     pol = policy if policy is not None else hx.policy_reference()
     counts = sorted(spp_in) if isinstance(spp_in, (list, tuple, np.ndarray)) else [int(spp_in)]
     ps = PairSet(ctx, len(seeds) * len(counts), width, height)
@@ -71,7 +91,14 @@ def render_pairs(ctx, seeds, width, height, spp_in, spp_target, bounces=8, polic
     for seed in seeds:
         hs, cam = variant_scene(seed, **(scene_kw or {}))
         sc = hx.Scene(ctx, hs)
-        f = hx.frame_desc(cam, width, height)
+        if full_res:
+            rng = np.random.default_rng(seed + 77)
+            x0 = int(rng.integers(0, full_res[0] - width + 1))
+            y0 = int(rng.integers(0, full_res[1] - height + 1))
+            f = crop_frame(hx.frame_desc(cam, full_res[0], full_res[1]), full_res[0], full_res[1], x0, y0, width,
+                           height)
+        else:
+            f = hx.frame_desc(cam, width, height)
         it = hx.PathIntegrator(ctx, sc, width, height, max_ray_bounces=bounces, max_samples=1 << 30, policy=pol)
         it.render(f, spp_target)
         it.resolve(ps.targets, ps.tgt_offset(k))

@@ -565,8 +565,7 @@ HX_API hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], floa
  * Features: per pixel 12 floats, NHWC — radiance rgb, 0, albedo rgb, depth
  * feature log1p(t)/8 (0 on a miss), shading normal xyz, 0.  Targets: per
  * pixel RGBA float radiance (alpha ignored).  The network predicts
- * log1p(radiance); the loss is the mean |y - log1p(target)| over pixels and
- * colour channels.  Parameters: one flat FP32 vector, per layer W[9][cout][cin]
+ * log1p(radiance); the loss is chosen by hx_denoiser_set_loss.  Parameters: one flat FP32 vector, per layer W[9][cout][cin]
  * (tap = ky*3 + kx) then b[cout].
  * ------------------------------------------------------------------------ */
 HX_API hx_status hx_denoiser_create(hx_context* ctx, hx_denoiser** out);
@@ -581,6 +580,11 @@ HX_API hx_status hx_denoiser_get_params(hx_denoiser* dn, float* host, uint64_t n
 HX_API hx_status hx_denoiser_forward_backward(hx_denoiser* dn, const float* d_features, const float* d_targets,
                                               uint32_t n, uint32_t h, uint32_t w, float* loss);
 HX_API hx_status hx_denoiser_get_gradients(hx_denoiser* dn, float* host, uint64_t n);
+/* Training loss: mean over pixels and colour channels of |y - log1p(t)|
+ * (default) or of (expm1(y) - t)^2 (squared error of the linear radiance). */
+#define HX_DN_LOSS_L1_LOG    0u
+#define HX_DN_LOSS_L2_LINEAR 1u
+HX_API hx_status hx_denoiser_set_loss(hx_denoiser* dn, uint32_t kind);
 HX_API hx_status hx_denoiser_adam_step(hx_denoiser* dn, float lr);
 HX_API hx_status hx_denoiser_train_step(hx_denoiser* dn, const float* d_features, const float* d_targets,
                                         uint32_t n, uint32_t h, uint32_t w, float lr, float* loss);

@@ -6,7 +6,7 @@ reference's AOV definitions (albedo and shading normal as in
 `include/gfx/renderer.h:27-35`).  This module restates the network the CUDA
 kernels run — same layer list, same parameter layout, same points where a
 tensor is rounded to BF16 — in float64 numpy, forward and backward, so the
-tests can check the device's activations and gradients.  With `bf16=False`
+tests can check the device's activations and gradients.  With `rnd=False`
 nothing is rounded, and `finite_difference_check` pins the backward pass to
 central differences of the forward pass.
 
@@ -28,7 +28,8 @@ nearest 2x upsampling, skip connections by concatenation):
     d0b = relu(conv(d0))             32
     y   = conv(d0b)                   3   (linear; log1p radiance)
 
-Loss: mean over pixels and the 3 channels of |y - log1p(target)|.
+Loss: mean over pixels and the 3 channels of |y - log1p(target)| ("l1log"),
+or of (expm1(y) - target)^2 ("l2lin").
 """
 import numpy as np
 
@@ -198,18 +199,26 @@ def forward(params, features, rnd=True):
     return t
 
 
-def loss_and_grad(params, features, targets, rnd=True):
-    """Forward + backward.  Returns (loss, flat gradient float64, tensors)."""
+def loss_and_grad(params, features, targets, rnd=True, loss="l1log"):
+    """Forward + backward.  Returns (loss, flat gradient float64, tensors).
+    loss: "l1log" = mean |y - log1p(t)|, "l2lin" = mean (expm1(y) - t)^2."""
     R = bf16 if rnd else (lambda a: a)
     t = forward(params, features, rnd)
     P = t["_params"]
-    tgt = np.log1p(np.maximum(np.asarray(targets, np.float64)[..., 0:3], 0.0))
-    diff = t["y"] - (np.asarray(tgt, np.float32).astype(np.float64) if rnd else tgt)
-    count = diff.size
-    loss = np.abs(diff).sum() / count
+    tl = np.maximum(np.asarray(targets, np.float64)[..., 0:3], 0.0)
+    if loss == "l2lin":
+        e = np.exp(t["y"])
+        diff = (e - 1.0) - tl
+        count = diff.size
+        lval = (diff * diff).sum() / count
+        gy = R(2.0 * diff * e)
+    else:
+        tgt = np.log1p(tl)
+        diff = t["y"] - (np.asarray(tgt, np.float32).astype(np.float64) if rnd else tgt)
+        count = diff.size
+        lval = np.abs(diff).sum() / count
+        gy = np.sign(diff)
     scale = 1.0 / count
-    gy = np.zeros(t["y"].shape[:3] + (3,))
-    gy[...] = np.sign(diff)
     grads = [None] * len(LAYERS)
     g = {"y": gy}
     # pre-activation gradients flow backwards; masks from the stored outputs
@@ -242,10 +251,10 @@ def loss_and_grad(params, features, targets, rnd=True):
                 gm = R(np.where(t[s] > 0, part, 0.0))
                 g[s] = R(g[s] + gm) if s in g else gm
     flat = np.concatenate([np.concatenate([dw.ravel(), db]) for dw, db in grads])
-    return loss, flat, t
+    return lval, flat, t
 
 
-def finite_difference_check(seed=0, n=1, h=16, w=16, probes=24, eps=1e-6):
+def finite_difference_check(seed=0, n=1, h=16, w=16, probes=24, eps=1e-6, loss="l1log"):
     """Analytic (float64, no rounding) vs central-difference gradients of the
     loss on random features; returns the worst relative error over probes."""
     rng = np.random.default_rng(seed)
@@ -253,15 +262,15 @@ def finite_difference_check(seed=0, n=1, h=16, w=16, probes=24, eps=1e-6):
     params += rng.normal(0, 0.01, params.shape)  # non-zero biases
     feats = rng.uniform(0, 1, (n, h, w, FEATURES))
     tg = rng.uniform(0, 2, (n, h, w, 4))
-    _, g, _ = loss_and_grad(params, feats, tg, rnd=False)
+    _, g, _ = loss_and_grad(params, feats, tg, rnd=False, loss=loss)
     worst = 0.0
     idx = rng.choice(params.size, probes, replace=False)
     for k in idx:
         p1, p2 = params.copy(), params.copy()
         p1[k] += eps
         p2[k] -= eps
-        l1, _, _ = loss_and_grad(p1, feats, tg, rnd=False)
-        l2, _, _ = loss_and_grad(p2, feats, tg, rnd=False)
+        l1, _, _ = loss_and_grad(p1, feats, tg, rnd=False, loss=loss)
+        l2, _, _ = loss_and_grad(p2, feats, tg, rnd=False, loss=loss)
         num = (l1 - l2) / (2 * eps)
         worst = max(worst, abs(num - g[k]) / max(1e-6, abs(num) + abs(g[k])))
     return worst

@@ -136,6 +136,31 @@ def test_each_kernel_matches_oracle_on_device_inputs(gpu_ctx, denoiser, shape):
     tb.close()
 
 
+def test_l2_linear_loss_matches_oracle(gpu_ctx, denoiser):
+    n, h, w = 1, 64, 64
+    params, feats, tg = _problem(17, n, h, w)
+    denoiser.set_params(params)
+    denoiser.set_loss(hx.DN_LOSS_L2_LINEAR)
+    fb = hx.DeviceBuffer(gpu_ctx, feats.nbytes)
+    tb = hx.DeviceBuffer(gpu_ctx, tg.nbytes)
+    fb.upload(feats)
+    tb.upload(tg)
+    try:
+        loss = denoiser.forward_backward(fb, tb, n, h, w)
+    finally:
+        denoiser.set_loss(hx.DN_LOSS_L1_LOG)
+    ref_loss, ref_grad, t = dr.loss_and_grad(params, feats, tg, rnd=True, loss="l2lin")
+    assert abs(loss - ref_loss) <= 1e-3 * ref_loss, (loss, ref_loss)
+    gy = denoiser.read_tensor("gy", gradient=True)[..., 0:3]
+    y = denoiser.read_output()[..., 0:3].astype(np.float64)
+    want = dr.bf16(2.0 * (np.expm1(y) - tg[..., 0:3]) * np.exp(y))
+    assert _rel(gy, want) < 1e-2
+    grad = denoiser.gradients()
+    assert _rel(grad, ref_grad) < 3e-2, _rel(grad, ref_grad)
+    fb.close()
+    tb.close()
+
+
 def test_adam_step_matches_oracle(gpu_ctx, denoiser):
     n, h, w = 1, 32, 32
     params, feats, tg = _problem(11, n, h, w)
