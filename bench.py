@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--scenes", type=int, default=8)
     p.add_argument("--tick-paths", type=int, default=4 << 20)
     p.add_argument("--arena-gb", type=float, default=64.0)
+    p.add_argument("--concurrent-ticks", type=int, default=4)
     p.add_argument("--precision", action="store_true", help="precision-form report (terrain scene)")
     p.add_argument("--terrain-size", type=int, default=4096)
     p.add_argument("--spp", type=int, default=256)
@@ -62,6 +63,7 @@ def parse():
     p.add_argument("--dn-steps", type=int, default=3000)
     p.add_argument("--dn-ref-spp", type=int, default=4096)
     p.add_argument("--dn-eval-seeds", type=int, nargs="+", default=[5000, 5001])
+    p.add_argument("--dn-save", default="", help="directory for the trained parameters (one .npy per loss)")
     p.add_argument("--dn-losses", nargs="+", default=["hybrid"], choices=["l1log", "l2lin", "hybrid"],
                    help="train one network per loss on the same data (hybrid: l1log for the first 20%% of "
                         "the steps, then l2lin)")
@@ -381,7 +383,18 @@ def run_serving(args, dist):
     rng = np.random.default_rng(1234)
     pol = make_policy(hx)
     srv = hx.Server(ctx, arena_bytes=int(args.arena_gb * (1 << 30)), max_paths_per_tick=args.tick_paths,
-                    max_ray_bounces=DEPTH, policy=pol)
+                    max_ray_bounces=DEPTH, policy=pol, max_concurrent_ticks=args.concurrent_ticks)
+    dn = hx.Denoiser(ctx)
+    wpath = os.path.join(ROOT, "helios_gb300", "weights", "denoiser.npy")
+    if os.path.exists(wpath):
+        import numpy as np_
+        dn.set_params(np_.load(wpath))
+        weights = "trained (helios_gb300/weights/denoiser.npy)"
+    else:
+        from oracle import denoiser_ref as dr
+        dn.set_params(dr.init_params(0))
+        weights = "seeded initial weights (latency does not depend on the weights)"
+    srv.set_denoiser(dn)
     pool = []
     t0 = time.time()
     for k in range(args.scenes):
@@ -416,7 +429,7 @@ def run_serving(args, dist):
             for a in range(3):
                 cam.position[a] += float(rng.normal(0, 0.05 if sid < 2 else 1.0))
             denoise = int(rng.random() < 0.5)
-            rid = srv.submit(sid, hx.frame_desc(cam, w, h), w, h, spp, user_tag=i)
+            rid = srv.submit(sid, hx.frame_desc(cam, w, h), w, h, spp, user_tag=i, denoise=bool(denoise))
             meta[rid] = (w, h, spp, denoise, sid)
             i += 1
         for r in srv.poll(wait_seconds=0.0005):
@@ -429,6 +442,7 @@ def run_serving(args, dist):
     s1 = srv.stats()
     paths = s1.paths - s0.paths
     srv.close()
+    dn.close()
 
     def pct(v, q):
         return float(np.percentile(v, q)) if len(v) else None
@@ -436,7 +450,8 @@ def run_serving(args, dist):
     lat = [r.latency_ms for r in results]
     classes = {}
     for r in results:
-        w, h, spp, dn, sid = meta[r.request_id]
+        w, h, spp, dz, sid = meta[r.request_id]
+        classes.setdefault("%dx%d/%dspp%s" % (w, h, spp, "/denoise" if dz else ""), []).append(r.latency_ms)
         classes.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.latency_ms)
     offered = sum(w * h * spp for (w, h, spp, dn, sid) in meta.values())
     line = {"metric": "serving latency p50/p99 (ms) and Mpaths/s", "mode": "serving", "n_gpus": 1,
@@ -445,8 +460,9 @@ def run_serving(args, dist):
             "throughput_mpaths_per_s": paths / elapsed / 1e6, "offered_mpaths_per_s": offered / args.duration / 1e6,
             "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
             "per_class_latency_ms": {k: {"n": len(v), "p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(classes.items())},
-            "tick_paths": args.tick_paths, "arena_gb": args.arena_gb, "denoise": "flag recorded; no denoiser applied",
-            "data": "synthetic"}
+            "tick_paths": args.tick_paths, "concurrent_ticks": args.concurrent_ticks, "arena_gb": args.arena_gb,
+            "denoise": "Bernoulli(0.5) per request; denoiser weights: " + weights,
+            "requests_denoised": s1.requests_denoised - s0.requests_denoised, "data": "synthetic"}
     print(json.dumps(line), flush=True)
 
 
@@ -587,6 +603,10 @@ def run_denoise(args, dist):
                                  "conv_tflops": step_flops / (train_ms / args.dn_steps * 1e-3) / 1e12,
                                  "loss": [(s, round(l, 5)) for s, l in hist]}
         nets[loss] = dn
+        if args.dn_save:
+            import numpy as np_
+            os.makedirs(args.dn_save, exist_ok=True)
+            np_.save(os.path.join(args.dn_save, "denoiser_%s.npy" % loss), dn.get_params())
     data.close()
     # held-out evaluation at 1920x1080
     W, H = WIDTH, HEIGHT

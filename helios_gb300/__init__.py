@@ -711,8 +711,10 @@ class Server:
     """Resident render-serving loop (hx_server_*): scenes stay on the device,
     requests are admitted by HBM budget and batched into CUDA-graph ticks."""
 
-    def __init__(self, ctx, arena_bytes=4 << 30, max_paths_per_tick=4 << 20, max_ray_bounces=8, policy=None):
+    def __init__(self, ctx, arena_bytes=4 << 30, max_paths_per_tick=4 << 20, max_ray_bounces=8, policy=None,
+                 max_concurrent_ticks=0):
         d = ServerDesc()
+        d.max_concurrent_ticks = max_concurrent_ticks
         d.request_arena_bytes = arena_bytes
         d.max_paths_per_tick = max_paths_per_tick
         d.max_ray_bounces = max_ray_bounces

@@ -23,7 +23,7 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr uint32_t kLeafMax = 3;  // triangles per leaf slot
+constexpr uint32_t kLeafMax = 1;  // triangles per leaf slot
 
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {
     v = (v * 0x00010001u) & 0xFF0000FFu;

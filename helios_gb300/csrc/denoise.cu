@@ -71,6 +71,7 @@ struct ConvArgs {
     int och0, och1;            // channels of out0 / out1 (EPI_DGRAD splits at och0)
     const bf16* mask0;         // EPI_DGRAD: zero the gradient where mask <= 0
     const bf16* mask1;
+    const bf16* resid;         // EPI_LINEAR_F32: network input (32 ch); channels 0-2 are added to the output
     int n_store;               // channels written (EPI_RELU_BF16)
     uint32_t* err;
 };
@@ -208,9 +209,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                         store16_bf16(reinterpret_cast<bf16*>(a.out0) + pix * a.och0 + col, f);
                     }
                 } else if (a.mode == EPI_LINEAR_F32) {
-                    if (col == 0)
+                    if (col == 0) {
+                        // residual output: the input's log1p radiance + the predicted correction
+                        const __nv_bfloat162 r01 = *reinterpret_cast<const __nv_bfloat162*>(a.resid + pix * 32);
+                        const float r2 = __bfloat162float(a.resid[pix * 32 + 2]);
                         reinterpret_cast<float4*>(a.out0)[pix] =
-                            make_float4(f[0] + a.bias[0], f[1] + a.bias[1], f[2] + a.bias[2], 0.0f);
+                            make_float4((f[0] + a.bias[0]) + __low2float(r01), (f[1] + a.bias[1]) + __high2float(r01),
+                                        (f[2] + a.bias[2]) + r2, 0.0f);
+                    }
                 } else {
                     const bool hi = col >= a.och0;
                     const int och = hi ? a.och1 : a.och0, lc = hi ? col - a.och0 : col;
@@ -909,6 +915,7 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
             a.mode = EPI_LINEAR_F32;
             a.out0 = p->y;
             a.och0 = 4;
+            a.resid = p->t[X];
         }
     } else {
         const int gout = S.out >= 0 ? S.out : GYT;

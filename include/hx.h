@@ -565,7 +565,8 @@ HX_API hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], floa
  * Features: per pixel 12 floats, NHWC — radiance rgb, 0, albedo rgb, depth
  * feature log1p(t)/8 (0 on a miss), shading normal xyz, 0.  Targets: per
  * pixel RGBA float radiance (alpha ignored).  The network predicts
- * log1p(radiance); the loss is chosen by hx_denoiser_set_loss.  Parameters: one flat FP32 vector, per layer W[9][cout][cin]
+ * log1p(radiance) as the input's log1p radiance plus a learned correction;
+ * the loss is chosen by hx_denoiser_set_loss.  Parameters: one flat FP32 vector, per layer W[9][cout][cin]
  * (tap = ky*3 + kx) then b[cout].
  * ------------------------------------------------------------------------ */
 HX_API hx_status hx_denoiser_create(hx_context* ctx, hx_denoiser** out);

@@ -26,7 +26,8 @@ nearest 2x upsampling, skip connections by concatenation):
     d1  = relu(conv([up(d2), a1]))   64
     d0  = relu(conv([up(d1), a0b]))  32
     d0b = relu(conv(d0))             32
-    y   = conv(d0b)                   3   (linear; log1p radiance)
+    y   = x[..., 0:3] + conv(d0b)     3   (residual: the input's log1p radiance
+                                           + a linear correction)
 
 Loss: mean over pixels and the 3 channels of |y - log1p(target)| ("l1log"),
 or of (expm1(y) - target)^2 ("l2lin").
@@ -194,6 +195,7 @@ def forward(params, features, rnd=True):
         if relu:
             t[OUTPUT_OF[i]] = R(np.maximum(o, 0.0))
         else:
+            o = o + t["x"][..., 0:3]
             t[OUTPUT_OF[i]] = np.asarray(o, np.float32).astype(np.float64) if rnd else o
     t["_params"] = P
     return t

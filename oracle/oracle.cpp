@@ -429,6 +429,10 @@ static void assign_octant_slots(int nk, const float (*klo)[3], const float (*khi
     }
 }
 
+// Triangles per BVH8 leaf slot (the device builder's kLeafMax): one — a
+// triangle's own 8-bit box culls it before the triangle test.
+constexpr uint32_t kLeafMax = 1;
+
 static void build_bvh(Scene& s) {
     Bvh& b = s.bvh;
     int n = (int)s.prims.size();
@@ -548,7 +552,7 @@ static void build_bvh(Scene& s) {
                 float best_area = -1.0f;
                 for (int c = 0; c < nk; ++c) {
                     uint32_t it = kids[c];
-                    if ((it & 0x80000000u) || b.count[it] <= 3) continue;
+                    if ((it & 0x80000000u) || b.count[it] <= kLeafMax) continue;
                     float a = half_area(&b.lo[3 * (size_t)it], &b.hi[3 * (size_t)it]);
                     if (best < 0 || a > best_area || (a == best_area && it < kids[best])) { best = c; best_area = a; }
                 }
@@ -584,7 +588,7 @@ static void build_bvh(Scene& s) {
             }
             uint32_t it = kids[slot_kid[c]];
             for (int a = 0; a < 3; ++a) { clo[c][a] = klo[slot_kid[c]][a]; chi[c][a] = khi[slot_kid[c]][a]; }
-            if (!(it & 0x80000000u) && b.count[it] > 3) {
+            if (!(it & 0x80000000u) && b.count[it] > kLeafMax) {
                 node.meta[c] = (uint8_t)(0x80u | rank);
                 node.internal_mask |= (uint8_t)(1u << c);
                 ++rank;
