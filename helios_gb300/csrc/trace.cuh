@@ -130,7 +130,7 @@ HXD float byte_biased(uint32_t w, int k) { return __uint_as_float(__byte_perm(w,
 // reciprocal (1 + 2^-21).
 HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, const uint4 w3, const uint4 w4,
                                 const RayPre& r, float fix, float fiy, float fiz, uint32_t oct_inv, float tmin,
-                                float lim, uint32_t* nearest = nullptr) {
+                                float lim) {
     const int ex = (int)(int8_t)(w0.w & 0xffu), ey = (int)(int8_t)((w0.w >> 8) & 0xffu), ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
     const float Sx = __uint_as_float((uint32_t)(ex + 127) << 23), Sy = __uint_as_float((uint32_t)(ey + 127) << 23),
                 Sz = __uint_as_float((uint32_t)(ez + 127) << 23);
@@ -147,8 +147,7 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
     const float2 Ox2 = make_float2(Ox, Ox), Oy2 = make_float2(Oy, Oy), Oz2 = make_float2(Oz, Oz);
     const float2 ox2 = make_float2(r.o.x, r.o.x), oy2 = make_float2(r.o.y, r.o.y), oz2 = make_float2(r.o.z, r.o.z);
     const float2 ix2 = make_float2(r.ix, fix), iy2 = make_float2(r.iy, fiy), iz2 = make_float2(r.iz, fiz);
-    uint32_t hits = 0, near_bit = 0;
-    float near_t = INFINITY;
+    uint32_t hits = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const uint32_t m = byte_of(c < 4 ? w1.z : w1.w, c & 3);
@@ -163,19 +162,10 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
         const float tn = fmaxf(max3f(tx.x, ty.x, tz.x), tmin);
         const float tf = fminf(min3f(tx.y, ty.y, tz.y), lim);
         if (m != 0u && tn <= tf) {
-            if (m & 0x80u) {
-                const uint32_t b = 1u << (24 + (c ^ oct_inv));
-                hits |= b;
-                if (tn < near_t) {
-                    near_t = tn;
-                    near_bit = b;
-                }
-            } else {
-                hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-            }
+            if (m & 0x80u) hits |= 1u << (24 + (c ^ oct_inv));
+            else hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
         }
     }
-    if (nearest) *nearest = near_bit;
     return hits;
 }
 
@@ -280,7 +270,6 @@ struct TravState {
     float tmin, best_t, bu, bv;
     uint32_t best;
     uint32_t g_base, g_mask, t_base, t_mask;
-    uint32_t near;  // group bit of the nearest internal child of the last node visited
     int sp;
     uint32_t visits_left;
     bool any_hit;
@@ -301,7 +290,6 @@ HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, flo
     st.g_mask = s.num_nodes ? ((1u << (24 + st.oct_inv)) | 1u) : 0u;
     st.t_base = 0;
     st.t_mask = 0;
-    st.near = 0;
     st.sp = 0;
     st.visits_left = s.num_nodes + 16;
     st.any_hit = any_hit;
@@ -314,10 +302,7 @@ constexpr int kPostponeLanes = 8;  // postpone triangle tests below this many la
 template <bool SHADOW, bool COUNT, bool POSTPONE = false>
 HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflow, TraverseCount* tc) {
     if (st.g_mask > 0x00ffffffu) {
-        // the nearest internal child of a freshly visited node first, then
-        // the rest of the group in octant order
-        const uint32_t bit = 31u - __clz(st.near & st.g_mask ? st.near : st.g_mask);
-        st.near = 0;
+        const uint32_t bit = 31u - __clz(st.g_mask);
         st.g_mask &= ~(1u << bit);
         const uint32_t slot = (bit - 24u) ^ st.oct_inv;
         const uint32_t child = st.g_base + __popc(st.g_mask & 0xffu & ((1u << slot) - 1u));
@@ -333,7 +318,7 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
         if (COUNT) tc->nodes++;
         const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.fix, st.fiy, st.fiz, st.oct_inv, st.tmin,
-                                               st.best_t * 1.000001f, &st.near);
+                                               st.best_t * 1.000001f);
         st.g_base = w1.x;
         st.g_mask = (hm & 0xff000000u) | (w0.w >> 24);
         st.t_base = w1.y;
