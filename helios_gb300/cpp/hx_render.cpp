@@ -1,9 +1,11 @@
 // hx_render — headless C++ driver over the hx C-ABI (the role of the
 // reference's viewer loop, src/viewer/main.cpp:66-76, without a window):
 // uploads a procedural scene, renders N progressive frames through
-// helios::PathIntegrator / helios::Renderer and writes the tone-mapped image.
+// helios::PathIntegrator / helios::Renderer and writes the tone-mapped image;
+// with a parameter file of the learned denoiser (raw FP32, hx.h layout) it
+// also writes the denoised image next to it (<out>.denoised.ppm).
 //
-//   hx_render <box|icospheres> <width> <height> <frames> <out.ppm>
+//   hx_render <box|icospheres> <width> <height> <frames> <out.ppm> [denoiser.f32]
 #include "helios_gb300.hpp"
 
 #include <chrono>
@@ -13,7 +15,7 @@
 
 int main(int argc, char** argv) {
     if (argc < 6) {
-        std::fprintf(stderr, "usage: %s <box|icospheres> <width> <height> <frames> <out.ppm>\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <box|icospheres> <width> <height> <frames> <out.ppm> [denoiser.f32]\n", argv[0]);
         return 2;
     }
     const bool box = std::strcmp(argv[1], "box") == 0;
@@ -45,6 +47,24 @@ int main(int argc, char** argv) {
         renderer.save_image_to_disk(argv[5], w, h);
         std::printf("rendered %u frames of %ux%u (%u samples accumulated) in %.3f s: %.1f Mpaths/s\n", frames, w, h,
                     integrator->num_accumulated_samples(), s, (double)frames * w * h / s / 1e6);
+        if (argc > 6) {
+            helios::Denoiser dn(ctx);
+            std::vector<float> params(dn.num_params());
+            FILE* f = std::fopen(argv[6], "rb");
+            if (!f || std::fread(params.data(), 4, params.size(), f) != params.size())
+                throw std::runtime_error(std::string("cannot read ") + std::to_string(params.size()) +
+                                         " parameters from " + argv[6]);
+            std::fclose(f);
+            dn.set_params(params);
+            std::vector<uint8_t> px = dn.denoise(*integrator, frame, w, h);
+            std::string out = std::string(argv[5]) + ".denoised.ppm";
+            FILE* o = std::fopen(out.c_str(), "wb");
+            if (!o) throw std::runtime_error("cannot open " + out);
+            std::fprintf(o, "P6\n%u %u\n255\n", w, h);
+            for (size_t i = 0; i < (size_t)w * h; ++i) std::fwrite(&px[4 * i], 1, 3, o);
+            std::fclose(o);
+            std::printf("denoised image: %s\n", out.c_str());
+        }
         hx_host_scene_destroy(hs);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "hx_render: %s\n", e.what());

@@ -145,4 +145,83 @@ private:
     float m_exposure = 1.0f;
 };
 
+// The learned denoiser (no reference counterpart): parameters in, denoised
+// tone-mapped frames out of a PathIntegrator's accumulation.
+class Denoiser {
+public:
+    using Ptr = std::shared_ptr<Denoiser>;
+    explicit Denoiser(Context::Ptr ctx) : m_ctx(std::move(ctx)) { hx_check(hx_denoiser_create(m_ctx->handle(), &m_dn)); }
+    ~Denoiser() { hx_denoiser_destroy(m_dn); }
+    Denoiser(const Denoiser&) = delete;
+    Denoiser& operator=(const Denoiser&) = delete;
+    uint64_t num_params() const {
+        uint64_t n = 0;
+        hx_check(hx_denoiser_num_params(m_dn, &n));
+        return n;
+    }
+    void set_params(const std::vector<float>& p) { hx_check(hx_denoiser_set_params(m_dn, p.data(), p.size())); }
+    std::vector<float> params() const {
+        std::vector<float> p(num_params());
+        hx_check(hx_denoiser_get_params(m_dn, p.data(), p.size()));
+        return p;
+    }
+    // Denoised, tone-mapped RGBA8 of the integrator's current accumulation.
+    std::vector<uint8_t> denoise(PathIntegrator& it, const hx_frame_desc& frame, uint32_t width, uint32_t height,
+                                 ToneMapOperator op = TONE_MAP_OPERATOR_ACES, float exposure = 1.0f) {
+        std::vector<uint8_t> px((size_t)width * height * 4);
+        hx_check(hx_integrator_denoise(it.handle(), m_dn, &frame, (uint32_t)op, exposure, px.data(), nullptr));
+        return px;
+    }
+    hx_denoiser* handle() const { return m_dn; }
+
+private:
+    Context::Ptr m_ctx;
+    hx_denoiser* m_dn = nullptr;
+};
+
+// Resident render-serving loop over several GpuScenes.
+class Server {
+public:
+    Server(Context::Ptr ctx, const hx_server_desc& desc) : m_ctx(std::move(ctx)) {
+        hx_check(hx_server_create(m_ctx->handle(), &desc, &m_srv));
+    }
+    ~Server() { hx_server_destroy(m_srv); }
+    Server(const Server&) = delete;
+    Server& operator=(const Server&) = delete;
+    uint32_t add_scene(const GpuScene::Ptr& scene) {
+        uint32_t id = 0;
+        hx_check(hx_server_add_scene(m_srv, scene->handle(), &id));
+        m_scenes.push_back(scene);
+        return id;
+    }
+    void set_denoiser(const Denoiser::Ptr& dn) {
+        hx_check(hx_server_set_denoiser(m_srv, dn->handle()));
+        m_dn = dn;
+    }
+    void start() { hx_check(hx_server_start(m_srv)); }
+    uint64_t submit(const hx_request_desc& r) {
+        uint64_t id = 0;
+        hx_check(hx_server_submit(m_srv, &r, &id));
+        return id;
+    }
+    std::vector<hx_request_result> poll(double wait_seconds, uint32_t capacity = 64) {
+        std::vector<hx_request_result> out(capacity);
+        uint32_t n = 0;
+        hx_check(hx_server_poll(m_srv, out.data(), capacity, &n, wait_seconds));
+        out.resize(n);
+        return out;
+    }
+    std::vector<uint8_t> fetch(uint64_t id, uint32_t width, uint32_t height) {
+        std::vector<uint8_t> px((size_t)width * height * 4);
+        hx_check(hx_server_fetch(m_srv, id, px.data()));
+        return px;
+    }
+
+private:
+    Context::Ptr m_ctx;
+    hx_server* m_srv = nullptr;
+    std::vector<GpuScene::Ptr> m_scenes;
+    Denoiser::Ptr m_dn;
+};
+
 }  // namespace helios
