@@ -621,7 +621,16 @@ def run_denoise(args, dist):
         it = hx.PathIntegrator(ctx, sc, W, H, max_ray_bounces=DEPTH, max_samples=1 << 30, policy=hx.policy_reference())
         it.render(f, args.dn_ref_spp)
         ref = it.read_accumulation()[..., 0:3].astype(np.float64)
+        # plain frame time (no AOV accumulation), warm
         it.restart_bake()
+        it.render(f, 4)
+        e0.record()
+        it.render(f, 32)
+        e1.record()
+        ctx.synchronize()
+        frame_ms_plain = e0.elapsed_ms(e1) / 32
+        it.restart_bake()
+        it.set_aov_accumulation(True)
         plain, dnz, done, frame_ms = {}, {k: {} for k in nets}, 0, 0.0
         for c in checkpoints:
             e0.record()
@@ -653,9 +662,10 @@ def run_denoise(args, dist):
         ctx.synchronize()
         infer_ms = e0.elapsed_ms(e1) / 10
         e256 = plain[256]
-        t_plain = 256 * frame_ms
-        res = {"seed": seed, "ref_spp": args.dn_ref_spp, "frame_ms": frame_ms, "features_plus_infer_ms": dn_ms,
-               "infer_ms": infer_ms, "rel_rmse_plain": plain}
+        t_plain = 256 * frame_ms_plain
+        res = {"seed": seed, "ref_spp": args.dn_ref_spp, "frame_ms_plain": frame_ms_plain,
+               "frame_ms_with_aov": frame_ms, "features_plus_infer_ms": dn_ms, "infer_ms": infer_ms,
+               "rel_rmse_plain": plain}
         for k in nets:
             ok = [c for c in sorted(dnz[k]) if dnz[k][c] <= e256]
             s_star = ok[0] if ok else None

@@ -252,6 +252,7 @@ _SIGS = {
     "hx_integrator_denoise": (C.c_int, [_P, _P, C.POINTER(FrameDesc), C.c_uint32, C.c_float, _P, _P]),
     "hx_server_set_denoiser": (C.c_int, [_P, _P]),
     "hx_denoiser_set_loss": (C.c_int, [_P, C.c_uint32]),
+    "hx_integrator_set_aov_accumulation": (C.c_int, [_P, C.c_uint32]),
 }
 
 _lib_handle = None
@@ -554,6 +555,9 @@ class PathIntegrator:
         out = np.zeros((self.width * self.height, 3), np.float32)
         check(lib().hx_integrator_sample_radiance(self.handle, C.byref(frame), frame_index, _ptr(out)))
         return out
+
+    def set_aov_accumulation(self, on=True):
+        check(lib().hx_integrator_set_aov_accumulation(self.handle, 1 if on else 0))
 
     def features(self, frame, buf, offset=0, frame_index=0):
         """Denoiser features (width*height*12 floats) into a DeviceBuffer at a byte offset."""

@@ -90,6 +90,9 @@ struct hx_integrator {
     uchar4* ldr = nullptr;
     hx_hit* hits_host_layout = nullptr;
     float* rgb_tmp = nullptr;
+    float4* aov_a = nullptr;      // accumulated first-hit albedo + depth feature (AOV accumulation on)
+    float4* aov_n = nullptr;      // accumulated first-hit shading normal
+    bool aov = false;
     float* feat = nullptr;        // denoiser features (12 floats per pixel), on first use
     float4* denoised = nullptr;
     // progressive state (path_integrator.h:46-53)
@@ -267,6 +270,15 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             it->stats.trace_launches++;
             it->stats.kernel_launches++;
         }
+        if (b == 0 && it->aov && accumulate) {
+            if (fp16)
+                k_aov_accumulate<true><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
+                                                                          it->aov_n, it->desc.width);
+            else
+                k_aov_accumulate<false><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
+                                                                           it->aov_n, it->desc.width);
+            it->stats.kernel_launches++;
+        }
         HX_CUDA(cudaMemsetAsync(it->q.counters + (cur ^ 1), 0, 4, st));
         HX_CUDA(cudaMemsetAsync(it->q.counters + 2, 0, 4, st));
         {
@@ -300,6 +312,29 @@ static void clear_images(hx_integrator* it) {  // renderer.cpp:212-223
     cudaMemsetAsync(it->acc, 0, 16 * npix, it->ctx->stream);
     cudaMemsetAsync(it->comp, 0, 16 * npix, it->ctx->stream);
     cudaMemsetAsync(it->count_map, 0, 4 * npix, it->ctx->stream);
+    if (it->aov_a) {
+        cudaMemsetAsync(it->aov_a, 0, 16 * npix, it->ctx->stream);
+        cudaMemsetAsync(it->aov_n, 0, 16 * npix, it->ctx->stream);
+    }
+}
+
+extern "C" hx_status hx_integrator_set_aov_accumulation(hx_integrator* it, uint32_t enabled) {
+    HX_CHECK_ARG(it, "null integrator");
+    if (enabled && !it->aov_a) {
+        const size_t npix = (size_t)it->desc.width * it->desc.height;
+        HX_TRY(hx_alloc_t(it->ctx, &it->aov_a, npix));
+        it->allocs.push_back(it->aov_a);
+        HX_TRY(hx_alloc_t(it->ctx, &it->aov_n, npix));
+        it->allocs.push_back(it->aov_n);
+        HX_CUDA(cudaMemsetAsync(it->aov_a, 0, 16 * npix, it->ctx->stream));
+        HX_CUDA(cudaMemsetAsync(it->aov_n, 0, 16 * npix, it->ctx->stream));
+    }
+    if ((enabled != 0) != it->aov) {  // AOVs must cover the same samples as the image
+        it->accumulated = 0;
+        it->tile_idx = 0;
+    }
+    it->aov = enabled != 0;
+    return HX_OK;
 }
 
 extern "C" hx_status hx_integrator_render_frames(hx_integrator* it, const hx_frame_desc* frame, uint32_t num_frames) {
@@ -473,6 +508,11 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     HX_CHECK_ARG((uint64_t)n <= it->capacity, "frame exceeds wavefront capacity");
     bool kahan = it->desc.policy.accumulation == HX_ACCUM_KAHAN;
     k_resolve<<<it->grid_gen, kGenThreads, 0, st>>>(it->acc, it->count_map, n, kahan ? 1u : 0u, it->resolved);
+    if (it->aov && it->accumulated > 0) {
+        k_features_accumulated<<<it->grid_gen, kGenThreads, 0, st>>>(it->resolved, it->aov_a, it->aov_n, n, d_features);
+        HX_CUDA(cudaGetLastError());
+        return HX_OK;
+    }
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
     k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);

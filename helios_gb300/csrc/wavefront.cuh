@@ -458,4 +458,65 @@ __global__ void k_features(DevScene s, const float4* __restrict__ hit, const flo
     }
 }
 
+// First-hit AOVs accumulated per pixel over the frames of a wavefront, in
+// frame order (exact running mean), right after the primary-ray trace:
+// albedo rgb + depth feature log1p(t)/8 in aov_a, shading normal in aov_n;
+// zeros on a miss.  These are the denoiser's auxiliary features averaged over
+// the same jittered samples as the radiance.
+template <bool FP16>
+__global__ void k_aov_accumulate(DevScene s, Rect rect, uint32_t frame0, uint32_t nframes, const float4* __restrict__ hit,
+                                 float4* __restrict__ aov_a, float4* __restrict__ aov_n, uint32_t W) {
+    const uint32_t npix = rect.w * rect.h;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
+        const uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        const size_t o = (size_t)y * W + x;
+        float4 a = aov_a[o], nn = aov_n[o];
+        for (uint32_t fr = 0; fr < nframes; ++fr) {
+            const uint32_t p = fr * npix + pix;
+            uint32_t prim;
+            float t, u, v;
+            if (FP16) {
+                const uint2 hh = reinterpret_cast<const uint2*>(hit)[p];
+                prim = hh.x;
+                __half2 uv = *reinterpret_cast<const __half2*>(&hh.y);
+                u = __low2float(uv);
+                v = __high2float(uv);
+                t = 1.0f;  // the 8-byte hit record carries no distance
+            } else {
+                const float4 h = hit[p];
+                prim = __float_as_uint(h.y);
+                t = h.x;
+                u = h.z;
+                v = h.w;
+            }
+            V3 alb = v3(0.0f), nrm = v3(0.0f);
+            float depth = 0.0f;
+            if (prim != kNoHit) {
+                Surface sf = populate(s, prim, u, v);
+                alb = sf.albedo;
+                nrm = normalize(sf.normal);
+                depth = log1pf(t) * 0.125f;
+            }
+            const float w = 1.0f / (float)(frame0 + fr + 1);
+            a = make_float4(a.x + (alb.x - a.x) * w, a.y + (alb.y - a.y) * w, a.z + (alb.z - a.z) * w,
+                            a.w + (depth - a.w) * w);
+            nn = make_float4(nn.x + (nrm.x - nn.x) * w, nn.y + (nrm.y - nn.y) * w, nn.z + (nrm.z - nn.z) * w, 0.0f);
+        }
+        aov_a[o] = a;
+        aov_n[o] = nn;
+    }
+}
+
+// Denoiser features from the accumulated image and accumulated AOVs.
+__global__ void k_features_accumulated(const float4* __restrict__ img, const float4* __restrict__ aov_a,
+                                       const float4* __restrict__ aov_n, uint32_t n, float* __restrict__ feat) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 r = img[i];
+        float4* o = reinterpret_cast<float4*>(feat + 12 * (size_t)i);
+        o[0] = make_float4(r.x, r.y, r.z, 0.0f);
+        o[1] = aov_a[i];
+        o[2] = aov_n[i];
+    }
+}
+
 }  // namespace

@@ -80,7 +80,8 @@ def render_pairs(ctx, seeds, width, height, spp_in, spp_target, bounces=8, polic
     spp_target; the inputs are the features of the progressive image after
     each count in spp_in (ascending; an int means one count).  The input
     samples are the first frames of the same sample sequence as the target,
-    a shared fraction of spp_in / spp_target.  With full_res = (W, H) each
+    a shared fraction of spp_in / spp_target; the auxiliary features are
+    averaged over the same samples as the input radiance.  With full_res = (W, H) each
     image is a seeded width x height window of the W x H view (the pixel
     scale of full-resolution renders), else the whole view at width x height."""
     pol = policy if policy is not None else hx.policy_reference()
@@ -105,6 +106,7 @@ def render_pairs(ctx, seeds, width, height, spp_in, spp_target, bounces=8, polic
         for j in range(1, len(counts)):
             ps.targets.copy_from(ps.targets, width * height * TARGET_BYTES, ps.tgt_offset(k + j), ps.tgt_offset(k))
         it.restart_bake()
+        it.set_aov_accumulation(True)  # input features: AOVs averaged over the input's samples
         done = 0
         for c in counts:
             it.render(f, c - done)

@@ -603,9 +603,14 @@ HX_API hx_status hx_denoiser_read_tensor(hx_denoiser* dn, uint32_t training, uin
                                          void* host, uint64_t bytes);
 HX_API hx_status hx_denoiser_read_output(hx_denoiser* dn, uint32_t training, float* host, uint64_t count);
 
+/* First-hit AOV accumulation (albedo, shading normal, depth feature averaged
+ * over the same frames as the image; off by default).  Switching it restarts
+ * the progressive accumulation. */
+HX_API hx_status hx_integrator_set_aov_accumulation(hx_integrator* it, uint32_t enabled);
 /* Denoiser inputs from an integrator: the current accumulated image plus
- * albedo / normal / depth of the primary hits of sample frame_index, into
- * d_features (width*height*12 floats, device memory). */
+ * albedo / normal / depth — the accumulated AOVs when AOV accumulation is on,
+ * else those of the primary hits of sample frame_index — into d_features
+ * (width*height*12 floats, device memory). */
 HX_API hx_status hx_integrator_features(hx_integrator* it, const hx_frame_desc* frame, uint32_t frame_index,
                                         float* d_features);
 /* The accumulated image (resolved RGBA floats) into device memory. */

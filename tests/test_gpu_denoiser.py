@@ -222,3 +222,34 @@ def test_trained_denoiser_beats_plain_accumulation(gpu_ctx):
     dn.close()
     data.close()
 
+
+
+def test_accumulated_aovs_are_the_mean_of_per_sample_aovs(gpu_ctx):
+    """AOV accumulation: the features' albedo / depth / normal after N frames
+    equal the mean of the N per-sample primary-hit AOVs (same jitter)."""
+    from tests.helpers import small_icosphere_scene
+    hs = small_icosphere_scene(level=3, quads=2000, pool=4, mask=64, env=(128, 64))
+    sc = hx.Scene(gpu_ctx, hs)
+    W, H, N = 96, 64, 4
+    f = hx.frame_desc(hs.camera(), W, H)
+    pol = hx.policy_reference()
+    a = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=4, policy=pol)
+    a.set_aov_accumulation(True)
+    a.render(f, 2)
+    a.render(f, N - 2)  # two wavefronts: the running mean carries across calls
+    buf = hx.DeviceBuffer(gpu_ctx, W * H * 48)
+    a.features(f, buf)
+    got = buf.download((H, W, 12))
+    b = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=4, policy=pol)
+    acc = np.zeros((H, W, 12))
+    for k in range(N):
+        b.features(f, buf, frame_index=k)
+        acc += buf.download((H, W, 12))
+    acc /= N
+    for lo, hi in ((4, 8), (8, 11)):
+        assert np.allclose(got[..., lo:hi], acc[..., lo:hi], atol=1e-5), (lo, np.abs(got[..., lo:hi] - acc[..., lo:hi]).max())
+    assert np.allclose(got[..., 0:3], a.read_accumulation()[..., 0:3])
+    a.close()
+    b.close()
+    buf.close()
+    sc.close()
