@@ -42,6 +42,8 @@ struct Chunk {              // device request-table entry: samples x pixels of o
 struct SlotDev {            // per admitted request, device side
     hx_frame_desc frame;
     float4* acc;
+    float4* aov_a;          // denoise requests: accumulated first-hit albedo + depth feature (else null)
+    float4* aov_n;          // and shading normal
     uint32_t width, height, pad[2];
 };
 
@@ -113,6 +115,39 @@ __global__ void k_accumulate_multi(const TableHeader* hdr, const Chunk* chunks, 
     }
 }
 
+// First-hit AOVs of denoise requests, accumulated per pixel in sample order
+// right after the primary-ray trace (the integrator's k_aov_accumulate over
+// the request table).
+__global__ void k_aov_accumulate_multi(const TableHeader* hdr, const Chunk* chunks, const SlotDev* slots, DevScene s,
+                                       const float4* __restrict__ hit) {
+    const uint32_t total = hdr->total_acc, nc = hdr->num_chunks;
+    for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < total; a += gridDim.x * blockDim.x) {
+        const Chunk c = chunks[find_chunk(chunks, nc, a, true)];
+        const SlotDev& sd = slots[c.slot];
+        if (!sd.aov_a) continue;
+        const uint32_t i = a - c.acc_begin;
+        float4 av = sd.aov_a[c.pixel_begin + i], nv = sd.aov_n[c.pixel_begin + i];
+        for (uint32_t smp = 0; smp < c.nsamples; ++smp) {
+            const float4 h = hit[(size_t)c.path_begin + (size_t)smp * c.npix + i];
+            const uint32_t prim = __float_as_uint(h.y);
+            V3 alb = v3(0.0f), nrm = v3(0.0f);
+            float depth = 0.0f;
+            if (prim != kNoHit) {
+                Surface sf = populate(s, prim, h.z, h.w);
+                alb = sf.albedo;
+                nrm = normalize(sf.normal);
+                depth = log1pf(h.x) * 0.125f;
+            }
+            const float w = 1.0f / (float)(c.sample_begin + smp + 1);
+            av = make_float4(av.x + (alb.x - av.x) * w, av.y + (alb.y - av.y) * w, av.z + (alb.z - av.z) * w,
+                             av.w + (depth - av.w) * w);
+            nv = make_float4(nv.x + (nrm.x - nv.x) * w, nv.y + (nrm.y - nv.y) * w, nv.z + (nrm.z - nv.z) * w, 0.0f);
+        }
+        sd.aov_a[c.pixel_begin + i] = av;
+        sd.aov_n[c.pixel_begin + i] = nv;
+    }
+}
+
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -134,6 +169,8 @@ struct ServerRequest {
     uchar4* ldr = nullptr;
     float* feat = nullptr;        // denoise: features (12 floats per pixel)
     float4* den = nullptr;        // denoise: denoised radiance
+    float4* aov_a = nullptr;      // denoise: accumulated first-hit AOVs
+    float4* aov_n = nullptr;
     uint8_t* host_ldr = nullptr;  // pinned
     uint32_t samples_done = 0, pixel_cursor = 0;
     bool in_flight = false, finishing = false, done = false;
@@ -202,11 +239,12 @@ struct hx_server {
 static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // Arena bytes of a request: accumulation (16 B/px) + RGBA8 (4 B/px), and
-// with denoise its features (48 B/px) and denoised image (16 B/px).
+// with denoise its features (48 B/px), denoised image (16 B/px) and
+// accumulated AOVs (2 x 16 B/px).
 static size_t request_bytes(const hx_request_desc& d) {
     size_t npix = (size_t)d.width * d.height;
     size_t b = round256(16 * npix) + round256(4 * npix);
-    if (d.denoise) b += round256(48 * npix) + round256(16 * npix);
+    if (d.denoise) b += round256(48 * npix) + 3 * round256(16 * npix);
     return b;
 }
 
@@ -297,6 +335,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
         cudaMemsetAsync(b->q.counters + 4, 0, 8, st);
         k_trace<false><<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q.o[cur], b->q.d[cur], b->q.p[cur], b->q.counters + cur,
                                                              b->q.hit, b->q.stats, b->q.status, b->q.counters + 4);
+        if (bo == 0)
+            k_aov_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, sc, b->q.hit);
         cudaMemsetAsync(b->q.counters + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(b->q.counters + 2, 0, 4, st);
         k_shade<false><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
@@ -355,6 +395,8 @@ static void admit(hx_server* s) {
         if (r->desc.denoise) {
             r->feat = (float*)(s->arena + off + round256(16 * npix) + round256(4 * npix));
             r->den = (float4*)((char*)r->feat + round256(48 * npix));
+            r->aov_a = (float4*)((char*)r->den + round256(16 * npix));
+            r->aov_n = (float4*)((char*)r->aov_a + round256(16 * npix));
         }
         r->t_admit = now_s();
         s->admitted.push_back(r);
@@ -414,25 +456,13 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
     return HX_OK;
 }
 
-// Denoise a finished request: features of its sample-0 primary hits (rays
-// generated and traced in row bands that fit the batch's queues, on the
-// batch stream), then the denoiser on the context stream; the batch stream
-// waits for the result before tone mapping.
+// Denoise a finished request: its features are the accumulated image and
+// the first-hit AOVs accumulated over the same samples (batch stream); the
+// denoiser runs on the context stream and the batch stream waits for it
+// before tone mapping.
 static hx_status denoise_request(hx_server* s, SceneBatch* b, ServerRequest* r) {
     const uint32_t W = r->desc.width, H = r->desc.height;
-    const uint32_t rows = std::max<uint32_t>(1, std::min<uint32_t>(H, s->desc.max_paths_per_tick / W));
-    const DevScene& sc = b->scene->d;
-    Policy P = make_policy(s->desc.policy);
-    for (uint32_t y0 = 0; y0 < H; y0 += rows) {
-        Rect rc{0, y0, W, std::min(rows, H - y0)};
-        const uint32_t n = rc.w * rc.h;
-        k_raygen<false><<<b->grid_gen, kGenThreads, 0, b->stream>>>(r->desc.frame, rc, W, H, 0, 1, P.rng, b->q);
-        HX_CUDA(cudaMemsetAsync(b->q.counters + 4, 0, 4, b->stream));
-        k_trace<false><<<b->grid_trace, kTraceThreads, 0, b->stream>>>(sc, b->q.o[0], b->q.d[0], b->q.p[0], b->q.counters,
-                                                                      b->q.hit, b->q.stats, b->q.status, b->q.counters + 4);
-        k_features<<<b->grid_gen, kGenThreads, 0, b->stream>>>(sc, b->q.hit, r->acc + (size_t)y0 * W, n,
-                                                              r->feat + 12 * (size_t)y0 * W);
-    }
+    k_features_accumulated<<<b->grid_gen, kGenThreads, 0, b->stream>>>(r->acc, r->aov_a, r->aov_n, W * H, r->feat);
     HX_CUDA(cudaGetLastError());
     HX_CUDA(cudaEventRecord(s->dn_ready, b->stream));
     HX_CUDA(cudaStreamWaitEvent(s->ctx->stream, s->dn_ready, 0));
@@ -509,10 +539,16 @@ static hx_status upload_new_slots(hx_server* s, cudaStream_t st, const std::vect
         std::memset(&sd, 0, sizeof(sd));
         sd.frame = r->desc.frame;
         sd.acc = r->acc;
+        sd.aov_a = r->aov_a;
+        sd.aov_n = r->aov_n;
         sd.width = r->desc.width;
         sd.height = r->desc.height;
         HX_CUDA(cudaMemcpyAsync(s->d_slots + r->slot, &sd, sizeof(sd), cudaMemcpyHostToDevice, st));
         HX_CUDA(cudaMemsetAsync(r->acc, 0, 16ull * r->desc.width * r->desc.height, st));
+        if (r->aov_a) {
+            HX_CUDA(cudaMemsetAsync(r->aov_a, 0, 16ull * r->desc.width * r->desc.height, st));
+            HX_CUDA(cudaMemsetAsync(r->aov_n, 0, 16ull * r->desc.width * r->desc.height, st));
+        }
     }
     if (!fresh.empty()) HX_CUDA(cudaStreamSynchronize(st));
     return HX_OK;

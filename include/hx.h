@@ -484,8 +484,8 @@ HX_API hx_status hx_server_create(hx_context* ctx, const hx_server_desc* desc, h
 /* Makes a resident scene servable (captures its tick as a CUDA graph). */
 HX_API hx_status hx_server_add_scene(hx_server* server, const hx_scene* scene, uint32_t* scene_id);
 /* Attaches the learned denoiser used for requests with denoise set (same
- * context; before hx_server_start).  A finished request then gets first-hit
- * features traced on its scene's stream and is denoised on the context
+ * context; before hx_server_start).  Such a request accumulates first-hit
+ * AOVs while it renders; when it finishes it is denoised on the context
  * stream before tone mapping. */
 HX_API hx_status hx_server_set_denoiser(hx_server* server, hx_denoiser* denoiser);
 /* Starts the worker thread (admission, batching, launches). */

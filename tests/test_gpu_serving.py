@@ -108,8 +108,9 @@ def test_admission_by_hbm_budget(gpu_ctx, scenes):
 
 def test_denoised_requests_identical_alone_in_the_mix_and_to_the_integrator(gpu_ctx, scenes):
     """Requests with denoise set: the served RGBA8 equals the integrator's
-    denoise of the same view and sample count, alone and in a mix with plain
-    requests (the denoiser's kernels are deterministic)."""
+    denoise (with AOV accumulation) of the same view and sample count, alone
+    and in a mix with plain requests (the denoiser's kernels are
+    deterministic)."""
     from oracle import denoiser_ref as dr
     (box, s_box), (ico, s_ico) = scenes
     pol = hx.policy_reference()
@@ -119,7 +120,7 @@ def test_denoised_requests_identical_alone_in_the_mix_and_to_the_integrator(gpu_
     ii = srv.add_scene(s_ico)
     srv.set_denoiser(dn)
     srv.start()
-    w, h, spp = 640, 360, 2  # 230,400 px: features traced in row bands of a 2^18-path tick
+    w, h, spp = 640, 360, 2  # 230,400 px: one sample per 2^18-path tick
     f = hx.frame_desc(ico.camera(), w, h)
     rid = srv.submit(ii, f, w, h, spp, denoise=True)
     _wait_all(srv, [rid])
@@ -132,6 +133,7 @@ def test_denoised_requests_identical_alone_in_the_mix_and_to_the_integrator(gpu_
     assert np.array_equal(alone, imgs[ids[1]])
     assert st.requests_denoised == 2
     it = hx.PathIntegrator(gpu_ctx, s_ico, w, h, max_ray_bounces=6, max_samples=spp, policy=pol)
+    it.set_aov_accumulation(True)
     it.render(f, spp)
     ldr, _ = it.denoise(dn, f, op=hx.TONEMAP_ACES, exposure=1.0, hdr=False, ldr=True)
     it.close()
