@@ -77,7 +77,11 @@ extern "C" hx_status hx_context_create(int device, uint64_t budget, hx_context**
     ctx->device = device;
     ctx->budget = budget;
     ctx->num_sms = prop.multiProcessorCount;
-    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    // highest priority: the serving loop's denoiser and short requests share
+    // the device with long ticks on low-priority streams
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    e = cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, hi_prio);
     if (e != cudaSuccess) {
         delete ctx;
         hx_set_error("cudaStreamCreate: %s", cudaGetErrorString(e));

@@ -200,6 +200,9 @@ struct SceneBatch {
     bool finish_busy = false;
     uint64_t ticks = 0;
     int grid_trace = 0, grid_gen = 0;
+    cudaStream_t hi = nullptr;   // high-priority stream for ticks of short requests
+    cudaStream_t run = nullptr;  // stream of the tick in flight (and its finishing work)
+    bool urgent = false;         // the tick in flight serves a short request
 };
 
 struct hx_server {
@@ -309,7 +312,11 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     HX_TRY(A((void**)&b->d_hdr, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks));
     b->d_chunks = (Chunk*)(b->d_hdr + 1);
     HX_CUDA(cudaMallocHost(&b->h_table, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks));
-    HX_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    int lo_prio = 0, hi_prio = 0;
+    HX_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    HX_CUDA(cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, lo_prio));
+    HX_CUDA(cudaStreamCreateWithPriority(&b->hi, cudaStreamNonBlocking, hi_prio));
+    b->run = b->stream;
     HX_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
     HX_CUDA(cudaEventCreateWithFlags(&b->finish_ev, cudaEventDisableTiming));
     HX_CUDA(cudaMemsetAsync(b->q.stats, 0, 64, b->stream));
@@ -361,6 +368,10 @@ static void batch_free(hx_server* s, SceneBatch* b) {
     if (b->done) cudaEventDestroy(b->done);
     if (b->finish_ev) cudaEventDestroy(b->finish_ev);
     if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->hi) {
+        cudaStreamSynchronize(b->hi);
+        cudaStreamDestroy(b->hi);
+    }
     delete b;
 }
 
@@ -372,7 +383,12 @@ static void admit(hx_server* s) {
     for (auto it = s->pending.begin(); it != s->pending.end();) {
         ServerRequest* r = it->second;
         if (s->free_slots.empty()) break;
-        if (!s->admitted.empty() && s->admitted_work + r->work > s->desc.admitted_work_paths) break;
+        // the admitted-work cap holds back long requests only: a request
+        // that fits in one tick is always admitted (memory permitting), so a
+        // long request admitted into an idle server cannot block short ones
+        if (!s->admitted.empty() && r->work > s->desc.max_paths_per_tick &&
+            s->admitted_work + r->work > s->desc.admitted_work_paths)
+            break;
         size_t off, hoff;
         if (!arena_alloc(s->arena_free, r->arena_bytes, &off)) {
             ++it;
@@ -447,8 +463,13 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
     hdr->num_chunks = nc;
     hdr->total_paths = paths;
     hdr->total_acc = accs;
-    HX_CUDA(cudaGraphLaunch(b->graph, b->stream));
-    HX_CUDA(cudaEventRecord(b->done, b->stream));
+    // a tick whose shortest request fits in one tick runs on the
+    // high-priority stream: its kernels overtake long requests' kernels at
+    // kernel boundaries (the graph takes the priority of its launch stream)
+    b->urgent = remaining(cand.front()) <= (uint64_t)cap;
+    b->run = b->urgent ? b->hi : b->stream;
+    HX_CUDA(cudaGraphLaunch(b->graph, b->run));
+    HX_CUDA(cudaEventRecord(b->done, b->run));
     b->busy = true;
     b->ticks++;
     s->ticks_total++;
@@ -462,13 +483,13 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
 // before tone mapping.
 static hx_status denoise_request(hx_server* s, SceneBatch* b, ServerRequest* r) {
     const uint32_t W = r->desc.width, H = r->desc.height;
-    k_features_accumulated<<<b->grid_gen, kGenThreads, 0, b->stream>>>(r->acc, r->aov_a, r->aov_n, W * H, r->feat);
+    k_features_accumulated<<<b->grid_gen, kGenThreads, 0, b->run>>>(r->acc, r->aov_a, r->aov_n, W * H, r->feat);
     HX_CUDA(cudaGetLastError());
-    HX_CUDA(cudaEventRecord(s->dn_ready, b->stream));
+    HX_CUDA(cudaEventRecord(s->dn_ready, b->run));
     HX_CUDA(cudaStreamWaitEvent(s->ctx->stream, s->dn_ready, 0));
     HX_TRY(hx_denoiser_infer(s->denoiser, r->feat, 1, H, W, reinterpret_cast<float*>(r->den)));
     HX_CUDA(cudaEventRecord(s->dn_done, s->ctx->stream));
-    HX_CUDA(cudaStreamWaitEvent(b->stream, s->dn_done, 0));
+    HX_CUDA(cudaStreamWaitEvent(b->run, s->dn_done, 0));
     s->denoised++;
     return HX_OK;
 }
@@ -492,16 +513,16 @@ static hx_status retire_tick(hx_server* s, SceneBatch* b) {
             // (denoise, then) tone map to RGBA8 and copy to the request's pinned host buffer
             r->finishing = true;
             if (r->desc.denoise) HX_TRY(denoise_request(s, b, r));
-            k_tonemap<<<s->ctx->num_sms * 4, kGenThreads, 0, b->stream>>>(r->desc.denoise ? r->den : r->acc, nullptr,
+            k_tonemap<<<s->ctx->num_sms * 4, kGenThreads, 0, b->run>>>(r->desc.denoise ? r->den : r->acc, nullptr,
                                                                            r->desc.width, r->desc.height,
                                                                            r->desc.tonemap_op, r->desc.exposure, r->ldr);
-            HX_CUDA(cudaMemcpyAsync(r->host_ldr, r->ldr, 4ull * npix_img, cudaMemcpyDeviceToHost, b->stream));
+            HX_CUDA(cudaMemcpyAsync(r->host_ldr, r->ldr, 4ull * npix_img, cudaMemcpyDeviceToHost, b->run));
             b->finishing.push_back(r);
         }
     }
     b->running.clear();
     if (!b->finishing.empty()) {
-        HX_CUDA(cudaEventRecord(b->finish_ev, b->stream));
+        HX_CUDA(cudaEventRecord(b->finish_ev, b->run));
         b->finish_busy = true;
     }
     b->busy = false;
@@ -570,16 +591,20 @@ static void worker_main(hx_server* s) {
         hx_status st = upload_new_slots(s, setup, fresh);
         if (st == HX_OK) {
             std::unique_lock<std::mutex> lk(s->mu);
-            uint32_t ticking = 0;
+            uint32_t ticking = 0, urgent = 0;
             for (uint32_t k = 0; k < s->batches.size() && st == HX_OK; ++k) {
                 SceneBatch* b = s->batches[k];
                 if (b->finish_busy && cudaEventQuery(b->finish_ev) == cudaSuccess) complete_finished(s, b);
                 if (b->busy && cudaEventQuery(b->done) == cudaSuccess) st = retire_tick(s, b);
-                if (b->busy) ++ticking;
+                if (b->busy) {
+                    ++ticking;
+                    if (b->urgent) ++urgent;
+                }
             }
             // start ticks up to the concurrency limit, scene of the globally
-            // smallest remaining request first (shortest remaining work)
-            while (st == HX_OK && ticking < s->desc.max_concurrent_ticks) {
+            // smallest remaining request first (shortest remaining work); a
+            // request that fits in one tick may start one tick beyond the limit
+            while (st == HX_OK) {
                 int best = -1;
                 uint64_t best_work = ~0ull;
                 for (ServerRequest* r : s->admitted) {
@@ -590,8 +615,11 @@ static void worker_main(hx_server* s) {
                     if (w < best_work) { best_work = w; best = (int)r->desc.scene_id; }
                 }
                 if (best < 0) break;
+                const bool short_req = best_work <= s->desc.max_paths_per_tick;
+                if (ticking >= s->desc.max_concurrent_ticks && !(short_req && urgent == 0)) break;
                 st = launch_tick(s, s->batches[best], (uint32_t)best);
                 ++ticking;
+                if (s->batches[best]->urgent) ++urgent;
             }
             for (SceneBatch* b : s->batches)
                 if (b->busy || b->finish_busy) idle = false;
