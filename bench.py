@@ -666,12 +666,30 @@ def run_denoise(args, dist):
         res = {"seed": seed, "ref_spp": args.dn_ref_spp, "frame_ms_plain": frame_ms_plain,
                "frame_ms_with_aov": frame_ms, "features_plus_infer_ms": dn_ms, "infer_ms": infer_ms,
                "rel_rmse_plain": plain}
+        # plain spp reaching a given error: log-log interpolation of the
+        # measured curve, extrapolated past 256 spp with its last slope
+        cs = sorted(plain)
+        lx, ly = np.log([float(c) for c in cs]), np.log([plain[c] for c in cs])
+
+        def plain_spp_for(err):
+            le = np.log(err)
+            for j in range(len(cs) - 1):
+                if ly[j] >= le >= ly[j + 1] and ly[j] > ly[j + 1]:
+                    return float(np.exp(lx[j] + (le - ly[j]) * (lx[j + 1] - lx[j]) / (ly[j + 1] - ly[j])))
+            if le > ly[0]:
+                return float(cs[0])
+            slope = (ly[-1] - ly[-2]) / (lx[-1] - lx[-2])
+            return float(np.exp(lx[-1] + (le - ly[-1]) / slope))
+
         for k in nets:
             ok = [c for c in sorted(dnz[k]) if dnz[k][c] <= e256]
             s_star = ok[0] if ok else None
             t_den = (s_star * frame_ms + dn_ms) if s_star else None
+            eq = {c: plain_spp_for(e) for c, e in dnz[k].items()}
             res[k] = {"rel_rmse_denoised": dnz[k], "denoised_spp_reaching_plain_256": s_star,
-                      "speedup_vs_plain_256": (t_plain / t_den) if t_den else None}
+                      "speedup_vs_plain_256": (t_plain / t_den) if t_den else None,
+                      "plain_spp_at_equal_rmse": eq,
+                      "speedup_at_equal_rmse": {c: eq[c] * frame_ms_plain / (c * frame_ms + dn_ms) for c in eq}}
         evals.append(res)
         it.close()
         sc.close()

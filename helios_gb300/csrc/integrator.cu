@@ -93,6 +93,7 @@ struct hx_integrator {
     float4* aov_a = nullptr;      // accumulated first-hit albedo + depth feature (AOV accumulation on)
     float4* aov_n = nullptr;      // accumulated first-hit shading normal
     bool aov = false;
+    uint32_t aov_frames = 0;      // frames in the AOV buffers since they were cleared
     float* feat = nullptr;        // denoiser features (12 floats per pixel), on first use
     float4* denoised = nullptr;
     // progressive state (path_integrator.h:46-53)
@@ -277,6 +278,7 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             else
                 k_aov_accumulate<false><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
                                                                            it->aov_n, it->desc.width);
+            it->aov_frames += nframes;
             it->stats.kernel_launches++;
         }
         HX_CUDA(cudaMemsetAsync(it->q.counters + (cur ^ 1), 0, 4, st));
@@ -316,6 +318,7 @@ static void clear_images(hx_integrator* it) {  // renderer.cpp:212-223
         cudaMemsetAsync(it->aov_a, 0, 16 * npix, it->ctx->stream);
         cudaMemsetAsync(it->aov_n, 0, 16 * npix, it->ctx->stream);
     }
+    it->aov_frames = 0;
 }
 
 extern "C" hx_status hx_integrator_set_aov_accumulation(hx_integrator* it, uint32_t enabled) {
@@ -508,7 +511,9 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     HX_CHECK_ARG((uint64_t)n <= it->capacity, "frame exceeds wavefront capacity");
     bool kahan = it->desc.policy.accumulation == HX_ACCUM_KAHAN;
     k_resolve<<<it->grid_gen, kGenThreads, 0, st>>>(it->acc, it->count_map, n, kahan ? 1u : 0u, it->resolved);
-    if (it->aov && it->accumulated > 0) {
+    // (the progressive counter wraps to 0 when max_samples is reached, the
+    // image and AOV buffers keep the finished frame)
+    if (it->aov && it->aov_frames > 0) {
         k_features_accumulated<<<it->grid_gen, kGenThreads, 0, st>>>(it->resolved, it->aov_a, it->aov_n, n, d_features);
         HX_CUDA(cudaGetLastError());
         return HX_OK;

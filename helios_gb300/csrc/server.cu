@@ -602,8 +602,8 @@ static void worker_main(hx_server* s) {
                 }
             }
             // start ticks up to the concurrency limit, scene of the globally
-            // smallest remaining request first (shortest remaining work); a
-            // request that fits in one tick may start one tick beyond the limit
+            // smallest remaining request first (shortest remaining work); up to
+            // two requests that fit in one tick may start beyond the limit
             while (st == HX_OK) {
                 int best = -1;
                 uint64_t best_work = ~0ull;
@@ -616,7 +616,10 @@ static void worker_main(hx_server* s) {
                 }
                 if (best < 0) break;
                 const bool short_req = best_work <= s->desc.max_paths_per_tick;
-                if (ticking >= s->desc.max_concurrent_ticks && !(short_req && urgent == 0)) break;
+                // while a short request's tick runs, no new long ticks start
+                // (they would interleave their kernels with it)
+                if (!short_req && urgent > 0) break;
+                if (ticking >= s->desc.max_concurrent_ticks && !(short_req && urgent < 2)) break;
                 st = launch_tick(s, s->batches[best], (uint32_t)best);
                 ++ticking;
                 if (s->batches[best]->urgent) ++urgent;
