@@ -449,10 +449,12 @@ def run_serving(args, dist):
 
     lat = [r.latency_ms for r in results]
     classes = {}
+    queue = {}
     for r in results:
         w, h, spp, dz, sid = meta[r.request_id]
         classes.setdefault("%dx%d/%dspp%s" % (w, h, spp, "/denoise" if dz else ""), []).append(r.latency_ms)
         classes.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.latency_ms)
+        queue.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.queue_ms)
     offered = sum(w * h * spp for (w, h, spp, dn, sid) in meta.values())
     line = {"metric": "serving latency p50/p99 (ms) and Mpaths/s", "mode": "serving", "n_gpus": 1,
             "rate_req_per_s": args.rate, "duration_s": args.duration, "requests_submitted": n_req,
@@ -460,6 +462,7 @@ def run_serving(args, dist):
             "throughput_mpaths_per_s": paths / elapsed / 1e6, "offered_mpaths_per_s": offered / args.duration / 1e6,
             "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
             "per_class_latency_ms": {k: {"n": len(v), "p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(classes.items())},
+            "per_class_admission_wait_ms": {k: {"p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(queue.items())},
             "tick_paths": args.tick_paths, "concurrent_ticks": args.concurrent_ticks, "arena_gb": args.arena_gb,
             "denoise": "Bernoulli(0.5) per request; denoiser weights: " + weights,
             "requests_denoised": s1.requests_denoised - s0.requests_denoised, "data": "synthetic"}
