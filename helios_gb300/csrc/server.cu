@@ -200,9 +200,8 @@ struct SceneBatch {
     bool finish_busy = false;
     uint64_t ticks = 0;
     int grid_trace = 0, grid_gen = 0;
-    cudaStream_t hi = nullptr;   // high-priority stream for ticks of short requests
     cudaStream_t run = nullptr;  // stream of the tick in flight (and its finishing work)
-    bool urgent = false;         // the tick in flight serves a short request
+    bool urgent = false;         // the short-request lane of its scene
 };
 
 struct hx_server {
@@ -314,8 +313,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     HX_CUDA(cudaMallocHost(&b->h_table, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks));
     int lo_prio = 0, hi_prio = 0;
     HX_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
-    HX_CUDA(cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, lo_prio));
-    HX_CUDA(cudaStreamCreateWithPriority(&b->hi, cudaStreamNonBlocking, hi_prio));
+    HX_CUDA(cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, b->urgent ? hi_prio : lo_prio));
     b->run = b->stream;
     HX_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
     HX_CUDA(cudaEventCreateWithFlags(&b->finish_ev, cudaEventDisableTiming));
@@ -368,10 +366,6 @@ static void batch_free(hx_server* s, SceneBatch* b) {
     if (b->done) cudaEventDestroy(b->done);
     if (b->finish_ev) cudaEventDestroy(b->finish_ev);
     if (b->stream) cudaStreamDestroy(b->stream);
-    if (b->hi) {
-        cudaStreamSynchronize(b->hi);
-        cudaStreamDestroy(b->hi);
-    }
     delete b;
 }
 
@@ -420,11 +414,22 @@ static void admit(hx_server* s) {
     }
 }
 
+static uint64_t remaining_work(const ServerRequest* r);
+
+// Requests that fit in one tick go to their scene's short lane, the others
+// to its long lane.
+static bool is_short(const hx_server* s, const ServerRequest* r) {
+    return remaining_work(r) <= (uint64_t)s->desc.max_paths_per_tick;
+}
+
 static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
-    // requests of this scene with work left and nothing in flight, shortest remaining work first
+    // requests of this scene and lane with work left and nothing in flight,
+    // shortest remaining work first
     std::vector<ServerRequest*> cand;
     for (ServerRequest* r : s->admitted)
-        if (r->desc.scene_id == scene_id && !r->in_flight && !r->finishing && r->samples_done < r->desc.spp) cand.push_back(r);
+        if (r->desc.scene_id == scene_id && !r->in_flight && !r->finishing && r->samples_done < r->desc.spp &&
+            is_short(s, r) == b->urgent)
+            cand.push_back(r);
     if (cand.empty()) return HX_OK;
     auto remaining = [](const ServerRequest* r) {
         return (uint64_t)(r->desc.spp - r->samples_done) * r->desc.width * r->desc.height - r->pixel_cursor;
@@ -463,11 +468,9 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
     hdr->num_chunks = nc;
     hdr->total_paths = paths;
     hdr->total_acc = accs;
-    // a tick whose shortest request fits in one tick runs on the
-    // high-priority stream: its kernels overtake long requests' kernels at
-    // kernel boundaries (the graph takes the priority of its launch stream)
-    b->urgent = remaining(cand.front()) <= (uint64_t)cap;
-    b->run = b->urgent ? b->hi : b->stream;
+    // the short lane's stream has the high priority: its kernels overtake
+    // long ticks' kernels at kernel boundaries (a graph takes the priority of
+    // its launch stream)
     HX_CUDA(cudaGraphLaunch(b->graph, b->run));
     HX_CUDA(cudaEventRecord(b->done, b->run));
     b->busy = true;
@@ -601,28 +604,28 @@ static void worker_main(hx_server* s) {
                     if (b->urgent) ++urgent;
                 }
             }
-            // start ticks up to the concurrency limit, scene of the globally
+            // start ticks up to the concurrency limit, the lane of the globally
             // smallest remaining request first (shortest remaining work); up to
-            // two requests that fit in one tick may start beyond the limit
+            // two short-lane ticks may run beyond the limit, and no new long
+            // tick starts while a short one runs (their kernels would interleave)
             while (st == HX_OK) {
                 int best = -1;
                 uint64_t best_work = ~0ull;
                 for (ServerRequest* r : s->admitted) {
                     if (r->in_flight || r->finishing || r->samples_done >= r->desc.spp) continue;
-                    SceneBatch* b = s->batches[r->desc.scene_id];
+                    const int lane = 2 * (int)r->desc.scene_id + (is_short(s, r) ? 1 : 0);
+                    SceneBatch* b = s->batches[lane];
                     if (b->busy || b->finish_busy) continue;
                     uint64_t w = remaining_work(r);
-                    if (w < best_work) { best_work = w; best = (int)r->desc.scene_id; }
+                    if (w < best_work) { best_work = w; best = lane; }
                 }
                 if (best < 0) break;
-                const bool short_req = best_work <= s->desc.max_paths_per_tick;
-                // while a short request's tick runs, no new long ticks start
-                // (they would interleave their kernels with it)
+                const bool short_req = (best & 1) != 0;
                 if (!short_req && urgent > 0) break;
                 if (ticking >= s->desc.max_concurrent_ticks && !(short_req && urgent < 2)) break;
-                st = launch_tick(s, s->batches[best], (uint32_t)best);
+                st = launch_tick(s, s->batches[best], (uint32_t)(best / 2));
                 ++ticking;
-                if (s->batches[best]->urgent) ++urgent;
+                if (short_req) ++urgent;
             }
             for (SceneBatch* b : s->batches)
                 if (b->busy || b->finish_busy) idle = false;
@@ -702,15 +705,21 @@ extern "C" hx_status hx_server_set_denoiser(hx_server* s, hx_denoiser* dn) {
 extern "C" hx_status hx_server_add_scene(hx_server* s, const hx_scene* scene, uint32_t* scene_id) {
     HX_CHECK_ARG(s && scene && scene_id, "hx_server_add_scene: null argument");
     HX_CHECK_ARG(!s->running.load(), "hx_server_add_scene: add scenes before hx_server_start");
-    SceneBatch* b = new SceneBatch();
-    b->scene = scene;
-    hx_status st = batch_init(s, b);
-    if (st != HX_OK) {
-        batch_free(s, b);
-        return st;
+    // two lanes per scene: long requests, and requests that fit in one tick
+    SceneBatch* lanes[2] = {nullptr, nullptr};
+    for (int k = 0; k < 2; ++k) {
+        lanes[k] = new SceneBatch();
+        lanes[k]->scene = scene;
+        lanes[k]->urgent = k == 1;
+        hx_status st = batch_init(s, lanes[k]);
+        if (st != HX_OK) {
+            for (int j = 0; j <= k; ++j) batch_free(s, lanes[j]);
+            return st;
+        }
     }
-    *scene_id = (uint32_t)s->batches.size();
-    s->batches.push_back(b);
+    *scene_id = (uint32_t)(s->batches.size() / 2);
+    s->batches.push_back(lanes[0]);
+    s->batches.push_back(lanes[1]);
     return HX_OK;
 }
 
@@ -723,7 +732,7 @@ extern "C" hx_status hx_server_start(hx_server* s) {
 
 extern "C" hx_status hx_server_submit(hx_server* s, const hx_request_desc* d, uint64_t* request_id) {
     HX_CHECK_ARG(s && d && request_id, "hx_server_submit: null argument");
-    HX_CHECK_ARG(d->scene_id < s->batches.size(), "hx_server_submit: unknown scene %u", d->scene_id);
+    HX_CHECK_ARG(d->scene_id < s->batches.size() / 2, "hx_server_submit: unknown scene %u", d->scene_id);
     HX_CHECK_ARG(d->width > 0 && d->height > 0 && (uint64_t)d->width * d->height <= 64ull << 20 && d->spp >= 1,
                  "hx_server_submit: bad request size");
     HX_CHECK_ARG(d->tonemap_op <= 2, "hx_server_submit: bad tone-map operator");
