@@ -236,6 +236,9 @@ struct hx_server {
     // learned denoiser for requests with denoise set (runs on the context stream)
     hx_denoiser* denoiser = nullptr;
     cudaEvent_t dn_ready = nullptr, dn_done = nullptr;
+    // slot-table uploads of newly admitted requests: ticks wait on this event
+    // instead of the worker thread waiting for the uploads
+    cudaEvent_t slots_ev = nullptr;
 };
 
 static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -471,6 +474,7 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
     // the short lane's stream has the high priority: its kernels overtake
     // long ticks' kernels at kernel boundaries (a graph takes the priority of
     // its launch stream)
+    HX_CUDA(cudaStreamWaitEvent(b->run, s->slots_ev, 0));
     HX_CUDA(cudaGraphLaunch(b->graph, b->run));
     HX_CUDA(cudaEventRecord(b->done, b->run));
     b->busy = true;
@@ -574,14 +578,16 @@ static hx_status upload_new_slots(hx_server* s, cudaStream_t st, const std::vect
             HX_CUDA(cudaMemsetAsync(r->aov_n, 0, 16ull * r->desc.width * r->desc.height, st));
         }
     }
-    if (!fresh.empty()) HX_CUDA(cudaStreamSynchronize(st));
+    if (!fresh.empty()) HX_CUDA(cudaEventRecord(s->slots_ev, st));
     return HX_OK;
 }
 
 static void worker_main(hx_server* s) {
     cudaSetDevice(s->ctx->device);
     cudaStream_t setup;
-    cudaStreamCreateWithFlags(&setup, cudaStreamNonBlocking);
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    cudaStreamCreateWithPriority(&setup, cudaStreamNonBlocking, hi_prio);
     while (s->running.load()) {
         std::vector<ServerRequest*> fresh;
         bool idle = true;
@@ -682,7 +688,8 @@ extern "C" hx_status hx_server_create(hx_context* ctx, const hx_server_desc* des
     }
     for (int k = (int)kMaxSlots - 1; k >= 0; --k) s->free_slots.push_back(k);
     if (cudaEventCreateWithFlags(&s->dn_ready, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s->dn_done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&s->dn_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->slots_ev, cudaEventDisableTiming) != cudaSuccess) {
         hx_free(ctx, s->arena);
         hx_free(ctx, s->d_slots);
         cudaFreeHost(s->harena);
@@ -838,6 +845,7 @@ extern "C" hx_status hx_server_destroy(hx_server* s) {
     if (s->d_slots) hx_free(s->ctx, s->d_slots);
     if (s->dn_ready) cudaEventDestroy(s->dn_ready);
     if (s->dn_done) cudaEventDestroy(s->dn_done);
+    if (s->slots_ev) cudaEventDestroy(s->slots_ev);
     delete s;
     return HX_OK;
 }
