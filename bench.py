@@ -12,10 +12,11 @@ value     = paths / device time of K frames (CUDA events on the library stream)
 e2e       = the same through the C-ABI with the frame constants passed from
             the host and the tone-mapped RGBA8 frame copied to pinned host
             memory every step (host wall clock)
-roofline  = closest-hit traversal kernel: algorithmic bytes per launch / its
-            mean launch time (bytes = rays x (ray 36 B + hit 16 B) +
-            node fetches x 80 B + triangle tests x 48 B, counted in a separate
-            counting pass of the same frame)
+roofline  = traversal kernel (k_extend: one bounce's extension rays + the
+            previous bounce's shadow rays): algorithmic bytes per launch / its
+            mean launch time (bytes = extension rays x (ray 36 B + hit 16 B)
+            + shadow rays x 48 B + node fetches x 80 B + triangle tests x
+            48 B, counted in a separate counting pass of the same frame)
 
 --impl reference times the oracle's scalar transcription of the reference
 shaders (the reference's Vulkan path cannot run without a graphics stack) on
@@ -262,7 +263,7 @@ def run_ours(args, dist):
     st = it.stats()
     segs_per_step = st.extension_rays + st.shadow_rays
     ms_trace_per_launch = st.ms_trace / max(1, st.trace_launches)
-    stage = {"raygen": st.ms_raygen, "trace": st.ms_trace, "shade": st.ms_shade, "shadow": st.ms_shadow,
+    stage = {"raygen": st.ms_raygen, "traverse (extension + shadow)": st.ms_trace, "shade": st.ms_shade,
              "accumulate": st.ms_accumulate}
     it.set_timing(False)
     # 2) counting pass: node fetches and triangle tests of the closest-hit launches
@@ -271,8 +272,14 @@ def run_ours(args, dist):
     ct = it.stats()
     it.set_counting(False)
     ext_rays = ct.extension_rays
+    sh_rays = ct.shadow_rays
     trav_bytes = ct.node_visits * 80 + ct.tri_tests * 48
-    alg_bytes_per_launch = (ext_rays * (36 + 16) + trav_bytes) / max(1, ct.trace_launches)
+    alg_bytes_per_launch = (ext_rays * (36 + 16) + sh_rays * 48 + trav_bytes) / max(1, ct.trace_launches)
+    simd = {"node_step_lanes": ct.node_visits / max(1, 32 * ct.warp_node_steps),
+            "tri_step_lanes": ct.tri_tests / max(1, 32 * ct.warp_tri_steps),
+            "loop_busy_lanes": ct.lane_loop_busy / max(1, 32 * ct.warp_loop_iters),
+            "warp_tri_steps_per_node_step": ct.warp_tri_steps / max(1, ct.warp_node_steps),
+            "alpha_tests_per_segment": ct.alpha_tests / max(1, ext_rays + sh_rays)}
 
     # 3) warm-up, then K device-timed frames
     for _ in range(args.warmup):
@@ -327,7 +334,8 @@ def run_ours(args, dist):
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "trace_kernel_traffic.json")))
-        traffic = prof["dram_bytes_per_extension_ray"] * ext_rays / max(1, ct.trace_launches)
+        if prof.get("kernel", "").startswith("k_extend"):
+            traffic = prof["dram_bytes_per_segment"] * (ext_rays + sh_rays) / max(1, ct.trace_launches)
     except Exception:
         pass
 
@@ -358,10 +366,12 @@ def run_ours(args, dist):
                 "gpu_launches": launches_e2e,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                              "frac": achieved / hbm_peak, "traffic": traffic,
-                             "kernel": "k_trace (closest hit)", "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                             "kernel": "k_extend (closest hit + shadow)",
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs",
                              "bytes_per_launch": alg_bytes_per_launch, "ms_per_launch": ms_trace_per_launch,
-                             "node_fetches_per_ray": ct.node_visits / max(1, ext_rays),
-                             "tri_tests_per_ray": ct.tri_tests / max(1, ext_rays)},
+                             "node_fetches_per_segment": ct.node_visits / max(1, ext_rays + sh_rays),
+                             "tri_tests_per_segment": ct.tri_tests / max(1, ext_rays + sh_rays),
+                             "simd_lanes": simd},
                 "clocks": clk,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)

@@ -125,7 +125,9 @@ class Stats(C.Structure):
                 ("ms_total", C.c_double), ("ms_raygen", C.c_double), ("ms_trace", C.c_double),
                 ("ms_shade", C.c_double), ("ms_shadow", C.c_double), ("ms_accumulate", C.c_double),
                 ("trace_launches", C.c_uint32), ("kernel_launches", C.c_uint32),
-                ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64)]
+                ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
+                ("warp_node_steps", C.c_uint64), ("warp_tri_steps", C.c_uint64),
+                ("warp_loop_iters", C.c_uint64), ("lane_loop_busy", C.c_uint64), ("alpha_tests", C.c_uint64)]
 
 
 class SceneInfo(C.Structure):

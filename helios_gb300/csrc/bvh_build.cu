@@ -24,6 +24,10 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr uint32_t kLeafMax = 1;  // triangles per leaf slot
+// meta bytes: the low 5 bits are the slot's bit in the traversal's hit mask
+constexpr uint8_t kMetaEmpty = 0x10;     // bit 16: outside the triangle and child masks
+constexpr uint8_t kMetaInternal = 0x98;  // | slot: bit 7 (internal) + bit 24 + slot
+constexpr uint8_t kMetaLeaf = 0x20;      // | offset: one triangle
 
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {
     v = (v * 0x00010001u) & 0xFF0000FFu;
@@ -345,19 +349,20 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
     for (uint32_t c = 0; c < 8; ++c) {
         if (slot_kid[c] == 0xffffffffu) {
             for (int a = 0; a < 3; ++a) { clo[c][a] = 0.0f; chi[c][a] = 0.0f; }
+            node.meta[c] = kMetaEmpty;
             continue;
         }
         uint32_t it = pl.kids[slot_kid[c]];
         for (int a = 0; a < 3; ++a) { clo[c][a] = klo[slot_kid[c]][a]; chi[c][a] = khi[slot_kid[c]][a]; }
         if (!(it & 0x80000000u) && count[it] > kLeafMax) {
-            node.meta[c] = (uint8_t)(0x80u | rank);
+            node.meta[c] = (uint8_t)(kMetaInternal | c);
             node.internal_mask |= (uint8_t)(1u << c);
             queue[node.child_base + rank] = it;
             ++rank;
         } else {
             uint32_t cnt = (it & 0x80000000u) ? 1u : count[it];
             uint32_t f = (it & 0x80000000u) ? (it & 0x7fffffffu) : first[it];
-            node.meta[c] = (uint8_t)((cnt << 5) | off);
+            node.meta[c] = (uint8_t)(kMetaLeaf | off);
             for (uint32_t q = 0; q < cnt; ++q) leaf_prims[node.prim_base + off + q] = sorted[f + q];
             off += cnt;
         }
@@ -365,7 +370,7 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
     // quantise the occupied slots on the node grid (conservative, exact decode)
     float plo[3] = {INFINITY, INFINITY, INFINITY}, phi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t c = 0; c < 8; ++c) {
-        if (node.meta[c] == 0) continue;
+        if (node.meta[c] == kMetaEmpty) continue;
         for (int a = 0; a < 3; ++a) {
             plo[a] = clo[c][a] < plo[a] ? clo[c][a] : plo[a];
             phi[a] = chi[c][a] > phi[a] ? chi[c][a] : phi[a];
@@ -384,7 +389,7 @@ __global__ void k_collapse_emit(uint32_t* __restrict__ queue, uint32_t level_beg
         node.exponent[a] = (int8_t)e;
         float inv = pow2f(-e);
         for (uint32_t c = 0; c < 8; ++c) {
-            if (node.meta[c] == 0) continue;
+            if (node.meta[c] == kMetaEmpty) continue;
             float fl = floorf((clo[c][a] - origin) * inv);
             int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
             while (ql > 0 && origin + (float)ql * scale > clo[c][a]) --ql;

@@ -8,12 +8,14 @@
 // accumulation then replays them in frame order, so the image is identical
 // to frame-by-frame rendering.
 //
-// Per bounce:  k_trace (closest hit)  ->  k_shade (surface, NEE sample,
-// BSDF sample, Russian roulette; appends shadow rays and next-bounce rays
-// with warp-aggregated atomics)  ->  k_shadow (any-hit visibility, adds the
-// NEE contribution).  Queue lengths live in device memory and every kernel
-// is a grid-stride loop over them, so a frame is enqueued without host
-// round trips.
+// Per bounce:  k_extend (closest hit of this bounce's rays + any-hit
+// visibility of the previous bounce's shadow rays, which add their NEE
+// contribution)  ->  k_shade (surface, NEE sample, BSDF sample, Russian
+// roulette; appends shadow rays and next-bounce rays with warp-aggregated
+// atomics); a last k_extend traces the final bounce's shadow rays.  Queue
+// lengths live in device memory and every kernel is a grid-stride or
+// persistent loop over them, so a frame is enqueued without host round
+// trips.
 #include "wavefront.cuh"
 
 #include <algorithm>
@@ -103,7 +105,7 @@ struct hx_integrator {
     bool timing = false;
     bool counting = false;
     hx_stats stats{};
-    int grid_trace = 0, grid_shadow = 0, grid_shade = 0, grid_gen = 0;
+    int grid_trace = 0, grid_shade = 0, grid_gen = 0;
 };
 
 static void compute_tiles(hx_integrator* it) {  // path_integrator.cpp:312-336
@@ -158,7 +160,7 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_A(it->q.L, 16 * cap);
     HX_A(it->q.rng, 8 * cap);
     HX_A(it->q.counters, 64);
-    HX_A(it->q.stats, 64);
+    HX_A(it->q.stats, 128);
     HX_A(it->q.status, 64);
     HX_A(it->acc, 16 * npix);
     HX_A(it->comp, 16 * npix);
@@ -172,13 +174,11 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_CUDA(cudaMemsetAsync(it->acc, 0, 16 * npix, st));
     HX_CUDA(cudaMemsetAsync(it->comp, 0, 16 * npix, st));
     HX_CUDA(cudaMemsetAsync(it->count_map, 0, 4 * npix, st));
-    HX_CUDA(cudaMemsetAsync(it->q.stats, 0, 64, st));
+    HX_CUDA(cudaMemsetAsync(it->q.stats, 0, 128, st));
     HX_CUDA(cudaMemsetAsync(it->q.status, 0, 64, st));
     int per_sm = 0;
-    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false>, kTraceThreads, 0));
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend<false, false>, kTraceThreads, 0));
     it->grid_trace = std::max(1, per_sm) * ctx->num_sms;
-    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow, kTraceThreads, 0));
-    it->grid_shadow = std::max(1, per_sm) * ctx->num_sms;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     it->grid_shade = std::max(1, per_sm) * ctx->num_sms;
     it->grid_gen = ctx->num_sms * 8;
@@ -251,50 +251,49 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, P.rng, it->q);
         it->stats.kernel_launches++;
     }
-    for (uint32_t b = 0; b < it->desc.max_ray_bounces; ++b) {
-        int cur = b & 1;
-        {
-            StageTimer t(it, &it->stats.ms_trace);
-            HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 8, st));
-#define HX_TRACE(COUNT, FP16)                                                                                       \
-    k_trace<COUNT, FP16><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q.o[cur], it->q.d[cur], it->q.p[cur],     \
-                                                                   it->q.counters + cur, it->q.hit, it->q.stats,     \
-                                                                   it->q.status, it->q.counters + 4)
-            if (it->counting) {
-                if (fp16) HX_TRACE(true, true);
-                else HX_TRACE(true, false);
-            } else {
-                if (fp16) HX_TRACE(false, true);
-                else HX_TRACE(false, false);
+    {
+        // bounce b: k_extend traces the extension rays of b and the shadow
+        // rays of b - 1; a last launch traces the final bounce's shadow rays
+        for (uint32_t b = 0; b <= it->desc.max_ray_bounces; ++b) {
+            const int cur = b & 1;
+            {
+                StageTimer t(it, &it->stats.ms_trace);
+                HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
+#define HX_EXTEND(COUNT, FP16)                                                                                      \
+    k_extend<COUNT, FP16><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q, it->q.o[cur], it->q.d[cur], it->q.p[cur], \
+                                                                    it->q.counters + cur, it->q.counters + 4)
+                if (it->counting) {
+                    if (fp16) HX_EXTEND(true, true);
+                    else HX_EXTEND(true, false);
+                } else {
+                    if (fp16) HX_EXTEND(false, true);
+                    else HX_EXTEND(false, false);
+                }
+#undef HX_EXTEND
+                it->stats.trace_launches++;
+                it->stats.kernel_launches++;
             }
-#undef HX_TRACE
-            it->stats.trace_launches++;
-            it->stats.kernel_launches++;
-        }
-        if (b == 0 && it->aov && accumulate) {
-            if (fp16)
-                k_aov_accumulate<true><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
-                                                                          it->aov_n, it->desc.width);
-            else
-                k_aov_accumulate<false><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
-                                                                           it->aov_n, it->desc.width);
-            it->aov_frames += nframes;
-            it->stats.kernel_launches++;
-        }
-        HX_CUDA(cudaMemsetAsync(it->q.counters + (cur ^ 1), 0, 4, st));
-        HX_CUDA(cudaMemsetAsync(it->q.counters + 2, 0, 4, st));
-        {
-            StageTimer t(it, &it->stats.ms_shade);
-            if (fp16)
-                k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
-            else
-                k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
-            it->stats.kernel_launches++;
-        }
-        {
-            StageTimer t(it, &it->stats.ms_shadow);
-            k_shadow<<<it->grid_shadow, kTraceThreads, 0, st>>>(s, it->q, it->q.counters + 5);
-            it->stats.kernel_launches++;
+            if (b == it->desc.max_ray_bounces) break;
+            if (b == 0 && it->aov && accumulate) {
+                if (fp16)
+                    k_aov_accumulate<true><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
+                                                                              it->aov_n, it->desc.width);
+                else
+                    k_aov_accumulate<false><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
+                                                                               it->aov_n, it->desc.width);
+                it->aov_frames += nframes;
+                it->stats.kernel_launches++;
+            }
+            HX_CUDA(cudaMemsetAsync(it->q.counters + (cur ^ 1), 0, 4, st));
+            HX_CUDA(cudaMemsetAsync(it->q.counters + 2, 0, 4, st));
+            {
+                StageTimer t(it, &it->stats.ms_shade);
+                if (fp16)
+                    k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
+                else
+                    k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
+                it->stats.kernel_launches++;
+            }
         }
     }
     if (accumulate) {
@@ -350,7 +349,7 @@ extern "C" hx_status hx_integrator_render_frames(hx_integrator* it, const hx_fra
         HX_CUDA(cudaEventCreate(&e1));
         HX_CUDA(cudaEventRecord(e0, it->ctx->stream));
     }
-    HX_CUDA(cudaMemsetAsync(it->q.stats, 0, 32, it->ctx->stream));
+    HX_CUDA(cudaMemsetAsync(it->q.stats, 0, 128, it->ctx->stream));
     uint32_t left = num_frames;
     while (left > 0 && it->tile_idx < it->tiles.size()) {
         Rect r = it->tiles[it->tile_idx];
@@ -381,12 +380,17 @@ extern "C" hx_status hx_integrator_render_frames(hx_integrator* it, const hx_fra
         it->stats.ms_total = ms;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        unsigned long long h[4];
-        HX_CUDA(cudaMemcpy(h, it->q.stats, 32, cudaMemcpyDeviceToHost));
+        unsigned long long h[9];
+        HX_CUDA(cudaMemcpy(h, it->q.stats, sizeof(h), cudaMemcpyDeviceToHost));
         it->stats.extension_rays = h[0];
         it->stats.shadow_rays = h[1];
         it->stats.node_visits = h[2];
         it->stats.tri_tests = h[3];
+        it->stats.warp_node_steps = h[4];
+        it->stats.warp_tri_steps = h[5];
+        it->stats.warp_loop_iters = h[6];
+        it->stats.lane_loop_busy = h[7];
+        it->stats.alpha_tests = h[8];
         HX_TRY(check_status(it));
     }
     return HX_OK;

@@ -326,7 +326,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     const DevScene& sc = b->scene->d;
     Policy P = make_policy(s->desc.policy);
     int per_sm = 0;
-    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false>, kTraceThreads, 0));
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend<false, false>, kTraceThreads, 0));
     const int grid_trace = std::max(1, per_sm) * ctx->num_sms;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     const int grid_shade = std::max(1, per_sm) * ctx->num_sms;
@@ -338,17 +338,19 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     HX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaMemcpyAsync(b->d_hdr, b->h_table, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks, cudaMemcpyHostToDevice, st);
     k_raygen_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, P.rng, b->q);
-    for (uint32_t bo = 0; bo < s->desc.max_ray_bounces; ++bo) {
+    // bounce bo: extension rays of bo + shadow rays of bo - 1 in one launch;
+    // the last launch traces the final bounce's shadow rays
+    for (uint32_t bo = 0; bo <= s->desc.max_ray_bounces; ++bo) {
         int cur = bo & 1;
-        cudaMemsetAsync(b->q.counters + 4, 0, 8, st);
-        k_trace<false><<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q.o[cur], b->q.d[cur], b->q.p[cur], b->q.counters + cur,
-                                                             b->q.hit, b->q.stats, b->q.status, b->q.counters + 4);
+        cudaMemsetAsync(b->q.counters + 4, 0, 4, st);
+        k_extend<false, false><<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.d[cur], b->q.p[cur],
+                                                                     b->q.counters + cur, b->q.counters + 4);
+        if (bo == s->desc.max_ray_bounces) break;
         if (bo == 0)
             k_aov_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, sc, b->q.hit);
         cudaMemsetAsync(b->q.counters + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(b->q.counters + 2, 0, 4, st);
         k_shade<false><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
-        k_shadow<<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q, b->q.counters + 5);
     }
     k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp, b->q.L);
     cudaError_t ce = cudaStreamEndCapture(st, &g);

@@ -71,21 +71,43 @@ HXD bool intersect_tri(const RayPre& r, V3 v0, V3 v1, V3 v2, float tmin, float t
     return true;
 }
 
+// q / 255 for a byte q, equal to the IEEE quotient (float)q / 255.0f for all
+// 256 values (checked exhaustively in exact arithmetic): a product with the
+// rounded reciprocal, corrected by one FMA residual step.
+HXD float unorm8(uint32_t q) {
+    const float c = 1.0f / 255.0f;
+    const float x = (float)q;
+    const float r = __fmul_rn(x, c);
+    const float e = __fmaf_rn(-r, 255.0f, x);
+    return __fmaf_rn(e, c, r);
+}
+
 // Software bilinear RGBA8 fetch, REPEAT addressing, level 0; channel c.
+// Power-of-two sizes wrap with a mask (the same integers as the modulo).
 HXD float tex_bilinear(const DevScene& s, uint32_t tex, float u, float v, int c) {
     uint4 td = s.tex_desc[tex];
     int W = (int)td.y, H = (int)td.z;
     float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
     float x0 = floorf(x), y0 = floorf(y);
     float fx = x - x0, fy = y - y0;
-    int ix0 = (((int)x0 % W) + W) % W, iy0 = (((int)y0 % H) + H) % H;
-    int ix1 = (ix0 + 1) % W, iy1 = (iy0 + 1) % H;
+    int ix0, iy0, ix1, iy1;
+    if (((W & (W - 1)) | (H & (H - 1))) == 0) {
+        ix0 = (int)x0 & (W - 1);
+        iy0 = (int)y0 & (H - 1);
+        ix1 = (ix0 + 1) & (W - 1);
+        iy1 = (iy0 + 1) & (H - 1);
+    } else {
+        ix0 = (((int)x0 % W) + W) % W;
+        iy0 = (((int)y0 % H) + H) % H;
+        ix1 = ix0 + 1 == W ? 0 : ix0 + 1;
+        iy1 = iy0 + 1 == H ? 0 : iy0 + 1;
+    }
     const uint32_t* t = s.texels + td.x;
     int sh = 8 * c;
-    float a00 = (float)((__ldg(t + iy0 * W + ix0) >> sh) & 0xffu) / 255.0f;
-    float a10 = (float)((__ldg(t + iy0 * W + ix1) >> sh) & 0xffu) / 255.0f;
-    float a01 = (float)((__ldg(t + iy1 * W + ix0) >> sh) & 0xffu) / 255.0f;
-    float a11 = (float)((__ldg(t + iy1 * W + ix1) >> sh) & 0xffu) / 255.0f;
+    float a00 = unorm8((__ldg(t + iy0 * W + ix0) >> sh) & 0xffu);
+    float a10 = unorm8((__ldg(t + iy0 * W + ix1) >> sh) & 0xffu);
+    float a01 = unorm8((__ldg(t + iy1 * W + ix0) >> sh) & 0xffu);
+    float a11 = unorm8((__ldg(t + iy1 * W + ix1) >> sh) & 0xffu);
     float top = a00 + (a10 - a00) * fx;
     float bot = a01 + (a11 - a01) * fx;
     return top + (bot - top) * fy;
@@ -122,8 +144,10 @@ HXD float byte_biased(uint32_t w, int k) { return __uint_as_float(__byte_perm(w,
 
 // Intersects the ray with the (up to) 8 children of a node held in five
 // 16-byte words and returns the hit mask in node-group form: bit
-// 24 + (slot ^ oct_inv) for a hit internal child, bits off..off+cnt-1 for the
-// triangles of a hit leaf.  Planes decode exactly (the builder snaps each
+// 24 + (slot ^ oct_inv) for a hit internal child, bit off for the triangle of
+// a hit leaf slot (bit 16, outside both masks, for an empty slot).  The meta
+// bytes carry these bit positions (internal slots: 24 + slot, flagged by bit
+// 7, which selects the XOR with the ray octant), four slots per word.  Planes decode exactly (the builder snaps each
 // node grid so origin + q 2^e is representable and |origin| < 2^23 2^e):
 // L = (2^23 + q) * 2^e + (origin - 2^23 2^e), one rounding-free FMA; then
 // t = (L - o) * inv, with the far planes multiplied by the slack-widened
@@ -147,10 +171,12 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
     const float2 Ox2 = make_float2(Ox, Ox), Oy2 = make_float2(Oy, Oy), Oz2 = make_float2(Oz, Oz);
     const float2 ox2 = make_float2(r.o.x, r.o.x), oy2 = make_float2(r.o.y, r.o.y), oz2 = make_float2(r.o.z, r.o.z);
     const float2 ix2 = make_float2(r.ix, fix), iy2 = make_float2(r.iy, fiy), iz2 = make_float2(r.iz, fiz);
+    const uint32_t mw0 = (w1.z ^ (((w1.z & 0x80808080u) >> 7) * oct_inv)) & 0x1f1f1f1fu;
+    const uint32_t mw1 = (w1.w ^ (((w1.w & 0x80808080u) >> 7) * oct_inv)) & 0x1f1f1f1fu;
     uint32_t hits = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-        const uint32_t m = byte_of(c < 4 ? w1.z : w1.w, c & 3);
+        const uint32_t pos = byte_of(c < 4 ? mw0 : mw1, c & 3);
         const int k = c & 3;
         // (near, far) pairs per axis in packed FP32x2: L = q' S + O, t = (L - o) inv
         const float2 Lx = fma2_rn(make_float2(byte_biased(c < 4 ? nx0 : nx1, k), byte_biased(c < 4 ? fx0 : fx1, k)), Sx2, Ox2);
@@ -161,17 +187,21 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
         const float2 tz = mul2_rn(sub2_rn(Lz, oz2), iz2);
         const float tn = fmaxf(max3f(tx.x, ty.x, tz.x), tmin);
         const float tf = fminf(min3f(tx.y, ty.y, tz.y), lim);
-        if (m != 0u && tn <= tf) {
-            if (m & 0x80u) hits |= 1u << (24 + (c ^ oct_inv));
-            else hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-        }
+        if (tn <= tf) hits |= 1u << pos;
     }
     return hits;
 }
 
+// Counting mode: lane-level node visits and triangle tests, and the
+// warp-level steps that executed them (lanes per warp step = SIMD
+// utilisation of each phase).
 struct TraverseCount {
     uint32_t nodes = 0, tris = 0;
+    uint32_t warp_nodes = 0, warp_tris = 0;
+    uint32_t alpha = 0;  // any-hit alpha tests
 };
+
+HXD bool lowest_active_lane() { return (threadIdx.x & 31u) == (uint32_t)(__ffs(__activemask()) - 1); }
 
 // Closest hit (shadow = false) or first accepted hit (shadow = true) over the
 // compressed 8-wide BVH.  Children are visited near-to-far by the octant
@@ -216,7 +246,7 @@ HXD bool trace_bvh8(const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool 
             g_base = w1.x;
             g_mask = (hm & 0xff000000u) | (w0.w >> 24);
             t_base = w1.y;
-            t_mask = hm & 0x00ffffffu;
+            t_mask = hm & 0xffu;
         } else {
             t_base = g_base;  // a postponed triangle group popped from the stack
             t_mask = g_mask;
@@ -273,6 +303,7 @@ struct TravState {
     int sp;
     uint32_t visits_left;
     bool any_hit;
+    bool shadow;  // first accepted hit ends the ray (read when trav_step's DYN is set)
 };
 
 HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool any_hit) {
@@ -293,13 +324,16 @@ HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, flo
     st.sp = 0;
     st.visits_left = s.num_nodes + 16;
     st.any_hit = any_hit;
+    st.shadow = false;
 }
 
 // Returns true when the ray is finished (traversal exhausted, or the first
 // accepted hit of a shadow ray).
 constexpr int kPostponeLanes = 8;  // postpone triangle tests below this many lanes
 
-template <bool SHADOW, bool COUNT, bool POSTPONE = false>
+// SHADOW: every ray of the launch is a shadow ray; DYN: the lane's st.shadow
+// decides (extension and shadow rays in one launch).
+template <bool SHADOW, bool COUNT, bool POSTPONE = false, bool DYN = false>
 HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflow, TraverseCount* tc) {
     if (st.g_mask > 0x00ffffffu) {
         const uint32_t bit = 31u - __clz(st.g_mask);
@@ -316,13 +350,16 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         }
         const uint4* np = reinterpret_cast<const uint4*>(s.nodes + child);
         const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-        if (COUNT) tc->nodes++;
+        if (COUNT) {
+            tc->nodes++;
+            if (lowest_active_lane()) tc->warp_nodes++;
+        }
         const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.fix, st.fiy, st.fiz, st.oct_inv, st.tmin,
                                                st.best_t * 1.000001f);
         st.g_base = w1.x;
         st.g_mask = (hm & 0xff000000u) | (w0.w >> 24);
         st.t_base = w1.y;
-        st.t_mask = hm & 0x00ffffffu;
+        st.t_mask = hm & 0xffu;
     } else {
         st.t_base = st.g_base;
         st.t_mask = st.g_mask;
@@ -345,7 +382,10 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
             overflow = true;
             return true;
         }
-        if (COUNT) tc->tris++;
+        if (COUNT) {
+            tc->tris++;
+            if (lowest_active_lane()) tc->warp_tris++;
+        }
         const float4 a = __ldg(&s.tri[3 * (size_t)k]);
         const float4 bb = __ldg(&s.tri[3 * (size_t)k + 1]);
         const float4 cc = __ldg(&s.tri[3 * (size_t)k + 2]);
@@ -353,9 +393,12 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         if (!intersect_tri(st.r, v3(a), v3(bb), v3(cc), st.tmin, st.best_t, t, u, v)) continue;
         const uint32_t prim = __float_as_uint(a.w);
         if (!(t < st.best_t || (t == st.best_t && prim < st.best))) continue;
-        if (st.any_hit && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE) && !alpha_pass(s, prim, u, v)) continue;
+        if (st.any_hit && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE)) {
+            if (COUNT) tc->alpha++;
+            if (!alpha_pass(s, prim, u, v)) continue;
+        }
         st.best_t = t; st.bu = u; st.bv = v; st.best = prim;
-        if (SHADOW) return true;
+        if (SHADOW || (DYN && st.shadow)) return true;
     }
     if (st.g_mask <= 0x00ffffffu) {
         if (st.sp == 0) return true;

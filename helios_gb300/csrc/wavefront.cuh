@@ -30,7 +30,7 @@ struct Queues {
     float4* L;          // radiance
     uint2* rng;
     uint32_t* counters; // [0],[1] ray queues, [2] shadow queue, [4],[5] trace / shadow fetch cursors
-    unsigned long long* stats;  // [0] extension rays, [1] shadow rays
+    unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2..8] counting mode (k_extend)
     uint32_t* status;   // bit 0: traversal stack overflow
 };
 
@@ -292,16 +292,37 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, u
     }
 }
 
-// Persistent-warp any-hit kernel for the shadow queue (fetch counter at
-// fetch[1]); an unoccluded entry adds its NEE contribution to its path.
-__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevScene s, Queues q, uint32_t* fetch) {
-    const uint32_t n = q.counters[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+// Persistent-warp traversal of one bounce's extension rays (qo/qd/qp, count,
+// closest hit) followed by the previous bounce's shadow rays (any hit; an
+// unoccluded entry adds its NEE contribution to its path) in one launch:
+// lanes pull from the concatenated index space [extension | shadow], so the
+// shadow rays fill the lanes that the extension rays' tail leaves idle and a
+// bounce costs one traversal launch instead of two.  The radiance is the same
+// as with separate launches: the shadow contribution of bounce b still lands
+// in L after shade(b) and before shade(b + 1).  Fetch counter at fetch[0];
+// stats [0] extension rays, [1] shadow rays, and in counting mode [2] node
+// visits, [3] triangle tests, [4] warp node steps, [5] warp triangle steps,
+// [6] warp loop iterations, [7] lane loop iterations with a ray, [8] alpha
+// tests.
+template <bool COUNT, bool FP16>
+__global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevScene s, Queues q, const float4* __restrict__ qo,
+                                                                           const float4* __restrict__ qd,
+                                                                           const uint32_t* __restrict__ qp,
+                                                                           const uint32_t* __restrict__ count,
+                                                                           uint32_t* fetch) {
+    const uint32_t n_ext = *count;
+    const uint32_t n = n_ext + q.counters[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&q.stats[0], (unsigned long long)n_ext);
+        atomicAdd(&q.stats[1], (unsigned long long)(n - n_ext));
+    }
     const uint32_t lane = threadIdx.x & 31u;
     bool overflow = false;
+    TraverseCount cnt;
+    uint32_t loop_iters = 0, loop_busy = 0;
     uint2 stack[kStackSize];
     TravState st;
-    uint32_t ray = kNoHit;
+    uint32_t ray = kNoHit;  // kNoHit: lane needs a ray; else the queue index (shadow: minus n_ext)
     bool done = false;
     for (;;) {
         const uint32_t need = __ballot_sync(0xffffffffu, ray == kNoHit && !done);
@@ -312,27 +333,60 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_shadow(DevSc
             base = __shfl_sync(0xffffffffu, base, leader);
             if (need & (1u << lane)) {
                 const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
-                if (i < n) {
+                if (i < n_ext) {
                     ray = i;
-                    const float4 o = q.so[i], d = q.sd[i];
+                    const bool any = (qp[i] & kAnyHitFlag) != 0;
+                    const float4 o = qo[i];
+                    if (FP16) {
+                        trav_init(st, s, v3(o), oct_decode(__float_as_uint(o.w)), any ? 0.001f : 0.0001f, 10000.0f, any);
+                    } else {
+                        const float4 d = qd[i];
+                        trav_init(st, s, v3(o), v3(d), o.w, d.w, any);
+                    }
+                } else if (i < n) {
+                    ray = i - n_ext;
+                    const float4 o = q.so[ray], d = q.sd[ray];
                     trav_init(st, s, v3(o), v3(d), 0.0001f, o.w, __float_as_uint(d.w) != 0u);
+                    st.shadow = true;
                 } else {
                     done = true;
                 }
             }
         }
-        if (__ballot_sync(0xffffffffu, ray != kNoHit) == 0) break;
+        const uint32_t busy = __ballot_sync(0xffffffffu, ray != kNoHit);
+        if (busy == 0) break;
+        if (COUNT) {
+            if (lane == 0) loop_iters++;
+            if (ray != kNoHit) loop_busy++;
+        }
         if (ray != kNoHit) {
-            if (trav_step<true, false>(st, stack, s, overflow, nullptr)) {
-                if (st.best == kNoHit) {
-                    const float4 c = q.sc[ray];
-                    const uint32_t path = __float_as_uint(c.w);
-                    const float4 L = q.L[path];
-                    q.L[path] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+            if (trav_step<false, COUNT, false, true>(st, stack, s, overflow, &cnt)) {
+                if (st.shadow) {
+                    if (st.best == kNoHit) {
+                        const float4 c = q.sc[ray];
+                        const uint32_t path = __float_as_uint(c.w);
+                        const float4 L = q.L[path];
+                        q.L[path] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+                    }
+                } else if (FP16) {
+                    reinterpret_cast<uint2*>(q.hit)[ray] =
+                        make_uint2(st.best, st.best != kNoHit ? half2_bits(st.bu, st.bv) : 0u);
+                } else {
+                    q.hit[ray] = st.best != kNoHit ? make_float4(st.best_t, __uint_as_float(st.best), st.bu, st.bv)
+                                                   : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
                 }
                 ray = kNoHit;
             }
         }
+    }
+    if (COUNT) {
+        atomicAdd(&q.stats[2], (unsigned long long)cnt.nodes);
+        atomicAdd(&q.stats[3], (unsigned long long)cnt.tris);
+        atomicAdd(&q.stats[4], (unsigned long long)cnt.warp_nodes);
+        atomicAdd(&q.stats[5], (unsigned long long)cnt.warp_tris);
+        atomicAdd(&q.stats[6], (unsigned long long)loop_iters);
+        atomicAdd(&q.stats[7], (unsigned long long)loop_busy);
+        atomicAdd(&q.stats[8], (unsigned long long)cnt.alpha);
     }
     if (overflow) atomicOr(q.status, 1u);
 }

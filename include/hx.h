@@ -272,9 +272,10 @@ typedef struct hx_hit {
 /* Compressed 8-wide BVH node (80 B).  Child boxes are stored as 8-bit
  * offsets on a per-node grid: lo = origin + q * 2^exponent (exact products,
  * one rounded add), quantised outward so every decoded child box contains
- * the exact one.  meta[i]: 0 = empty slot; 0x80 | k = internal child
- * (node child_base + k); (n << 5) | off = leaf with n (1..3) triangles at
- * leaf-triangle index prim_base + off. */
+ * the exact one.  meta[i] holds the slot's hit-bit position in its low 5
+ * bits: 0x10 = empty slot; 0x80 | (24 + i) = internal child (node
+ * child_base + the number of internal slots below i); 0x20 | off = leaf
+ * slot with one triangle at leaf-triangle index prim_base + off (off < 8). */
 typedef struct hx_bvh8_node {
     float    origin[3];
     int8_t   exponent[3];
@@ -291,11 +292,21 @@ typedef struct hx_stats {
     uint64_t extension_rays;   /* closest-hit queries                        */
     uint64_t shadow_rays;      /* any-hit visibility queries                 */
     double   ms_total;         /* device time of the last render call        */
-    double   ms_raygen, ms_trace, ms_shade, ms_shadow, ms_accumulate;
-    uint32_t trace_launches;   /* closest-hit launches in the last call      */
+    double   ms_raygen, ms_trace, ms_shade, ms_shadow, ms_accumulate;  /* ms_trace covers the
+                                  shadow rays too (one traversal launch per bounce); ms_shadow is 0 */
+    uint32_t trace_launches;   /* traversal launches in the last call        */
     uint32_t kernel_launches;  /* all kernel launches in the last call       */
-    uint64_t node_visits;      /* BVH8 nodes fetched by closest-hit traversal (counting mode) */
-    uint64_t tri_tests;        /* triangles tested by closest-hit traversal (counting mode)   */
+    uint64_t node_visits;      /* BVH8 nodes fetched by traversal (counting mode)             */
+    uint64_t tri_tests;        /* triangles tested by traversal (counting mode)               */
+    /* SIMD utilisation of the traversal launches (counting mode): warp-level
+     * steps of the node phase and of the triangle phase (node_visits /
+     * (32 * warp_node_steps) = lanes busy per node step), warp iterations of
+     * the persistent loop and lane iterations that held a ray. */
+    uint64_t warp_node_steps;
+    uint64_t warp_tri_steps;
+    uint64_t warp_loop_iters;
+    uint64_t lane_loop_busy;
+    uint64_t alpha_tests;      /* any-hit alpha tests (counting mode)                         */
 } hx_stats;
 
 /* Context: one CUDA device + stream + HBM budget (the role of vk::Backend). */
@@ -401,9 +412,10 @@ HX_API hx_status hx_integrator_read_accumulation(hx_integrator* integ, float* ho
 /* Device-timed statistics of the last render call (CUDA events on the
  * context stream when timing is on). */
 HX_API hx_status hx_integrator_set_timing(hx_integrator* integ, uint32_t enabled);
-/* Counting mode: closest-hit launches also count node fetches and triangle
- * tests (into hx_stats.node_visits / tri_tests); used to derive the
- * algorithmic bytes of the traversal, never in a timed run. */
+/* Counting mode: traversal launches also count node fetches, triangle tests
+ * and their warp-level steps (hx_stats.node_visits ... lane_loop_busy); used
+ * to derive the algorithmic bytes and the SIMD utilisation of the traversal,
+ * never in a timed run. */
 HX_API hx_status hx_integrator_set_counting(hx_integrator* integ, uint32_t enabled);
 HX_API hx_status hx_integrator_stats(const hx_integrator* integ, hx_stats* out);
 

@@ -354,11 +354,15 @@ static float half_area(const float* lo, const float* hi) {
     return dx * dy + dy * dz + dz * dx;
 }
 
-// Quantises the occupied slots (meta != 0) of a node on its own grid.
+// meta bytes (hx_bvh8_node): the low 5 bits are the slot's bit in the
+// traversal's hit mask.
+constexpr uint8_t kMetaEmpty = 0x10, kMetaInternal = 0x98, kMetaLeaf = 0x20;
+
+// Quantises the occupied slots (meta != empty) of a node on its own grid.
 static void quantise_node(hx_bvh8_node& node, const float (*clo)[3], const float (*chi)[3]) {
     float plo[3] = {INFINITY, INFINITY, INFINITY}, phi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int k = 0; k < 8; ++k) {
-        if (node.meta[k] == 0) continue;
+        if (node.meta[k] == kMetaEmpty) continue;
         for (int a = 0; a < 3; ++a) {
             plo[a] = clo[k][a] < plo[a] ? clo[k][a] : plo[a];
             phi[a] = chi[k][a] > phi[a] ? chi[k][a] : phi[a];
@@ -377,7 +381,7 @@ static void quantise_node(hx_bvh8_node& node, const float (*clo)[3], const float
         node.exponent[a] = (int8_t)e;
         float inv = pow2f(-e);
         for (int k = 0; k < 8; ++k) {
-            if (node.meta[k] == 0) { node.qlo[a][k] = 0; node.qhi[a][k] = 0; continue; }
+            if (node.meta[k] == kMetaEmpty) { node.qlo[a][k] = 0; node.qhi[a][k] = 0; continue; }
             float fl = std::floor((clo[k][a] - origin) * inv);
             int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
             while (ql > 0 && origin + (float)ql * scale > clo[k][a]) --ql;
@@ -584,19 +588,20 @@ static void build_bvh(Scene& s) {
         for (int c = 0; c < 8; ++c) {
             if (slot_kid[c] == 0xffffffffu) {
                 for (int a = 0; a < 3; ++a) { clo[c][a] = 0.0f; chi[c][a] = 0.0f; }
+                node.meta[c] = kMetaEmpty;
                 continue;
             }
             uint32_t it = kids[slot_kid[c]];
             for (int a = 0; a < 3; ++a) { clo[c][a] = klo[slot_kid[c]][a]; chi[c][a] = khi[slot_kid[c]][a]; }
             if (!(it & 0x80000000u) && b.count[it] > kLeafMax) {
-                node.meta[c] = (uint8_t)(0x80u | rank);
+                node.meta[c] = (uint8_t)(kMetaInternal | c);
                 node.internal_mask |= (uint8_t)(1u << c);
                 ++rank;
                 queue.push_back(it);
             } else {
                 uint32_t cnt = item_count(it), f = item_first(it);
                 uint32_t off = (uint32_t)b.leaf_prims.size() - node.prim_base;
-                node.meta[c] = (uint8_t)((cnt << 5) | off);
+                node.meta[c] = (uint8_t)(kMetaLeaf | off);
                 for (uint32_t q = 0; q < cnt; ++q) b.leaf_prims.push_back(b.sorted[f + q]);
             }
         }
@@ -762,15 +767,14 @@ static bool trace_bvh8_cpu(const Scene& s, V3<float> o, V3<float> d, float tmin,
                 }
                 tn = std::fmax(std::fmax(tna[0], tna[1]), std::fmax(tna[2], tmin));
                 tf = std::fmin(std::fmin(tfa[0], tfa[1]), std::fmin(tfa[2], lim));
-                if (m != 0u && tn <= tf) {
-                    if (m & 0x80u) hits |= 1u << (24 + (c ^ oct_inv));
-                    else hits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-                }
+                // hit bit: internal 24 + (slot ^ oct_inv), leaf its offset, empty 16
+                uint32_t pos = (m & 0x80u) ? ((m & 31u) ^ oct_inv) : (m & 31u);
+                if (tn <= tf) hits |= 1u << pos;
             }
             g_base = n.child_base;
             g_mask = (hits & 0xff000000u) | n.internal_mask;
             t_base = n.prim_base;
-            t_mask = hits & 0x00ffffffu;
+            t_mask = hits & 0xffu;
         }
         while (t_mask) {
             uint32_t bt = (uint32_t)__builtin_ctz(t_mask);

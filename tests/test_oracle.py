@@ -98,9 +98,10 @@ def test_bvh8_structure(kind):
         scale = np.ldexp(np.float32(1.0), node["exponent"].astype(np.int32)).astype(np.float32)
         for c in range(8):
             meta = int(node["meta"][c])
-            if meta == 0 or meta & 0x80:
+            if meta == 0x10 or meta & 0x80:  # empty or internal slot
                 continue
-            cnt, off = meta >> 5, meta & 31
+            assert meta >> 5 == 1  # one triangle per leaf slot
+            cnt, off = 1, meta & 31
             lo = (node["origin"] + node["qlo"][:, c].astype(np.float32) * scale).astype(np.float32)
             hi = (node["origin"] + node["qhi"][:, c].astype(np.float32) * scale).astype(np.float32)
             for q in range(cnt):
