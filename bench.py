@@ -51,9 +51,10 @@ def parse():
     p.add_argument("--rate", type=float, default=200.0)
     p.add_argument("--duration", type=float, default=8.0)
     p.add_argument("--scenes", type=int, default=8)
-    p.add_argument("--tick-paths", type=int, default=4 << 20)
+    p.add_argument("--tick-paths", type=int, default=2 << 20, help="paths per tick of requests that fit in one tick")
+    p.add_argument("--long-tick-paths", type=int, default=1 << 20, help="paths per tick of longer requests")
     p.add_argument("--arena-gb", type=float, default=64.0)
-    p.add_argument("--concurrent-ticks", type=int, default=4)
+    p.add_argument("--concurrent-ticks", type=int, default=1)
     p.add_argument("--precision", action="store_true", help="precision-form report (terrain scene)")
     p.add_argument("--terrain-size", type=int, default=4096)
     p.add_argument("--spp", type=int, default=256)
@@ -393,6 +394,7 @@ def run_serving(args, dist):
     rng = np.random.default_rng(1234)
     pol = make_policy(hx)
     srv = hx.Server(ctx, arena_bytes=int(args.arena_gb * (1 << 30)), max_paths_per_tick=args.tick_paths,
+                    max_paths_per_long_tick=args.long_tick_paths,
                     max_ray_bounces=DEPTH, policy=pol, max_concurrent_ticks=args.concurrent_ticks)
     dn = hx.Denoiser(ctx)
     wpath = os.path.join(ROOT, "helios_gb300", "weights", "denoiser.npy")
@@ -462,7 +464,8 @@ def run_serving(args, dist):
     queue = {}
     for r in results:
         w, h, spp, dz, sid = meta[r.request_id]
-        classes.setdefault("%dx%d/%dspp%s" % (w, h, spp, "/denoise" if dz else ""), []).append(r.latency_ms)
+        if dz:
+            classes.setdefault("%dx%d/%dspp/denoise" % (w, h, spp), []).append(r.latency_ms)
         classes.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.latency_ms)
         queue.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.queue_ms)
     offered = sum(w * h * spp for (w, h, spp, dn, sid) in meta.values())
@@ -473,7 +476,8 @@ def run_serving(args, dist):
             "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
             "per_class_latency_ms": {k: {"n": len(v), "p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(classes.items())},
             "per_class_admission_wait_ms": {k: {"p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(queue.items())},
-            "tick_paths": args.tick_paths, "concurrent_ticks": args.concurrent_ticks, "arena_gb": args.arena_gb,
+            "tick_paths": args.tick_paths, "long_tick_paths": args.long_tick_paths,
+            "concurrent_ticks": args.concurrent_ticks, "arena_gb": args.arena_gb,
             "denoise": "Bernoulli(0.5) per request; denoiser weights: " + weights,
             "requests_denoised": s1.requests_denoised - s0.requests_denoised, "data": "synthetic"}
     print(json.dumps(line), flush=True)

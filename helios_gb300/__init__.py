@@ -146,7 +146,8 @@ class ProceduralParams(C.Structure):
 class ServerDesc(C.Structure):
     _fields_ = [("request_arena_bytes", C.c_uint64), ("max_paths_per_tick", C.c_uint32),
                 ("max_ray_bounces", C.c_uint32), ("policy", Policy), ("result_arena_bytes", C.c_uint64),
-                ("admitted_work_paths", C.c_uint64), ("max_concurrent_ticks", C.c_uint32), ("reserved", C.c_uint32)]
+                ("admitted_work_paths", C.c_uint64), ("max_concurrent_ticks", C.c_uint32),
+                ("max_paths_per_long_tick", C.c_uint32)]
 
 
 class RequestDesc(C.Structure):
@@ -718,9 +719,10 @@ class Server:
     requests are admitted by HBM budget and batched into CUDA-graph ticks."""
 
     def __init__(self, ctx, arena_bytes=4 << 30, max_paths_per_tick=4 << 20, max_ray_bounces=8, policy=None,
-                 max_concurrent_ticks=0):
+                 max_concurrent_ticks=0, max_paths_per_long_tick=0):
         d = ServerDesc()
         d.max_concurrent_ticks = max_concurrent_ticks
+        d.max_paths_per_long_tick = max_paths_per_long_tick
         d.request_arena_bytes = arena_bytes
         d.max_paths_per_tick = max_paths_per_tick
         d.max_ray_bounces = max_ray_bounces

@@ -117,6 +117,7 @@ struct DevScene {
     const hx_light* lights;
     const uint4* tex_desc;       // per texture: texel offset, width, height, 0
     const uint32_t* texels;      // RGBA8 packed
+    const uint8_t* alpha8;       // alpha channel of every texture (same texel offsets): the any-hit test's working set
     const float4* alpha_uv;      // 2 per flattened prim: (u0,v0,u1,v1), (u2,v2,tex,0)
     DevEnv env;
 };

@@ -105,7 +105,7 @@ struct hx_integrator {
     bool timing = false;
     bool counting = false;
     hx_stats stats{};
-    int grid_trace = 0, grid_shade = 0, grid_gen = 0;
+    int grid_trace = 0, grid_shade = 0, grid_gen = 0, grid_batched = 0;
 };
 
 static void compute_tiles(hx_integrator* it) {  // path_integrator.cpp:312-336
@@ -150,11 +150,14 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     for (int k = 0; k < 2; ++k) {
         HX_A(it->q.o[k], 16 * cap);
         HX_A(it->q.d[k], 16 * cap);
+        HX_A(it->q.r0[k], 16 * cap);  // FP32 payloads (the policy may change after creation)
+        HX_A(it->q.r1[k], 16 * cap);
         HX_A(it->q.p[k], 4 * cap);
     }
     HX_A(it->q.hit, 16 * cap);
     HX_A(it->q.so, 16 * cap);
-    HX_A(it->q.sd, 16 * cap);
+    HX_A(it->q.sr0, 16 * cap);
+    HX_A(it->q.sr1, 16 * cap);
     HX_A(it->q.sc, 16 * cap);
     HX_A(it->q.T, 16 * cap);
     HX_A(it->q.L, 16 * cap);
@@ -182,6 +185,8 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     it->grid_shade = std::max(1, per_sm) * ctx->num_sms;
     it->grid_gen = ctx->num_sms * 8;
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_batched<false>, kTraceThreads, 0));
+    it->grid_batched = std::max(1, per_sm) * ctx->num_sms;
     compute_tiles(it);
     *out = it;
     return HX_OK;
@@ -260,8 +265,16 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
                 StageTimer t(it, &it->stats.ms_trace);
                 HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
 #define HX_EXTEND(COUNT, FP16)                                                                                      \
-    k_extend<COUNT, FP16><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q, it->q.o[cur], it->q.d[cur], it->q.p[cur], \
-                                                                    it->q.counters + cur, it->q.counters + 4)
+    do {                                                                                                            \
+        if (!FP16 && s.num_prims < (1u << 27) && b < kBatchedBounces)                                               \
+            k_extend_batched<COUNT><<<it->grid_batched, kTraceThreads, 0, st>>>(                                    \
+                s, it->q, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.counters + cur, it->q.counters + 4,     \
+                kFlushTris, kFlushParked);                                                                          \
+        else                                                                                                        \
+            k_extend<COUNT, FP16><<<it->grid_trace, kTraceThreads, 0, st>>>(                                        \
+                s, it->q, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.p[cur], it->q.counters + cur,           \
+                it->q.counters + 4);                                                                                \
+    } while (0)
                 if (it->counting) {
                     if (fp16) HX_EXTEND(true, true);
                     else HX_EXTEND(true, false);
@@ -487,6 +500,19 @@ extern "C" hx_status hx_integrator_stats(const hx_integrator* it, hx_stats* out)
     return HX_OK;
 }
 
+// Closest hits of the primary rays k_raygen<false> just queued, with the
+// kernel a frame's first bounce uses (no shadow rays are queued).
+static void launch_primary_trace(hx_integrator* it, cudaStream_t st) {
+    const DevScene& s = it->scene->d;
+    if (s.num_prims < (1u << 27))
+        k_extend_batched<false><<<it->grid_batched, kTraceThreads, 0, st>>>(s, it->q, it->q.o[0], it->q.r0[0], it->q.r1[0],
+                                                                            it->q.counters, it->q.counters + 4, kFlushTris,
+                                                                            kFlushParked);
+    else
+        k_extend<false, false><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q, it->q.o[0], it->q.r0[0], it->q.r1[0],
+                                                                         it->q.p[0], it->q.counters, it->q.counters + 4);
+}
+
 extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_frame_desc* f, uint32_t frame_index,
                                                 hx_hit* host) {
     HX_CHECK_ARG(it && f && host, "hx_integrator_primary_hits: null argument");
@@ -497,8 +523,7 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     Policy P = make_policy(it->desc.policy);
     k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
-    k_trace<false><<<it->grid_trace, kTraceThreads, 0, st>>>(it->scene->d, it->q.o[0], it->q.d[0], it->q.p[0], it->q.counters,
-                                                             it->q.hit, it->q.stats, it->q.status, it->q.counters + 4);
+    launch_primary_trace(it, st);
     uint32_t n = W * H;
     k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(it->q.hit, n, it->hits_host_layout);
     HX_CUDA(cudaGetLastError());
@@ -526,8 +551,7 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     Policy P = make_policy(it->desc.policy);
     k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
-    k_trace<false><<<it->grid_trace, kTraceThreads, 0, st>>>(it->scene->d, it->q.o[0], it->q.d[0], it->q.p[0], it->q.counters,
-                                                             it->q.hit, it->q.stats, it->q.status, it->q.counters + 4);
+    launch_primary_trace(it, st);
     k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, n, d_features);
     HX_CUDA(cudaGetLastError());
     HX_TRY(check_status(it));

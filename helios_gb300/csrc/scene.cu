@@ -190,6 +190,13 @@ hx_status hx_env_build(hx_context* ctx, hx_scene* s, const hx_environment_desc& 
     return HX_OK;
 }
 
+// Alpha channel copy of the RGBA8 texels: the alpha test reads one byte per
+// texel instead of four (a quarter of the cache footprint).
+__global__ void k_alpha8(const uint32_t* __restrict__ texels, size_t n, uint8_t* __restrict__ alpha8) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        alpha8[i] = (uint8_t)(texels[i] >> 24);
+}
+
 static hx_status scene_fail(hx_scene* s, hx_status st) {
     hx_scene_destroy(s);
     return st;
@@ -373,7 +380,13 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
             size_t cnt = (size_t)desc->textures[t].width * desc->textures[t].height;
             HX_CUDA(cudaMemcpyAsync(texels + htd[t].x, desc->textures[t].rgba8, 4 * cnt, cudaMemcpyHostToDevice, st));
         }
+        uint8_t* alpha8;
+        if ((rc = hx_alloc_t(ctx, &alpha8, ntexels)) != HX_OK) return scene_fail(s, rc);
+        s->allocs.push_back(alpha8);
+        k_alpha8<<<ctx->num_sms * 4, 256, 0, st>>>(texels, ntexels, alpha8);
+        HX_CUDA(cudaGetLastError());
         s->d.texels = texels;
+        s->d.alpha8 = alpha8;
     }
     s->d.num_prims = (uint32_t)nprims;
     s->d.num_instances = desc->num_instances;

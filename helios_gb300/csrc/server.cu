@@ -81,6 +81,10 @@ __global__ void k_raygen_multi(const TableHeader* hdr, const Chunk* chunks, cons
         q.rng[p] = make_uint2(rng.s0, rng.s1);
         q.o[0][p] = make_float4(o.x, o.y, o.z, 0.001f);
         q.d[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+        float4 r0, r1;
+        ray_record(d, 10000.0f, true, r0, r1);
+        q.r0[0][p] = r0;
+        q.r1[0][p] = r1;
         q.p[0][p] = p | kAnyHitFlag;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -299,11 +303,14 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     for (int k = 0; k < 2; ++k) {
         HX_TRY(A((void**)&b->q.o[k], 16ull * cap));
         HX_TRY(A((void**)&b->q.d[k], 16ull * cap));
+        HX_TRY(A((void**)&b->q.r0[k], 16ull * cap));
+        HX_TRY(A((void**)&b->q.r1[k], 16ull * cap));
         HX_TRY(A((void**)&b->q.p[k], 4ull * cap));
     }
     HX_TRY(A((void**)&b->q.hit, 16ull * cap));
     HX_TRY(A((void**)&b->q.so, 16ull * cap));
-    HX_TRY(A((void**)&b->q.sd, 16ull * cap));
+    HX_TRY(A((void**)&b->q.sr0, 16ull * cap));
+    HX_TRY(A((void**)&b->q.sr1, 16ull * cap));
     HX_TRY(A((void**)&b->q.sc, 16ull * cap));
     HX_TRY(A((void**)&b->q.T, 16ull * cap));
     HX_TRY(A((void**)&b->q.L, 16ull * cap));
@@ -328,6 +335,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     int per_sm = 0;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend<false, false>, kTraceThreads, 0));
     const int grid_trace = std::max(1, per_sm) * ctx->num_sms;
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_batched<false>, kTraceThreads, 0));
+    const int grid_batched = std::max(1, per_sm) * ctx->num_sms;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     const int grid_shade = std::max(1, per_sm) * ctx->num_sms;
     const int grid_gen = ctx->num_sms * 8;
@@ -343,8 +352,13 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     for (uint32_t bo = 0; bo <= s->desc.max_ray_bounces; ++bo) {
         int cur = bo & 1;
         cudaMemsetAsync(b->q.counters + 4, 0, 4, st);
-        k_extend<false, false><<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.d[cur], b->q.p[cur],
-                                                                     b->q.counters + cur, b->q.counters + 4);
+        if (bo < kBatchedBounces && sc.num_prims < (1u << 27))
+            k_extend_batched<false><<<grid_batched, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.r0[cur], b->q.r1[cur],
+                                                                            b->q.counters + cur, b->q.counters + 4,
+                                                                            kFlushTris, kFlushParked);
+        else
+            k_extend<false, false><<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.r0[cur], b->q.r1[cur], b->q.p[cur],
+                                                                         b->q.counters + cur, b->q.counters + 4);
         if (bo == s->desc.max_ray_bounces) break;
         if (bo == 0)
             k_aov_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, sc, b->q.hit);
@@ -443,7 +457,7 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
     TableHeader* hdr = (TableHeader*)b->h_table;
     Chunk* ch = (Chunk*)(hdr + 1);
     uint32_t nc = 0, paths = 0, accs = 0;
-    const uint32_t cap = s->desc.max_paths_per_tick;
+    const uint32_t cap = b->urgent ? s->desc.max_paths_per_tick : s->desc.max_paths_per_long_tick;
     b->running.clear();
     // slot table updates for newly admitted requests happen before the tick
     for (ServerRequest* r : cand) {
@@ -667,6 +681,9 @@ extern "C" hx_status hx_server_create(hx_context* ctx, const hx_server_desc* des
     if (!s->desc.result_arena_bytes) s->desc.result_arena_bytes = std::max<uint64_t>(1u << 20, desc->request_arena_bytes / 4);
     if (!s->desc.admitted_work_paths) s->desc.admitted_work_paths = 4ull * desc->max_paths_per_tick;
     if (!s->desc.max_concurrent_ticks) s->desc.max_concurrent_ticks = 4;
+    if (!s->desc.max_paths_per_long_tick || s->desc.max_paths_per_long_tick > desc->max_paths_per_tick)
+        s->desc.max_paths_per_long_tick = desc->max_paths_per_tick;
+    s->desc.max_paths_per_long_tick = std::max<uint32_t>(s->desc.max_paths_per_long_tick, 1024);
     hx_status st = hx_alloc(ctx, (void**)&s->arena, desc->request_arena_bytes);
     if (st != HX_OK) {
         delete s;

@@ -113,6 +113,36 @@ HXD float tex_bilinear(const DevScene& s, uint32_t tex, float u, float v, int c)
     return top + (bot - top) * fy;
 }
 
+// Bilinear alpha from the scene's A8 copy of the textures: the same texel
+// bytes and arithmetic as tex_bilinear(..., 3).
+HXD float tex_alpha_bilinear(const DevScene& s, uint32_t tex, float u, float v) {
+    uint4 td = s.tex_desc[tex];
+    int W = (int)td.y, H = (int)td.z;
+    float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+    float x0 = floorf(x), y0 = floorf(y);
+    float fx = x - x0, fy = y - y0;
+    int ix0, iy0, ix1, iy1;
+    if (((W & (W - 1)) | (H & (H - 1))) == 0) {
+        ix0 = (int)x0 & (W - 1);
+        iy0 = (int)y0 & (H - 1);
+        ix1 = (ix0 + 1) & (W - 1);
+        iy1 = (iy0 + 1) & (H - 1);
+    } else {
+        ix0 = (((int)x0 % W) + W) % W;
+        iy0 = (((int)y0 % H) + H) % H;
+        ix1 = ix0 + 1 == W ? 0 : ix0 + 1;
+        iy1 = iy0 + 1 == H ? 0 : iy0 + 1;
+    }
+    const uint8_t* t = s.alpha8 + td.x;
+    float a00 = unorm8(__ldg(t + iy0 * W + ix0));
+    float a10 = unorm8(__ldg(t + iy0 * W + ix1));
+    float a01 = unorm8(__ldg(t + iy1 * W + ix0));
+    float a11 = unorm8(__ldg(t + iy1 * W + ix1));
+    float top = a00 + (a10 - a00) * fx;
+    float bot = a01 + (a11 - a01) * fx;
+    return top + (bot - top) * fy;
+}
+
 // Any-hit alpha test: interpolated UV, albedo alpha, reject below 0.1.
 HXD bool alpha_pass(const DevScene& s, uint32_t prim, float u, float v) {
     float4 a = __ldg(&s.alpha_uv[2 * (size_t)prim]);
@@ -124,7 +154,7 @@ HXD bool alpha_pass(const DevScene& s, uint32_t prim, float u, float v) {
         float b0 = 1.0f - u - v;
         float tu = a.x * b0 + a.z * u + b.x * v;
         float tv = a.y * b0 + a.w * u + b.y * v;
-        alpha = tex_bilinear(s, tex, tu, tv, 3);
+        alpha = tex_alpha_bilinear(s, tex, tu, tv);
     }
     return !(alpha < 0.1f);
 }
@@ -303,7 +333,7 @@ struct TravState {
     int sp;
     uint32_t visits_left;
     bool any_hit;
-    bool shadow;  // first accepted hit ends the ray (read when trav_step's DYN is set)
+    bool shadow;  // first accepted hit ends the ray
 };
 
 HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool any_hit) {
@@ -327,13 +357,54 @@ HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, flo
     st.shadow = false;
 }
 
-// Returns true when the ray is finished (traversal exhausted, or the first
-// accepted hit of a shadow ray).
-constexpr int kPostponeLanes = 8;  // postpone triangle tests below this many lanes
+// Traversal record of a ray, computed where the ray is made (ray generation
+// and shading, which run convergent) so that the persistent traversal's
+// refill only loads it:
+//   r0 = (1/dx, 1/dy, 1/dz [safe_inv], tmax)
+//   r1 = (Sx, Sy, Sz, bits)   the watertight test's shear; bits: kx | ky << 2 |
+//        kz << 4 | octant << 6 | any-hit << 9 (octant from the signs of d, as
+//        trav_init)
+// The values are those ray_prepare computes, so traversal from a record is
+// bit-identical to traversal from (o, d).
+HXD void ray_record(V3 d, float tmax, bool any_hit, float4& r0, float4& r1) {
+    const RayPre p = ray_prepare(v3(0.0f), d);
+    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    const uint32_t bits = (uint32_t)p.kx | ((uint32_t)p.ky << 2) | ((uint32_t)p.kz << 4) | (oct << 6) |
+                          (any_hit ? 1u << 9 : 0u);
+    r0 = make_float4(p.ix, p.iy, p.iz, tmax);
+    r1 = make_float4(p.sx, p.sy, p.sz, __uint_as_float(bits));
+}
 
-// SHADOW: every ray of the launch is a shadow ray; DYN: the lane's st.shadow
-// decides (extension and shadow rays in one launch).
-template <bool SHADOW, bool COUNT, bool POSTPONE = false, bool DYN = false>
+HXD void trav_init_record(TravState& st, const DevScene& s, float4 o_tmin, float4 r0, float4 r1) {
+    const uint32_t bits = __float_as_uint(r1.w);
+    st.r.o = v3(o_tmin);
+    st.r.kx = (int)(bits & 3u);
+    st.r.ky = (int)((bits >> 2) & 3u);
+    st.r.kz = (int)((bits >> 4) & 3u);
+    st.r.sx = r1.x; st.r.sy = r1.y; st.r.sz = r1.z;
+    st.r.ix = r0.x; st.r.iy = r0.y; st.r.iz = r0.z;
+    st.fix = r0.x * 1.000000477f;
+    st.fiy = r0.y * 1.000000477f;
+    st.fiz = r0.z * 1.000000477f;
+    st.oct_inv = 7u - ((bits >> 6) & 7u);
+    st.tmin = o_tmin.w;
+    st.best_t = r0.w;
+    st.bu = st.bv = 0.0f;
+    st.best = kNoHit;
+    st.g_base = 0;
+    st.g_mask = s.num_nodes ? ((1u << (24 + st.oct_inv)) | 1u) : 0u;
+    st.t_base = 0;
+    st.t_mask = 0;
+    st.sp = 0;
+    st.visits_left = s.num_nodes + 16;
+    st.any_hit = (bits >> 9) & 1u;
+    st.shadow = false;
+}
+
+// One step of a lane's traversal: visits one node and tests the triangles it
+// exposed.  Returns true when the ray is finished (traversal exhausted, or
+// the first accepted hit of a shadow ray, st.shadow).
+template <bool COUNT>
 HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflow, TraverseCount* tc) {
     if (st.g_mask > 0x00ffffffu) {
         const uint32_t bit = 31u - __clz(st.g_mask);
@@ -366,15 +437,6 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         st.g_mask = 0;
     }
     while (st.t_mask) {
-        // Postpone the triangles when few lanes of the warp test triangles
-        // now and this lane still has nodes to visit: push the group and
-        // keep the warp on node steps (Ylitie et al. 2017).  A pushed group
-        // has no bit >= 24, so it is popped as a triangle group.
-        if (POSTPONE && st.g_mask > 0x00ffffffu && __popc(__activemask()) < kPostponeLanes && st.sp + 1 < kStackSize) {
-            stack[st.sp++] = make_uint2(st.t_base, st.t_mask);
-            st.t_mask = 0;
-            break;
-        }
         const uint32_t b = __ffs(st.t_mask) - 1u;
         st.t_mask &= st.t_mask - 1u;
         const uint32_t k = st.t_base + b;
@@ -398,7 +460,7 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
             if (!alpha_pass(s, prim, u, v)) continue;
         }
         st.best_t = t; st.bu = u; st.bv = v; st.best = prim;
-        if (SHADOW || (DYN && st.shadow)) return true;
+        if (st.shadow) return true;
     }
     if (st.g_mask <= 0x00ffffffu) {
         if (st.sp == 0) return true;
@@ -407,4 +469,134 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         st.g_mask = e.y;
     }
     return false;
+}
+
+// ---------------------------------------------------------------------------
+// Batched traversal: lanes visit nodes on their own rays, but the triangles
+// their nodes expose go to a per-warp queue that the whole warp tests
+// together, one triangle per lane (a triangle test by one lane of a warp
+// otherwise holds the other 31 idle).  The closest hit of a ray is the
+// lexicographic minimum of (t, triangle id) over its accepted triangles —
+// independent of the order they are tested in — kept as one 64-bit key per
+// ray in shared memory (atomicMin).
+// ---------------------------------------------------------------------------
+
+// One node visit: pops the next internal child of the current group,
+// intersects its children against [tmin, best_t] and returns the leaf
+// triangles it hit (bits over t_base).  Afterwards g_mask holds the next
+// group to visit (from the stack when the node hit no internal child) or is
+// <= 0xffffff when the ray has no node left.
+template <bool COUNT>
+HXD uint32_t node_step(TravState& st, uint2* stack, const DevScene& s, float best_t, bool& overflow, TraverseCount* tc,
+                       uint32_t& t_base) {
+    const uint32_t bit = 31u - __clz(st.g_mask);
+    st.g_mask &= ~(1u << bit);
+    const uint32_t slot = (bit - 24u) ^ st.oct_inv;
+    const uint32_t child = st.g_base + __popc(st.g_mask & 0xffu & ((1u << slot) - 1u));
+    if (st.g_mask > 0x00ffffffu) {
+        if (st.sp < kStackSize) stack[st.sp++] = make_uint2(st.g_base, st.g_mask);
+        else overflow = true;
+    }
+    if (st.visits_left-- == 0 || child >= s.num_nodes) {
+        overflow = true;
+        st.g_mask = 0;
+        st.sp = 0;
+        return 0u;
+    }
+    const uint4* np = reinterpret_cast<const uint4*>(s.nodes + child);
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    if (COUNT) {
+        tc->nodes++;
+        if (lowest_active_lane()) tc->warp_nodes++;
+    }
+    const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.fix, st.fiy, st.fiz, st.oct_inv, st.tmin,
+                                           best_t * 1.000001f);
+    st.g_base = w1.x;
+    st.g_mask = (hm & 0xff000000u) | (w0.w >> 24);
+    t_base = w1.y;
+    if (st.g_mask <= 0x00ffffffu && st.sp > 0) {
+        const uint2 e = stack[--st.sp];
+        st.g_base = e.x;
+        st.g_mask = e.y;
+    }
+    return hm & 0xffu;
+}
+
+// Per-warp shared state of the batched traversal: per lane the best key of
+// its ray (t bits << 32 | triangle id), the barycentrics of that hit and the
+// ray's queue index; the queue of triangles to test (owner lane << 27 |
+// leaf-triangle index).  The testing lane reads the owner's origin and shear
+// from the ray's traversal record in global memory.
+constexpr uint32_t kTriQueueCap = 64;
+constexpr uint32_t kShadowRid = 0x80000000u;
+struct WarpTris {
+    unsigned long long key[32];
+    float2 uv[32];
+    uint32_t rid[32];  // queue index | kShadowRid
+    uint32_t tri[kTriQueueCap];
+};
+
+// Tests the first n queued triangles, one per lane and round (all 32 lanes
+// call it together); accepted hits lower their ray's key.
+template <bool COUNT>
+HXD void warp_test_tris(WarpTris& w, uint32_t lane, uint32_t n, const DevScene& s, const float4* __restrict__ qo,
+                        const float4* __restrict__ qr1, const float4* __restrict__ so, const float4* __restrict__ sr1,
+                        bool& overflow, TraverseCount* tc) {
+    for (uint32_t b0 = 0; b0 < n; b0 += 32u) {
+        const uint32_t e = b0 + lane;
+        unsigned long long cand = ~0ull;
+        uint32_t own = 0;
+        float cu = 0.0f, cv = 0.0f;
+        if (e < n) {
+            const uint32_t ent = w.tri[e];
+            const uint32_t k = ent & 0x07ffffffu;
+            own = ent >> 27;
+            if (COUNT) {
+                tc->tris++;
+                if (lowest_active_lane()) tc->warp_tris++;
+            }
+            if (k < s.num_prims) {
+                const float4 a = __ldg(&s.tri[3 * (size_t)k]);
+                const float4 bb = __ldg(&s.tri[3 * (size_t)k + 1]);
+                const float4 cc = __ldg(&s.tri[3 * (size_t)k + 2]);
+                const uint32_t rid = w.rid[own];
+                const uint32_t ri = rid & ~kShadowRid;
+                const float4 ra = (rid & kShadowRid) ? so[ri] : qo[ri];
+                const float4 rb = (rid & kShadowRid) ? sr1[ri] : qr1[ri];
+                const unsigned long long key = w.key[own];
+                const uint32_t bits = __float_as_uint(rb.w);
+                RayPre r;
+                r.o = v3(ra);
+                r.kx = (int)(bits & 3u);
+                r.ky = (int)((bits >> 2) & 3u);
+                r.kz = (int)((bits >> 4) & 3u);
+                r.sx = rb.x; r.sy = rb.y; r.sz = rb.z;
+                r.ix = r.iy = r.iz = 0.0f;
+                const float best_t = __uint_as_float((uint32_t)(key >> 32));
+                const uint32_t best = (uint32_t)key;
+                float t, u, v;
+                if (intersect_tri(r, v3(a), v3(bb), v3(cc), ra.w, best_t, t, u, v)) {
+                    const uint32_t prim = __float_as_uint(a.w);
+                    if (t < best_t || (t == best_t && prim < best)) {
+                        bool pass = true;
+                        if ((bits & (1u << 9)) && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE)) {
+                            if (COUNT) tc->alpha++;
+                            pass = alpha_pass(s, prim, u, v);
+                        }
+                        if (pass) {
+                            cand = ((unsigned long long)__float_as_uint(t) << 32) | prim;
+                            atomicMin(&w.key[own], cand);
+                            cu = u;
+                            cv = v;
+                        }
+                    }
+                }
+            } else {
+                overflow = true;
+            }
+        }
+        __syncwarp();
+        if (cand != ~0ull && w.key[own] == cand) w.uv[own] = make_float2(cu, cv);
+        __syncwarp();
+    }
 }

@@ -461,7 +461,9 @@ typedef struct hx_server_desc {
     uint64_t  result_arena_bytes;   /* pinned host memory for finished images (0: 1/4 of the HBM arena) */
     uint64_t  admitted_work_paths;  /* admit while admitted remaining work <= this (0: 4 ticks) */
     uint32_t  max_concurrent_ticks; /* scene ticks in flight at once (0: 4)                */
-    uint32_t  reserved;
+    uint32_t  max_paths_per_long_tick; /* paths of one tick of requests that do not fit in
+                                          one tick (0: max_paths_per_tick); smaller long
+                                          ticks bound the wait of a short request behind one */
 } hx_server_desc;
 
 typedef struct hx_request_desc {
