@@ -251,9 +251,9 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
     {
         StageTimer t(it, &it->stats.ms_raygen);
         if (fp16)
-            k_raygen<true><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, P.rng, it->q);
+            k_raygen<true><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, 0, total, P.rng, it->q);
         else
-            k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, P.rng, it->q);
+            k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, 0, total, P.rng, it->q);
         it->stats.kernel_launches++;
     }
     {
@@ -521,7 +521,7 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     HX_CHECK_ARG((uint64_t)W * H <= it->capacity, "frame exceeds wavefront capacity");
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
-    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
+    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 0, W * H, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
     launch_primary_trace(it, st);
     uint32_t n = W * H;
@@ -549,7 +549,7 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     }
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
-    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, P.rng, it->q);
+    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 0, W * H, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
     launch_primary_trace(it, st);
     k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, n, d_features);

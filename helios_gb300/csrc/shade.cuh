@@ -107,7 +107,7 @@ HXD Surface populate(const DevScene& s, uint32_t prim, float u, float v) {
     if (m.texture_indices0[0] == -1) p.albedo = v3(m.albedo[0], m.albedo[1], m.albedo[2]);
     else {
         uint32_t t = (uint32_t)m.texture_indices0[0];
-        p.albedo = v3(tex_bilinear(s, t, tu, tv, 0), tex_bilinear(s, t, tu, tv, 1), tex_bilinear(s, t, tu, tv, 2));
+        p.albedo = tex_bilinear_rgb(s, t, tu, tv);
     }
     p.roughness = m.texture_indices0[2] == -1 ? m.roughness_metallic[0]
                                                : tex_bilinear(s, (uint32_t)m.texture_indices0[2], tu, tv, m.texture_indices1[2]);
@@ -116,7 +116,7 @@ HXD Surface populate(const DevScene& s, uint32_t prim, float u, float v) {
     if (m.texture_indices1[0] == -1) p.emissive = v3(m.emissive[0], m.emissive[1], m.emissive[2]);
     else {
         uint32_t t = (uint32_t)m.texture_indices1[0];
-        p.emissive = v3(tex_bilinear(s, t, tu, tv, 0), tex_bilinear(s, t, tu, tv, 1), tex_bilinear(s, t, tu, tv, 2));
+        p.emissive = tex_bilinear_rgb(s, t, tu, tv);
     }
     p.roughness = gmax(p.roughness, kMinRoughnessF);
     p.F0 = v3(0.03f) * (1.0f - p.metallic) + p.albedo * p.metallic;
@@ -145,7 +145,8 @@ HXD V3 env_lookup(const DevEnv& e, V3 d) {
     float fx = x - x0, fy = y - y0;
     int W = (int)e.width, H = (int)e.height;
     int ix = (int)x0, iy = (int)y0;
-    int ix0 = ((ix % W) + W) % W, ix1 = (ix0 + 1) % W;
+    int ix0 = (W & (W - 1)) == 0 ? ix & (W - 1) : ((ix % W) + W) % W;
+    int ix1 = ix0 + 1 == W ? 0 : ix0 + 1;
     int iy0 = iy < 0 ? 0 : (iy >= H ? H - 1 : iy);
     int iy1 = iy + 1 < 0 ? 0 : (iy + 1 >= H ? H - 1 : iy + 1);
     V3 a00 = env_texel(e, ix0, iy0), a10 = env_texel(e, ix1, iy0), a01 = env_texel(e, ix0, iy1), a11 = env_texel(e, ix1, iy1);

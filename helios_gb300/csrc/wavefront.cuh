@@ -95,12 +95,15 @@ HXD uint32_t half2_bits(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
+// Camera rays of paths [path_base, path_base + path_count) of the rect's
+// nframes frames (path p = frame * npix + pixel); path p goes to ray-queue
+// slot p - path_base, its state (T, L, rng) stays indexed by p.
 template <bool FP16>
-__global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uint32_t frame0, uint32_t nframes,
-                         uint32_t kind, Queues q) {
+__global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uint32_t frame0, uint32_t path_base,
+                         uint32_t path_count, uint32_t kind, Queues q) {
     uint32_t npix = rect.w * rect.h;
-    uint32_t total = npix * nframes;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < path_count; k += gridDim.x * blockDim.x) {
+        const uint32_t p = path_base + k;
         uint32_t fr = p / npix, pix = p - fr * npix;
         uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
         Rng rng = rng_init(kind, x, y, W, frame0 + fr);
@@ -110,19 +113,19 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
         q.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         q.rng[p] = make_uint2(rng.s0, rng.s1);
         if (FP16) {
-            q.o[0][p] = make_float4(o.x, o.y, o.z, __uint_as_float(oct_encode(d)));
+            q.o[0][k] = make_float4(o.x, o.y, o.z, __uint_as_float(oct_encode(d)));
         } else {
-            q.o[0][p] = make_float4(o.x, o.y, o.z, 0.001f);
-            q.d[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+            q.o[0][k] = make_float4(o.x, o.y, o.z, 0.001f);
+            q.d[0][k] = make_float4(d.x, d.y, d.z, 10000.0f);
             float4 r0, r1;
             ray_record(d, 10000.0f, true, r0, r1);
-            q.r0[0][p] = r0;
-            q.r1[0][p] = r1;
+            q.r0[0][k] = r0;
+            q.r1[0][k] = r1;
         }
-        q.p[0][p] = p | kAnyHitFlag;
+        q.p[0][k] = p | kAnyHitFlag;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        q.counters[0] = total;
+        q.counters[0] = path_count;
         q.counters[1] = 0;
         q.counters[2] = 0;
     }
