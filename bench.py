@@ -179,7 +179,8 @@ class Clocks:
 
 def cpu_sample(hs, hx, pol, seconds, threads=0):
     """Oracle (scalar FP32 transcription of the reference shaders) on whole
-    image rows of the same frame until the time budget is used."""
+    image rows of the same frame (wrapping around the frame) until the time
+    budget is used."""
     from oracle import binding as ob
     osc = ob.OracleScene(hs)
     d = idesc(hx, pol)
@@ -190,7 +191,7 @@ def cpu_sample(hs, hx, pol, seconds, threads=0):
     rows_done = 0
     chunk = 8
     thr = 0
-    while secs < seconds and rows_done < HEIGHT:
+    while secs < seconds:
         r0 = (row + rows_done) % HEIGHT
         n = min(chunk, HEIGHT - r0)
         import numpy as np
