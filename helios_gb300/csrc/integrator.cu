@@ -24,19 +24,24 @@
 
 namespace {
 
-__global__ void k_trace_rays(DevScene s, const float* __restrict__ rays, uint32_t n, uint32_t any_hit, hx_hit* out,
-                             uint32_t* status) {
-    bool overflow = false;
+// Traversal records of caller rays (origin xyz, tmin, direction xyz, tmax)
+// for the production traversal kernels; the queue holds n extension rays and
+// no shadow ray.
+__global__ void k_ray_records(const float* __restrict__ rays, uint32_t n, uint32_t any_hit, float4* __restrict__ qo,
+                              float4* __restrict__ qr0, float4* __restrict__ qr1, uint32_t* counters) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float* r = rays + 8 * (size_t)i;
-        HitRec h;
-        bool hit = trace_bvh8(s, v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), r[3], r[7], any_hit != 0, false, h, overflow);
-        out[i].t = hit ? h.t : 0.0f;
-        out[i].prim = hit ? h.prim : kNoHit;
-        out[i].u = hit ? h.u : 0.0f;
-        out[i].v = hit ? h.v : 0.0f;
+        float4 r0, r1;
+        ray_record(v3(r[4], r[5], r[6]), r[7], any_hit != 0, r0, r1);
+        qo[i] = make_float4(r[0], r[1], r[2], r[3]);
+        qr0[i] = r0;
+        qr1[i] = r1;
     }
-    if (overflow) atomicOr(status, 1u);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counters[0] = n;
+        counters[2] = 0;
+        counters[4] = 0;
+    }
 }
 
 __global__ void k_rng_streams(uint32_t kind, const uint32_t* seeds, uint32_t n, uint32_t draws, uint32_t* out) {
@@ -611,18 +616,37 @@ extern "C" hx_status hx_scene_trace(const hx_scene* scene, const float* host_ray
     if (n == 0) return HX_OK;
     hx_context* ctx = scene->ctx;
     cudaStream_t st = ctx->stream;
+    // the rays go through the kernels a frame's bounces use
+    const size_t N = n;
     DevBuffer buf;
-    HX_TRY(buf.reserve(ctx, 32 * (size_t)n + sizeof(hx_hit) * (size_t)n + 256));
-    float* d_rays = buf.as<float>();
-    hx_hit* d_hits = (hx_hit*)(buf.as<char>() + 32 * (size_t)n);
-    uint32_t* d_status = (uint32_t*)(buf.as<char>() + 32 * (size_t)n + sizeof(hx_hit) * (size_t)n);
-    HX_CUDA(cudaMemcpyAsync(d_rays, host_rays, 32 * (size_t)n, cudaMemcpyHostToDevice, st));
-    HX_CUDA(cudaMemsetAsync(d_status, 0, 4, st));
-    k_trace_rays<<<ctx->num_sms * 8, kTraceThreads, 0, st>>>(scene->d, d_rays, n, any_hit, d_hits, d_status);
+    HX_TRY(buf.reserve(ctx, 32 * N + 4 * 16 * N + sizeof(hx_hit) * N + 512));
+    char* base = buf.as<char>();
+    float* d_rays = reinterpret_cast<float*>(base);
+    Queues q{};
+    q.o[0] = reinterpret_cast<float4*>(base + 32 * N);
+    q.r0[0] = q.o[0] + N;
+    q.r1[0] = q.r0[0] + N;
+    q.hit = q.r1[0] + N;
+    hx_hit* d_hits = reinterpret_cast<hx_hit*>(q.hit + N);
+    q.counters = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(d_hits) + sizeof(hx_hit) * N);
+    q.stats = reinterpret_cast<unsigned long long*>(q.counters + 16);
+    q.status = reinterpret_cast<uint32_t*>(q.stats + 16);
+    HX_CUDA(cudaMemcpyAsync(d_rays, host_rays, 32 * N, cudaMemcpyHostToDevice, st));
+    HX_CUDA(cudaMemsetAsync(q.counters, 0, 64 + 128 + 4, st));
+    k_ray_records<<<ctx->num_sms * 4, 256, 0, st>>>(d_rays, n, any_hit, q.o[0], q.r0[0], q.r1[0], q.counters);
+    const DevScene& s = scene->d;
+    const int grid = ctx->num_sms * kTraceMinBlocks;
+    if (s.num_prims < (1u << 27))
+        k_extend_batched<false><<<grid, kTraceThreads, 0, st>>>(s, q, q.o[0], q.r0[0], q.r1[0], q.counters, q.counters + 4,
+                                                               kFlushTris, kFlushParked);
+    else
+        k_extend<false, false><<<grid, kTraceThreads, 0, st>>>(s, q, q.o[0], q.r0[0], q.r1[0], nullptr, q.counters,
+                                                              q.counters + 4);
+    k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(q.hit, n, d_hits);
     HX_CUDA(cudaGetLastError());
     uint32_t status = 0;
-    HX_CUDA(cudaMemcpyAsync(host_hits, d_hits, sizeof(hx_hit) * (size_t)n, cudaMemcpyDeviceToHost, st));
-    HX_CUDA(cudaMemcpyAsync(&status, d_status, 4, cudaMemcpyDeviceToHost, st));
+    HX_CUDA(cudaMemcpyAsync(host_hits, d_hits, sizeof(hx_hit) * N, cudaMemcpyDeviceToHost, st));
+    HX_CUDA(cudaMemcpyAsync(&status, q.status, 4, cudaMemcpyDeviceToHost, st));
     HX_CUDA(cudaStreamSynchronize(st));
     buf.release();
     if (status) {

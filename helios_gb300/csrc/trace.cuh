@@ -195,11 +195,6 @@ HXD bool alpha_pass(const DevScene& s, uint32_t prim, float u, float v) {
     return !(alpha < 0.1f);
 }
 
-struct HitRec {
-    float t, u, v;
-    uint32_t prim;
-};
-
 constexpr int kStackSize = 32;
 
 HXD uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
@@ -268,90 +263,6 @@ struct TraverseCount {
 };
 
 HXD bool lowest_active_lane() { return (threadIdx.x & 31u) == (uint32_t)(__ffs(__activemask()) - 1); }
-
-// Closest hit (shadow = false) or first accepted hit (shadow = true) over the
-// compressed 8-wide BVH.  Children are visited near-to-far by the octant
-// order of their slots (slot ^ ray octant), no per-ray sorting; the stack
-// holds node groups (first child index, remaining child bits | internal
-// mask).  Sets overflow when the stack or the node-visit cap overflowed or
-// an index was out of range (the host reports HX_ERR_DEVICE).
-template <bool COUNT = false>
-HXD bool trace_bvh8(const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool any_hit, bool shadow, HitRec& hit,
-                    bool& overflow, TraverseCount* tc = nullptr) {
-    if (s.num_nodes == 0) return false;
-    const RayPre r = ray_prepare(o, d);
-    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-    const uint32_t oct_inv = 7u - oct;
-    float best_t = tmax, bu = 0.0f, bv = 0.0f;
-    uint32_t best = kNoHit;
-    uint2 stack[kStackSize];
-    int sp = 0;
-    // the root is slot 0 of a virtual parent whose only child is internal
-    uint32_t g_base = 0, g_mask = (1u << (24 + oct_inv)) | 1u;
-    uint32_t t_base = 0, t_mask = 0;
-    uint32_t visits_left = s.num_nodes + 16;
-    for (;;) {
-        if (g_mask > 0x00ffffffu) {
-            const uint32_t bit = 31u - __clz(g_mask);
-            g_mask &= ~(1u << bit);
-            const uint32_t slot = (bit - 24u) ^ oct_inv;
-            const uint32_t child = g_base + __popc(g_mask & 0xffu & ((1u << slot) - 1u));
-            if (g_mask > 0x00ffffffu) {
-                if (sp < kStackSize) stack[sp++] = make_uint2(g_base, g_mask);
-                else overflow = true;
-            }
-            if (visits_left-- == 0 || child >= s.num_nodes) {
-                overflow = true;
-                break;
-            }
-            const uint4* np = reinterpret_cast<const uint4*>(s.nodes + child);
-            const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-            if (COUNT) tc->nodes++;
-            const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, r, r.ix * 1.000000477f, r.iy * 1.000000477f,
-                                                   r.iz * 1.000000477f, oct_inv, tmin, best_t * 1.000001f);
-            g_base = w1.x;
-            g_mask = (hm & 0xff000000u) | (w0.w >> 24);
-            t_base = w1.y;
-            t_mask = hm & 0xffu;
-        } else {
-            t_base = g_base;  // a postponed triangle group popped from the stack
-            t_mask = g_mask;
-            g_mask = 0;
-        }
-        while (t_mask) {
-            const uint32_t b = __ffs(t_mask) - 1u;
-            t_mask &= t_mask - 1u;
-            const uint32_t k = t_base + b;
-            if (k >= s.num_prims) {
-                overflow = true;
-                break;
-            }
-            if (COUNT) tc->tris++;
-            const float4 a = __ldg(&s.tri[3 * (size_t)k]);
-            const float4 bb = __ldg(&s.tri[3 * (size_t)k + 1]);
-            const float4 cc = __ldg(&s.tri[3 * (size_t)k + 2]);
-            float t, u, v;
-            if (!intersect_tri(r, v3(a), v3(bb), v3(cc), tmin, best_t, t, u, v)) continue;
-            const uint32_t prim = __float_as_uint(a.w);
-            if (!(t < best_t || (t == best_t && prim < best))) continue;
-            if (any_hit && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE) && !alpha_pass(s, prim, u, v)) continue;
-            best_t = t; bu = u; bv = v; best = prim;
-            if (shadow) {
-                hit.t = t; hit.u = u; hit.v = v; hit.prim = prim;
-                return true;
-            }
-        }
-        if (g_mask <= 0x00ffffffu) {
-            if (sp == 0) break;
-            const uint2 e = stack[--sp];
-            g_base = e.x;
-            g_mask = e.y;
-        }
-    }
-    if (best == kNoHit) return false;
-    hit.t = best_t; hit.u = bu; hit.v = bv; hit.prim = best;
-    return true;
-}
 
 // ---------------------------------------------------------------------------
 // Persistent-warp traversal: per-lane state machine.  One call of step()

@@ -430,7 +430,8 @@ HX_API hx_status hx_integrator_sample_radiance(hx_integrator* integ, const hx_fr
                                                uint32_t frame_index, float* host_rgb);
 
 /* Parity hook: closest-hit queries for caller rays (origin xyz, tmin,
- * direction xyz, tmax) x n, alpha testing when any_hit != 0. */
+ * direction xyz, tmax) x n, alpha testing when any_hit != 0, traced by the
+ * same traversal kernel as a frame's bounces. */
 HX_API hx_status hx_scene_trace(const hx_scene* scene, const float* host_rays, uint32_t n,
                                 uint32_t any_hit, hx_hit* host_hits);
 

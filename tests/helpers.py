@@ -38,3 +38,53 @@ def random_rays(n, lo, hi, seed=1, tmin=0.0001, tmax=1e4):
     r[:, 4:7] = d.astype(np.float32)
     r[:, 7] = tmax
     return r
+
+
+class TriangleSoupScene:
+    """One opaque mesh of free triangles (N x 3 x 3 float32), one grey
+    material, an identity instance, no lights and no environment: a scene for
+    traversal tests.  .desc points at its hx_scene_desc (arrays kept alive)."""
+
+    def __init__(self, tris):
+        tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 3, 3)
+        n = tris.shape[0]
+        self._verts = (hx.Vertex * (3 * n))()
+        for i in range(n):
+            for c in range(3):
+                v = self._verts[3 * i + c]
+                v.position[0], v.position[1], v.position[2], v.position[3] = (float(tris[i, c, 0]), float(tris[i, c, 1]),
+                                                                              float(tris[i, c, 2]), 0.0)
+                v.normal[1] = 1.0
+        self._idx = (C.c_uint32 * (3 * n))(*range(3 * n))
+        self._sub = (hx.Submesh * 1)()
+        self._sub[0].base_index, self._sub[0].index_count, self._sub[0].material, self._sub[0].flags = 0, 3 * n, 0, 0
+        self._mesh = (hx.MeshDesc * 1)()
+        m = self._mesh[0]
+        m.vertices, m.num_vertices = self._verts, 3 * n
+        m.indices, m.num_indices = self._idx, 3 * n
+        m.submeshes, m.num_submeshes = self._sub, 1
+        self._mat = (hx.Material * 1)()
+        mat = self._mat[0]
+        for k in range(4):
+            mat.texture_indices0[k] = -1
+            mat.texture_indices1[k] = -1
+        mat.albedo[0] = mat.albedo[1] = mat.albedo[2] = 0.5
+        mat.roughness_metallic[0] = 0.5
+        self._inst = (hx.Instance * 1)()
+        inst = self._inst[0]
+        for k in range(4):
+            inst.model_matrix[5 * k] = 1.0
+            inst.normal_matrix[5 * k] = 1.0
+        inst.mesh_index, inst.material_override = 0, -1
+        self._desc = hx.SceneDesc()
+        d = self._desc
+        d.meshes, d.num_meshes = self._mesh, 1
+        d.instances, d.num_instances = self._inst, 1
+        d.materials, d.num_materials = self._mat, 1
+        d.num_textures = 0
+        d.num_punctual_lights = 0
+        d.environment.kind = 0
+
+    @property
+    def desc(self):
+        return C.pointer(self._desc)

@@ -12,7 +12,7 @@ import pytest
 
 import helios_gb300 as hx
 from oracle import binding as ob
-from tests.helpers import integrator_desc, random_rays, rel_rmse, small_icosphere_scene
+from tests.helpers import TriangleSoupScene, integrator_desc, random_rays, rel_rmse, small_icosphere_scene
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -63,6 +63,7 @@ def test_bvh_bit_exact(which, box, ico):
 @pytest.mark.parametrize("which", ["box", "ico"])
 @pytest.mark.parametrize("any_hit", [False, True])
 def test_trace_hits_bit_exact(which, any_hit, box, ico):
+    # caller rays through the production traversal kernel (hx_scene_trace)
     hs, sc, osc = box if which == "box" else ico
     lo, hi = (0.05, 0.95) if which == "box" else (-25, 25)
     rays = random_rays(20000, lo, hi, seed=11)
@@ -72,6 +73,41 @@ def test_trace_hits_bit_exact(which, any_hit, box, ico):
     hit = o["prim"] != hx.NO_HIT
     assert np.array_equal(g["t"][hit], o["t"][hit])
     assert np.array_equal(g["u"][hit], o["u"][hit]) and np.array_equal(g["v"][hit], o["v"][hit])
+
+
+@pytest.mark.parametrize("origin", ["inside", "surface"])
+def test_dense_cluster_hits_bit_exact(origin, gpu_ctx):
+    # 30k small triangles in a unit cube: node visits expose many triangles at
+    # once, so the warp's shared triangle queue fills, lanes carry triangles
+    # across flushes, and rays starting on a triangle must skip it (tmin)
+    rng = np.random.default_rng(21)
+    centres = rng.uniform(0.0, 1.0, (30000, 1, 3))
+    tris = (centres + rng.normal(0.0, 0.02, (30000, 3, 3))).astype(np.float32)
+    soup = TriangleSoupScene(tris)
+    sc = hx.Scene(gpu_ctx, soup)
+    osc = ob.OracleScene(soup)
+    n = 20000
+    if origin == "inside":
+        rays = random_rays(n, 0.1, 0.9, seed=22)
+    else:
+        k = rng.integers(0, len(tris), n)
+        u, v = rng.random(n), rng.random(n)
+        flip = u + v > 1.0
+        u[flip], v[flip] = 1.0 - u[flip], 1.0 - v[flip]
+        t = tris[k].astype(np.float64)
+        o = t[:, 0] * (1 - u - v)[:, None] + t[:, 1] * u[:, None] + t[:, 2] * v[:, None]
+        d = rng.normal(size=(n, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        rays = np.zeros((n, 8), np.float32)
+        rays[:, 0:3], rays[:, 3], rays[:, 4:7], rays[:, 7] = o, 1e-4, d, 1e4
+    g = sc.trace(rays)
+    o = osc.trace(rays)
+    assert np.array_equal(g["prim"], o["prim"])
+    hit = o["prim"] != hx.NO_HIT
+    assert hit.mean() > 0.3
+    assert np.array_equal(g["t"][hit], o["t"][hit])
+    assert np.array_equal(g["u"][hit], o["u"][hit]) and np.array_equal(g["v"][hit], o["v"][hit])
+    sc.close()
 
 
 @pytest.mark.parametrize("which,policy", [("box", "spec"), ("box", "reference"), ("ico", "reference")])
