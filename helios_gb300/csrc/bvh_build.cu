@@ -24,6 +24,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr uint32_t kLeafMax = 1;  // triangles per leaf slot
+constexpr int kTreeletPasses = 3;
 // meta bytes: the low 5 bits are the slot's bit in the traversal's hit mask
 constexpr uint8_t kMetaEmpty = 0x10;     // bit 16: outside the triangle and child masks
 constexpr uint8_t kMetaInternal = 0x98;  // | slot: bit 7 (internal) + bit 24 + slot
@@ -204,6 +205,179 @@ __global__ void k_fit(uint32_t n, const uint32_t* __restrict__ children, const i
     }
 }
 
+__device__ __forceinline__ float half_area(const float* lo, const float* hi) {
+    float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// Treelet restructuring of the binary LBVH (Karras & Aila, "Fast Parallel
+// Construction of High-Quality Bounding Volume Hierarchies", HPG 2013), one
+// pass: threads climb from the leaves like k_fit, the second to arrive at a
+// node processes it, so a node is handled after all its descendants.  A node
+// R with >= 3 triangles grows a treelet of up to 7 leaves (open the leaf with
+// the largest surface area, ties: the first), finds the binary topology over
+// those leaves with the least surface-area cost by dynamic programming over
+// leaf subsets (partitions enumerated downwards, ties: the first) and
+// rebuilds the treelet with it when that is cheaper, reusing its internal
+// nodes in pre-order and updating boxes, triangle counts, costs and parent
+// links.  The oracle's builder runs the same steps in a topological order;
+// the result depends only on each node's subtree, so the trees are equal.
+constexpr int kTreeletLeaves = 7;
+constexpr float kTreeletCi = 1.2f, kTreeletCt = 1.0f;
+
+struct TreeletCtx {
+    uint32_t* children;
+    int* parent_int;
+    int* parent_leaf;
+    const float* llo;
+    const float* lhi;
+    float* blo;
+    float* bhi;
+    uint32_t* count;
+    float* cost;
+};
+
+__device__ __forceinline__ void item_box(const TreeletCtx& t, uint32_t c, float lo[3], float hi[3]) {
+    const float* l = (c & 0x80000000u) ? t.llo + 3 * (size_t)(c & 0x7fffffffu) : t.blo + 3 * (size_t)c;
+    const float* h = (c & 0x80000000u) ? t.lhi + 3 * (size_t)(c & 0x7fffffffu) : t.bhi + 3 * (size_t)c;
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = __ldcg(l + a);
+        hi[a] = __ldcg(h + a);
+    }
+}
+__device__ __forceinline__ float item_cost(const TreeletCtx& t, uint32_t c) {
+    if (c & 0x80000000u) {
+        float lo[3], hi[3];
+        item_box(t, c, lo, hi);
+        return kTreeletCt * half_area(lo, hi);
+    }
+    return __ldcg(t.cost + c);
+}
+__device__ __forceinline__ uint32_t item_count(const TreeletCtx& t, uint32_t c) {
+    return (c & 0x80000000u) ? 1u : __ldcg(t.count + c);
+}
+
+__device__ void treelet_node(const TreeletCtx& t, uint32_t R) {
+    const uint32_t l0 = __ldcg(t.children + 2 * (size_t)R), r0 = __ldcg(t.children + 2 * (size_t)R + 1);
+    float lo[3], hi[3];
+    item_box(t, R, lo, hi);
+    const float cR = kTreeletCi * half_area(lo, hi) + (item_cost(t, l0) + item_cost(t, r0));
+    __stcg(t.cost + R, cR);
+    if (__ldcg(t.count + R) < 3u) return;
+    uint32_t leaves[kTreeletLeaves], used[kTreeletLeaves - 1];
+    int nl = 2, nu = 1;
+    leaves[0] = l0;
+    leaves[1] = r0;
+    used[0] = R;
+    while (nl < kTreeletLeaves) {
+        int bi = -1;
+        float ba = 0.0f;
+        for (int k = 0; k < nl; ++k) {
+            if (leaves[k] & 0x80000000u) continue;
+            item_box(t, leaves[k], lo, hi);
+            const float a = half_area(lo, hi);
+            if (bi < 0 || a > ba) { bi = k; ba = a; }
+        }
+        if (bi < 0) break;
+        const uint32_t x = leaves[bi];
+        used[nu++] = x;
+        leaves[bi] = __ldcg(t.children + 2 * (size_t)x);
+        leaves[nl++] = __ldcg(t.children + 2 * (size_t)x + 1);
+    }
+    float llo_[kTreeletLeaves][3], lhi_[kTreeletLeaves][3];
+    for (int k = 0; k < nl; ++k) item_box(t, leaves[k], llo_[k], lhi_[k]);
+    const int full = (1 << nl) - 1;
+    float sarea[1 << kTreeletLeaves], scost[1 << kTreeletLeaves];
+    uint8_t spart[1 << kTreeletLeaves];
+    for (int S = 1; S <= full; ++S) {
+        float slo[3] = {INFINITY, INFINITY, INFINITY}, shi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int k = 0; k < nl; ++k) {
+            if (!(S >> k & 1)) continue;
+            for (int a = 0; a < 3; ++a) {
+                slo[a] = llo_[k][a] < slo[a] ? llo_[k][a] : slo[a];
+                shi[a] = lhi_[k][a] > shi[a] ? lhi_[k][a] : shi[a];
+            }
+        }
+        sarea[S] = half_area(slo, shi);
+    }
+    for (int S = 1; S <= full; ++S) {
+        if ((S & (S - 1)) == 0) {
+            scost[S] = item_cost(t, leaves[__ffs(S) - 1]);
+            spart[S] = 0;
+            continue;
+        }
+        const int low = S & -S;
+        float best = INFINITY;
+        int bp = 0;
+        for (int P = (S - 1) & S; P > 0; P = (P - 1) & S) {
+            if (!(P & low)) continue;
+            const float c = scost[P] + scost[S ^ P];
+            if (c < best) { best = c; bp = P; }
+        }
+        scost[S] = kTreeletCi * sarea[S] + best;
+        spart[S] = (uint8_t)bp;
+    }
+    if (!(scost[full] < cR * 0.99999f)) return;
+    uint32_t node_of[1 << kTreeletLeaves];
+    int seq[kTreeletLeaves - 1], ns = 0, stk[kTreeletLeaves], sp = 0, ui = 0;
+    stk[sp++] = full;
+    while (sp > 0) {
+        const int S = stk[--sp];
+        node_of[S] = used[ui++];
+        seq[ns++] = S;
+        const int P = spart[S], Q = S ^ P;
+        if (Q & (Q - 1)) stk[sp++] = Q;
+        if (P & (P - 1)) stk[sp++] = P;
+    }
+    for (int j = 0; j < ns; ++j) {
+        const uint32_t node = node_of[seq[j]];
+        const int P = spart[seq[j]], Q = seq[j] ^ P;
+        const uint32_t l = (P & (P - 1)) == 0 ? leaves[__ffs(P) - 1] : node_of[P];
+        const uint32_t r = (Q & (Q - 1)) == 0 ? leaves[__ffs(Q) - 1] : node_of[Q];
+        __stcg(t.children + 2 * (size_t)node, l);
+        __stcg(t.children + 2 * (size_t)node + 1, r);
+        if (l & 0x80000000u) __stcg(t.parent_leaf + (l & 0x7fffffffu), (int)node);
+        else __stcg(t.parent_int + l, (int)node);
+        if (r & 0x80000000u) __stcg(t.parent_leaf + (r & 0x7fffffffu), (int)node);
+        else __stcg(t.parent_int + r, (int)node);
+    }
+    for (int j = ns - 1; j >= 0; --j) {
+        const uint32_t node = node_of[seq[j]];
+        const uint32_t l = __ldcg(t.children + 2 * (size_t)node), r = __ldcg(t.children + 2 * (size_t)node + 1);
+        float al[3], ah[3], bl[3], bh[3];
+        item_box(t, l, al, ah);
+        item_box(t, r, bl, bh);
+        float nlo[3], nhi[3];
+        for (int a = 0; a < 3; ++a) {
+            nlo[a] = al[a] < bl[a] ? al[a] : bl[a];
+            nhi[a] = ah[a] > bh[a] ? ah[a] : bh[a];
+            __stcg(t.blo + 3 * (size_t)node + a, nlo[a]);
+            __stcg(t.bhi + 3 * (size_t)node + a, nhi[a]);
+        }
+        __stcg(t.count + node, item_count(t, l) + item_count(t, r));
+        __stcg(t.cost + node, kTreeletCi * half_area(nlo, nhi) + (item_cost(t, l) + item_cost(t, r)));
+    }
+}
+
+__global__ void k_treelet(uint32_t n, TreeletCtx t, uint32_t* flags, uint32_t* status) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = __ldcg(t.parent_leaf + i);
+    uint32_t steps = 0;
+    while (node >= 0) {
+        if (++steps > n + 1) {
+            atomicOr(status, 1u);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0) return;
+        __threadfence();
+        treelet_node(t, (uint32_t)node);
+        __threadfence();
+        node = __ldcg(t.parent_int + node);
+    }
+}
+
 __device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(e < -126 ? 1 : e + 127) << 23); }
 __device__ __forceinline__ int ceil_log2f(float x) {
     uint32_t b = __float_as_uint(x);
@@ -225,11 +399,6 @@ __device__ __forceinline__ int grid_exponent(float lo, float hi) {
     e = e > e_min ? e : e_min;
     return e < -126 ? -126 : (e > 119 ? 119 : e);
 }
-__device__ __forceinline__ float half_area(const float* lo, const float* hi) {
-    float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
-    return dx * dy + dy * dz + dz * dx;
-}
-
 struct Plan {
     uint32_t kids[8];
     uint32_t nk;
@@ -466,6 +635,7 @@ hx_status hx_build_bvh(hx_context* ctx, hx_scene* s, const float* d_world, uint3
     size_t o_llo = carve(12 * (size_t)n), o_lhi = carve(12 * (size_t)n);
     size_t o_blo = carve(12 * (size_t)std::max<uint32_t>(ni, 1)), o_bhi = carve(12 * (size_t)std::max<uint32_t>(ni, 1));
     size_t o_flags = carve(4 * (size_t)std::max<uint32_t>(ni, 1));
+    size_t o_cost = carve(4 * (size_t)std::max<uint32_t>(ni, 1));
     size_t o_queue = carve(4 * (size_t)max_nodes);
     size_t o_plans = carve(sizeof(Plan) * (size_t)max_nodes);
     size_t o_nint = carve(4 * (size_t)max_nodes), o_nleaf = carve(4 * (size_t)max_nodes);
@@ -488,6 +658,7 @@ hx_status hx_build_bvh(hx_context* ctx, hx_scene* s, const float* d_world, uint3
     float* blo = (float*)(base + o_blo);
     float* bhi = (float*)(base + o_bhi);
     uint32_t* flags = (uint32_t*)(base + o_flags);
+    float* cost = (float*)(base + o_cost);
     uint32_t* queue = (uint32_t*)(base + o_queue);
     Plan* plans = (Plan*)(base + o_plans);
     uint32_t* nint = (uint32_t*)(base + o_nint);
@@ -511,6 +682,11 @@ hx_status hx_build_bvh(hx_context* ctx, hx_scene* s, const float* d_world, uint3
     if (ni > 0) {
         HX_CUDA(cudaMemsetAsync(flags, 0, 4 * (size_t)ni, st));
         k_fit<<<blocks_for(n), kThreads, 0, st>>>(n, children, pint, pleaf, llo, lhi, blo, bhi, flags, tot + 2);
+        TreeletCtx tc{children, pint, pleaf, llo, lhi, blo, bhi, count, cost};
+        for (int pass = 0; pass < kTreeletPasses; ++pass) {
+            HX_CUDA(cudaMemsetAsync(flags, 0, 4 * (size_t)ni, st));
+            k_treelet<<<blocks_for(n), kThreads, 0, st>>>(n, tc, flags, tot + 2);
+        }
     }
     // breadth-first collapse
     uint32_t root = ni > 0 ? 0u : 0x80000000u;

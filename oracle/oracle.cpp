@@ -437,6 +437,127 @@ static void assign_octant_slots(int nk, const float (*klo)[3], const float (*khi
 // triangle's own 8-bit box culls it before the triangle test.
 constexpr uint32_t kLeafMax = 1;
 
+// Treelet restructuring of the binary LBVH (Karras & Aila, "Fast Parallel
+// Construction of High-Quality Bounding Volume Hierarchies", HPG 2013), the
+// same steps as the device builder (bvh_build.cu, k_treelet): in each pass,
+// every internal node R with >= 3 triangles, after all its descendants,
+// grows a treelet of up to 7 leaves by opening the leaf with the largest
+// surface area (ties: the first), finds the binary topology over those
+// leaves with the least surface-area cost by dynamic programming over leaf
+// subsets (partitions enumerated downwards, ties: the first), and rebuilds
+// the treelet with it when that is cheaper, reusing its internal nodes in
+// pre-order.  Cost: internal node Ci * area + children, leaf Ct * area.
+// The result depends only on each node's subtree, so any bottom-up order
+// (the device's arrival order, this topological order) gives the same tree.
+constexpr int kTreeletLeaves = 7, kTreeletPasses = 3;
+constexpr float kTreeletCi = 1.2f, kTreeletCt = 1.0f;
+
+static void restructure_treelets(Bvh& b, int n, const std::vector<float>& llo, const std::vector<float>& lhi) {
+    const int ni = n - 1;
+    if (ni < 2) return;
+    auto box = [&](uint32_t c, const float*& lo, const float*& hi) {
+        if (c & 0x80000000u) { lo = &llo[3 * (size_t)(c & 0x7fffffffu)]; hi = &lhi[3 * (size_t)(c & 0x7fffffffu)]; }
+        else { lo = &b.lo[3 * (size_t)c]; hi = &b.hi[3 * (size_t)c]; }
+    };
+    std::vector<float> cost(ni, 0.0f);
+    auto area_of = [&](uint32_t c) { const float *lo, *hi; box(c, lo, hi); return half_area(lo, hi); };
+    auto cost_of = [&](uint32_t c) { return (c & 0x80000000u) ? kTreeletCt * area_of(c) : cost[c]; };
+    auto cnt_of = [&](uint32_t c) { return (c & 0x80000000u) ? 1u : b.count[c]; };
+    std::vector<int> order(ni);
+    for (int pass = 0; pass < kTreeletPasses; ++pass) {
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b.count[x] < b.count[y]; });
+        for (int R : order) {
+            cost[R] = kTreeletCi * area_of((uint32_t)R) + (cost_of(b.children[2 * (size_t)R]) + cost_of(b.children[2 * (size_t)R + 1]));
+            if (b.count[R] < 3) continue;
+            uint32_t leaves[kTreeletLeaves], used[kTreeletLeaves - 1];
+            int nl = 2, nu = 1;
+            leaves[0] = b.children[2 * (size_t)R];
+            leaves[1] = b.children[2 * (size_t)R + 1];
+            used[0] = (uint32_t)R;
+            while (nl < kTreeletLeaves) {
+                int bi = -1;
+                float ba = 0.0f;
+                for (int k = 0; k < nl; ++k) {
+                    if (leaves[k] & 0x80000000u) continue;
+                    float a = area_of(leaves[k]);
+                    if (bi < 0 || a > ba) { bi = k; ba = a; }
+                }
+                if (bi < 0) break;
+                const uint32_t x = leaves[bi];
+                used[nu++] = x;
+                leaves[bi] = b.children[2 * (size_t)x];
+                leaves[nl++] = b.children[2 * (size_t)x + 1];
+            }
+            const int full = (1 << nl) - 1;
+            float sarea[1 << kTreeletLeaves], scost[1 << kTreeletLeaves];
+            uint8_t spart[1 << kTreeletLeaves];
+            for (int S = 1; S <= full; ++S) {
+                float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+                for (int k = 0; k < nl; ++k) {
+                    if (!(S >> k & 1)) continue;
+                    const float *l, *h;
+                    box(leaves[k], l, h);
+                    for (int a = 0; a < 3; ++a) {
+                        lo[a] = l[a] < lo[a] ? l[a] : lo[a];
+                        hi[a] = h[a] > hi[a] ? h[a] : hi[a];
+                    }
+                }
+                sarea[S] = half_area(lo, hi);
+            }
+            for (int S = 1; S <= full; ++S) {
+                if ((S & (S - 1)) == 0) {
+                    scost[S] = cost_of(leaves[__builtin_ctz((unsigned)S)]);
+                    spart[S] = 0;
+                    continue;
+                }
+                const int low = S & -S;
+                float best = INFINITY;
+                int bp = 0;
+                for (int P = (S - 1) & S; P > 0; P = (P - 1) & S) {
+                    if (!(P & low)) continue;
+                    const float c = scost[P] + scost[S ^ P];
+                    if (c < best) { best = c; bp = P; }
+                }
+                scost[S] = kTreeletCi * sarea[S] + best;
+                spart[S] = (uint8_t)bp;
+            }
+            if (!(scost[full] < cost[R] * 0.99999f)) continue;
+            // internal nodes to subsets in pre-order (left part first)
+            uint32_t node_of[1 << kTreeletLeaves];
+            int seq[kTreeletLeaves - 1], ns = 0, stk[kTreeletLeaves], sp = 0, ui = 0;
+            stk[sp++] = full;
+            while (sp > 0) {
+                const int S = stk[--sp];
+                node_of[S] = used[ui++];
+                seq[ns++] = S;
+                const int P = spart[S], Q = S ^ P;
+                if (Q & (Q - 1)) stk[sp++] = Q;
+                if (P & (P - 1)) stk[sp++] = P;
+            }
+            auto item = [&](int C) { return (C & (C - 1)) == 0 ? leaves[__builtin_ctz((unsigned)C)] : node_of[C]; };
+            for (int j = 0; j < ns; ++j) {
+                const uint32_t node = node_of[seq[j]];
+                b.children[2 * (size_t)node] = item(spart[seq[j]]);
+                b.children[2 * (size_t)node + 1] = item(seq[j] ^ spart[seq[j]]);
+            }
+            for (int j = ns - 1; j >= 0; --j) {
+                const uint32_t node = node_of[seq[j]];
+                const uint32_t l = b.children[2 * (size_t)node], r = b.children[2 * (size_t)node + 1];
+                const float *al, *ah, *bl, *bh;
+                box(l, al, ah);
+                box(r, bl, bh);
+                for (int a = 0; a < 3; ++a) {
+                    b.lo[3 * (size_t)node + a] = al[a] < bl[a] ? al[a] : bl[a];
+                    b.hi[3 * (size_t)node + a] = ah[a] > bh[a] ? ah[a] : bh[a];
+                }
+                b.count[node] = cnt_of(l) + cnt_of(r);
+                cost[node] = kTreeletCi * half_area(&b.lo[3 * (size_t)node], &b.hi[3 * (size_t)node]) + (cost_of(l) + cost_of(r));
+            }
+        }
+    }
+}
+
 static void build_bvh(Scene& s) {
     Bvh& b = s.bvh;
     int n = (int)s.prims.size();
@@ -534,6 +655,8 @@ static void build_bvh(Scene& s) {
             b.hi[3 * (size_t)i + a] = ah[a] > bh[a] ? ah[a] : bh[a];
         }
     }
+
+    restructure_treelets(b, n, llo, lhi);
 
     // BVH8 collapse, breadth-first.
     b.nodes.clear();
