@@ -306,13 +306,15 @@ __device__ void treelet_node(const TreeletCtx& t, uint32_t R) {
             spart[S] = 0;
             continue;
         }
-        const int low = S & -S;
+        // partitions (P, S ^ P) with P holding the lowest leaf, P descending
+        const int low = S & -S, rest = S ^ low;
         float best = INFINITY;
         int bp = 0;
-        for (int P = (S - 1) & S; P > 0; P = (P - 1) & S) {
-            if (!(P & low)) continue;
+        for (int Q = (rest - 1) & rest;; Q = (Q - 1) & rest) {
+            const int P = Q | low;
             const float c = scost[P] + scost[S ^ P];
             if (c < best) { best = c; bp = P; }
+            if (Q == 0) break;
         }
         scost[S] = kTreeletCi * sarea[S] + best;
         spart[S] = (uint8_t)bp;
