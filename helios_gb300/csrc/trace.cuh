@@ -199,28 +199,48 @@ constexpr int kStackSize = 32;
 
 HXD uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
-// 2^23 + q for byte k of w, built with one byte permute (bits 0x4B000000 | q:
-// the byte fills the low mantissa byte of 2^23).
-HXD float byte_biased(uint32_t w, int k) { return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k)); }
+// 1 + q 2^-15 for byte k of w, built with one byte permute (bits
+// 0x3F80 | q << 8 | 0x00: the byte fills mantissa bits 15..8 of 1.0).
+HXD float byte_plane(uint32_t w, int k) { return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (k << 4))); }
+
+// Slab distances of one node axis in the form t = f A + C, f = 1 + q 2^-15
+// the byte-plane value of a child plane q: with the node grid origin g and
+// step S = 2^e, the plane is L = g + q S, so
+//   t = (L - o) inv = b + q S inv = f A + (b - A),  A = 2^(e+15) inv,
+//   b = (g - o) inv
+// (A is exact: a power-of-two multiple of inv).  Rounding of b, of b - A and
+// of the final FMA is below 2^-22 (|b| + |A|) in total, and the reciprocal's
+// own rounding below 2^-24 (|b| + |A|) of the true distance, so moving the
+// near constant down and the far constant up by 2^-21 (|b| + |A|) keeps every
+// child slab conservative: a box the ray meets is never culled.
+struct AxisSlab {
+    float2 A;   // (A, A)
+    float2 C;   // (b - A - delta, b - A + delta)
+};
+HXD AxisSlab axis_slab(uint32_t origin_bits, uint32_t exp_byte, float o, float inv) {
+    const int e = (int)(int8_t)exp_byte;
+    const float A = __uint_as_float((uint32_t)(e + 142) << 23) * inv;
+    const float b = (__uint_as_float(origin_bits) - o) * inv;
+    const float C = b - A;
+    const float delta = (fabsf(b) + fabsf(A)) * 4.76837158203125e-7f;  // 2^-21
+    AxisSlab r;
+    r.A = make_float2(A, A);
+    r.C = make_float2(C - delta, C + delta);
+    return r;
+}
 
 // Intersects the ray with the (up to) 8 children of a node held in five
 // 16-byte words and returns the hit mask in node-group form: bit
 // 24 + (slot ^ oct_inv) for a hit internal child, bit off for the triangle of
 // a hit leaf slot (bit 16, outside both masks, for an empty slot).  The meta
 // bytes carry these bit positions (internal slots: 24 + slot, flagged by bit
-// 7, which selects the XOR with the ray octant), four slots per word.  Planes decode exactly (the builder snaps each
-// node grid so origin + q 2^e is representable and |origin| < 2^23 2^e):
-// L = (2^23 + q) * 2^e + (origin - 2^23 2^e), one rounding-free FMA; then
-// t = (L - o) * inv, with the far planes multiplied by the slack-widened
-// reciprocal (1 + 2^-21).
+// 7, which selects the XOR with the ray octant), four slots per word.  Each
+// child axis costs one packed FMA (near, far): t = f A + C (axis_slab).
 HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, const uint4 w3, const uint4 w4,
-                                const RayPre& r, float fix, float fiy, float fiz, uint32_t oct_inv, float tmin,
-                                float lim) {
-    const int ex = (int)(int8_t)(w0.w & 0xffu), ey = (int)(int8_t)((w0.w >> 8) & 0xffu), ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
-    const float Sx = __uint_as_float((uint32_t)(ex + 127) << 23), Sy = __uint_as_float((uint32_t)(ey + 127) << 23),
-                Sz = __uint_as_float((uint32_t)(ez + 127) << 23);
-    const float Ox = __fmaf_rn(-8388608.0f, Sx, __uint_as_float(w0.x)), Oy = __fmaf_rn(-8388608.0f, Sy, __uint_as_float(w0.y)),
-                Oz = __fmaf_rn(-8388608.0f, Sz, __uint_as_float(w0.z));
+                                const RayPre& r, uint32_t oct_inv, float tmin, float lim) {
+    const AxisSlab X = axis_slab(w0.x, w0.w & 0xffu, r.o.x, r.ix);
+    const AxisSlab Y = axis_slab(w0.y, (w0.w >> 8) & 0xffu, r.o.y, r.iy);
+    const AxisSlab Z = axis_slab(w0.z, (w0.w >> 16) & 0xffu, r.o.z, r.iz);
     // near/far byte planes per axis chosen by the direction sign
     const bool nx = r.ix < 0.0f, ny = r.iy < 0.0f, nz = r.iz < 0.0f;
     const uint32_t lox0 = w2.x, lox1 = w2.y, loy0 = w2.z, loy1 = w2.w, loz0 = w3.x, loz1 = w3.y;
@@ -228,10 +248,6 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
     const uint32_t nx0 = nx ? hix0 : lox0, nx1 = nx ? hix1 : lox1, fx0 = nx ? lox0 : hix0, fx1 = nx ? lox1 : hix1;
     const uint32_t ny0 = ny ? hiy0 : loy0, ny1 = ny ? hiy1 : loy1, fy0 = ny ? loy0 : hiy0, fy1 = ny ? loy1 : hiy1;
     const uint32_t nz0 = nz ? hiz0 : loz0, nz1 = nz ? hiz1 : loz1, fz0 = nz ? loz0 : hiz0, fz1 = nz ? loz1 : hiz1;
-    const float2 Sx2 = make_float2(Sx, Sx), Sy2 = make_float2(Sy, Sy), Sz2 = make_float2(Sz, Sz);
-    const float2 Ox2 = make_float2(Ox, Ox), Oy2 = make_float2(Oy, Oy), Oz2 = make_float2(Oz, Oz);
-    const float2 ox2 = make_float2(r.o.x, r.o.x), oy2 = make_float2(r.o.y, r.o.y), oz2 = make_float2(r.o.z, r.o.z);
-    const float2 ix2 = make_float2(r.ix, fix), iy2 = make_float2(r.iy, fiy), iz2 = make_float2(r.iz, fiz);
     const uint32_t mw0 = (w1.z ^ (((w1.z & 0x80808080u) >> 7) * oct_inv)) & 0x1f1f1f1fu;
     const uint32_t mw1 = (w1.w ^ (((w1.w & 0x80808080u) >> 7) * oct_inv)) & 0x1f1f1f1fu;
     uint32_t hits = 0;
@@ -239,13 +255,9 @@ HXD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, 
     for (int c = 0; c < 8; ++c) {
         const uint32_t pos = byte_of(c < 4 ? mw0 : mw1, c & 3);
         const int k = c & 3;
-        // (near, far) pairs per axis in packed FP32x2: L = q' S + O, t = (L - o) inv
-        const float2 Lx = fma2_rn(make_float2(byte_biased(c < 4 ? nx0 : nx1, k), byte_biased(c < 4 ? fx0 : fx1, k)), Sx2, Ox2);
-        const float2 Ly = fma2_rn(make_float2(byte_biased(c < 4 ? ny0 : ny1, k), byte_biased(c < 4 ? fy0 : fy1, k)), Sy2, Oy2);
-        const float2 Lz = fma2_rn(make_float2(byte_biased(c < 4 ? nz0 : nz1, k), byte_biased(c < 4 ? fz0 : fz1, k)), Sz2, Oz2);
-        const float2 tx = mul2_rn(sub2_rn(Lx, ox2), ix2);
-        const float2 ty = mul2_rn(sub2_rn(Ly, oy2), iy2);
-        const float2 tz = mul2_rn(sub2_rn(Lz, oz2), iz2);
+        const float2 tx = fma2_rn(make_float2(byte_plane(c < 4 ? nx0 : nx1, k), byte_plane(c < 4 ? fx0 : fx1, k)), X.A, X.C);
+        const float2 ty = fma2_rn(make_float2(byte_plane(c < 4 ? ny0 : ny1, k), byte_plane(c < 4 ? fy0 : fy1, k)), Y.A, Y.C);
+        const float2 tz = fma2_rn(make_float2(byte_plane(c < 4 ? nz0 : nz1, k), byte_plane(c < 4 ? fz0 : fz1, k)), Z.A, Z.C);
         const float tn = fmaxf(max3f(tx.x, ty.x, tz.x), tmin);
         const float tf = fminf(min3f(tx.y, ty.y, tz.y), lim);
         if (tn <= tf) hits |= 1u << pos;
@@ -272,7 +284,6 @@ HXD bool lowest_active_lane() { return (threadIdx.x & 31u) == (uint32_t)(__ffs(_
 // ---------------------------------------------------------------------------
 struct TravState {
     RayPre r;
-    float fix, fiy, fiz;  // far-plane reciprocals widened by 1 + 2^-21
     uint32_t oct_inv;
     float tmin, best_t, bu, bv;
     uint32_t best;
@@ -285,9 +296,6 @@ struct TravState {
 
 HXD void trav_init(TravState& st, const DevScene& s, V3 o, V3 d, float tmin, float tmax, bool any_hit) {
     st.r = ray_prepare(o, d);
-    st.fix = st.r.ix * 1.000000477f;
-    st.fiy = st.r.iy * 1.000000477f;
-    st.fiz = st.r.iz * 1.000000477f;
     const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
     st.oct_inv = 7u - oct;
     st.tmin = tmin;
@@ -330,9 +338,6 @@ HXD void trav_init_record(TravState& st, const DevScene& s, float4 o_tmin, float
     st.r.kz = (int)((bits >> 4) & 3u);
     st.r.sx = r1.x; st.r.sy = r1.y; st.r.sz = r1.z;
     st.r.ix = r0.x; st.r.iy = r0.y; st.r.iz = r0.z;
-    st.fix = r0.x * 1.000000477f;
-    st.fiy = r0.y * 1.000000477f;
-    st.fiz = r0.z * 1.000000477f;
     st.oct_inv = 7u - ((bits >> 6) & 7u);
     st.tmin = o_tmin.w;
     st.best_t = r0.w;
@@ -372,7 +377,7 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
             tc->nodes++;
             if (lowest_active_lane()) tc->warp_nodes++;
         }
-        const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.fix, st.fiy, st.fiz, st.oct_inv, st.tmin,
+        const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.oct_inv, st.tmin,
                                                st.best_t * 1.000001f);
         st.g_base = w1.x;
         st.g_mask = (hm & 0xff000000u) | (w0.w >> 24);
@@ -456,7 +461,7 @@ HXD uint32_t node_step(TravState& st, uint2* stack, const DevScene& s, float bes
         tc->nodes++;
         if (lowest_active_lane()) tc->warp_nodes++;
     }
-    const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.fix, st.fiy, st.fiz, st.oct_inv, st.tmin,
+    const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, st.r, st.oct_inv, st.tmin,
                                            best_t * 1.000001f);
     st.g_base = w1.x;
     st.g_mask = (hm & 0xff000000u) | (w0.w >> 24);

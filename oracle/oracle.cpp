@@ -842,8 +842,9 @@ static bool trace(const Scene& s, V3<R> o, V3<R> d, R tmin, R tmax, bool any_hit
 }
 
 // ---------------------------------------------------------------------------
-// BVH8 traversal in the device's arithmetic (exact plane decode, far planes
-// widened by 1 + 2^-21, octant-ordered node groups).  Checks on the CPU that
+// BVH8 traversal in the device's arithmetic (one FMA per child plane on
+// per-node constants widened outward by 2^-21 of their magnitude,
+// octant-ordered node groups; trace.cuh axis_slab).  Checks on the CPU that
 // the quantised 8-wide tree never loses a hit; not used by the radiance path.
 // ---------------------------------------------------------------------------
 static bool trace_bvh8_cpu(const Scene& s, V3<float> o, V3<float> d, float tmin, float tmax, bool any_hit, float& t_out,
@@ -853,7 +854,6 @@ static bool trace_bvh8_cpu(const Scene& s, V3<float> o, V3<float> d, float tmin,
     if (b.nodes.empty()) return false;
     RayPre<float> r = ray_prepare(o, d);
     float ix = safe_inv(d.x), iy = safe_inv(d.y), iz = safe_inv(d.z);
-    float fix = ix * 1.000000477f, fiy = iy * 1.000000477f, fiz = iz * 1.000000477f;
     uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
     uint32_t oct_inv = 7u - oct;
     float best_t = tmax;
@@ -871,12 +871,18 @@ static bool trace_bvh8_cpu(const Scene& s, V3<float> o, V3<float> d, float tmin,
             const hx_bvh8_node& n = b.nodes[child];
             if (node_visits) ++*node_visits;
             uint32_t hits = 0;
-            float S[3], O[3];
+            // per axis t = f A + C with f = 1 + q 2^-15 (trace.cuh axis_slab):
+            // A = 2^(e+15) inv, b = (g - o) inv, C = b - A -/+ 2^-21 (|b| + |A|)
+            const float inv[3] = {ix, iy, iz}, org[3] = {o.x, o.y, o.z};
+            float A[3], Cn[3], Cf[3];
             for (int a = 0; a < 3; ++a) {
-                S[a] = pow2f(n.exponent[a]);
-                O[a] = std::fma(-8388608.0f, S[a], n.origin[a]);
+                A[a] = pow2f(n.exponent[a] + 15) * inv[a];
+                const float bb = (n.origin[a] - org[a]) * inv[a];
+                const float C = bb - A[a];
+                const float delta = (std::fabs(bb) + std::fabs(A[a])) * 4.76837158203125e-7f;
+                Cn[a] = C - delta;
+                Cf[a] = C + delta;
             }
-            const float inv[3] = {ix, iy, iz}, finv[3] = {fix, fiy, fiz}, org[3] = {o.x, o.y, o.z};
             float lim = best_t * 1.000001f;
             for (int c = 0; c < 8; ++c) {
                 uint32_t m = n.meta[c];
@@ -885,10 +891,9 @@ static bool trace_bvh8_cpu(const Scene& s, V3<float> o, V3<float> d, float tmin,
                 for (int a = 0; a < 3; ++a) {
                     bool neg = inv[a] < 0.0f;
                     uint32_t qn = neg ? n.qhi[a][c] : n.qlo[a][c], qf = neg ? n.qlo[a][c] : n.qhi[a][c];
-                    float un = f32_bits(0x4B000000u | qn), uf = f32_bits(0x4B000000u | qf);
-                    float Ln = std::fma(un, S[a], O[a]), Lf = std::fma(uf, S[a], O[a]);
-                    tna[a] = (Ln - org[a]) * inv[a];
-                    tfa[a] = (Lf - org[a]) * finv[a];
+                    float un = f32_bits(0x3F800000u | (qn << 8)), uf = f32_bits(0x3F800000u | (qf << 8));
+                    tna[a] = std::fma(un, A[a], Cn[a]);
+                    tfa[a] = std::fma(uf, A[a], Cf[a]);
                 }
                 tn = std::fmax(std::fmax(tna[0], tna[1]), std::fmax(tna[2], tmin));
                 tf = std::fmin(std::fmin(tfa[0], tfa[1]), std::fmin(tfa[2], lim));
