@@ -13,8 +13,11 @@ namespace {
 constexpr uint32_t kAnyHitFlag = 0x80000000u;
 constexpr int kTraceThreads = 128;
 // 8 blocks of 128 threads per SM caps the traversal kernels at 64 registers:
-// 32 resident warps instead of 28 (measured 4% faster than 72 registers).
+// 32 resident warps instead of 28 (measured 4% faster than 72 registers;
+// 9 and 10 blocks spill and measured 0.3-2.6% slower).  The shade kernel
+// runs at the same cap (1.11 ms per frame, 1.12 ms at 72 registers).
 constexpr int kTraceMinBlocks = 8;
+constexpr int kShadeMinBlocks = 8;
 constexpr int kShadeThreads = 128;
 constexpr int kGenThreads = 256;
 
@@ -132,7 +135,7 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
 }
 
 template <bool FP16>
-__global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene s, Policy P, uint32_t max_bounces, float bias, int cur,
+__global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevScene s, Policy P, uint32_t max_bounces, float bias, int cur,
                                                          Queues q) {
     const uint32_t n = q.counters[cur];
     const int nxt = cur ^ 1;
