@@ -271,7 +271,7 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
                 HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
 #define HX_EXTEND(COUNT, FP16)                                                                                      \
     do {                                                                                                            \
-        if (!FP16 && s.num_prims < (1u << 27) && b < kBatchedBounces)                                               \
+        if (!FP16 && s.num_prims < (1u << 27))                                                                      \
             k_extend_batched<COUNT><<<it->grid_batched, kTraceThreads, 0, st>>>(                                    \
                 s, it->q, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.counters + cur, it->q.counters + 4,     \
                 kFlushTris, kFlushParked);                                                                          \

@@ -352,7 +352,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     for (uint32_t bo = 0; bo <= s->desc.max_ray_bounces; ++bo) {
         int cur = bo & 1;
         cudaMemsetAsync(b->q.counters + 4, 0, 4, st);
-        if (bo < kBatchedBounces && sc.num_prims < (1u << 27))
+        if (sc.num_prims < (1u << 27))
             k_extend_batched<false><<<grid_batched, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.r0[cur], b->q.r1[cur],
                                                                             b->q.counters + cur, b->q.counters + 4,
                                                                             kFlushTris, kFlushParked);

@@ -351,11 +351,12 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
     if (overflow) atomicOr(q.status, 1u);
 }
 
-// Batched triangle tests pay on the large early bounces (coherent primary
-// rays, alpha-tested first bounces); the small late launches, where lanes
-// would wait on a flush, use k_extend.  Flush after 24 queued triangles or 4
-// waiting lanes (measured on the 1.18 M-triangle scene at 1080p).
-constexpr uint32_t kFlushTris = 24, kFlushParked = 4, kBatchedBounces = 4;
+// Batched triangle tests run every bounce of the FP32-payload path (with
+// three node visits per iteration they also beat the lane-local k_extend on
+// the small late launches: +0.7%); k_extend serves the 16-bit payload form.
+// Flush after 24 queued triangles or 4 waiting lanes (measured on the
+// 1.18 M-triangle scene at 1080p).
+constexpr uint32_t kFlushTris = 24, kFlushParked = 4;
 // Node visits per loop iteration for a lane whose nodes expose no triangle:
 // spreads the warp's per-iteration queue bookkeeping over more visits
 // (measured 1: 263.7, 2: 265.7, 3: 269.2, 4: 268.0, 6: 263.1 Mpaths/s).
