@@ -256,6 +256,8 @@ _SIGS = {
     "hx_server_set_denoiser": (C.c_int, [_P, _P]),
     "hx_denoiser_set_loss": (C.c_int, [_P, C.c_uint32]),
     "hx_integrator_set_aov_accumulation": (C.c_int, [_P, C.c_uint32]),
+    "hx_encode_png": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "hx_save_png": (C.c_int, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
 }
 
 _lib_handle = None
@@ -313,6 +315,22 @@ def hosek_wilkie_coefficients(sun_direction, turbidity=3.0, normalized_sun_y=1.1
     out = (C.c_float * 40)()
     check(lib().hx_hosek_wilkie_coefficients(d, turbidity, normalized_sun_y, out))
     return np.array(out[:], dtype=np.float32).reshape(10, 4)[:, :3]
+
+
+def encode_png(rgba8):
+    """PNG file bytes of an (H, W, 4) uint8 image (Renderer::save_image_to_disk's format)."""
+    img = np.ascontiguousarray(rgba8, dtype=np.uint8)
+    h, w = img.shape[0], img.shape[1]
+    n = C.c_uint64()
+    check(lib().hx_encode_png(_ptr(img), w, h, None, 0, C.byref(n)))
+    out = np.zeros(n.value, np.uint8)
+    check(lib().hx_encode_png(_ptr(img), w, h, _ptr(out), out.size, C.byref(n)))
+    return out.tobytes()
+
+
+def save_png(path, rgba8):
+    img = np.ascontiguousarray(rgba8, dtype=np.uint8)
+    check(lib().hx_save_png(os.fsencode(path), _ptr(img), img.shape[1], img.shape[0]))
 
 
 class HostScene:

@@ -24,7 +24,7 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden", "-Wall"]
 
 CU_SOURCES = ["context.cu", "sort.cu", "bvh_build.cu", "scene.cu", "integrator.cu", "server.cu", "denoise.cu"]
-CPP_SOURCES = ["procedural.cpp"]
+CPP_SOURCES = ["procedural.cpp", "image_io.cpp"]
 
 
 def _run(cmd):

@@ -3,9 +3,9 @@
 // uploads a procedural scene, renders N progressive frames through
 // helios::PathIntegrator / helios::Renderer and writes the tone-mapped image;
 // with a parameter file of the learned denoiser (raw FP32, hx.h layout) it
-// also writes the denoised image next to it (<out>.denoised.ppm).
+// also writes the denoised image next to it (<out>.denoised.png).
 //
-//   hx_render <box|icospheres> <width> <height> <frames> <out.ppm> [denoiser.f32]
+//   hx_render <box|icospheres> <width> <height> <frames> <out.png> [denoiser.f32]
 #include "helios_gb300.hpp"
 
 #include <chrono>
@@ -15,7 +15,7 @@
 
 int main(int argc, char** argv) {
     if (argc < 6) {
-        std::fprintf(stderr, "usage: %s <box|icospheres> <width> <height> <frames> <out.ppm> [denoiser.f32]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <box|icospheres> <width> <height> <frames> <out.png> [denoiser.f32]\n", argv[0]);
         return 2;
     }
     const bool box = std::strcmp(argv[1], "box") == 0;
@@ -57,12 +57,8 @@ int main(int argc, char** argv) {
             std::fclose(f);
             dn.set_params(params);
             std::vector<uint8_t> px = dn.denoise(*integrator, frame, w, h);
-            std::string out = std::string(argv[5]) + ".denoised.ppm";
-            FILE* o = std::fopen(out.c_str(), "wb");
-            if (!o) throw std::runtime_error("cannot open " + out);
-            std::fprintf(o, "P6\n%u %u\n255\n", w, h);
-            for (size_t i = 0; i < (size_t)w * h; ++i) std::fwrite(&px[4 * i], 1, 3, o);
-            std::fclose(o);
+            std::string out = std::string(argv[5]) + ".denoised.png";
+            helios::hx_check(hx_save_png(out.c_str(), px.data(), w, h));
             std::printf("denoised image: %s\n", out.c_str());
         }
         hx_host_scene_destroy(hs);

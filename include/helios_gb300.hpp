@@ -129,14 +129,10 @@ public:
         hx_check(hx_integrator_tonemap(m_integrator->handle(), (uint32_t)m_op, m_exposure, px.data()));
         return px;
     }
-    // Binary PPM instead of stb's PNG (no image-library dependency).
+    // The tone-mapped frame as an RGBA PNG (renderer.cpp:637-713).
     void save_image_to_disk(const std::string& path, uint32_t width, uint32_t height) {
         std::vector<uint8_t> px = read_ldr(width, height);
-        FILE* f = std::fopen(path.c_str(), "wb");
-        if (!f) throw std::runtime_error("cannot open " + path);
-        std::fprintf(f, "P6\n%u %u\n255\n", width, height);
-        for (size_t i = 0; i < (size_t)width * height; ++i) std::fwrite(&px[4 * i], 1, 3, f);
-        std::fclose(f);
+        hx_check(hx_save_png(path.c_str(), px.data(), width, height));
     }
 
 private:

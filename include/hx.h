@@ -562,6 +562,16 @@ HX_API const hx_scene_desc* hx_host_scene_desc(const hx_host_scene* scene);
 HX_API hx_status hx_host_scene_camera(const hx_host_scene* scene, hx_camera* out);
 HX_API hx_status hx_host_scene_destroy(hx_host_scene* scene);
 
+/* PNG export: replaces the stb_image_write call behind
+ * Renderer::save_image_to_disk (renderer.h:97, renderer.cpp:637-713), which
+ * writes the tone-mapped RGBA8 frame as a PNG.  8-bit RGBA rows top to
+ * bottom (the layout hx_integrator_tonemap returns).  hx_encode_png writes
+ * the file bytes to out (out = NULL: only *size is set); hx_save_png writes
+ * them to path.  Host-only: needs no GPU. */
+HX_API hx_status hx_encode_png(const uint8_t* rgba8, uint32_t width, uint32_t height, uint8_t* out,
+                               uint64_t capacity, uint64_t* size);
+HX_API hx_status hx_save_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
+
 /* Hosek-Wilkie RGB coefficients (A..I, Z; 10 x vec4) for the given sun
  * direction, turbidity 3 or 4 and ground albedo 0.1, normalised so the
  * luminance toward the sun is normalized_sun_y

@@ -88,3 +88,29 @@ class TriangleSoupScene:
     @property
     def desc(self):
         return C.pointer(self._desc)
+
+
+def decode_png(data):
+    """Independent PNG reader (stdlib zlib): checks the signature and every
+    chunk CRC, returns (H, W, 4) uint8 for 8-bit RGBA with filter 0 rows."""
+    import struct
+    import zlib
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, ihdr = 8, b"", None
+    while pos < len(data):
+        (n,) = struct.unpack(">I", data[pos:pos + 4])
+        typ, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        (crc,) = struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])
+        assert crc == zlib.crc32(typ + body) & 0xffffffff, typ
+        if typ == b"IHDR":
+            ihdr = struct.unpack(">IIBBBBB", body)
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    assert typ == b"IEND" and pos == len(data)
+    w, h, depth, ctype, comp, filt, inter = ihdr
+    assert (depth, ctype, comp, filt, inter) == (8, 6, 0, 0, 0)
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 4 * w + 1)
+    assert (raw[:, 0] == 0).all()
+    return raw[:, 1:].reshape(h, w, 4)
+

@@ -12,7 +12,7 @@ import pytest
 
 import helios_gb300 as hx
 from oracle import binding as ob
-from tests.helpers import TriangleSoupScene, integrator_desc, random_rays, rel_rmse, small_icosphere_scene
+from tests.helpers import TriangleSoupScene, decode_png, integrator_desc, random_rays, rel_rmse, small_icosphere_scene
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -282,9 +282,9 @@ def test_cpp_driver_renders(tmp_path):
     import subprocess
     from helios_gb300 import build as b
     exe = b.build_driver()
-    out = tmp_path / "box.ppm"
+    out = tmp_path / "box.png"
     r = subprocess.run([exe, "box", "128", "128", "16", str(out)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
-    data = out.read_bytes()
-    assert data.startswith(b"P6\n128 128\n255\n") and len(data) == 15 + 128 * 128 * 3
+    img = decode_png(out.read_bytes())
+    assert img.shape == (128, 128, 4) and (img[..., 3] == 255).all() and img[..., :3].max() > 0
     assert "16 samples accumulated" in r.stdout

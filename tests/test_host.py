@@ -9,6 +9,7 @@ import re
 import numpy as np
 
 import helios_gb300 as hx
+from tests.helpers import decode_png
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -90,3 +91,22 @@ def test_cpp_driver_builds_and_links():
     exe = b.build_driver()
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+def test_png_export_round_trip(tmp_path):
+    """hx_save_png / hx_encode_png (the stb_image_write PNG behind
+    Renderer::save_image_to_disk): a valid PNG whose pixels are the input's,
+    for a 1x1 image, odd sizes and one spanning several 64 KiB deflate blocks."""
+    rng = np.random.default_rng(4)
+    for h, w in ((1, 1), (3, 7), (181, 97)):
+        img = rng.integers(0, 256, size=(h, w, 4), dtype=np.uint8)
+        data = hx.encode_png(img)
+        assert np.array_equal(decode_png(data), img)
+        p = tmp_path / ("img_%d_%d.png" % (h, w))
+        hx.save_png(str(p), img)
+        assert p.read_bytes() == data
+    try:
+        hx.save_png(str(tmp_path / "no_such_dir" / "x.png"), np.zeros((2, 2, 4), np.uint8))
+        assert False, "writing into a missing directory must fail"
+    except hx.HxError as e:
+        assert "cannot open" in str(e)
