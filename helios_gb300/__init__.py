@@ -24,6 +24,7 @@ ACCUM_RUNNING_MEAN, ACCUM_KAHAN = 0, 1
 ENV_SAMPLE_COSINE, ENV_SAMPLE_IMPORTANCE = 0, 1
 PAYLOAD_FP32, PAYLOAD_FP16 = 0, 1
 TONEMAP_ACES, TONEMAP_REINHARD, TONEMAP_NONE = 0, 1, 2
+OUTPUT_ALBEDO, OUTPUT_NORMALS, OUTPUT_ROUGHNESS, OUTPUT_METALLIC, OUTPUT_EMISSIVE, OUTPUT_FINAL = 0, 1, 2, 3, 4, 5
 SCENE_BOX, SCENE_ICOSPHERES, SCENE_TERRAIN = 0, 1, 2
 SUBMESH_NON_OPAQUE = 1
 NO_HIT = 0xFFFFFFFF
@@ -91,7 +92,7 @@ class Policy(C.Structure):
     _fields_ = [("rng", C.c_uint32), ("rr_start_depth", C.c_uint32), ("rr_clamp", C.c_uint32),
                 ("radiance_clamp", C.c_float), ("accumulation", C.c_uint32), ("area_count_from_x", C.c_uint32),
                 ("area_w_one", C.c_uint32), ("env_sampling", C.c_uint32), ("payload", C.c_uint32),
-                ("reserved", C.c_uint32 * 3)]
+                ("visualize_nans", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class IntegratorDesc(C.Structure):
@@ -204,6 +205,7 @@ _SIGS = {
     "hx_integrator_progress": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "hx_integrator_tonemap": (C.c_int, [_P, C.c_uint32, C.c_float, _P]),
     "hx_integrator_read_accumulation": (C.c_int, [_P, _P]),
+    "hx_integrator_render_output": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
     "hx_integrator_set_timing": (C.c_int, [_P, C.c_uint32]),
     "hx_integrator_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "hx_integrator_set_counting": (C.c_int, [_P, C.c_uint32]),
@@ -549,6 +551,12 @@ class PathIntegrator:
     def read_accumulation(self):
         out = np.zeros((self.height, self.width, 4), np.float32)
         check(lib().hx_integrator_read_accumulation(self.handle, _ptr(out)))
+        return out
+
+    def render_output(self, frame, output_buffer):
+        """Renderer output buffer (OUTPUT_ALBEDO .. OUTPUT_FINAL): (H, W, 4) float32, display row order."""
+        out = np.zeros((self.height, self.width, 4), np.float32)
+        check(lib().hx_integrator_render_output(self.handle, C.byref(frame), output_buffer, _ptr(out)))
         return out
 
     def tonemap(self, op=TONEMAP_ACES, exposure=1.0, to_host=True):

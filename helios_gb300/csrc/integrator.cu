@@ -134,6 +134,8 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_CHECK_ARG(desc->width > 0 && desc->height > 0 && desc->width <= 16384 && desc->height <= 16384,
                  "hx_integrator_create: bad extents %ux%u", desc->width, desc->height);
     HX_CHECK_ARG(desc->policy.rng <= 1 && desc->policy.accumulation <= 1, "hx_integrator_create: bad policy");
+    HX_CHECK_ARG(!(desc->policy.visualize_nans && desc->policy.accumulation == HX_ACCUM_KAHAN),
+                 "hx_integrator_create: visualize_nans needs running-mean accumulation");
     HX_CUDA(cudaSetDevice(ctx->device));
     hx_integrator* it = new hx_integrator();
     it->ctx = ctx;
@@ -318,7 +320,8 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
         StageTimer t(it, &it->stats.ms_accumulate);
         bool kahan = it->desc.policy.accumulation == HX_ACCUM_KAHAN;
         k_accumulate<<<it->grid_gen, kGenThreads, 0, st>>>(rect, it->desc.width, frame0, nframes, it->desc.policy.radiance_clamp,
-                                                           kahan ? 1u : 0u, it->q.L, it->acc, it->comp);
+                                                           kahan ? 1u : 0u, it->desc.policy.visualize_nans ? 1u : 0u, it->q.L,
+                                                           it->acc, it->comp);
         k_count_add<<<it->grid_gen, kGenThreads, 0, st>>>(rect, it->desc.width, nframes, it->count_map);
         it->stats.kernel_launches += 2;
     }
@@ -447,6 +450,8 @@ extern "C" hx_status hx_integrator_set_tiled(hx_integrator* it, uint32_t tiled) 
 }
 extern "C" hx_status hx_integrator_set_policy(hx_integrator* it, const hx_policy* p) {
     HX_CHECK_ARG(it && p && p->rng <= 1 && p->accumulation <= 1, "hx_integrator_set_policy: bad policy");
+    HX_CHECK_ARG(!(p->visualize_nans && p->accumulation == HX_ACCUM_KAHAN),
+                 "hx_integrator_set_policy: visualize_nans needs running-mean accumulation");
     it->desc.policy = *p;
     return HX_OK;
 }
@@ -487,6 +492,110 @@ extern "C" hx_status hx_integrator_read_accumulation(hx_integrator* it, float* h
     HX_CUDA(cudaMemcpyAsync(host, it->resolved, 16 * (size_t)n, cudaMemcpyDeviceToHost, st));
     HX_CUDA(cudaStreamSynchronize(st));
     return HX_OK;
+}
+
+// Output-buffer views of Renderer::render_debug_visualization
+// (renderer.cpp:491-545; debug_visualization.vert:54-64,
+// debug_visualization.frag:71-161), rendered headless by ray casting: per
+// pixel one camera ray through the pixel centre (the raster pass samples
+// fragments there; pinhole, no jitter), the closest triangle with no alpha
+// test (the fragment shader never discards), then the fragment shader's value:
+//   albedo     material albedo or the bilinear texel RGB (level 0)
+//   normals    the interpolated per-vertex normalize(mat3(normal_matrix) n),
+//              not renormalised (no normal maps), * 0.5 + 0.5
+//   roughness  material roughness or the selected texture channel (no
+//              MIN_ROUGHNESS clamp), metallic likewise, emissive as albedo
+// Misses keep the clear colour (0, 0, 0, 1).  Rows are in display order (the
+// pass renders with a negative-height viewport, renderer.cpp:498-506): output
+// row r is the camera row H - 1 - r of the path tracer's launch grid, the same
+// orientation hx_integrator_tonemap returns.  HX_OUTPUT_FINAL is the resolved
+// accumulation in that orientation.
+__global__ void k_output_view(DevScene s, hx_frame_desc f, uint32_t W, uint32_t H, uint32_t which,
+                              const float4* __restrict__ resolved, float4* __restrict__ out, uint32_t* status) {
+    const uint32_t n = W * H;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % W, row = i / W, y = H - 1 - row;
+        if (which == HX_OUTPUT_FINAL) {
+            out[i] = resolved[(size_t)y * W + x];
+            continue;
+        }
+        const float tx = ((float)x + 0.5f) / (float)W, ty = ((float)y + 0.5f) / (float)H;
+        const float nx = tx * 2.0f - 1.0f, ny = ty * 2.0f - 1.0f;
+        const float* m = f.view_proj_inverse;
+        const float tw = mat4_row(m, 3, nx, ny, 0.0f, 1.0f);
+        const V3 target = v3(mat4_row(m, 0, nx, ny, 0.0f, 1.0f) / tw, mat4_row(m, 1, nx, ny, 0.0f, 1.0f) / tw,
+                             mat4_row(m, 2, nx, ny, 0.0f, 1.0f) / tw);
+        const V3 cam = light_v3(f.camera_pos);
+        const V3 d = normalize(target - cam);
+        TravState st;
+        uint2 stack[kStackSize];
+        bool overflow = false;
+        trav_init(st, s, cam, d, 0.001f, 10000.0f, false);
+        while (!trav_step<false>(st, stack, s, overflow, nullptr)) {
+        }
+        if (overflow) atomicOr(status, 1u);
+        float4 c = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        if (st.best != kNoHit) {
+            const uint4 pi = s.prim_info[st.best];
+            const DevInstance& inst = s.inst[pi.x];
+            const uint32_t i0 = s.indices[3 * pi.y], i1 = s.indices[3 * pi.y + 1], i2 = s.indices[3 * pi.y + 2];
+            const float4 p0 = s.vtx[2 * (size_t)i0], n0 = s.vtx[2 * (size_t)i0 + 1];
+            const float4 p1 = s.vtx[2 * (size_t)i1], n1 = s.vtx[2 * (size_t)i1 + 1];
+            const float4 p2 = s.vtx[2 * (size_t)i2], n2 = s.vtx[2 * (size_t)i2 + 1];
+            const float b0 = 1.0f - st.bu - st.bv, b1 = st.bu, b2 = st.bv;
+            const float tu = p0.w * b0 + p1.w * b1 + p2.w * b2;
+            const float tv = n0.w * b0 + n1.w * b1 + n2.w * b2;
+            const hx_material& mt = s.materials[pi.z];
+            V3 v = v3(0.0f);
+            if (which == HX_OUTPUT_ALBEDO) {
+                v = mt.texture_indices0[0] == -1 ? v3(mt.albedo[0], mt.albedo[1], mt.albedo[2])
+                                                 : tex_bilinear_rgb(s, (uint32_t)mt.texture_indices0[0], tu, tv);
+            } else if (which == HX_OUTPUT_NORMALS) {
+                const V3 a = normalize(mat3_mul(inst.normal, v3(n0.x, n0.y, n0.z)));
+                const V3 b = normalize(mat3_mul(inst.normal, v3(n1.x, n1.y, n1.z)));
+                const V3 e = normalize(mat3_mul(inst.normal, v3(n2.x, n2.y, n2.z)));
+                const V3 nn = v3(a.x * b0 + b.x * b1 + e.x * b2, a.y * b0 + b.y * b1 + e.y * b2, a.z * b0 + b.z * b1 + e.z * b2);
+                v = nn * 0.5f + v3(0.5f);
+            } else if (which == HX_OUTPUT_ROUGHNESS) {
+                const float r = mt.texture_indices0[2] == -1
+                                    ? mt.roughness_metallic[0]
+                                    : tex_bilinear(s, (uint32_t)mt.texture_indices0[2], tu, tv, mt.texture_indices1[2]);
+                v = v3(r);
+            } else if (which == HX_OUTPUT_METALLIC) {
+                const float r = mt.texture_indices0[3] == -1
+                                    ? mt.roughness_metallic[1]
+                                    : tex_bilinear(s, (uint32_t)mt.texture_indices0[3], tu, tv, mt.texture_indices1[3]);
+                v = v3(r);
+            } else {
+                v = mt.texture_indices1[0] == -1 ? v3(mt.emissive[0], mt.emissive[1], mt.emissive[2])
+                                                 : tex_bilinear_rgb(s, (uint32_t)mt.texture_indices1[0], tu, tv);
+            }
+            c = make_float4(v.x, v.y, v.z, 1.0f);
+        }
+        out[i] = c;
+    }
+}
+
+extern "C" hx_status hx_integrator_render_output(hx_integrator* it, const hx_frame_desc* frame, uint32_t output_buffer,
+                                                 float* host_rgba32f) {
+    HX_CHECK_ARG(it && frame && host_rgba32f, "hx_integrator_render_output: null argument");
+    HX_CHECK_ARG(output_buffer <= HX_OUTPUT_FINAL, "hx_integrator_render_output: output buffer %u (0..%u)", output_buffer,
+                 (unsigned)HX_OUTPUT_FINAL);
+    const uint32_t W = it->desc.width, H = it->desc.height, n = W * H;
+    cudaStream_t st = it->ctx->stream;
+    if (output_buffer == HX_OUTPUT_FINAL) {
+        const bool kahan = it->desc.policy.accumulation == HX_ACCUM_KAHAN;
+        k_resolve<<<it->grid_gen, kGenThreads, 0, st>>>(it->acc, it->count_map, n, kahan ? 1u : 0u, it->resolved);
+        HX_CUDA(cudaGetLastError());
+    }
+    // the view goes to the flattened-hits staging buffer (sizeof(hx_hit) = 16 B per pixel)
+    float4* out = reinterpret_cast<float4*>(it->hits_host_layout);
+    k_output_view<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, *frame, W, H, output_buffer, it->resolved, out,
+                                                         it->q.status);
+    HX_CUDA(cudaGetLastError());
+    it->stats.kernel_launches++;
+    HX_CUDA(cudaMemcpyAsync(host_rgba32f, out, 16 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    return check_status(it);
 }
 
 extern "C" hx_status hx_integrator_set_timing(hx_integrator* it, uint32_t enabled) {

@@ -97,7 +97,7 @@ __global__ void k_raygen_multi(const TableHeader* hdr, const Chunk* chunks, cons
 // Running-mean accumulation (path_trace_rgen.glsl:217-248) per request pixel,
 // samples of the chunk in order.
 __global__ void k_accumulate_multi(const TableHeader* hdr, const Chunk* chunks, const SlotDev* slots, float clampv,
-                                   const float4* __restrict__ L) {
+                                   uint32_t nan_red, const float4* __restrict__ L) {
     const uint32_t total = hdr->total_acc, nc = hdr->num_chunks;
     for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < total; a += gridDim.x * blockDim.x) {
         const Chunk c = chunks[find_chunk(chunks, nc, a, true)];
@@ -113,6 +113,11 @@ __global__ void k_accumulate_multi(const TableHeader* hdr, const Chunk* chunks, 
             uint32_t frame = c.sample_begin + s;
             float* av = &v.x;
             for (int k = 0; k < 3; ++k) av[k] = frame == 0 ? cc[k] : av[k] + (cc[k] - av[k]) / (float)frame;
+            if (nan_red && (isnan(l.x) || isnan(l.y) || isnan(l.z))) {
+                v.x = 1.0f;
+                v.y = 0.0f;
+                v.z = 0.0f;
+            }
             v.w = 1.0f;
         }
         *dst = v;
@@ -366,7 +371,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
         cudaMemsetAsync(b->q.counters + 2, 0, 4, st);
         k_shade<false><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
     }
-    k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp, b->q.L);
+    k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp,
+                                                         s->desc.policy.visualize_nans ? 1u : 0u, b->q.L);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (ce != cudaSuccess) {
         hx_set_error("server: graph capture failed: %s", cudaGetErrorString(ce));

@@ -507,8 +507,12 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
 
 // Accumulation (path_trace_rgen.glsl:217-248): clamp, then running mean
 // prev + (c - prev) / num_frames with frame 0 stored raw; or Kahan sum.
+// With nan_red, a sample whose radiance has a NaN stores (1, 0, 0) in its
+// pixel in place of the running mean (VISUALIZE_NANS, path_trace_rgen.glsl:
+// 225-244; running mean only).
 __global__ void k_accumulate(Rect rect, uint32_t W, uint32_t frame0, uint32_t nframes, float clampv, uint32_t kahan,
-                             const float4* __restrict__ L, float4* __restrict__ acc, float4* __restrict__ comp) {
+                             uint32_t nan_red, const float4* __restrict__ L, float4* __restrict__ acc,
+                             float4* __restrict__ comp) {
     uint32_t npix = rect.w * rect.h;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
         uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
@@ -532,6 +536,11 @@ __global__ void k_accumulate(Rect rect, uint32_t W, uint32_t frame0, uint32_t nf
                 } else {
                     av[k] = frame == 0 ? c[k] : av[k] + (c[k] - av[k]) / (float)frame;
                 }
+            }
+            if (nan_red && (isnan(l.x) || isnan(l.y) || isnan(l.z))) {
+                a.x = 1.0f;
+                a.y = 0.0f;
+                a.z = 0.0f;
             }
             a.w = 1.0f;
         }

@@ -203,7 +203,10 @@ typedef struct hx_policy {
     uint32_t area_w_one;          /* 1: transform area-light vertices with w = 1            */
     uint32_t env_sampling;        /* HX_ENV_SAMPLE_*                                       */
     uint32_t payload;             /* HX_PAYLOAD_*                                          */
-    uint32_t reserved[3];
+    uint32_t visualize_nans;      /* 1: a sample whose radiance has a NaN stores (1, 0, 0)
+                                     in its pixel (VISUALIZE_NANS, path_trace_rgen.glsl:
+                                     225-244); running-mean accumulation only             */
+    uint32_t reserved[2];
 } hx_policy;
 
 /* Reference-faithful policy (every reference quirk reproduced). */
@@ -408,6 +411,23 @@ HX_API hx_status hx_integrator_tonemap(hx_integrator* integ, uint32_t op, float 
 /* Reads the RGBA32F accumulation image (the ping-pong output image of
  * renderer.cpp:1483-1506) into width*height*4 floats. */
 HX_API hx_status hx_integrator_read_accumulation(hx_integrator* integ, float* host_rgba32f);
+
+/* Output buffers of Renderer::set_current_output_buffer (renderer.h:27-35,
+ * 85) and its debug-visualization pass (renderer.cpp:491-545,
+ * debug_visualization.frag:71-161).  Rendered headless: one camera ray
+ * through each pixel centre, the closest triangle without alpha test (the
+ * raster pass never discards), the fragment shader's value (albedo; normals
+ * * 0.5 + 0.5; roughness; metallic; emissive), misses (0, 0, 0, 1); width *
+ * height RGBA32F in display order, like hx_integrator_tonemap.
+ * HX_OUTPUT_FINAL returns the resolved accumulation in that order. */
+#define HX_OUTPUT_ALBEDO    0u
+#define HX_OUTPUT_NORMALS   1u
+#define HX_OUTPUT_ROUGHNESS 2u
+#define HX_OUTPUT_METALLIC  3u
+#define HX_OUTPUT_EMISSIVE  4u
+#define HX_OUTPUT_FINAL     5u
+HX_API hx_status hx_integrator_render_output(hx_integrator* integ, const hx_frame_desc* frame,
+                                             uint32_t output_buffer, float* host_rgba32f);
 
 /* Device-timed statistics of the last render call (CUDA events on the
  * context stream when timing is on). */

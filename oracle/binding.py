@@ -23,6 +23,7 @@ class Counters(C.Structure):
 _SIGS = {
     "oracle_scene_create": (_P, [_P]),
     "oracle_scene_destroy": (None, [_P]),
+    "oracle_output_view": (None, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
     "oracle_scene_num_prims": (C.c_uint32, [_P]),
     "oracle_scene_num_bvh8_nodes": (C.c_uint32, [_P]),
     "oracle_scene_num_lights": (C.c_uint32, [_P]),
@@ -111,6 +112,12 @@ class OracleScene:
         hits = np.zeros(rays.shape[0], HIT_DTYPE)
         lib().oracle_trace(self.handle, _ptr(rays), rays.shape[0], 1 if any_hit else 0, 1 if brute else 0, _ptr(hits))
         return hits
+
+    def output_view(self, frame, width, height, which):
+        """Output-buffer view (albedo 0 .. emissive 4), (H, W, 4) float32, display row order."""
+        out = np.zeros((height, width, 4), np.float32)
+        lib().oracle_output_view(self.handle, C.byref(frame), width, height, which, _ptr(out))
+        return out
 
     def trace_bvh8(self, rays, any_hit=False):
         """Closest hits through the 8-wide tree in the device arithmetic."""

@@ -1473,6 +1473,75 @@ void oracle_primary_rays(const hx_integrator_desc* d, const hx_frame_desc* f, ui
         }
 }
 
+// Output-buffer views (renderer.cpp:491-545, debug_visualization.vert:54-64,
+// debug_visualization.frag:71-161): a camera ray through each pixel centre,
+// the closest triangle without alpha test, the fragment shader's value;
+// misses (0, 0, 0, 1); display row r = camera row H - 1 - r.  FP32, the
+// device's operation order.  which: 0 albedo, 1 normals, 2 roughness,
+// 3 metallic, 4 emissive.
+void oracle_output_view(void* h, const hx_frame_desc* f, uint32_t W, uint32_t H, uint32_t which, float* out) {
+    Scene* s = (Scene*)h;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long row = 0; row < (long)H; ++row) {
+        const uint32_t y = H - 1 - (uint32_t)row;
+        for (uint32_t x = 0; x < W; ++x) {
+            float* o = &out[4 * ((size_t)row * W + x)];
+            const float tx = ((float)x + 0.5f) / (float)W, ty = ((float)y + 0.5f) / (float)H;
+            const float nx = tx * 2.0f - 1.0f, ny = ty * 2.0f - 1.0f;
+            float tg[4];
+            mat4_mul(f->view_proj_inverse, nx, ny, 0.0f, 1.0f, tg);
+            const V3<float> target(tg[0] / tg[3], tg[1] / tg[3], tg[2] / tg[3]);
+            const V3<float> cam = fv3<float>(f->camera_pos);
+            const V3<float> d = normalize(target - cam);
+            float t, u, v;
+            uint32_t prim;
+            o[0] = o[1] = o[2] = 0.0f;
+            o[3] = 1.0f;
+            if (!trace<float>(*s, cam, d, 0.001f, 10000.0f, false, false, false, t, u, v, prim)) continue;
+            const PrimInfo& pi = s->prims[prim];
+            const hx_instance& inst = s->instances[pi.instance];
+            const uint32_t mesh = inst.mesh_index;
+            const hx_vertex& a = mesh_vertex<float>(*s, mesh, pi.mesh_prim, 0);
+            const hx_vertex& b = mesh_vertex<float>(*s, mesh, pi.mesh_prim, 1);
+            const hx_vertex& c = mesh_vertex<float>(*s, mesh, pi.mesh_prim, 2);
+            const float b0 = 1.0f - u - v, b1 = u, b2 = v;
+            const float tu = a.tex_coord[0] * b0 + b.tex_coord[0] * b1 + c.tex_coord[0] * b2;
+            const float tv = a.tex_coord[1] * b0 + b.tex_coord[1] * b1 + c.tex_coord[1] * b2;
+            const hx_material& m = s->materials[pi.material];
+            V3<float> r(0.0f, 0.0f, 0.0f);
+            auto rgb = [&](int tex) {
+                const Tex& tt = s->textures[tex];
+                return V3<float>(tex_bilinear<float>(tt, tu, tv, 0), tex_bilinear<float>(tt, tu, tv, 1),
+                                 tex_bilinear<float>(tt, tu, tv, 2));
+            };
+            if (which == 0) {
+                r = m.texture_indices0[0] == -1 ? V3<float>(m.albedo[0], m.albedo[1], m.albedo[2]) : rgb(m.texture_indices0[0]);
+            } else if (which == 1) {
+                const float* N = inst.normal_matrix;
+                const V3<float> na = normalize(mat3_mul(N, V3<float>(a.normal[0], a.normal[1], a.normal[2])));
+                const V3<float> nb = normalize(mat3_mul(N, V3<float>(b.normal[0], b.normal[1], b.normal[2])));
+                const V3<float> nc = normalize(mat3_mul(N, V3<float>(c.normal[0], c.normal[1], c.normal[2])));
+                const V3<float> nn(na.x * b0 + nb.x * b1 + nc.x * b2, na.y * b0 + nb.y * b1 + nc.y * b2,
+                                   na.z * b0 + nb.z * b1 + nc.z * b2);
+                r = nn * 0.5f + V3<float>(0.5f);
+            } else if (which == 2) {
+                r = V3<float>(m.texture_indices0[2] == -1
+                                  ? m.roughness_metallic[0]
+                                  : tex_bilinear<float>(s->textures[m.texture_indices0[2]], tu, tv, m.texture_indices1[2]));
+            } else if (which == 3) {
+                r = V3<float>(m.texture_indices0[3] == -1
+                                  ? m.roughness_metallic[1]
+                                  : tex_bilinear<float>(s->textures[m.texture_indices0[3]], tu, tv, m.texture_indices1[3]));
+            } else {
+                r = m.texture_indices1[0] == -1 ? V3<float>(m.emissive[0], m.emissive[1], m.emissive[2]) : rgb(m.texture_indices1[0]);
+            }
+            o[0] = r.x;
+            o[1] = r.y;
+            o[2] = r.z;
+        }
+    }
+}
+
 // Per-sample radiance L (before the clamp) of frame `frame` for the listed
 // pixels (pixel = y*width + x; NULL = all), precision 32 or 64.
 void oracle_sample_radiance(void* h, const hx_integrator_desc* d, const hx_frame_desc* f, uint32_t frame, uint32_t precision,
@@ -1542,6 +1611,11 @@ void oracle_render(void* h, const hx_integrator_desc* d, const hx_frame_desc* f,
                             acc[ch] = tk;
                         } else acc[ch] = fr == 0 ? v : acc[ch] + (v - acc[ch]) / (double)fr;
                     }
+                    // VISUALIZE_NANS (path_trace_rgen.glsl:225-244)
+                    if (d->policy.visualize_nans && (std::isnan(L.x) || std::isnan(L.y) || std::isnan(L.z))) {
+                        acc[0] = 1.0;
+                        acc[1] = acc[2] = 0.0;
+                    }
                 } else {
                     V3<float> L = trace_path<float>(*s, P, *f, x, y, fr, c, nullptr);
                     for (int ch = 0; ch < 3; ++ch) {
@@ -1552,6 +1626,10 @@ void oracle_render(void* h, const hx_integrator_desc* d, const hx_frame_desc* f,
                             compf[ch] = (tk - accf[ch]) - yk;
                             accf[ch] = tk;
                         } else accf[ch] = fr == 0 ? v : accf[ch] + (v - accf[ch]) / (float)fr;
+                    }
+                    if (d->policy.visualize_nans && (std::isnan(L.x) || std::isnan(L.y) || std::isnan(L.z))) {
+                        accf[0] = 1.0f;
+                        accf[1] = accf[2] = 0.0f;
                     }
                 }
             }
