@@ -206,6 +206,8 @@ _SIGS = {
     "hx_integrator_tonemap": (C.c_int, [_P, C.c_uint32, C.c_float, _P]),
     "hx_integrator_read_accumulation": (C.c_int, [_P, _P]),
     "hx_integrator_render_output": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
+    "hx_integrator_gather_debug_rays": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, C.c_uint32, C.c_uint32, _P,
+                                                  C.c_uint32, C.POINTER(C.c_uint32)]),
     "hx_integrator_set_timing": (C.c_int, [_P, C.c_uint32]),
     "hx_integrator_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "hx_integrator_set_counting": (C.c_int, [_P, C.c_uint32]),
@@ -558,6 +560,16 @@ class PathIntegrator:
         out = np.zeros((self.height, self.width, 4), np.float32)
         check(lib().hx_integrator_render_output(self.handle, C.byref(frame), output_buffer, _ptr(out)))
         return out
+
+    def gather_debug_rays(self, frame, pixel_x, pixel_y, num_debug_rays):
+        """Ray-debug segments through a display pixel: (V, 8) float32 vertices
+        (position xyz1, colour rgb1), two per segment, in shading order."""
+        cap = 2 * num_debug_rays * max(1, self.desc.max_ray_bounces)
+        out = np.zeros((cap, 8), np.float32)
+        n = C.c_uint32()
+        check(lib().hx_integrator_gather_debug_rays(self.handle, C.byref(frame), pixel_x, pixel_y, num_debug_rays,
+                                                    _ptr(out), cap, C.byref(n)))
+        return out[:n.value]
 
     def tonemap(self, op=TONEMAP_ACES, exposure=1.0, to_host=True):
         out = np.zeros((self.height, self.width, 4), np.uint8) if to_host else None

@@ -245,8 +245,14 @@ struct StageTimer {
 
 // Traces nframes frames of the rect through all bounces; leaves per-path
 // radiance in q.L.  With accumulate, folds them into the image.
+// Ray-debug launch (gather_debug_rays): n paths through one pixel, segments
+// recorded by k_shade<false, true> into q's debug buffers; no accumulation.
+struct DebugLaunch {
+    uint32_t px, py, n;
+};
+
 static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect rect, uint32_t frame0, uint32_t nframes,
-                               bool accumulate) {
+                               bool accumulate, const DebugLaunch* dbg = nullptr) {
     hx_context* ctx = it->ctx;
     cudaStream_t st = ctx->stream;
     const DevScene& s = it->scene->d;
@@ -257,7 +263,10 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
     it->stats.paths += total;
     {
         StageTimer t(it, &it->stats.ms_raygen);
-        if (fp16)
+        if (dbg)
+            k_raygen_debug<<<it->grid_gen, kGenThreads, 0, st>>>(f, dbg->px, dbg->py, it->desc.width, it->desc.height, dbg->n,
+                                                                 frame0, P.rng, it->q);
+        else if (fp16)
             k_raygen<true><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, 0, total, P.rng, it->q);
         else
             k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, 0, total, P.rng, it->q);
@@ -308,7 +317,10 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             HX_CUDA(cudaMemsetAsync(it->q.counters + 2, 0, 4, st));
             {
                 StageTimer t(it, &it->stats.ms_shade);
-                if (fp16)
+                if (dbg)
+                    k_shade<false, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces,
+                                                                                   it->desc.shadow_ray_bias, cur, it->q);
+                else if (fp16)
                     k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
                 else
                     k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
@@ -596,6 +608,76 @@ extern "C" hx_status hx_integrator_render_output(hx_integrator* it, const hx_fra
     it->stats.kernel_launches++;
     HX_CUDA(cudaMemcpyAsync(host_rgba32f, out, 16 * (size_t)n, cudaMemcpyDeviceToHost, st));
     return check_status(it);
+}
+
+// PathIntegrator::gather_debug_rays (path_integrator.cpp:88-104) with the
+// RAY_DEBUG_VIEW shaders (path_trace_rgen.glsl:136-147,183-188,
+// path_trace_rchit.glsl:548-567): num_debug_rays paths through the pixel
+// (pixel_x, pixel_y) given in display coordinates (the launch row is
+// height - pixel_y, path_integrator.cpp:146), seeded with the accumulated
+// sample count like a frame; every hit of a ray after the camera ray adds a
+// segment (two vertices: position, colour).  Segments appear in shading
+// order.  *count receives the number of vertices recorded (capped at
+// 2 * num_debug_rays * max_ray_bounces); at most capacity are copied out.
+extern "C" hx_status hx_integrator_gather_debug_rays(hx_integrator* it, const hx_frame_desc* frame, uint32_t pixel_x,
+                                                     uint32_t pixel_y, uint32_t num_debug_rays,
+                                                     hx_debug_ray_vertex* host_vertices, uint32_t capacity, uint32_t* count) {
+    HX_CHECK_ARG(it && frame && count && (host_vertices || capacity == 0), "hx_integrator_gather_debug_rays: null argument");
+    HX_CHECK_ARG(num_debug_rays >= 1 && num_debug_rays <= it->capacity,
+                 "hx_integrator_gather_debug_rays: %u rays (1..%u, the wavefront capacity)", num_debug_rays, it->capacity);
+    HX_CHECK_ARG(pixel_x < it->desc.width && pixel_y < it->desc.height,
+                 "hx_integrator_gather_debug_rays: pixel (%u, %u) outside %u x %u", pixel_x, pixel_y, it->desc.width,
+                 it->desc.height);
+    if (it->desc.policy.payload != HX_PAYLOAD_FP32) {
+        hx_set_error("hx_integrator_gather_debug_rays: needs FP32 payloads (16-bit hit records carry no distance)");
+        return HX_ERR_UNSUPPORTED;
+    }
+    const uint64_t max_vertices = 2ull * num_debug_rays * std::max<uint32_t>(1, it->desc.max_ray_bounces);
+    HX_CHECK_ARG(max_vertices <= 0xffffffffull, "hx_integrator_gather_debug_rays: too many rays");
+    cudaStream_t st = it->ctx->stream;
+    float4 *color = nullptr, *verts = nullptr;
+    uint32_t* cnt = nullptr;
+    hx_status rs = hx_alloc_t(it->ctx, &color, num_debug_rays);
+    if (rs == HX_OK) rs = hx_alloc_t(it->ctx, &verts, 2 * (size_t)max_vertices);
+    if (rs == HX_OK) rs = hx_alloc_t(it->ctx, &cnt, 1);
+    if (rs == HX_OK) {
+        it->q.dbg_color = color;
+        it->q.dbg_verts = verts;
+        it->q.dbg_count = cnt;
+        it->q.dbg_capacity = (uint32_t)max_vertices;
+        cudaError_t e = cudaMemsetAsync(cnt, 0, 4, st);
+        if (e != cudaSuccess) {
+            hx_set_error("hx_integrator_gather_debug_rays: %s", cudaGetErrorString(e));
+            rs = HX_ERR_DEVICE;
+        }
+        const DebugLaunch dl{pixel_x, it->desc.height - pixel_y, num_debug_rays};
+        const Rect r{0, 0, num_debug_rays, 1};
+        if (rs == HX_OK) rs = run_wavefront(it, *frame, r, it->accumulated, 1, false, &dl);
+        uint32_t n = 0;
+        if (rs == HX_OK && cudaMemcpyAsync(&n, cnt, 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+            cudaStreamSynchronize(st) == cudaSuccess) {
+            n = std::min<uint32_t>(n, (uint32_t)max_vertices);
+            *count = n;
+            const uint32_t m = std::min(n, capacity);
+            if (m && cudaMemcpyAsync(host_vertices, verts, 32 * (size_t)m, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+                hx_set_error("hx_integrator_gather_debug_rays: copy failed");
+                rs = HX_ERR_DEVICE;
+            }
+        } else if (rs == HX_OK) {
+            hx_set_error("hx_integrator_gather_debug_rays: %s", cudaGetErrorString(cudaGetLastError()));
+            rs = HX_ERR_DEVICE;
+        }
+        if (rs == HX_OK) rs = check_status(it);
+        it->q.dbg_color = nullptr;
+        it->q.dbg_verts = nullptr;
+        it->q.dbg_count = nullptr;
+        it->q.dbg_capacity = 0;
+    }
+    cudaStreamSynchronize(st);
+    if (color) hx_free(it->ctx, color);
+    if (verts) hx_free(it->ctx, verts);
+    if (cnt) hx_free(it->ctx, cnt);
+    return rs;
 }
 
 extern "C" hx_status hx_integrator_set_timing(hx_integrator* it, uint32_t enabled) {

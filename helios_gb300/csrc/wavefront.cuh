@@ -38,6 +38,12 @@ struct Queues {
     uint32_t* counters; // [0],[1] ray queues, [2] shadow queue, [4],[5] trace / shadow fetch cursors
     unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2..8] counting mode (k_extend)
     uint32_t* status;   // bit 0: traversal stack overflow
+    // ray-debug capture (k_raygen_debug, k_shade<_, true>): per-path segment
+    // colour, recorded vertices (position, colour: two float4 each), their count
+    float4* dbg_color = nullptr;
+    float4* dbg_verts = nullptr;
+    uint32_t* dbg_count = nullptr;
+    uint32_t dbg_capacity = 0;  // vertices
 };
 
 struct Rect {
@@ -134,7 +140,45 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
     }
 }
 
-template <bool FP16>
+// Camera rays of the ray-debug view (RAY_DEBUG_VIEW, path_trace_rgen.glsl:
+// 136-147, 183-188; PathIntegrator::gather_debug_rays, path_integrator.cpp:
+// 88-104): n paths all through pixel (px, py) of the W x H frame, path k
+// seeded as launch (k, 0) of an n x 1 launch; three draws give the path's
+// segment colour (each * 0.5 + 0.5) before the camera ray's own draws.  FP32
+// payloads.
+__global__ void k_raygen_debug(hx_frame_desc f, uint32_t px, uint32_t py, uint32_t W, uint32_t H, uint32_t n,
+                               uint32_t frame, uint32_t kind, Queues q) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        Rng rng = rng_init(kind, k, 0, n, frame);
+        const float cr = next_float(kind, rng) * 0.5f + 0.5f;
+        const float cg = next_float(kind, rng) * 0.5f + 0.5f;
+        const float cb = next_float(kind, rng) * 0.5f + 0.5f;
+        V3 o, d;
+        generate_ray(f, kind, px, py, W, H, rng, o, d);
+        q.T[k] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+        q.L[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        q.rng[k] = make_uint2(rng.s0, rng.s1);
+        q.o[0][k] = make_float4(o.x, o.y, o.z, 0.001f);
+        q.d[0][k] = make_float4(d.x, d.y, d.z, 10000.0f);
+        float4 r0, r1;
+        ray_record(d, 10000.0f, true, r0, r1);
+        q.r0[0][k] = r0;
+        q.r1[0][k] = r1;
+        q.p[0][k] = k | kAnyHitFlag;
+        q.dbg_color[k] = make_float4(cr, cg, cb, 1.0f);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        q.counters[0] = n;
+        q.counters[1] = 0;
+        q.counters[2] = 0;
+    }
+}
+
+// DEBUG: also records each hit of a ray after the camera ray as a segment
+// (ray origin, hit point; the path's colour) in q.dbg_verts
+// (path_trace_rchit.glsl:548-567); the order of segments is the order their
+// hits are shaded.
+template <bool FP16, bool DEBUG = false>
 __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevScene s, Policy P, uint32_t max_bounces, float bias, int cur,
                                                          Queues q) {
     const uint32_t n = q.counters[cur];
@@ -180,6 +224,18 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevSce
                 L = L + (depth == 0 ? e : T * e);
                 q.L[path] = make_float4(L.x, L.y, L.z, 0.0f);
             } else {
+                if (DEBUG && depth > 0) {
+                    const float4 o4 = q.o[cur][i];
+                    const float t = h.x;
+                    const float4 c = q.dbg_color[path];
+                    const uint32_t v = atomicAdd(q.dbg_count, 2u);
+                    if (v + 2u <= q.dbg_capacity) {
+                        q.dbg_verts[2 * (size_t)v] = make_float4(o4.x, o4.y, o4.z, 1.0f);
+                        q.dbg_verts[2 * (size_t)v + 1] = c;
+                        q.dbg_verts[2 * (size_t)v + 2] = make_float4(o4.x + d.x * t, o4.y + d.y * t, o4.z + d.z * t, 1.0f);
+                        q.dbg_verts[2 * (size_t)v + 3] = c;
+                    }
+                }
                 Surface p = populate(s, prim, h.z, h.w);
                 if (depth == 0 && !is_black(p.emissive)) L = L + p.emissive;
                 V3 Wo = -d;

@@ -12,6 +12,7 @@
 
 #include "hx.h"
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <memory>
@@ -93,6 +94,17 @@ public:
     void set_shadow_ray_bias(const float& b) { hx_check(hx_integrator_set_shadow_ray_bias(m_it, b)); }
     void set_tiled(bool tiled) { hx_check(hx_integrator_set_tiled(m_it, tiled ? 1u : 0u)); }
     void render(const hx_frame_desc& frame) { hx_check(hx_integrator_render(m_it, &frame)); }
+    // Segments of num_debug_rays paths through a display pixel
+    // (path_integrator.h:35), two vertices per segment.
+    std::vector<hx_debug_ray_vertex> gather_debug_rays(const hx_frame_desc& frame, uint32_t pixel_x, uint32_t pixel_y,
+                                                       uint32_t num_debug_rays, uint32_t max_ray_bounces) {
+        std::vector<hx_debug_ray_vertex> v((size_t)2 * num_debug_rays * (max_ray_bounces ? max_ray_bounces : 1));
+        uint32_t n = 0;
+        hx_check(hx_integrator_gather_debug_rays(m_it, &frame, pixel_x, pixel_y, num_debug_rays, v.data(),
+                                                 (uint32_t)v.size(), &n));
+        v.resize(std::min<size_t>(n, v.size()));
+        return v;
+    }
     void render(const hx_camera& camera, uint32_t width, uint32_t height) {
         hx_frame_desc f;
         hx_check(hx_camera_to_frame_desc(&camera, width, height, &f));
@@ -112,6 +124,15 @@ private:
 };
 
 enum ToneMapOperator { TONE_MAP_OPERATOR_ACES = HX_TONEMAP_ACES, TONE_MAP_OPERATOR_REINHARD = HX_TONEMAP_REINHARD };
+// renderer.h:27-35
+enum OutputBuffer {
+    OUTPUT_BUFFER_ALBEDO = HX_OUTPUT_ALBEDO,
+    OUTPUT_BUFFER_NORMALS = HX_OUTPUT_NORMALS,
+    OUTPUT_BUFFER_ROUGHNESS = HX_OUTPUT_ROUGHNESS,
+    OUTPUT_BUFFER_METALLIC = HX_OUTPUT_METALLIC,
+    OUTPUT_BUFFER_EMISSIVE = HX_OUTPUT_EMISSIVE,
+    OUTPUT_BUFFER_FINAL = HX_OUTPUT_FINAL
+};
 
 // The render / tone-map / save part of helios::Renderer (renderer.h:83-97).
 class Renderer {
@@ -119,6 +140,15 @@ public:
     explicit Renderer(PathIntegrator::Ptr integrator) : m_integrator(std::move(integrator)) {}
     void set_tone_map_operator(ToneMapOperator op) { m_op = op; }
     void set_exposure(float e) { m_exposure = e; }
+    void set_current_output_buffer(OutputBuffer b) { m_output = b; }
+    OutputBuffer current_output_buffer() const { return m_output; }
+    // The current output buffer as RGBA32F in display order: a debug view, or
+    // for OUTPUT_BUFFER_FINAL the accumulated radiance (renderer.cpp:329-333).
+    std::vector<float> read_output(const hx_frame_desc& frame, uint32_t width, uint32_t height) {
+        std::vector<float> px((size_t)width * height * 4);
+        hx_check(hx_integrator_render_output(m_integrator->handle(), &frame, (uint32_t)m_output, px.data()));
+        return px;
+    }
     void render(const hx_frame_desc& frame) {
         m_integrator->render(frame);
         hx_check(hx_integrator_tonemap(m_integrator->handle(), (uint32_t)m_op, m_exposure, nullptr));
@@ -138,6 +168,7 @@ public:
 private:
     PathIntegrator::Ptr m_integrator;
     ToneMapOperator m_op = TONE_MAP_OPERATOR_ACES;
+    OutputBuffer m_output = OUTPUT_BUFFER_FINAL;
     float m_exposure = 1.0f;
 };
 

@@ -429,6 +429,26 @@ HX_API hx_status hx_integrator_read_accumulation(hx_integrator* integ, float* ho
 HX_API hx_status hx_integrator_render_output(hx_integrator* integ, const hx_frame_desc* frame,
                                              uint32_t output_buffer, float* host_rgba32f);
 
+/* Ray-debug capture: PathIntegrator::gather_debug_rays
+ * (include/gfx/path_integrator.h:35, path_integrator.cpp:88-104) with the
+ * RAY_DEBUG_VIEW shaders (path_trace_rgen.glsl:136-147,183-188,
+ * path_trace_rchit.glsl:548-567).  Traces num_debug_rays paths through
+ * display pixel (pixel_x, pixel_y) (launch row height - pixel_y, as
+ * path_integrator.cpp:146), each with its own colour (three draws, each
+ * * 0.5 + 0.5); every closest hit after the camera ray records a line
+ * segment: ray origin and hit point, two DebugRayVertex records
+ * (common.glsl:54-58).  Nothing is accumulated.  *count = vertices recorded;
+ * at most capacity are copied to host_vertices.  FP32 payloads only
+ * (HX_ERR_UNSUPPORTED otherwise). */
+typedef struct hx_debug_ray_vertex {
+    float position[4]; /* xyz, 1 */
+    float color[4];    /* rgb, 1 */
+} hx_debug_ray_vertex;
+HX_API hx_status hx_integrator_gather_debug_rays(hx_integrator* integ, const hx_frame_desc* frame, uint32_t pixel_x,
+                                                 uint32_t pixel_y, uint32_t num_debug_rays,
+                                                 hx_debug_ray_vertex* host_vertices, uint32_t capacity,
+                                                 uint32_t* count);
+
 /* Device-timed statistics of the last render call (CUDA events on the
  * context stream when timing is on). */
 HX_API hx_status hx_integrator_set_timing(hx_integrator* integ, uint32_t enabled);

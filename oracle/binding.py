@@ -24,6 +24,7 @@ _SIGS = {
     "oracle_scene_create": (_P, [_P]),
     "oracle_scene_destroy": (None, [_P]),
     "oracle_output_view": (None, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
+    "oracle_debug_rays": (C.c_uint32, [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, C.c_uint32]),
     "oracle_scene_num_prims": (C.c_uint32, [_P]),
     "oracle_scene_num_bvh8_nodes": (C.c_uint32, [_P]),
     "oracle_scene_num_lights": (C.c_uint32, [_P]),
@@ -118,6 +119,14 @@ class OracleScene:
         out = np.zeros((height, width, 4), np.float32)
         lib().oracle_output_view(self.handle, C.byref(frame), width, height, which, _ptr(out))
         return out
+
+    def debug_rays(self, idesc, frame, px, py, num_rays, sample_index):
+        """Ray-debug segments: (V, 8) float32 vertices (position xyz1, colour rgb1), paths in order."""
+        cap = 2 * num_rays * max(1, idesc.max_ray_bounces)
+        out = np.zeros((cap, 8), np.float32)
+        n = lib().oracle_debug_rays(self.handle, C.byref(idesc), C.byref(frame), px, py, num_rays, sample_index,
+                                    _ptr(out), cap)
+        return out[:n]
 
     def trace_bvh8(self, rays, any_hit=False):
         """Closest hits through the 8-wide tree in the device arithmetic."""

@@ -1240,10 +1240,23 @@ static float payload_bary(float x) { return half_to_float(float_to_half(x)); }
 // One camera sample: ray-gen + the closest-hit recursion unrolled into a
 // loop (the payload recursion of path_trace_rchit.glsl:487-536 sums L in the
 // same order: emission, direct light, then the deeper bounces).
+// Ray-debug launch (RAY_DEBUG_VIEW): the path is launch (ray, 0) of a
+// num_rays x 1 launch through pixel (x, y); its colour takes three draws
+// first (path_trace_rgen.glsl:183-188) and every hit after the camera ray
+// appends a segment (origin, hit point) with that colour
+// (path_trace_rchit.glsl:548-567).
+struct DebugPath {
+    uint32_t ray, num_rays;
+    std::vector<float>* verts;  // 8 floats per vertex: position xyz1, colour rgb1
+};
+
 template <typename R>
 static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f, uint32_t x, uint32_t y, uint32_t frame,
-                        Counters& cnt, hx_hit* primary) {
-    RNG rng = rng_init(P.pol.rng, x, y, P.width, frame);
+                        Counters& cnt, hx_hit* primary, const DebugPath* dbg = nullptr) {
+    RNG rng = dbg ? rng_init(P.pol.rng, dbg->ray, 0, dbg->num_rays, frame) : rng_init(P.pol.rng, x, y, P.width, frame);
+    float dcol[3] = {0.0f, 0.0f, 0.0f};
+    if (dbg)
+        for (int k = 0; k < 3; ++k) dcol[k] = next_float(rng) * 0.5f + 0.5f;
     V3<R> L(R(0)), T(R(1));
     uint32_t depth = 0;
     V3<R> o, d;
@@ -1269,6 +1282,12 @@ static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f,
             V3<R> e = env_lookup(s, d);
             L = L + (depth == 0 ? e : T * e);
             break;
+        }
+        if (dbg && depth > 0) {
+            const float seg[16] = {(float)o.x, (float)o.y, (float)o.z, 1.0f, dcol[0], dcol[1], dcol[2], 1.0f,
+                                   (float)(o.x + d.x * t), (float)(o.y + d.y * t), (float)(o.z + d.z * t), 1.0f,
+                                   dcol[0], dcol[1], dcol[2], 1.0f};
+            dbg->verts->insert(dbg->verts->end(), seg, seg + 16);
         }
         float su = (float)hu, sv = (float)hv;
         if (fp16) {
@@ -1540,6 +1559,25 @@ void oracle_output_view(void* h, const hx_frame_desc* f, uint32_t W, uint32_t H,
             o[2] = r.z;
         }
     }
+}
+
+// Ray-debug capture (gather_debug_rays, path_integrator.cpp:88-104): the
+// segments of num_rays FP32 paths through display pixel (px, py) (launch row
+// height - py), seeded with sample index `frame`; out gets 8 floats per
+// vertex, paths in order; returns the vertex count (at most capacity copied).
+uint32_t oracle_debug_rays(void* h, const hx_integrator_desc* d, const hx_frame_desc* f, uint32_t px, uint32_t py,
+                           uint32_t num_rays, uint32_t frame, float* out, uint32_t capacity) {
+    Scene* s = (Scene*)h;
+    Params P = make_params(*d, (uint32_t)s->lights.size());
+    std::vector<float> verts;
+    Counters c;
+    for (uint32_t k = 0; k < num_rays; ++k) {
+        DebugPath dp{k, num_rays, &verts};
+        trace_path<float>(*s, P, *f, px, d->height - py, frame, c, nullptr, &dp);
+    }
+    const uint32_t n = (uint32_t)(verts.size() / 8);
+    std::memcpy(out, verts.data(), 32 * (size_t)std::min(n, capacity));
+    return n;
 }
 
 // Per-sample radiance L (before the clamp) of frame `frame` for the listed

@@ -137,3 +137,55 @@ def test_visualize_nans_marks_nan_samples_red(gpu_ctx):
         hx.PathIntegrator(gpu_ctx, sc, W, H, policy=d.policy)
     assert e.value.status == hx.HX_ERR_INVALID_ARG
     sc.close()
+
+
+def _paths(v):
+    """(V, 8) vertices -> {path colour: (S, 16) segments in bounce order}."""
+    seg = v.reshape(-1, 16)
+    out = {}
+    for row in seg:
+        out.setdefault(tuple(row[4:7].tolist()), []).append(row)
+    return {k: np.array(r) for k, r in out.items()}
+
+
+@pytest.mark.parametrize("policy", ["reference", "spec"])
+def test_gather_debug_rays_matches_oracle(gpu_ctx, scene, policy):
+    """Ray-debug capture (gather_debug_rays / RAY_DEBUG_VIEW): the same
+    segments as the oracle's paths through the same pixel — origins, hit
+    points and per-path colours — after the camera ray."""
+    from tests.helpers import integrator_desc
+    kind, hs, sc, osc = scene
+    W, H = 64, 48
+    f = hx.frame_desc(hs.camera(), W, H)
+    d = integrator_desc(W, H, bounces=5, policy=policy)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=5, policy=d.policy)
+    # a display pixel whose camera rays hit geometry (display row r is launch
+    # row H - 1 - r; the capture's pixel row py is launch row H - py)
+    alb = it.render_output(f, hx.OUTPUT_ALBEDO)
+    hit = np.argwhere(np.any(alb[:-1, :, :3] != 0.0, axis=-1))
+    r, x = hit[len(hit) // 2]
+    it.render(f, 2)  # the capture is seeded with the accumulated sample count
+    total = 0
+    for px, py in ((int(x), int(r) + 1), (W // 2, H // 2), (5, 40)):
+        g = it.gather_debug_rays(f, px, py, 256)
+        o = osc.debug_rays(d, f, px, py, 256, 2)
+        assert g.shape == o.shape and g.shape[0] % 2 == 0
+        total += g.shape[0]
+        if g.shape[0] == 0:
+            continue
+        assert np.all(g[:, 3] == 1.0) and np.all(g[:, 7] == 1.0)
+        assert np.all((g[:, 4:7] >= 0.5) & (g[:, 4:7] < 1.0))
+        gp, op = _paths(g), _paths(o)
+        assert gp.keys() == op.keys()
+        bad = [(k, gp[k].shape[0], op[k].shape[0], float(np.max(np.abs(gp[k] - op[k]))) if gp[k].shape == op[k].shape else -1.0)
+               for k in op if gp[k].shape != op[k].shape or np.max(np.abs(gp[k] - op[k])) > 1e-4]
+        assert not bad, "%d of %d paths differ, e.g. %s; first device / oracle segments %s / %s" % (
+            len(bad), len(op), bad[:4], gp[bad[0][0]][:2].tolist(), op[bad[0][0]][:2].tolist())
+    assert total > 0
+    # the accumulation is untouched
+    before = it.read_accumulation()
+    it.gather_debug_rays(f, 3, 3, 64)
+    assert np.array_equal(before, it.read_accumulation())
+    with pytest.raises(hx.HxError):
+        it.gather_debug_rays(f, W, 0, 16)
+    it.close()
