@@ -71,7 +71,8 @@ class Instance(C.Structure):
 
 
 class TextureDesc(C.Structure):
-    _fields_ = [("rgba8", C.POINTER(C.c_uint8)), ("width", C.c_uint32), ("height", C.c_uint32)]
+    _fields_ = [("rgba8", C.POINTER(C.c_uint8)), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("srgb", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class EnvironmentDesc(C.Structure):

@@ -111,11 +111,13 @@ struct DevScene {
     const uint4* prim_info;      // per flattened prim: instance, global tri, material, flags
     const uint32_t* indices;     // global index buffer (absolute vertex ids)
     const float4* vtx;           // 2 per vertex: pos.xyz|u, normal.xyz|v
+    const float4* vtx_tb;        // 2 per vertex: tangent.xyz|0, bitangent.xyz|0 (only with normal maps)
+    const float* srgb_lut;       // 256 entries: sRGB byte -> linear (texture flag bit 0 of tex_desc.w)
     const float* vtx_w;          // position.w per vertex
     const DevInstance* inst;
     const hx_material* materials;
     const hx_light* lights;
-    const uint4* tex_desc;       // per texture: texel offset, width, height, 0
+    const uint4* tex_desc;       // per texture: texel offset, width, height, flags (bit 0: sRGB)
     const uint32_t* texels;      // RGBA8 packed
     const uint8_t* alpha8;       // alpha channel of every texture (same texel offsets): the any-hit test's working set
     const float4* alpha_uv;      // 2 per flattened prim: (u0,v0,u1,v1), (u2,v2,tex,0)

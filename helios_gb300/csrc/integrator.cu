@@ -563,10 +563,25 @@ __global__ void k_output_view(DevScene s, hx_frame_desc f, uint32_t W, uint32_t 
                 v = mt.texture_indices0[0] == -1 ? v3(mt.albedo[0], mt.albedo[1], mt.albedo[2])
                                                  : tex_bilinear_rgb(s, (uint32_t)mt.texture_indices0[0], tu, tv);
             } else if (which == HX_OUTPUT_NORMALS) {
-                const V3 a = normalize(mat3_mul(inst.normal, v3(n0.x, n0.y, n0.z)));
-                const V3 b = normalize(mat3_mul(inst.normal, v3(n1.x, n1.y, n1.z)));
-                const V3 e = normalize(mat3_mul(inst.normal, v3(n2.x, n2.y, n2.z)));
-                const V3 nn = v3(a.x * b0 + b.x * b1 + e.x * b2, a.y * b0 + b.y * b1 + e.y * b2, a.z * b0 + b.z * b1 + e.z * b2);
+                // FS_IN_* = interpolated normalize(mat3(normal_matrix) x) per vertex
+                auto lerp_n = [&](V3 x0, V3 x1, V3 x2) {
+                    const V3 a = normalize(mat3_mul(inst.normal, x0)), b = normalize(mat3_mul(inst.normal, x1)),
+                             e = normalize(mat3_mul(inst.normal, x2));
+                    return v3(a.x * b0 + b.x * b1 + e.x * b2, a.y * b0 + b.y * b1 + e.y * b2, a.z * b0 + b.z * b1 + e.z * b2);
+                };
+                V3 nn = lerp_n(v3(n0.x, n0.y, n0.z), v3(n1.x, n1.y, n1.z), v3(n2.x, n2.y, n2.z));
+                if (mt.texture_indices0[1] != -1) {  // debug_visualization.frag:77-90
+                    const float4 ta = s.vtx_tb[2 * (size_t)i0], ba = s.vtx_tb[2 * (size_t)i0 + 1];
+                    const float4 tb = s.vtx_tb[2 * (size_t)i1], bb = s.vtx_tb[2 * (size_t)i1 + 1];
+                    const float4 tc = s.vtx_tb[2 * (size_t)i2], bc = s.vtx_tb[2 * (size_t)i2 + 1];
+                    const V3 T = normalize(lerp_n(v3(ta.x, ta.y, ta.z), v3(tb.x, tb.y, tb.z), v3(tc.x, tc.y, tc.z)));
+                    const V3 B = normalize(lerp_n(v3(ba.x, ba.y, ba.z), v3(bb.x, bb.y, bb.z), v3(bc.x, bc.y, bc.z)));
+                    const V3 N = normalize(nn);
+                    const V3 mp = tex_bilinear_rgb(s, (uint32_t)mt.texture_indices0[1], tu, tv);
+                    const V3 nm = normalize(mp * 2.0f - v3(1.0f));
+                    nn = normalize(v3(T.x * nm.x + B.x * nm.y + N.x * nm.z, T.y * nm.x + B.y * nm.y + N.y * nm.z,
+                                      T.z * nm.x + B.z * nm.y + N.z * nm.z));
+                }
                 v = nn * 0.5f + v3(0.5f);
             } else if (which == HX_OUTPUT_ROUGHNESS) {
                 const float r = mt.texture_indices0[2] == -1

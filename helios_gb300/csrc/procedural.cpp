@@ -353,7 +353,7 @@ hx_status build_icospheres(hx_host_scene* s, const hx_procedural_params& P) {
     for (uint32_t k = 0; k < pool; ++k) {
         s->texels.emplace_back();
         value_noise_mask(rng, P.mask_size, s->texels.back());
-        hx_texture_desc td;
+        hx_texture_desc td{};
         td.rgba8 = nullptr;
         td.width = P.mask_size;
         td.height = P.mask_size;

@@ -231,7 +231,6 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
             HX_CHECK_ARG(mt.texture_indices0[a] < (int32_t)desc->num_textures, "material %u: texture out of range", k);
         }
         HX_CHECK_ARG(mt.texture_indices1[0] < (int32_t)desc->num_textures, "material %u: texture out of range", k);
-        HX_CHECK_ARG(mt.texture_indices0[1] == -1, "material %u: normal maps are not supported", k);
     }
     for (uint32_t t = 0; t < desc->num_textures; ++t)
         HX_CHECK_ARG(desc->textures[t].rgba8 && desc->textures[t].width > 0 && desc->textures[t].height > 0,
@@ -254,7 +253,10 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
         nv += desc->meshes[m].num_vertices;
         ni += desc->meshes[m].num_indices;
     }
+    bool normal_maps = false;
+    for (uint32_t k = 0; k < desc->num_materials; ++k) normal_maps |= desc->materials[k].texture_indices0[1] != -1;
     std::vector<float4> hv(2 * nv);
+    std::vector<float4> htb(normal_maps ? 2 * nv : 0);
     std::vector<float> hw(nv);
     std::vector<uint32_t> hidx(ni);
     for (uint32_t m = 0; m < desc->num_meshes; ++m) {
@@ -264,6 +266,10 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
             hv[2 * (vbase[m] + v)] = make_float4(x.position[0], x.position[1], x.position[2], x.tex_coord[0]);
             hv[2 * (vbase[m] + v) + 1] = make_float4(x.normal[0], x.normal[1], x.normal[2], x.tex_coord[1]);
             hw[vbase[m] + v] = x.position[3];
+            if (normal_maps) {
+                htb[2 * (vbase[m] + v)] = make_float4(x.tangent[0], x.tangent[1], x.tangent[2], 0.0f);
+                htb[2 * (vbase[m] + v) + 1] = make_float4(x.bitangent[0], x.bitangent[1], x.bitangent[2], 0.0f);
+            }
         }
         for (uint32_t i = 0; i < md.num_indices; ++i) hidx[(size_t)tbase[m] * 3 + i] = vbase[m] + md.indices[i];
     }
@@ -343,7 +349,8 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
     std::vector<uint4> htd(desc->num_textures);
     size_t ntexels = 0;
     for (uint32_t t = 0; t < desc->num_textures; ++t) {
-        htd[t] = make_uint4((uint32_t)ntexels, desc->textures[t].width, desc->textures[t].height, 0);
+        htd[t] = make_uint4((uint32_t)ntexels, desc->textures[t].width, desc->textures[t].height,
+                            desc->textures[t].srgb ? 1u : 0u);
         ntexels += (size_t)desc->textures[t].width * desc->textures[t].height;
     }
     HX_CHECK_ARG(ntexels < 0xffffffffull, "textures too large");
@@ -359,7 +366,16 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
     hx_status rc;
 #define UP(field, vec) \
     if ((rc = up((void**)&(field), (vec).data(), (vec).size() * sizeof((vec)[0]))) != HX_OK) return scene_fail(s, rc)
+    // sRGB transfer function per byte (IEC 61966-2-1, as the Vulkan spec
+    // decodes *_SRGB texels): c <= 0.04045 ? c / 12.92 : ((c + 0.055) / 1.055)^2.4
+    std::vector<float> hlut(256);
+    for (uint32_t q = 0; q < 256; ++q) {
+        const double c = q / 255.0;
+        hlut[q] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+    }
     UP(s->d.vtx, hv);
+    UP(s->d.vtx_tb, htb);
+    UP(s->d.srgb_lut, hlut);
     UP(s->d.vtx_w, hw);
     UP(s->d.indices, hidx);
     UP(s->d.inst, hinst);

@@ -104,6 +104,20 @@ HXD Surface populate(const DevScene& s, uint32_t prim, float u, float v) {
     p.position = mat4_mul3(inst.model, pos.x, pos.y, pos.z, 1.0f);
     p.normal = mat3_mul(inst.normal, nrm);
     const hx_material& m = s.materials[pi.z];
+    if (m.texture_indices0[1] != -1) {  // get_normal_from_map, path_trace_rchit.glsl:190-219
+        const float4 ta = __ldg(&s.vtx_tb[2 * (size_t)i0]), ba = __ldg(&s.vtx_tb[2 * (size_t)i0 + 1]);
+        const float4 tb = __ldg(&s.vtx_tb[2 * (size_t)i1]), bb = __ldg(&s.vtx_tb[2 * (size_t)i1 + 1]);
+        const float4 tc = __ldg(&s.vtx_tb[2 * (size_t)i2]), bc = __ldg(&s.vtx_tb[2 * (size_t)i2 + 1]);
+        const V3 tan = normalize(v3(ta.x * b0 + tb.x * b1 + tc.x * b2, ta.y * b0 + tb.y * b1 + tc.y * b2,
+                                    ta.z * b0 + tb.z * b1 + tc.z * b2));
+        const V3 bit = normalize(v3(ba.x * b0 + bb.x * b1 + bc.x * b2, ba.y * b0 + bb.y * b1 + bc.y * b2,
+                                    ba.z * b0 + bb.z * b1 + bc.z * b2));
+        const V3 T = normalize(mat3_mul(inst.normal, tan)), B = normalize(mat3_mul(inst.normal, bit)), N = normalize(p.normal);
+        const V3 mp = tex_bilinear_rgb(s, (uint32_t)m.texture_indices0[1], tu, tv);
+        const V3 nm = normalize(mp * 2.0f - v3(1.0f));
+        p.normal = normalize(v3(T.x * nm.x + B.x * nm.y + N.x * nm.z, T.y * nm.x + B.y * nm.y + N.y * nm.z,
+                                T.z * nm.x + B.z * nm.y + N.z * nm.z));
+    }
     if (m.texture_indices0[0] == -1) p.albedo = v3(m.albedo[0], m.albedo[1], m.albedo[2]);
     else {
         uint32_t t = (uint32_t)m.texture_indices0[0];

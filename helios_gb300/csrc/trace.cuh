@@ -82,8 +82,13 @@ HXD float unorm8(uint32_t q) {
     return __fmaf_rn(e, c, r);
 }
 
+// Texel channel value: q / 255, or for an sRGB texture's RGB the decoded
+// linear value (alpha is never sRGB-encoded).
+HXD float texel_value(const DevScene& s, uint32_t q, bool srgb) { return srgb ? __ldg(s.srgb_lut + q) : unorm8(q); }
+
 // Software bilinear RGBA8 fetch, REPEAT addressing, level 0; channel c.
 // Power-of-two sizes wrap with a mask (the same integers as the modulo).
+// sRGB textures decode texels before filtering, as sampled *_SRGB images do.
 HXD float tex_bilinear(const DevScene& s, uint32_t tex, float u, float v, int c) {
     uint4 td = s.tex_desc[tex];
     int W = (int)td.y, H = (int)td.z;
@@ -104,10 +109,11 @@ HXD float tex_bilinear(const DevScene& s, uint32_t tex, float u, float v, int c)
     }
     const uint32_t* t = s.texels + td.x;
     int sh = 8 * c;
-    float a00 = unorm8((__ldg(t + iy0 * W + ix0) >> sh) & 0xffu);
-    float a10 = unorm8((__ldg(t + iy0 * W + ix1) >> sh) & 0xffu);
-    float a01 = unorm8((__ldg(t + iy1 * W + ix0) >> sh) & 0xffu);
-    float a11 = unorm8((__ldg(t + iy1 * W + ix1) >> sh) & 0xffu);
+    const bool srgb = (td.w & 1u) && c < 3;
+    float a00 = texel_value(s, (__ldg(t + iy0 * W + ix0) >> sh) & 0xffu, srgb);
+    float a10 = texel_value(s, (__ldg(t + iy0 * W + ix1) >> sh) & 0xffu, srgb);
+    float a01 = texel_value(s, (__ldg(t + iy1 * W + ix0) >> sh) & 0xffu, srgb);
+    float a11 = texel_value(s, (__ldg(t + iy1 * W + ix1) >> sh) & 0xffu, srgb);
     float top = a00 + (a10 - a00) * fx;
     float bot = a01 + (a11 - a01) * fx;
     return top + (bot - top) * fy;
@@ -136,12 +142,13 @@ HXD V3 tex_bilinear_rgb(const DevScene& s, uint32_t tex, float u, float v) {
     const uint32_t* t = s.texels + td.x;
     const uint32_t t00 = __ldg(t + iy0 * W + ix0), t10 = __ldg(t + iy0 * W + ix1);
     const uint32_t t01 = __ldg(t + iy1 * W + ix0), t11 = __ldg(t + iy1 * W + ix1);
+    const bool srgb = td.w & 1u;
     float r[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int sh = 8 * c;
-        float a00 = unorm8((t00 >> sh) & 0xffu), a10 = unorm8((t10 >> sh) & 0xffu);
-        float a01 = unorm8((t01 >> sh) & 0xffu), a11 = unorm8((t11 >> sh) & 0xffu);
+        float a00 = texel_value(s, (t00 >> sh) & 0xffu, srgb), a10 = texel_value(s, (t10 >> sh) & 0xffu, srgb);
+        float a01 = texel_value(s, (t01 >> sh) & 0xffu, srgb), a11 = texel_value(s, (t11 >> sh) & 0xffu, srgb);
         float top = a00 + (a10 - a00) * fx;
         float bot = a01 + (a11 - a01) * fx;
         r[c] = top + (bot - top) * fy;

@@ -143,10 +143,17 @@ typedef struct hx_instance {
 
 /* RGBA8 texture, linear UNORM, sampled bilinearly with REPEAT addressing at
  * level 0 (textureLod(...,0) with the trilinear sampler, vk.cpp:3559-3580). */
+/* srgb = 1: the texture's RGB is sRGB-encoded (the reference creates such
+ * textures with *_SRGB formats, resource_manager.cpp:48-67), so samples
+ * decode each texel's RGB with the sRGB transfer function before filtering;
+ * alpha stays linear.  srgb = 0: UNORM.  Normal maps (texture_indices0[1])
+ * use the vertex tangent and bitangent (path_trace_rchit.glsl:190-219). */
 typedef struct hx_texture_desc {
     const uint8_t* rgba8;
     uint32_t       width;
     uint32_t       height;
+    uint32_t       srgb;
+    uint32_t       reserved;
 } hx_texture_desc;
 
 #define HX_ENV_NONE          0u  /* black environment                        */

@@ -47,6 +47,7 @@ struct PrimInfo {
 struct Tex {
     std::vector<uint8_t> rgba;
     uint32_t w = 0, h = 0;
+    bool srgb = false;  // RGB sRGB-encoded (resource_manager.cpp:48-67)
 };
 
 struct Bvh {
@@ -740,6 +741,15 @@ static void build_bvh(Scene& s) {
 // ---------------------------------------------------------------------------
 static inline uint8_t tex_fetch(const Tex& t, long x, long y, int c) { return t.rgba[((size_t)y * t.w + x) * 4 + c]; }
 
+// A texel channel as a value in [0, 1]: q / 255, or for the RGB of an sRGB
+// texture the sRGB transfer function (IEC 61966-2-1, the decode of *_SRGB
+// formats), applied before filtering; in FP32 the exact value rounded once.
+template <typename R> static R texel_value(uint8_t q, bool srgb) {
+    if (!srgb) return R(q) / R(255);
+    const double c = q / 255.0;
+    return R(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+}
+
 // Software bilinear filter, REPEAT addressing, level 0.
 template <typename R> static R tex_bilinear(const Tex& t, R u, R v, int c) {
     R x = u * R(t.w) - R(0.5), y = v * R(t.h) - R(0.5);
@@ -748,8 +758,9 @@ template <typename R> static R tex_bilinear(const Tex& t, R u, R v, int c) {
     long W = t.w, H = t.h;
     long ix0 = (((long)x0 % W) + W) % W, iy0 = (((long)y0 % H) + H) % H;
     long ix1 = (ix0 + 1) % W, iy1 = (iy0 + 1) % H;
-    R a00 = R(tex_fetch(t, ix0, iy0, c)) / R(255), a10 = R(tex_fetch(t, ix1, iy0, c)) / R(255);
-    R a01 = R(tex_fetch(t, ix0, iy1, c)) / R(255), a11 = R(tex_fetch(t, ix1, iy1, c)) / R(255);
+    const bool srgb = t.srgb && c < 3;
+    R a00 = texel_value<R>(tex_fetch(t, ix0, iy0, c), srgb), a10 = texel_value<R>(tex_fetch(t, ix1, iy0, c), srgb);
+    R a01 = texel_value<R>(tex_fetch(t, ix0, iy1, c), srgb), a11 = texel_value<R>(tex_fetch(t, ix1, iy1, c), srgb);
     R top = a00 + (a10 - a00) * fx;
     R bot = a01 + (a11 - a01) * fx;
     return top + (bot - top) * fy;
@@ -1038,6 +1049,16 @@ template <typename R> static Surface<R> populate(const Scene& s, uint32_t prim, 
     p.position = V3<R>(wp[0], wp[1], wp[2]);
     p.normal = mat3_mul(N, nrm);
     const hx_material& m = s.materials[pi.material];
+    if (m.texture_indices0[1] != -1) {  // fetch_normal / get_normal_from_map, rchit.glsl:190-219
+        V3<R> tan = normalize(lerp3(a.tangent, b.tangent, c.tangent));
+        V3<R> bit = normalize(lerp3(a.bitangent, b.bitangent, c.bitangent));
+        V3<R> Tm = normalize(mat3_mul(N, tan)), Bm = normalize(mat3_mul(N, bit)), Nm = normalize(p.normal);
+        const Tex& nt = s.textures[m.texture_indices0[1]];
+        V3<R> mp(tex_bilinear<R>(nt, tu, tv, 0), tex_bilinear<R>(nt, tu, tv, 1), tex_bilinear<R>(nt, tu, tv, 2));
+        V3<R> nm = normalize(mp * R(2) - V3<R>(R(1)));
+        p.normal = normalize(V3<R>(Tm.x * nm.x + Bm.x * nm.y + Nm.x * nm.z, Tm.y * nm.x + Bm.y * nm.y + Nm.y * nm.z,
+                                   Tm.z * nm.x + Bm.z * nm.y + Nm.z * nm.z));
+    }
     if (m.texture_indices0[0] == -1) {
         p.albedo = V3<R>(R(m.albedo[0]), R(m.albedo[1]), R(m.albedo[2]));
         p.albedo_a = R(m.albedo[3]);
@@ -1384,6 +1405,7 @@ void* oracle_scene_create(const hx_scene_desc* d) {
         tx.w = d->textures[t].width;
         tx.h = d->textures[t].height;
         tx.rgba.assign(d->textures[t].rgba8, d->textures[t].rgba8 + (size_t)tx.w * tx.h * 4);
+        tx.srgb = d->textures[t].srgb != 0;
         s->textures.push_back(std::move(tx));
     }
     s->punctual.assign(d->punctual_lights, d->punctual_lights + d->num_punctual_lights);
@@ -1537,11 +1559,24 @@ void oracle_output_view(void* h, const hx_frame_desc* f, uint32_t W, uint32_t H,
                 r = m.texture_indices0[0] == -1 ? V3<float>(m.albedo[0], m.albedo[1], m.albedo[2]) : rgb(m.texture_indices0[0]);
             } else if (which == 1) {
                 const float* N = inst.normal_matrix;
-                const V3<float> na = normalize(mat3_mul(N, V3<float>(a.normal[0], a.normal[1], a.normal[2])));
-                const V3<float> nb = normalize(mat3_mul(N, V3<float>(b.normal[0], b.normal[1], b.normal[2])));
-                const V3<float> nc = normalize(mat3_mul(N, V3<float>(c.normal[0], c.normal[1], c.normal[2])));
-                const V3<float> nn(na.x * b0 + nb.x * b1 + nc.x * b2, na.y * b0 + nb.y * b1 + nc.y * b2,
-                                   na.z * b0 + nb.z * b1 + nc.z * b2);
+                // FS_IN_* = interpolated normalize(mat3(normal_matrix) x) per vertex
+                auto lerp_n = [&](const float* x0, const float* x1, const float* x2) {
+                    const V3<float> na = normalize(mat3_mul(N, V3<float>(x0[0], x0[1], x0[2])));
+                    const V3<float> nb = normalize(mat3_mul(N, V3<float>(x1[0], x1[1], x1[2])));
+                    const V3<float> nc = normalize(mat3_mul(N, V3<float>(x2[0], x2[1], x2[2])));
+                    return V3<float>(na.x * b0 + nb.x * b1 + nc.x * b2, na.y * b0 + nb.y * b1 + nc.y * b2,
+                                     na.z * b0 + nb.z * b1 + nc.z * b2);
+                };
+                V3<float> nn = lerp_n(a.normal, b.normal, c.normal);
+                if (m.texture_indices0[1] != -1) {  // debug_visualization.frag:77-90
+                    const V3<float> T = normalize(lerp_n(a.tangent, b.tangent, c.tangent));
+                    const V3<float> B = normalize(lerp_n(a.bitangent, b.bitangent, c.bitangent));
+                    const V3<float> Nn = normalize(nn);
+                    const V3<float> mp = rgb(m.texture_indices0[1]);
+                    const V3<float> nm = normalize(mp * 2.0f - V3<float>(1.0f));
+                    nn = normalize(V3<float>(T.x * nm.x + B.x * nm.y + Nn.x * nm.z, T.y * nm.x + B.y * nm.y + Nn.y * nm.z,
+                                             T.z * nm.x + B.z * nm.y + Nn.z * nm.z));
+                }
                 r = nn * 0.5f + V3<float>(0.5f);
             } else if (which == 2) {
                 r = V3<float>(m.texture_indices0[2] == -1

@@ -114,3 +114,101 @@ def decode_png(data):
     assert (raw[:, 0] == 0).all()
     return raw[:, 1:].reshape(h, w, 4)
 
+
+
+class TexturedQuadScene:
+    """A floor quad (y = 0, x and z in [-1, 1], 4 x 4 UV repeats) with one
+    GGX/Lambert material: an RGBA8 albedo texture (optionally sRGB-encoded),
+    an optional tangent-space normal map, tangent +x and bitangent +z; one
+    point light above; no environment.  .desc points at its hx_scene_desc,
+    .camera() looks down at the quad."""
+
+    def __init__(self, albedo, albedo_srgb=True, normal_map=None, roughness=0.5):
+        self._tex_data = [np.ascontiguousarray(albedo, np.uint8)]
+        if normal_map is not None:
+            self._tex_data.append(np.ascontiguousarray(normal_map, np.uint8))
+        pos = [(-1, 0, -1), (1, 0, -1), (1, 0, 1), (-1, 0, 1)]
+        uv = [(0, 0), (4, 0), (4, 4), (0, 4)]
+        self._verts = (hx.Vertex * 4)()
+        for i in range(4):
+            v = self._verts[i]
+            v.position[0], v.position[1], v.position[2], v.position[3] = pos[i][0], pos[i][1], pos[i][2], 0.0
+            v.tex_coord[0], v.tex_coord[1] = uv[i]
+            v.normal[1] = 1.0
+            v.tangent[0] = 1.0
+            v.bitangent[2] = 1.0
+        self._idx = (C.c_uint32 * 6)(0, 2, 1, 0, 3, 2)
+        self._sub = (hx.Submesh * 1)()
+        self._sub[0].base_index, self._sub[0].index_count, self._sub[0].material, self._sub[0].flags = 0, 6, 0, 0
+        self._mesh = (hx.MeshDesc * 1)()
+        m = self._mesh[0]
+        m.vertices, m.num_vertices = self._verts, 4
+        m.indices, m.num_indices = self._idx, 6
+        m.submeshes, m.num_submeshes = self._sub, 1
+        self._mat = (hx.Material * 1)()
+        mat = self._mat[0]
+        for k in range(4):
+            mat.texture_indices0[k] = -1
+            mat.texture_indices1[k] = -1
+        mat.texture_indices0[0] = 0
+        if normal_map is not None:
+            mat.texture_indices0[1] = 1
+        mat.albedo[0] = mat.albedo[1] = mat.albedo[2] = mat.albedo[3] = 1.0
+        mat.roughness_metallic[0] = roughness
+        self._tex = (hx.TextureDesc * len(self._tex_data))()
+        for k, t in enumerate(self._tex_data):
+            self._tex[k].rgba8 = t.ctypes.data_as(C.POINTER(C.c_uint8))
+            self._tex[k].height, self._tex[k].width = t.shape[0], t.shape[1]
+            self._tex[k].srgb = 1 if (k == 0 and albedo_srgb) else 0
+        self._inst = (hx.Instance * 1)()
+        inst = self._inst[0]
+        for k in range(4):
+            inst.model_matrix[5 * k] = 1.0
+            inst.normal_matrix[5 * k] = 1.0
+        inst.mesh_index, inst.material_override = 0, -1
+        self._light = (hx.Light * 1)()
+        lt = self._light[0]
+        lt.data0[0], lt.data0[1], lt.data0[2], lt.data0[3] = float(hx.LIGHT_POINT), 1.0, 0.9, 0.8
+        lt.data1[3] = 4.0
+        lt.data2[0], lt.data2[1], lt.data2[2], lt.data2[3] = 0.3, 1.2, -0.2, 0.05
+        self._desc = hx.SceneDesc()
+        d = self._desc
+        d.meshes, d.num_meshes = self._mesh, 1
+        d.instances, d.num_instances = self._inst, 1
+        d.materials, d.num_materials = self._mat, 1
+        d.textures, d.num_textures = self._tex, len(self._tex_data)
+        d.punctual_lights, d.num_punctual_lights = self._light, 1
+        d.environment.kind = 0
+
+    @property
+    def desc(self):
+        return C.pointer(self._desc)
+
+    def camera(self):
+        cam = hx.Camera()
+        cam.position[:] = [0.0, 1.6, 1.9]
+        cam.target[:] = [0.0, 0.0, 0.0]
+        cam.up[:] = [0.0, 1.0, 0.0]
+        cam.fov_y_degrees, cam.near_plane, cam.far_plane = 50.0, 1.0, 1000.0
+        cam.focal_length, cam.aperture_radius = 8.0, 0.0
+        return cam
+
+
+def bump_normal_map(size=64, freq=3, amp=0.35):
+    """Tangent-space normal map (RGB = n * 0.5 + 0.5) of a sinusoidal height field."""
+    u = (np.arange(size) + 0.5) / size
+    du = amp * 2 * np.pi * freq * np.cos(2 * np.pi * freq * u)
+    nx, ny = np.meshgrid(-du, -du)
+    n = np.stack([nx, ny, np.ones_like(nx)], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    rgba = np.empty((size, size, 4), np.uint8)
+    rgba[..., :3] = np.clip(np.round((n * 0.5 + 0.5) * 255), 0, 255).astype(np.uint8)
+    rgba[..., 3] = 255
+    return rgba
+
+
+def checker_texture(size=32, a=(200, 180, 150), b=(40, 60, 90)):
+    y, x = np.mgrid[0:size, 0:size]
+    sel = ((x // 4 + y // 4) % 2 == 0)[..., None]
+    rgba = np.where(sel, np.array(a + (255,), np.uint8), np.array(b + (255,), np.uint8)).astype(np.uint8)
+    return rgba

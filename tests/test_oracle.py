@@ -167,3 +167,23 @@ def test_policy_differences_change_the_image():
     b, _ = osc.render(integrator_desc(32, 32, policy="reference"), f, 16)
     # the reference samples only triangle 0 of the quad light (light_data1.z is never written)
     assert a.mean() > b.mean()
+
+
+def test_oracle_srgb_texture_decode():
+    """An sRGB-flagged texture decodes its RGB with the sRGB transfer function
+    before filtering (resource_manager.cpp:48-67 creates such textures with
+    *_SRGB formats); a UNORM one reads q / 255.  A constant texture makes the
+    filtered value the decoded texel itself."""
+    from tests.helpers import TexturedQuadScene
+    tex = np.full((8, 8, 4), 128, np.uint8)
+    c = 128 / 255.0
+    want = {True: np.float32(((c + 0.055) / 1.055) ** 2.4), False: np.float32(128) / np.float32(255)}
+    for srgb in (True, False):
+        qs = TexturedQuadScene(tex, albedo_srgb=srgb)
+        osc = ob.OracleScene(qs)
+        W, H = 40, 30
+        f = hx.frame_desc(qs.camera(), W, H)
+        alb = osc.output_view(f, W, H, hx.OUTPUT_ALBEDO)
+        hit = np.any(alb[..., :3] != 0, axis=-1)
+        assert hit.mean() > 0.3
+        assert np.all(alb[hit][:, :3] == want[srgb]), (srgb, np.unique(alb[hit][:, :3]))
