@@ -411,7 +411,8 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
 // three node visits per iteration they also beat the lane-local k_extend on
 // the small late launches: +0.7%); k_extend serves the 16-bit payload form.
 // Flush after 24 queued triangles or 4 waiting lanes (measured on the
-// 1.18 M-triangle scene at 1080p).
+// 1.18 M-triangle scene at 1080p: 16-24 queued and 2-4 waiting lanes within
+// 0.2 % of each other, 12 queued -0.8 %, 32 queued -1.5 %).
 constexpr uint32_t kFlushTris = 24, kFlushParked = 4;
 // Node visits per loop iteration for a lane whose nodes expose no triangle:
 // spreads the warp's per-iteration queue bookkeeping over more visits
