@@ -40,6 +40,16 @@ HXD V3 reflect(V3 i, V3 n) {
 HXD bool is_black(V3 c) { return c.x == 0.0f && c.y == 0.0f && c.z == 0.0f; }
 HXD float comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 
+// first index k in [lo, hi) with a[k] > x (a sorted ascending), hi if none
+HXD int upper_bound_f(const float* a, int lo, int hi, float x) {
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) > x) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
 // column-major mat4 * (x, y, z, w), left to right per component
 HXD V3 mat4_mul3(const float* m, float x, float y, float z, float w) {
     return v3(m[0] * x + m[4] * y + m[8] * z + m[12] * w, m[1] * x + m[5] * y + m[9] * z + m[13] * w,

@@ -102,6 +102,14 @@ struct DevEnv {
     const float* rowsum;  // height: row weight / total (for the pdf)
     const float* cellw;   // height * width: texel weight / row weight
     float total;
+    // Guide tables of the two CDF searches: for bucket b of a power-of-two
+    // count K, the search result at b / K, so a value in [b / K, (b + 1) / K)
+    // is searched only between entries b and b + 1 (the same index as the
+    // full search).  marg_guide: km + 1 entries; cond_guide: height rows of
+    // kc + 1 entries.
+    const uint32_t* marg_guide;
+    const uint32_t* cond_guide;
+    uint32_t km, kc;
 };
 
 struct DevScene {

@@ -138,7 +138,25 @@ bool material_emissive(const hx_material& m) {  // Material::is_emissive, materi
     return m.emissive[0] > 0.0f || m.emissive[1] > 0.0f || m.emissive[2] > 0.0f;
 }
 
+// Guide table of a search over n + 1 ascending CDF entries a[0..n] (search
+// range [1, n + 1)): entry b in [0, k] is the search result at b / k (exact:
+// k is a power of two).  rows > 1: one table per row of stride n + 1.
+__global__ void k_env_guide(const float* __restrict__ a, uint32_t n, uint32_t rows, uint32_t k, uint32_t* __restrict__ g) {
+    const size_t total = (size_t)rows * (k + 1);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t r = (uint32_t)(t / (k + 1)), b = (uint32_t)(t % (k + 1));
+        const float x = (float)b * (1.0f / (float)k);
+        g[t] = (uint32_t)upper_bound_f(a + (size_t)r * (n + 1), 1, (int)n + 1, x);
+    }
+}
+
 }  // namespace
+
+static uint32_t pow2_at_least(uint32_t v) {
+    uint32_t k = 1;
+    while (k < v) k <<= 1;
+    return k;
+}
 
 hx_status hx_env_build(hx_context* ctx, hx_scene* s, const hx_environment_desc& e) {
     DevEnv& env = s->d.env;
@@ -180,6 +198,15 @@ hx_status hx_env_build(hx_context* ctx, hx_scene* s, const hx_environment_desc& 
     k_env_row_lum<<<h, 256, 0, st>>>(rgb, w, rowlum);
     k_env_rows<<<h, 256, 0, st>>>(rgb, w, h, rowlum, cond, rowsum);
     k_env_marg<<<1, 32, 0, st>>>(rowsum, h, marg, total);
+    env.km = pow2_at_least(h);
+    env.kc = pow2_at_least(w);
+    uint32_t *mg, *cg;
+    HX_TRY(hx_alloc_t(ctx, &mg, (size_t)env.km + 1)); s->allocs.push_back(mg);
+    HX_TRY(hx_alloc_t(ctx, &cg, (size_t)h * (env.kc + 1))); s->allocs.push_back(cg);
+    k_env_guide<<<(env.km + 256) / 256, 256, 0, st>>>(marg, h, 1, env.km, mg);
+    k_env_guide<<<(unsigned)std::min<size_t>(((size_t)h * (env.kc + 1) + 255) / 256, 65535), 256, 0, st>>>(cond, w, h, env.kc, cg);
+    env.marg_guide = mg;
+    env.cond_guide = cg;
     HX_CUDA(cudaGetLastError());
     env.rgb = rgb;
     env.cond = cond;

@@ -169,22 +169,17 @@ HXD V3 env_lookup(const DevEnv& e, V3 d) {
     return top + (bot - top) * fy;
 }
 
-// first index k in [lo, hi) with a[k] > x (a sorted ascending), hi if none
-HXD int upper_bound_f(const float* a, int lo, int hi, float x) {
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (__ldg(a + mid) > x) hi = mid;
-        else lo = mid + 1;
-    }
-    return lo;
-}
 
 HXD V3 env_sample(const DevEnv& e, float r0, float r1, float& pdf) {
     int W = (int)e.width, H = (int)e.height;
-    int j = upper_bound_f(e.marg, 1, H + 1, r1) - 1;
+    // r * k is exact (k a power of two) and r < 1, so b <= k - 1
+    const uint32_t bm = (uint32_t)(r1 * (float)e.km);
+    int j = upper_bound_f(e.marg, (int)__ldg(e.marg_guide + bm), (int)__ldg(e.marg_guide + bm + 1), r1) - 1;
     j = j < 0 ? 0 : (j >= H ? H - 1 : j);
     const float* row = e.cond + (size_t)j * (W + 1);
-    int i = upper_bound_f(row, 1, W + 1, r0) - 1;
+    const uint32_t* g = e.cond_guide + (size_t)j * (e.kc + 1);
+    const uint32_t bc = (uint32_t)(r0 * (float)e.kc);
+    int i = upper_bound_f(row, (int)__ldg(g + bc), (int)__ldg(g + bc + 1), r0) - 1;
     i = i < 0 ? 0 : (i >= W ? W - 1 : i);
     float m0 = __ldg(e.marg + j), m1 = __ldg(e.marg + j + 1);
     float c0 = __ldg(row + i), c1 = __ldg(row + i + 1);
