@@ -24,6 +24,7 @@ ACCUM_RUNNING_MEAN, ACCUM_KAHAN = 0, 1
 ENV_SAMPLE_COSINE, ENV_SAMPLE_IMPORTANCE = 0, 1
 PAYLOAD_FP32, PAYLOAD_FP16 = 0, 1
 TONEMAP_ACES, TONEMAP_REINHARD, TONEMAP_NONE = 0, 1, 2
+TEXTURE_RGBA8, TEXTURE_BC1_RGB, TEXTURE_BC1_RGBA, TEXTURE_BC2, TEXTURE_BC3, TEXTURE_BC4, TEXTURE_BC5 = range(7)
 OUTPUT_ALBEDO, OUTPUT_NORMALS, OUTPUT_ROUGHNESS, OUTPUT_METALLIC, OUTPUT_EMISSIVE, OUTPUT_FINAL = 0, 1, 2, 3, 4, 5
 SCENE_BOX, SCENE_ICOSPHERES, SCENE_TERRAIN = 0, 1, 2
 SUBMESH_NON_OPAQUE = 1
@@ -72,7 +73,7 @@ class Instance(C.Structure):
 
 class TextureDesc(C.Structure):
     _fields_ = [("rgba8", C.POINTER(C.c_uint8)), ("width", C.c_uint32), ("height", C.c_uint32),
-                ("srgb", C.c_uint32), ("reserved", C.c_uint32)]
+                ("srgb", C.c_uint32), ("format", C.c_uint32)]
 
 
 class EnvironmentDesc(C.Structure):
@@ -263,6 +264,7 @@ _SIGS = {
     "hx_integrator_set_aov_accumulation": (C.c_int, [_P, C.c_uint32]),
     "hx_encode_png": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "hx_save_png": (C.c_int, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
+    "hx_texture_decode": (C.c_int, [C.POINTER(TextureDesc), _P]),
 }
 
 _lib_handle = None
@@ -331,6 +333,17 @@ def encode_png(rgba8):
     out = np.zeros(n.value, np.uint8)
     check(lib().hx_encode_png(_ptr(img), w, h, _ptr(out), out.size, C.byref(n)))
     return out.tobytes()
+
+
+def texture_decode(data, width, height, fmt):
+    """RGBA8 (height, width, 4) of a texture in format fmt (TEXTURE_*): data = its bytes."""
+    buf = np.ascontiguousarray(data, np.uint8)
+    t = TextureDesc()
+    t.rgba8 = buf.ctypes.data_as(C.POINTER(C.c_uint8))
+    t.width, t.height, t.format = width, height, fmt
+    out = np.zeros((height, width, 4), np.uint8)
+    check(lib().hx_texture_decode(C.byref(t), _ptr(out)))
+    return out
 
 
 def save_png(path, rgba8):

@@ -139,3 +139,119 @@ extern "C" hx_status hx_save_png(const char* path, const uint8_t* rgba8, uint32_
     }
     return HX_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Block-compressed textures (BC1-BC5, the S3TC / RGTC block formats of the
+// reference's assets, resource_manager.cpp:14-30) decoded to RGBA8 at upload.
+// Palettes round to nearest in integers; colour endpoints expand from RGB565
+// by bit replication.
+// ---------------------------------------------------------------------------
+namespace {
+
+uint32_t block_bytes(uint32_t fmt) {
+    return (fmt == HX_TEXTURE_BC1_RGB || fmt == HX_TEXTURE_BC1_RGBA || fmt == HX_TEXTURE_BC4) ? 8u : 16u;
+}
+
+uint64_t le64(const uint8_t* p) {
+    uint64_t v = 0;
+    for (int k = 7; k >= 0; --k) v = (v << 8) | p[k];
+    return v;
+}
+
+// 4x4 colour block: 16 RGBA texels (alpha 255, or 0 for the transparent
+// entry of the 3-colour mode when transparent is set).
+void decode_colour(const uint8_t* b, bool four_always, bool transparent, uint8_t out[16][4]) {
+    const uint32_t c0 = b[0] | (b[1] << 8), c1 = b[2] | (b[3] << 8);
+    const uint32_t idx = b[4] | (b[5] << 8) | (b[6] << 16) | ((uint32_t)b[7] << 24);
+    uint32_t p[4][4];
+    for (int e = 0; e < 2; ++e) {
+        const uint32_t c = e ? c1 : c0;
+        const uint32_t r5 = c >> 11, g6 = (c >> 5) & 63u, b5 = c & 31u;
+        p[e][0] = (r5 << 3) | (r5 >> 2);
+        p[e][1] = (g6 << 2) | (g6 >> 4);
+        p[e][2] = (b5 << 3) | (b5 >> 2);
+        p[e][3] = 255;
+    }
+    if (four_always || c0 > c1) {
+        for (int ch = 0; ch < 3; ++ch) {
+            p[2][ch] = (2 * p[0][ch] + p[1][ch] + 1) / 3;
+            p[3][ch] = (p[0][ch] + 2 * p[1][ch] + 1) / 3;
+        }
+        p[2][3] = p[3][3] = 255;
+    } else {
+        for (int ch = 0; ch < 3; ++ch) {
+            p[2][ch] = (p[0][ch] + p[1][ch] + 1) / 2;
+            p[3][ch] = 0;
+        }
+        p[2][3] = 255;
+        p[3][3] = transparent ? 0 : 255;
+    }
+    for (int t = 0; t < 16; ++t) {
+        const uint32_t k = (idx >> (2 * t)) & 3u;
+        for (int ch = 0; ch < 4; ++ch) out[t][ch] = (uint8_t)p[k][ch];
+    }
+}
+
+// 4x4 single-channel block (BC4 / BC3 alpha / BC5 halves): 16 values.
+void decode_channel(const uint8_t* b, uint8_t out[16]) {
+    const uint32_t a0 = b[0], a1 = b[1];
+    uint32_t p[8];
+    p[0] = a0;
+    p[1] = a1;
+    if (a0 > a1) {
+        for (uint32_t k = 2; k < 8; ++k) p[k] = ((8 - k) * a0 + (k - 1) * a1 + 3) / 7;
+    } else {
+        for (uint32_t k = 2; k < 6; ++k) p[k] = ((6 - k) * a0 + (k - 1) * a1 + 2) / 5;
+        p[6] = 0;
+        p[7] = 255;
+    }
+    const uint64_t idx = le64(b) >> 16;
+    for (int t = 0; t < 16; ++t) out[t] = (uint8_t)p[(idx >> (3 * t)) & 7u];
+}
+
+}  // namespace
+
+extern "C" hx_status hx_texture_decode(const hx_texture_desc* tex, uint8_t* out) {
+    HX_CHECK_ARG(tex && out && tex->rgba8 && tex->width > 0 && tex->height > 0, "hx_texture_decode: null argument or empty texture");
+    HX_CHECK_ARG(tex->format <= HX_TEXTURE_BC5, "hx_texture_decode: unknown format %u", tex->format);
+    const uint32_t W = tex->width, H = tex->height;
+    if (tex->format == HX_TEXTURE_RGBA8) {
+        std::copy(tex->rgba8, tex->rgba8 + (size_t)W * H * 4, out);
+        return HX_OK;
+    }
+    const uint32_t bw = (W + 3) / 4, bh = (H + 3) / 4, bb = block_bytes(tex->format);
+    for (uint32_t by = 0; by < bh; ++by)
+        for (uint32_t bx = 0; bx < bw; ++bx) {
+            const uint8_t* b = tex->rgba8 + ((size_t)by * bw + bx) * bb;
+            uint8_t px[16][4];
+            uint8_t ch[16];
+            switch (tex->format) {
+                case HX_TEXTURE_BC1_RGB: decode_colour(b, false, false, px); break;
+                case HX_TEXTURE_BC1_RGBA: decode_colour(b, false, true, px); break;
+                case HX_TEXTURE_BC2:
+                    decode_colour(b + 8, true, false, px);
+                    for (int t = 0; t < 16; ++t) px[t][3] = (uint8_t)(((le64(b) >> (4 * t)) & 15u) * 17u);
+                    break;
+                case HX_TEXTURE_BC3:
+                    decode_colour(b + 8, true, false, px);
+                    decode_channel(b, ch);
+                    for (int t = 0; t < 16; ++t) px[t][3] = ch[t];
+                    break;
+                case HX_TEXTURE_BC4:
+                    decode_channel(b, ch);
+                    for (int t = 0; t < 16; ++t) { px[t][0] = ch[t]; px[t][1] = px[t][2] = 0; px[t][3] = 255; }
+                    break;
+                default:  // BC5
+                    decode_channel(b, ch);
+                    for (int t = 0; t < 16; ++t) { px[t][0] = ch[t]; px[t][2] = 0; px[t][3] = 255; }
+                    decode_channel(b + 8, ch);
+                    for (int t = 0; t < 16; ++t) px[t][1] = ch[t];
+                    break;
+            }
+            for (uint32_t t = 0; t < 16; ++t) {
+                const uint32_t x = bx * 4 + (t & 3), y = by * 4 + (t >> 2);
+                if (x < W && y < H) std::copy(px[t], px[t] + 4, out + ((size_t)y * W + x) * 4);
+            }
+        }
+    return HX_OK;
+}

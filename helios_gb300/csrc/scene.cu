@@ -259,9 +259,12 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
         }
         HX_CHECK_ARG(mt.texture_indices1[0] < (int32_t)desc->num_textures, "material %u: texture out of range", k);
     }
-    for (uint32_t t = 0; t < desc->num_textures; ++t)
+    for (uint32_t t = 0; t < desc->num_textures; ++t) {
         HX_CHECK_ARG(desc->textures[t].rgba8 && desc->textures[t].width > 0 && desc->textures[t].height > 0,
                      "texture %u: empty", t);
+        HX_CHECK_ARG(desc->textures[t].format <= HX_TEXTURE_BC5, "texture %u: unknown format %u", t,
+                     desc->textures[t].format);
+    }
     for (uint32_t l = 0; l < desc->num_punctual_lights; ++l) {
         uint32_t ty = (uint32_t)desc->punctual_lights[l].data0[0];
         HX_CHECK_ARG(ty == HX_LIGHT_DIRECTIONAL || ty == HX_LIGHT_POINT || ty == HX_LIGHT_SPOT,
@@ -419,10 +422,19 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
         uint32_t* texels;
         if ((rc = hx_alloc_t(ctx, &texels, ntexels)) != HX_OK) return scene_fail(s, rc);
         s->allocs.push_back(texels);
+        // block-compressed textures are decoded to RGBA8 on the host first
+        std::vector<std::vector<uint8_t>> decoded;
         for (uint32_t t = 0; t < desc->num_textures; ++t) {
             size_t cnt = (size_t)desc->textures[t].width * desc->textures[t].height;
-            HX_CUDA(cudaMemcpyAsync(texels + htd[t].x, desc->textures[t].rgba8, 4 * cnt, cudaMemcpyHostToDevice, st));
+            const uint8_t* src = desc->textures[t].rgba8;
+            if (desc->textures[t].format != HX_TEXTURE_RGBA8) {
+                decoded.emplace_back(4 * cnt);
+                if ((rc = hx_texture_decode(&desc->textures[t], decoded.back().data())) != HX_OK) return scene_fail(s, rc);
+                src = decoded.back().data();
+            }
+            HX_CUDA(cudaMemcpyAsync(texels + htd[t].x, src, 4 * cnt, cudaMemcpyHostToDevice, st));
         }
+        if (!decoded.empty()) HX_CUDA(cudaStreamSynchronize(st));
         uint8_t* alpha8;
         if ((rc = hx_alloc_t(ctx, &alpha8, ntexels)) != HX_OK) return scene_fail(s, rc);
         s->allocs.push_back(alpha8);

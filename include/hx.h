@@ -147,14 +147,34 @@ typedef struct hx_instance {
  * textures with *_SRGB formats, resource_manager.cpp:48-67), so samples
  * decode each texel's RGB with the sRGB transfer function before filtering;
  * alpha stays linear.  srgb = 0: UNORM.  Normal maps (texture_indices0[1])
- * use the vertex tangent and bitangent (path_trace_rchit.glsl:190-219). */
+ * use the vertex tangent and bitangent (path_trace_rchit.glsl:190-219).
+ * format: HX_TEXTURE_RGBA8 (rgba8 = width * height * 4 bytes) or one of the
+ * block-compressed formats of the reference's assets
+ * (kCompressedFormats, resource_manager.cpp:14-30), then rgba8 points at
+ * ceil(width / 4) * ceil(height / 4) blocks in row-major block order; they
+ * are decoded to RGBA8 at upload (hx_texture_decode). */
+#define HX_TEXTURE_RGBA8    0u
+#define HX_TEXTURE_BC1_RGB  1u  /* 8-byte blocks, alpha 255                          */
+#define HX_TEXTURE_BC1_RGBA 2u  /* 8-byte blocks, 1-bit alpha in the 3-colour mode   */
+#define HX_TEXTURE_BC2      3u  /* 16-byte blocks: explicit 4-bit alpha + colour      */
+#define HX_TEXTURE_BC3      4u  /* 16-byte blocks: interpolated alpha + colour        */
+#define HX_TEXTURE_BC4      5u  /* 8-byte blocks: R (G = B = 0, A = 255)              */
+#define HX_TEXTURE_BC5      6u  /* 16-byte blocks: R, G (B = 0, A = 255)              */
 typedef struct hx_texture_desc {
     const uint8_t* rgba8;
     uint32_t       width;
     uint32_t       height;
     uint32_t       srgb;
-    uint32_t       reserved;
+    uint32_t       format;  /* HX_TEXTURE_* */
 } hx_texture_desc;
+
+/* Host-only: decodes a texture of any HX_TEXTURE_* format to width * height
+ * RGBA8 texels (rows top to bottom).  Colour endpoints expand from RGB565 by
+ * bit replication; interpolated palette entries round to nearest:
+ * (2a + b + 1) / 3 and (a + b + 1) / 2 for colour, ((8 - k) a + (k - 1) b + 3) / 7
+ * and ((6 - k) a + (k - 1) b + 2) / 5 for BC4-style channels; BC2 alpha is
+ * a4 * 17.  The 3-colour mode (c0 <= c1) exists in BC1 blocks only. */
+HX_API hx_status hx_texture_decode(const hx_texture_desc* texture, uint8_t* rgba8_out);
 
 #define HX_ENV_NONE          0u  /* black environment                        */
 #define HX_ENV_EQUIRECT      1u  /* caller-supplied RGBA32F lat-long map     */

@@ -80,6 +80,8 @@ class OracleScene:
         self._src = scene
         ptr = scene.desc if hasattr(scene, "desc") else scene
         self.handle = lib().oracle_scene_create(C.cast(ptr, C.c_void_p))
+        if not self.handle:
+            raise ValueError("oracle scene: textures must be RGBA8")
 
     @property
     def num_prims(self):

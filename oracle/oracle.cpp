@@ -1390,7 +1390,11 @@ struct oracle_counters {
     int threads;
 };
 
+// Textures must be RGBA8 (the oracle does not restate the block decoders;
+// those are pinned by oracle/texture_ref.py): NULL otherwise.
 void* oracle_scene_create(const hx_scene_desc* d) {
+    for (uint32_t t = 0; t < d->num_textures; ++t)
+        if (d->textures[t].format != HX_TEXTURE_RGBA8) return nullptr;
     Scene* s = new Scene();
     for (uint32_t m = 0; m < d->num_meshes; ++m) {
         const hx_mesh_desc& md = d->meshes[m];

@@ -123,7 +123,8 @@ class TexturedQuadScene:
     point light above; no environment.  .desc points at its hx_scene_desc,
     .camera() looks down at the quad."""
 
-    def __init__(self, albedo, albedo_srgb=True, normal_map=None, roughness=0.5):
+    def __init__(self, albedo, albedo_srgb=True, normal_map=None, roughness=0.5, albedo_format=0, albedo_wh=None):
+        # albedo: (H, W, 4) RGBA8, or block-compressed bytes with albedo_format / albedo_wh = (W, H)
         self._tex_data = [np.ascontiguousarray(albedo, np.uint8)]
         if normal_map is not None:
             self._tex_data.append(np.ascontiguousarray(normal_map, np.uint8))
@@ -158,7 +159,11 @@ class TexturedQuadScene:
         self._tex = (hx.TextureDesc * len(self._tex_data))()
         for k, t in enumerate(self._tex_data):
             self._tex[k].rgba8 = t.ctypes.data_as(C.POINTER(C.c_uint8))
-            self._tex[k].height, self._tex[k].width = t.shape[0], t.shape[1]
+            if k == 0 and albedo_format:
+                self._tex[k].width, self._tex[k].height = albedo_wh
+                self._tex[k].format = albedo_format
+            else:
+                self._tex[k].height, self._tex[k].width = t.shape[0], t.shape[1]
             self._tex[k].srgb = 1 if (k == 0 and albedo_srgb) else 0
         self._inst = (hx.Instance * 1)()
         inst = self._inst[0]

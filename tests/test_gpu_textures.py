@@ -75,3 +75,28 @@ def test_normal_map_and_srgb_change_the_result(gpu_ctx):
     dn = np.abs(out["nmap"][2] - out["plain"][2])[hit].max()
     assert dn > 0.05
     assert rel_rmse(out["nmap"][0], out["plain"][0]) > 0.01
+
+
+@pytest.mark.parametrize("fmt", [hx.TEXTURE_BC1_RGB, hx.TEXTURE_BC3, hx.TEXTURE_BC5])
+def test_block_compressed_albedo_renders_like_its_decoded_texels(gpu_ctx, fmt):
+    """A BCn albedo texture (decoded at upload) gives the same accumulated
+    image and albedo view, bit for bit, as uploading its RGBA8 decode."""
+    from oracle import texture_ref as tr
+    rng = np.random.default_rng(fmt)
+    w, h = 30, 22
+    nb = ((w + 3) // 4) * ((h + 3) // 4)
+    data = rng.integers(0, 256, size=nb * tr.BLOCK_BYTES[fmt], dtype=np.uint8)
+    texels = tr.decode(data, w, h, fmt)
+    W, H = 64, 48
+    out = []
+    for kw in (dict(albedo=data, albedo_format=fmt, albedo_wh=(w, h)), dict(albedo=texels)):
+        qs = TexturedQuadScene(albedo_srgb=True, normal_map=bump_normal_map(), **kw)
+        sc = hx.Scene(gpu_ctx, qs)
+        f = hx.frame_desc(qs.camera(), W, H)
+        it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=3)
+        it.render(f, 4)
+        out.append((it.read_accumulation(), it.render_output(f, hx.OUTPUT_ALBEDO)))
+        it.close()
+        sc.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert np.any(out[0][1][..., :3] != 0)
