@@ -192,6 +192,7 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     it->grid_shade = std::max(1, per_sm) * ctx->num_sms;
     it->grid_gen = ctx->num_sms * 8;
+    HX_CUDA(set_carveouts(k_extend_batched<false>, k_extend_batched<true>));
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_batched<false>, kTraceThreads, 0));
     it->grid_batched = std::max(1, per_sm) * ctx->num_sms;
     compute_tiles(it);

@@ -340,6 +340,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     int per_sm = 0;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend<false, false>, kTraceThreads, 0));
     const int grid_trace = std::max(1, per_sm) * ctx->num_sms;
+    HX_CUDA(set_carveouts(k_extend_batched<false>, k_extend_batched<false>));
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_batched<false>, kTraceThreads, 0));
     const int grid_batched = std::max(1, per_sm) * ctx->num_sms;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));

@@ -18,6 +18,20 @@ constexpr int kTraceThreads = 128;
 // runs at the same cap (1.11 ms per frame, 1.12 ms at 72 registers).
 constexpr int kTraceMinBlocks = 8;
 constexpr int kShadeMinBlocks = 8;
+// Preferred shared-memory carve-out of the batched traversal, in percent of
+// the SM's maximum: 10 % selects the 32 KB configuration (8 blocks of 3 KB +
+// the driver's 1 KB each), the rest of the SM's memory is L1.  Without it
+// the driver chose 100 KB.
+constexpr int kBatchedCarveoutPct = 10;
+
+// Applies the carve-out preferences to this translation unit's traversal
+// and shading kernels (each unit has its own instances).
+template <typename F1, typename F2>
+static inline cudaError_t set_carveouts(F1 batched0, F2 batched1) {
+    cudaError_t e = cudaFuncSetAttribute(batched0, cudaFuncAttributePreferredSharedMemoryCarveout, kBatchedCarveoutPct);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(batched1, cudaFuncAttributePreferredSharedMemoryCarveout, kBatchedCarveoutPct);
+    return e;
+}
 constexpr int kShadeThreads = 128;
 constexpr int kGenThreads = 256;
 
