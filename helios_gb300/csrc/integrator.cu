@@ -169,6 +169,8 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_A(it->q.T, 16 * cap);
     HX_A(it->q.L, 16 * cap);
     HX_A(it->q.rng, 8 * cap);
+    HX_A(it->q.shade_list, 4 * cap);
+    it->q.shade_cap = (uint32_t)cap;
     HX_A(it->q.counters, 64);
     HX_A(it->q.stats, 128);
     HX_A(it->q.status, 64);
@@ -280,7 +282,7 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             const int cur = b & 1;
             {
                 StageTimer t(it, &it->stats.ms_trace);
-                HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
+                HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));  // fetch cursor, miss / hit counts
 #define HX_EXTEND(COUNT, FP16)                                                                                      \
     do {                                                                                                            \
         if (!FP16 && s.num_prims < (1u << 27))                                                                      \
@@ -734,7 +736,7 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
     k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 0, W * H, P.rng, it->q);
-    HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
+    HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));
     launch_primary_trace(it, st);
     uint32_t n = W * H;
     k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(it->q.hit, n, it->hits_host_layout);
@@ -762,7 +764,7 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
     k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 0, W * H, P.rng, it->q);
-    HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 4, st));
+    HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));
     launch_primary_trace(it, st);
     k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, n, d_features);
     HX_CUDA(cudaGetLastError());

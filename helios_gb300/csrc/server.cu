@@ -320,6 +320,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     HX_TRY(A((void**)&b->q.T, 16ull * cap));
     HX_TRY(A((void**)&b->q.L, 16ull * cap));
     HX_TRY(A((void**)&b->q.rng, 8ull * cap));
+    HX_TRY(A((void**)&b->q.shade_list, 4ull * cap));
+    b->q.shade_cap = cap;
     HX_TRY(A((void**)&b->q.counters, 64));
     HX_TRY(A((void**)&b->q.stats, 64));
     HX_TRY(A((void**)&b->q.status, 64));
@@ -357,7 +359,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     // the last launch traces the final bounce's shadow rays
     for (uint32_t bo = 0; bo <= s->desc.max_ray_bounces; ++bo) {
         int cur = bo & 1;
-        cudaMemsetAsync(b->q.counters + 4, 0, 4, st);
+        cudaMemsetAsync(b->q.counters + 4, 0, 24, st);  // fetch cursor, miss / hit counts
         if (sc.num_prims < (1u << 27))
             k_extend_batched<false><<<grid_batched, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.r0[cur], b->q.r1[cur],
                                                                             b->q.counters + cur, b->q.counters + 4,

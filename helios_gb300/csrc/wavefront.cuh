@@ -49,7 +49,13 @@ struct Queues {
     float4* T;          // throughput + depth bits
     float4* L;          // radiance
     uint2* rng;
-    uint32_t* counters; // [0],[1] ray queues, [2] shadow queue, [4],[5] trace / shadow fetch cursors
+    uint32_t* counters; // [0],[1] ray queues, [2] shadow queue, [4] trace fetch cursor, [8] misses, [9] hits
+    // Shading order (optional): the traversal appends each finished extension
+    // ray's queue slot to the front (misses, counters[8]) or the back (hits,
+    // counters[9]) of this list, so shading runs misses and hits as two
+    // contiguous ranges; nullptr: shade in queue order.
+    uint32_t* shade_list = nullptr;
+    uint32_t shade_cap = 0;
     unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2..8] counting mode (k_extend)
     uint32_t* status;   // bit 0: traversal stack overflow
     // ray-debug capture (k_raygen_debug, k_shade<_, true>): per-path segment
@@ -63,6 +69,21 @@ struct Queues {
 struct Rect {
     uint32_t x0, y0, w, h;
 };
+
+// Appends a finished extension ray's queue slot to the shading list (misses
+// at the front, hits at the back), aggregated over the lanes that finish in
+// the same step: called only by those lanes, one atomic per kind.
+__device__ __forceinline__ void shade_list_append(const Queues& q, bool miss, uint32_t slot) {
+    const uint32_t active = __activemask();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t same = __ballot_sync(active, miss) ^ (miss ? 0u : active);
+    const uint32_t leader = __ffs(same) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(q.counters + (miss ? 8 : 9), __popc(same));
+    base = __shfl_sync(active, base, leader);
+    const uint32_t k = base + __popc(same & ((1u << lane) - 1u));
+    if (k < q.shade_cap) q.shade_list[miss ? k : q.shade_cap - 1u - k] = slot;
+}
 
 // Warp-aggregated queue append: one atomic per warp, slots in lane order.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
@@ -195,7 +216,10 @@ __global__ void k_raygen_debug(hx_frame_desc f, uint32_t px, uint32_t py, uint32
 template <bool FP16, bool DEBUG = false>
 __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevScene s, Policy P, uint32_t max_bounces, float bias, int cur,
                                                          Queues q) {
-    const uint32_t n = q.counters[cur];
+    // with a shading list: misses [0, n_miss) then hits, else queue order
+    const bool listed = q.shade_list != nullptr;
+    const uint32_t n_miss = listed ? q.counters[8] : 0u;
+    const uint32_t n = listed ? min(n_miss + q.counters[9], q.counters[cur]) : q.counters[cur];
     const int nxt = cur ^ 1;
     const uint32_t num_lights = s.num_lights;
     // grid-stride with warp-uniform trip count so the append ballots see whole warps
@@ -205,6 +229,7 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevSce
     for (uint32_t it = 0; it < iters; ++it) {
         uint32_t i = start + it * stride;
         bool active = i < n;
+        if (active && listed) i = i < n_miss ? q.shade_list[i] : q.shade_list[q.shade_cap - 1u - (i - n_miss)];
         bool emit_shadow = false, emit_ray = false;
         float4 so = make_float4(0, 0, 0, 0), sr0 = make_float4(0, 0, 0, 0), sr1 = make_float4(0, 0, 0, 0),
                sc = make_float4(0, 0, 0, 0);
@@ -398,12 +423,15 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
                         const float4 L = q.L[path];
                         q.L[path] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
                     }
-                } else if (FP16) {
-                    reinterpret_cast<uint2*>(q.hit)[ray] =
-                        make_uint2(st.best, st.best != kNoHit ? half2_bits(st.bu, st.bv) : 0u);
                 } else {
-                    q.hit[ray] = st.best != kNoHit ? make_float4(st.best_t, __uint_as_float(st.best), st.bu, st.bv)
-                                                   : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                    if (FP16) {
+                        reinterpret_cast<uint2*>(q.hit)[ray] =
+                            make_uint2(st.best, st.best != kNoHit ? half2_bits(st.bu, st.bv) : 0u);
+                    } else {
+                        q.hit[ray] = st.best != kNoHit ? make_float4(st.best_t, __uint_as_float(st.best), st.bu, st.bv)
+                                                       : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                    }
+                    if (q.shade_list) shade_list_append(q, st.best == kNoHit, ray);
                 }
                 ray = kNoHit;
             }
@@ -558,6 +586,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
                     q.hit[ray] = best != kNoHit
                                      ? make_float4(__uint_as_float((uint32_t)(key >> 32)), __uint_as_float(best), uv.x, uv.y)
                                      : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                    if (q.shade_list) shade_list_append(q, best == kNoHit, ray);
                 }
                 ray = kNoHit;
             }
