@@ -263,6 +263,11 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
     uint32_t npix = rect.w * rect.h;
     uint32_t total = npix * nframes;
     const bool fp16 = it->desc.policy.payload == HX_PAYLOAD_FP16;
+    // the traversal and shading launches' queues: the 16-bit payload form
+    // shades in queue order (its lane-local traversal finishes rays too
+    // scattered for the shading list: -10 % on the terrain scene)
+    Queues qs = it->q;
+    if (fp16) qs.shade_list = nullptr;
     it->stats.paths += total;
     {
         StageTimer t(it, &it->stats.ms_raygen);
@@ -287,11 +292,11 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
     do {                                                                                                            \
         if (!FP16 && s.num_prims < (1u << 27))                                                                      \
             k_extend_batched<COUNT><<<it->grid_batched, kTraceThreads, 0, st>>>(                                    \
-                s, it->q, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.counters + cur, it->q.counters + 4,     \
+                s, qs, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.counters + cur, it->q.counters + 4,        \
                 kFlushTris, kFlushParked);                                                                          \
         else                                                                                                        \
             k_extend<COUNT, FP16><<<it->grid_trace, kTraceThreads, 0, st>>>(                                        \
-                s, it->q, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.p[cur], it->q.counters + cur,           \
+                s, qs, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.p[cur], it->q.counters + cur,              \
                 it->q.counters + 4);                                                                                \
     } while (0)
                 if (it->counting) {
@@ -322,11 +327,11 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
                 StageTimer t(it, &it->stats.ms_shade);
                 if (dbg)
                     k_shade<false, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces,
-                                                                                   it->desc.shadow_ray_bias, cur, it->q);
+                                                                                   it->desc.shadow_ray_bias, cur, qs);
                 else if (fp16)
-                    k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
+                    k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, qs);
                 else
-                    k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, it->q);
+                    k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, qs);
                 it->stats.kernel_launches++;
             }
         }
