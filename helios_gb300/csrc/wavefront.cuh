@@ -458,7 +458,8 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
 constexpr uint32_t kFlushTris = 24, kFlushParked = 4;
 // Node visits per loop iteration for a lane whose nodes expose no triangle:
 // spreads the warp's per-iteration queue bookkeeping over more visits
-// (measured 1: 263.7, 2: 265.7, 3: 269.2, 4: 268.0, 6: 263.1 Mpaths/s).
+// (measured 1: 263.7, 2: 265.7, 3: 269.2, 4: 268.0, 6: 263.1 Mpaths/s; with
+// the 32 KB shared-memory configuration 2: 269.7, 3: 279.2, 4: 277.0).
 constexpr uint32_t kNodeSteps = 3;
 
 // k_extend with batched triangle tests (trace.cuh, WarpTris), FP32 payloads:
