@@ -214,8 +214,10 @@ static hx_status check_status(hx_integrator* it) {
     uint32_t st = 0;
     HX_CUDA(cudaMemcpyAsync(&st, it->q.status, 4, cudaMemcpyDeviceToHost, it->ctx->stream));
     HX_CUDA(cudaStreamSynchronize(it->ctx->stream));
-    if (st & 1u) {
-        hx_set_error("BVH traversal stack overflow (status word 0x%x)", st);
+    if (st & 3u) {
+        hx_set_error((st & 1u) ? "BVH traversal stack overflow (status word 0x%x)"
+                               : "shading list does not cover the bounce's rays (status word 0x%x)",
+                     st);
         cudaMemsetAsync(it->q.status, 0, 4, it->ctx->stream);
         return HX_ERR_DEVICE;
     }

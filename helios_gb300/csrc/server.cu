@@ -200,6 +200,7 @@ struct SceneBatch {
     TableHeader* d_hdr = nullptr;
     Chunk* d_chunks = nullptr;
     char* h_table = nullptr;  // pinned: header + chunks
+    uint32_t* h_status = nullptr;  // pinned: the tick's device status word (traversal overflow, shading list)
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t done = nullptr;
     bool busy = false;
@@ -328,6 +329,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     HX_TRY(A((void**)&b->d_hdr, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks));
     b->d_chunks = (Chunk*)(b->d_hdr + 1);
     HX_CUDA(cudaMallocHost(&b->h_table, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks));
+    HX_CUDA(cudaMallocHost(&b->h_status, sizeof(uint32_t)));
+    *b->h_status = 0;
     int lo_prio = 0, hi_prio = 0;
     HX_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     HX_CUDA(cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, b->urgent ? hi_prio : lo_prio));
@@ -354,6 +357,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     cudaGraph_t g;
     HX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaMemcpyAsync(b->d_hdr, b->h_table, sizeof(TableHeader) + sizeof(Chunk) * kMaxChunks, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(b->q.status, 0, 4, st);
     k_raygen_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, P.rng, b->q);
     // bounce bo: extension rays of bo + shadow rays of bo - 1 in one launch;
     // the last launch traces the final bounce's shadow rays
@@ -376,6 +380,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     }
     k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp,
                                                          s->desc.policy.visualize_nans ? 1u : 0u, b->q.L);
+    cudaMemcpyAsync(b->h_status, b->q.status, 4, cudaMemcpyDeviceToHost, st);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (ce != cudaSuccess) {
         hx_set_error("server: graph capture failed: %s", cudaGetErrorString(ce));
@@ -391,6 +396,7 @@ static void batch_free(hx_server* s, SceneBatch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (void* p : b->allocs) hx_free(s->ctx, p);
     if (b->h_table) cudaFreeHost(b->h_table);
+    if (b->h_status) cudaFreeHost(b->h_status);
     if (b->done) cudaEventDestroy(b->done);
     if (b->finish_ev) cudaEventDestroy(b->finish_ev);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -527,8 +533,13 @@ static hx_status denoise_request(hx_server* s, SceneBatch* b, ServerRequest* r) 
 }
 
 static hx_status retire_tick(hx_server* s, SceneBatch* b) {
+    // a device-side problem in the tick (status word copied back by the graph)
+    // fails the requests that had work in it
+    const uint32_t dev_status = *b->h_status;
+    *b->h_status = 0;
     for (const PendingChunk& pc : b->running) {
         ServerRequest* r = pc.r;
+        if (dev_status) r->status = HX_ERR_DEVICE;
         r->in_flight = false;
         r->paths_traced += (uint64_t)pc.nsamples * pc.npix;
         s->admitted_work -= std::min<uint64_t>(s->admitted_work, (uint64_t)pc.nsamples * pc.npix);

@@ -220,6 +220,10 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevSce
     const bool listed = q.shade_list != nullptr;
     const uint32_t n_miss = listed ? q.counters[8] : 0u;
     const uint32_t n = listed ? min(n_miss + q.counters[9], q.counters[cur]) : q.counters[cur];
+    // every extension ray is listed exactly once as a miss or a hit; bit 1 of
+    // the status word reports a disagreement (rays would go unshaded)
+    if (listed && blockIdx.x == 0 && threadIdx.x == 0 && n_miss + q.counters[9] != q.counters[cur])
+        atomicOr(q.status, 2u);
     const int nxt = cur ^ 1;
     const uint32_t num_lights = s.num_lights;
     // grid-stride with warp-uniform trip count so the append ballots see whole warps

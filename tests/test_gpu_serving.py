@@ -30,6 +30,8 @@ def _wait_all(srv, ids, timeout=120.0, images=None):
     t0 = time.time()
     while len(done) < len(ids):
         for r in srv.poll(wait_seconds=0.5):
+            # every tick's device status word was clean
+            assert r.status == hx.HX_OK, (r.request_id, r.status)
             done[r.request_id] = r
             if images is not None:
                 images[r.request_id] = srv.fetch(r.request_id)
