@@ -15,9 +15,10 @@ constexpr int kTraceThreads = 128;
 // 8 blocks of 128 threads per SM caps the traversal kernels at 64 registers:
 // 32 resident warps instead of 28 (measured 4% faster than 72 registers;
 // 9 and 10 blocks spill and measured 0.3-2.6% slower).  The shade kernel
-// runs at the same cap (1.11 ms per frame, 1.12 ms at 72 registers).
+// runs 7 blocks per SM (73 registers; shading-list order: 0.973 ms per frame
+// vs 1.004 ms at 8 blocks and 0.998 ms at 6).
 constexpr int kTraceMinBlocks = 8;
-constexpr int kShadeMinBlocks = 8;
+constexpr int kShadeMinBlocks = 7;
 // Preferred shared-memory carve-out of the batched traversal, in percent of
 // the SM's maximum: 10 % selects the 32 KB configuration (8 blocks of 3 KB +
 // the driver's 1 KB each), the rest of the SM's memory is L1.  Without it
