@@ -45,7 +45,8 @@ HXD V3 evaluate_uber(const Surface& p, V3 Wo, V3 Wh, V3 Wi) {
     float NdotV = gmax(dot(p.normal, Wo), 0.0f);
     float NdotH = gmax(dot(p.normal, Wh), 0.0f);
     float VdotH = gmax(dot(Wi, Wh), 0.0f);
-    float f5 = powf(1.0f - VdotH, 5.0f);
+    const float x = 1.0f - VdotH, x2 = x * x;
+    float f5 = x2 * x2 * x;  // pow(1 - VdotH, 5.0) as products
     V3 F = p.F0 + (v3(1.0f) - p.F0) * f5;
     float D = D_ggx(NdotH, p.roughness * p.roughness);
     float G = G1_schlick_ggx(p.roughness, NdotL) * G1_schlick_ggx(p.roughness, NdotV);

@@ -35,11 +35,12 @@ HXD RayPre ray_prepare(V3 o, V3 d) {
     int ky = kx + 1 == 3 ? 0 : kx + 1;
     if (comp(d, kz) < 0.0f) { int t = kx; kx = ky; ky = t; }
     p.kx = kx; p.ky = ky; p.kz = kz;
-    float dz = comp(d, kz);
-    p.sx = comp(d, kx) / dz;
-    p.sy = comp(d, ky) / dz;
-    p.sz = 1.0f / dz;
     p.ix = safe_inv(d.x); p.iy = safe_inv(d.y); p.iz = safe_inv(d.z);
+    // |d_kz| is the largest component, so safe_inv(d_kz) = 1 / d_kz: the
+    // shear constants scale by it (one division per ray instead of three more)
+    p.sz = kz == 0 ? p.ix : (kz == 1 ? p.iy : p.iz);
+    p.sx = comp(d, kx) * p.sz;
+    p.sy = comp(d, ky) * p.sz;
     return p;
 }
 

@@ -979,7 +979,8 @@ template <typename R> static V3<R> evaluate_uber(const Surface<R>& p, V3<R> Wo, 
     R NdotV = gmax(dot(p.normal, Wo), R(0));
     R NdotH = gmax(dot(p.normal, Wh), R(0));
     R VdotH = gmax(dot(Wi, Wh), R(0));
-    R f5 = std::pow(R(1) - VdotH, R(5));
+    const R x = R(1) - VdotH, x2 = x * x;
+    R f5 = x2 * x2 * x;  // pow(1 - VdotH, 5.0) as products (the device's order)
     V3<R> F = p.F0 + (V3<R>(R(1)) - p.F0) * f5;
     R D = D_ggx(NdotH, p.roughness * p.roughness);
     R G = G1_schlick_ggx(p.roughness, NdotL) * G1_schlick_ggx(p.roughness, NdotV);

@@ -221,9 +221,12 @@ template <typename R> inline RayPre<R> ray_prepare(V3<R> o, V3<R> d) {
     int ky = kx + 1 == 3 ? 0 : kx + 1;
     if (d[kz] < R(0)) std::swap(kx, ky);
     p.kx = kx; p.ky = ky; p.kz = kz;
-    p.sx = d[kx] / d[kz];
-    p.sy = d[ky] / d[kz];
+    // one division: the shear constants scale by the reciprocal (the device
+    // takes it from its per-axis reciprocals; consistent for all triangles
+    // of the ray, which is what keeps the test watertight)
     p.sz = R(1) / d[kz];
+    p.sx = d[kx] * p.sz;
+    p.sy = d[ky] * p.sz;
     return p;
 }
 template <typename R>
