@@ -26,8 +26,10 @@ HXD float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 HXD V3 cross(V3 a, V3 b) { return v3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y); }
 HXD float length(V3 a) { return sqrtf(dot(a, a)); }
 HXD V3 normalize(V3 a) {
-    float l = length(a);
-    return v3(a.x / l, a.y / l, a.z / l);
+    // one division (the reciprocal length) and three products; the oracle's
+    // normalize is the same sequence
+    const float r = 1.0f / sqrtf(dot(a, a));
+    return v3(a.x * r, a.y * r, a.z * r);
 }
 // GLSL min/max/clamp (4.60 spec 8.3): min(x, y) = y < x ? y : x.
 HXD float gmin(float a, float b) { return b < a ? b : a; }

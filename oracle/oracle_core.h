@@ -52,7 +52,11 @@ template <typename R> inline V3<R> cross(V3<R> a, V3<R> b) {
 }
 template <typename R> inline R length(V3<R> a) { return std::sqrt(dot(a, a)); }
 // normalize(v) = v / length(v): three IEEE divisions by one IEEE sqrt.
-template <typename R> inline V3<R> normalize(V3<R> a) { R l = length(a); return V3<R>(a.x / l, a.y / l, a.z / l); }
+// one division (the reciprocal length) and three products, as the device
+template <typename R> inline V3<R> normalize(V3<R> a) {
+    const R r = R(1) / std::sqrt(dot(a, a));
+    return V3<R>(a.x * r, a.y * r, a.z * r);
+}
 // GLSL min/max: min(x, y) = y < x ? y : x (GLSL 4.60 spec 8.3).
 template <typename R> inline R gmin(R a, R b) { return b < a ? b : a; }
 template <typename R> inline R gmax(R a, R b) { return a < b ? b : a; }
