@@ -21,7 +21,11 @@ HXD V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
 HXD V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
 HXD V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
 HXD V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
-HXD V3 operator/(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+// vector / scalar as one division and three products (the oracle's operator/ is the same)
+HXD V3 operator/(V3 a, float s) {
+    const float r = 1.0f / s;
+    return v3(a.x * r, a.y * r, a.z * r);
+}
 HXD float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 HXD V3 cross(V3 a, V3 b) { return v3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y); }
 HXD float length(V3 a) { return sqrtf(dot(a, a)); }

@@ -45,7 +45,11 @@ template <typename R> inline V3<R> operator*(V3<R> a, V3<R> b) { return V3<R>(a.
 template <typename R> inline V3<R> operator/(V3<R> a, V3<R> b) { return V3<R>(a.x / b.x, a.y / b.y, a.z / b.z); }
 template <typename R> inline V3<R> operator*(V3<R> a, R s) { return V3<R>(a.x * s, a.y * s, a.z * s); }
 template <typename R> inline V3<R> operator*(R s, V3<R> a) { return V3<R>(s * a.x, s * a.y, s * a.z); }
-template <typename R> inline V3<R> operator/(V3<R> a, R s) { return V3<R>(a.x / s, a.y / s, a.z / s); }
+// vector / scalar as one division and three products, as the device
+template <typename R> inline V3<R> operator/(V3<R> a, R s) {
+    const R r = R(1) / s;
+    return V3<R>(a.x * r, a.y * r, a.z * r);
+}
 template <typename R> inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 template <typename R> inline V3<R> cross(V3<R> a, V3<R> b) {
     return V3<R>(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
