@@ -187,3 +187,50 @@ def test_oracle_srgb_texture_decode():
         hit = np.any(alb[..., :3] != 0, axis=-1)
         assert hit.mean() > 0.3
         assert np.all(alb[hit][:, :3] == want[srgb]), (srgb, np.unique(alb[hit][:, :3]))
+
+
+def test_oracle_albedo_view_reproduces_material_albedos():
+    """The oracle's output-buffer view (debug_visualization.frag fetch_albedo)
+    on the untextured box: every hit pixel holds exactly one of the scene's
+    material albedos, the clear colour elsewhere; roughness likewise."""
+    hs = hx.HostScene(hx.SCENE_BOX)
+    osc = ob.OracleScene(hs)
+    d = hs.desc.contents
+    mats = [d.materials[k] for k in range(d.num_materials)]
+    albedos = {tuple(np.float32(m.albedo[c]) for c in range(3)) for m in mats}
+    rough = {np.float32(m.roughness_metallic[0]) for m in mats}
+    W, H = 48, 40
+    f = hx.frame_desc(hs.camera(), W, H)
+    alb = osc.output_view(f, W, H, hx.OUTPUT_ALBEDO)
+    rgh = osc.output_view(f, W, H, hx.OUTPUT_ROUGHNESS)
+    hit = np.any(alb[..., :3] != 0, axis=-1)
+    assert hit.mean() > 0.5 and np.all(alb[..., 3] == 1.0)
+    assert {tuple(p) for p in alb[hit][:, :3].tolist()} <= {tuple(float(x) for x in a) for a in albedos}
+    assert set(np.unique(rgh[hit][:, 0]).tolist()) <= {float(r) for r in rough}
+
+
+def test_oracle_visualize_nans_marks_the_nan_surface():
+    """VISUALIZE_NANS in the oracle: a quad whose material emits NaN turns
+    exactly its covered pixels (1, 0, 0); the rest stays black (no lights)."""
+    from tests.helpers import TriangleSoupScene, integrator_desc
+    q = np.array([[[-1, -1, 0], [1, -1, 0], [1, 1, 0]], [[-1, -1, 0], [1, 1, 0], [-1, 1, 0]]], np.float32)
+    soup = TriangleSoupScene(q)
+    soup._mat[0].emissive[0] = float("nan")
+    cam = hx.Camera()
+    cam.position[:] = [0.0, 0.0, 4.0]
+    cam.target[:] = [0.0, 0.0, 0.0]
+    cam.up[:] = [0.0, 1.0, 0.0]
+    cam.fov_y_degrees, cam.near_plane, cam.far_plane = 60.0, 1.0, 1000.0
+    cam.focal_length, cam.aperture_radius = 8.0, 0.0
+    osc = ob.OracleScene(soup)
+    W, H = 32, 24
+    f = hx.frame_desc(cam, W, H)
+    d = integrator_desc(W, H, bounces=2, policy="reference")
+    d.policy.visualize_nans = 1
+    img, _ = osc.render(d, f, 1)
+    red = np.all(img == np.array([1.0, 0.0, 0.0]), axis=1)
+    assert 0.1 < red.mean() < 0.9
+    assert np.all(img[~red] == 0.0)
+    d.policy.visualize_nans = 0
+    raw, _ = osc.render(d, f, 1)
+    assert np.array_equal(np.isnan(raw[:, 0]), red)
