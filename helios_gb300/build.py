@@ -85,18 +85,6 @@ def build_oracle():
     return os.path.join(d, "liboracle.so")
 
 
-def build_reference_checks():
-    """Builds oracle/_ref from the reference tree when it is present."""
-    ref = os.environ.get("HELIOS_REFERENCE", "/root/reference")
-    if not os.path.isdir(ref):
-        return None
-    r = subprocess.run(["sh", os.path.join(ROOT, "oracle", "hosek", "build_ref.sh")], cwd=ROOT,
-                       capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("reference Hosek check failed:\n" + r.stdout + r.stderr)
-    return os.path.join(ROOT, "oracle", "_ref", "hosek_ref")
-
-
 if __name__ == "__main__":
     build_library(force="--force" in sys.argv, verbose=True)
     build_driver()

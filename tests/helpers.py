@@ -217,3 +217,184 @@ def checker_texture(size=32, a=(200, 180, 150), b=(40, 60, 90)):
     sel = ((x // 4 + y // 4) % 2 == 0)[..., None]
     rgba = np.where(sel, np.array(a + (255,), np.uint8), np.array(b + (255,), np.uint8)).astype(np.uint8)
     return rgba
+
+
+def _mat(model):
+    """(model, normal) matrices as column-major float lists; normal = inverse transpose."""
+    m = np.asarray(model, np.float64)
+    n = np.eye(4)
+    n[:3, :3] = np.linalg.inv(m[:3, :3]).T
+    return m.T.reshape(-1).tolist(), n.T.reshape(-1).tolist()
+
+
+def _rot_y(deg):
+    c, s = np.cos(np.radians(deg)), np.sin(np.radians(deg))
+    return np.array([[c, 0, s, 0], [0, 1, 0, 0], [-s, 0, c, 0], [0, 0, 0, 1]])
+
+
+def _translate_scale(t, s=1.0):
+    m = np.eye(4)
+    m[:3, :3] *= s
+    m[:3, 3] = t
+    return m
+
+
+class LightsScene:
+    """A small scene that exercises every light type and surface path of the
+    reference's closest-hit shader: a textured (sRGB albedo, tangent-space
+    normal map) floor, two instances of a GGX box mesh (rotated and scaled),
+    an emissive quad (area light), an alpha-tested quad (non-opaque submesh,
+    any-hit), and a point, a spot (distinct cone edges) and a directional
+    light, with a small lat-long environment.  .desc points at its
+    hx_scene_desc (arrays kept alive); .camera() frames it."""
+
+    def __init__(self, spot_equal_edges=False, env=True):
+        self._keep = []
+        verts, idx, subs = [], [], []
+
+        def vtx(p, n, uv, t=(1, 0, 0), b=(0, 0, 1), w=0.0):
+            v = hx.Vertex()
+            v.position[:] = [p[0], p[1], p[2], w]
+            v.normal[:] = [n[0], n[1], n[2], 0.0]
+            v.tex_coord[:] = [uv[0], uv[1], 0.0, 0.0]
+            v.tangent[:] = [t[0], t[1], t[2], 0.0]
+            v.bitangent[:] = [b[0], b[1], b[2], 0.0]
+            return v
+
+        def quad(c, u, v, n, uv_scale=1.0):
+            c, u, v = np.asarray(c, float), np.asarray(u, float), np.asarray(v, float)
+            ps = [c - u - v, c + u - v, c + u + v, c - u + v]
+            uvs = [(0, 0), (uv_scale, 0), (uv_scale, uv_scale), (0, uv_scale)]
+            tu, tv = u / np.linalg.norm(u), v / np.linalg.norm(v)
+            return [vtx(p, n, q, tu, tv) for p, q in zip(ps, uvs)], [0, 2, 1, 0, 3, 2]
+
+        meshes = []
+        # mesh 0: floor (material 0: sRGB checker albedo + normal map)
+        vs, ix = quad((0, 0, 0), (3, 0, 0), (0, 0, 3), (0, 1, 0), uv_scale=3.0)
+        meshes.append((vs, ix, [(0, 6, 0, 0)]))
+        # mesh 1: unit box (material 1: GGX metal)
+        bv, bi = [], []
+        for ax in range(3):
+            for sgn in (-1, 1):
+                n = np.zeros(3)
+                n[ax] = sgn
+                u = np.zeros(3)
+                u[(ax + 1) % 3] = 0.5
+                v = np.zeros(3)
+                v[(ax + 2) % 3] = 0.5 * sgn
+                qv, qi = quad(n * 0.5, u, v, n)
+                bi += [k + len(bv) for k in qi]
+                bv += qv
+        meshes.append((bv, bi, [(0, 36, 1, 0)]))
+        # mesh 2: emissive quad facing down (material 2), position.w = 0 (submesh index)
+        vs, ix = quad((0.2, 2.4, 0.3), (0.3, 0, 0), (0, 0, -0.25), (0, -1, 0))
+        meshes.append((vs, ix, [(0, 6, 2, 0)]))
+        # mesh 3: alpha-tested upright quad (material 3, non-opaque)
+        vs, ix = quad((0, 1.0, -1.5), (1.2, 0, 0), (0, 1.0, 0), (0, 0, 1), uv_scale=2.0)
+        meshes.append((vs, ix, [(0, 6, 3, HX_NON_OPAQUE)]))
+
+        self._mesh = (hx.MeshDesc * len(meshes))()
+        for k, (vs, ix, sm) in enumerate(meshes):
+            va = (hx.Vertex * len(vs))(*vs)
+            ia = (C.c_uint32 * len(ix))(*ix)
+            sa = (hx.Submesh * len(sm))()
+            for j, (base, cnt, mat, fl) in enumerate(sm):
+                sa[j].base_index, sa[j].index_count, sa[j].material, sa[j].flags = base, cnt, mat, fl
+            self._keep += [va, ia, sa]
+            m = self._mesh[k]
+            m.vertices, m.num_vertices = va, len(vs)
+            m.indices, m.num_indices = ia, len(ix)
+            m.submeshes, m.num_submeshes = sa, len(sm)
+
+        checker = checker_texture(32)
+        normal = bump_normal_map(32, freq=2, amp=0.3)
+        alpha = checker_texture(32, a=(230, 120, 60), b=(60, 160, 220)).copy()
+        yy, xx = np.mgrid[0:32, 0:32]
+        alpha[..., 3] = np.where(((xx // 8) + (yy // 8)) % 2 == 0, 255, 0)
+        self._tex_data = [checker, normal, alpha]
+        self._tex = (hx.TextureDesc * 3)()
+        for k, t in enumerate(self._tex_data):
+            self._tex[k].rgba8 = t.ctypes.data_as(C.POINTER(C.c_uint8))
+            self._tex[k].height, self._tex[k].width = t.shape[0], t.shape[1]
+            self._tex[k].srgb = 1 if k in (0, 2) else 0
+            self._tex[k].format = 0
+
+        mats = [dict(tex0=(0, 1, -1, -1), albedo=(1, 1, 1, 1), rm=(0.6, 0.2)),
+                dict(tex0=(-1, -1, -1, -1), albedo=(0.8, 0.6, 0.3, 1), rm=(0.3, 0.8)),
+                dict(tex0=(-1, -1, -1, -1), albedo=(0.9, 0.9, 0.9, 1), rm=(0.5, 0.0), emissive=(6.0, 5.0, 4.0)),
+                dict(tex0=(2, -1, -1, -1), albedo=(1, 1, 1, 1), rm=(0.4, 0.0))]
+        self._mat = (hx.Material * len(mats))()
+        for k, md in enumerate(mats):
+            m = self._mat[k]
+            for j in range(4):
+                m.texture_indices0[j] = md["tex0"][j]
+                m.texture_indices1[j] = -1
+            m.albedo[:] = list(md["albedo"])
+            m.emissive[:] = list(md.get("emissive", (0, 0, 0))) + [0.0]
+            m.roughness_metallic[0], m.roughness_metallic[1] = md["rm"]
+
+        inst = [(0, np.eye(4)), (1, _translate_scale((-1.0, 0.5, 0.0)) @ _rot_y(30.0)),
+                (1, _translate_scale((1.1, 0.25, 0.8), 0.5) @ _rot_y(-20.0)), (2, np.eye(4)), (3, np.eye(4))]
+        self._inst = (hx.Instance * len(inst))()
+        for k, (mesh, model) in enumerate(inst):
+            mm, nm = _mat(model)
+            self._inst[k].model_matrix[:] = mm
+            self._inst[k].normal_matrix[:] = nm
+            self._inst[k].mesh_index = mesh
+            self._inst[k].material_override = -1
+
+        self._light = (hx.Light * 3)()
+        pt, sp, di = self._light[0], self._light[1], self._light[2]
+        pt.data0[:] = [float(hx.LIGHT_POINT), 1.0, 0.9, 0.8]
+        pt.data1[3] = 6.0
+        pt.data2[:] = [0.5, 2.0, 1.0, 0.05]
+        sdir = np.array([1.0, -2.5, -1.5])
+        sdir /= np.linalg.norm(sdir)
+        sp.data0[:] = [float(hx.LIGHT_SPOT), 0.6, 0.8, 1.0]
+        sp.data1[:] = [float(sdir[0]), float(sdir[1]), float(sdir[2]), 15.0]
+        sp.data2[:] = [-1.5, 2.5, 1.5, 0.05]
+        sp.data3[0], sp.data3[1] = (0.9, 0.9) if spot_equal_edges else (0.95, 0.85)
+        ddir = np.array([-0.3, -1.0, -0.2])
+        ddir /= np.linalg.norm(ddir)
+        di.data0[:] = [float(hx.LIGHT_DIRECTIONAL), 1.0, 0.95, 0.9]
+        di.data1[:] = [float(ddir[0]), float(ddir[1]), float(ddir[2]), 2.0]
+        di.data2[3] = 0.02
+
+        self._desc = hx.SceneDesc()
+        d = self._desc
+        d.meshes, d.num_meshes = self._mesh, len(meshes)
+        d.instances, d.num_instances = self._inst, len(inst)
+        d.materials, d.num_materials = self._mat, len(mats)
+        d.textures, d.num_textures = self._tex, 3
+        d.punctual_lights, d.num_punctual_lights = self._light, 3
+        if env:
+            ew, eh = 64, 32
+            v = (np.arange(eh) + 0.5) / eh
+            u = (np.arange(ew) + 0.5) / ew
+            e = np.zeros((eh, ew, 4), np.float32)
+            e[..., 0] = 0.25 + 0.2 * np.cos(np.pi * v)[:, None]
+            e[..., 1] = 0.3 + 0.1 * np.sin(2 * np.pi * u)[None, :]
+            e[..., 2] = 0.5 + 0.3 * np.cos(np.pi * v)[:, None]
+            e[..., 3] = 1.0
+            self._env = np.ascontiguousarray(e)
+            d.environment.kind = hx.ENV_EQUIRECT
+            d.environment.width, d.environment.height = ew, eh
+            d.environment.rgba32f = self._env.ctypes.data_as(C.POINTER(C.c_float))
+        else:
+            d.environment.kind = 0
+
+    @property
+    def desc(self):
+        return C.pointer(self._desc)
+
+    def camera(self, aperture=0.0, focal_length=8.0):
+        cam = hx.Camera()
+        cam.position[:] = [0.3, 2.2, 4.5]
+        cam.target[:] = [0.0, 0.6, 0.0]
+        cam.up[:] = [0.0, 1.0, 0.0]
+        cam.fov_y_degrees, cam.near_plane, cam.far_plane = 45.0, 1.0, 1000.0
+        cam.focal_length, cam.aperture_radius = focal_length, aperture
+        return cam
+
+
+HX_NON_OPAQUE = 1
