@@ -177,6 +177,20 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def load_peaks():
+    """Roofline denominators: MEASURED_PEAKS.json when present, else the
+    pool's fallback figures (6.8 TB/s copy bandwidth, 1.9 / 1.7 PFLOP/s BF16
+    burst / sustained), with the source named."""
+    try:
+        p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return {"hbm_gbs": float(p["hbm_gbs"]), "bf16_tflops": float(p["bf16_tflops"]),
+                "bf16_tflops_sustained": float(p.get("bf16_tflops_sustained", p["bf16_tflops"])),
+                "source": "of measured (MEASURED_PEAKS.json)"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "source": "of fallback (MEASURED_PEAKS.json absent)"}
+
+
 def cpu_sample(hs, hx, pol, seconds, threads=0):
     """Oracle (scalar FP32 transcription of the reference shaders) on whole
     image rows of the same frame (wrapping around the frame) until the time
@@ -326,12 +340,8 @@ def run_ours(args, dist):
     launches_e2e = launches + args.steps  # + one tone-map launch per step
     out.close()
 
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peaks = load_peaks()
+    hbm_peak = peaks["hbm_gbs"]
     achieved = alg_bytes_per_launch / (ms_trace_per_launch / 1000.0) / 1e9
     traffic = None
     try:
@@ -355,7 +365,8 @@ def run_ours(args, dist):
         line = {"metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": dist.world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(workload_config(), parallelism="replicas" if dist.world > 1 else "single"),
+                "config": workload_config(),
+                "parallelism": "replicas" if dist.world > 1 else "single",
                 "mray_segments_per_s": seg_rate,
                 "frame_latency_ms": {"p50": float(np.percentile(fs, 50)), "p99": float(np.percentile(fs, 99)),
                                      "max": fs[-1]},
@@ -369,7 +380,7 @@ def run_ours(args, dist):
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                              "frac": achieved / hbm_peak, "traffic": traffic,
                              "kernel": "k_extend (closest hit + shadow)",
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                             "peak_source": peaks["source"],
                              "bytes_per_launch": alg_bytes_per_launch, "ms_per_launch": ms_trace_per_launch,
                              "node_fetches_per_segment": ct.node_visits / max(1, ext_rays + sh_rays),
                              "tri_tests_per_segment": ct.tri_tests / max(1, ext_rays + sh_rays),
@@ -404,8 +415,7 @@ def run_serving(args, dist):
         dn.set_params(np_.load(wpath))
         weights = "trained (helios_gb300/weights/denoiser.npy)"
     else:
-        from oracle import denoiser_ref as dr
-        dn.set_params(dr.init_params(0))
+        dn.init_params(0)
         weights = "seeded initial weights (latency does not depend on the weights)"
     srv.set_denoiser(dn)
     pool = []
@@ -428,6 +438,7 @@ def run_serving(args, dist):
     n_req = int(args.rate * args.duration)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n_req))
     meta = {}
+    submit_t = {}
     results = []
     start = time.perf_counter()
     s0 = srv.stats()
@@ -444,6 +455,7 @@ def run_serving(args, dist):
             denoise = int(rng.random() < 0.5)
             rid = srv.submit(sid, hx.frame_desc(cam, w, h), w, h, spp, user_tag=i, denoise=bool(denoise))
             meta[rid] = (w, h, spp, denoise, sid)
+            submit_t[rid] = time.perf_counter() - start
             i += 1
         for r in srv.poll(wait_seconds=0.0005):
             results.append(r)
@@ -460,22 +472,47 @@ def run_serving(args, dist):
     def pct(v, q):
         return float(np.percentile(v, q)) if len(v) else None
 
-    lat = [r.latency_ms for r in results]
+    # every submitted request counts: one unfinished at the window's end is
+    # right-censored at (window end - its submit time), a lower bound of its
+    # latency; a percentile that lands on a censored value is reported as a
+    # lower bound ("censored": true)
+    done_ids = {r.request_id for r in results}
+    samples = [(r.request_id, r.latency_ms, False) for r in results]
+    samples += [(rid, (elapsed - submit_t[rid]) * 1000.0, True) for rid in meta if rid not in done_ids]
+
+    def pct_c(v, q):
+        if not v:
+            return None
+        v = sorted(v)
+        k = min(len(v) - 1, int(np.ceil(q / 100.0 * len(v))) - 1)
+        return {"ms": v[k][0], "censored": v[k][1]}
+
+    lat_all = [(ms, c) for _, ms, c in samples]
     classes = {}
+    classes_all = {}
     queue = {}
+    lat = [r.latency_ms for r in results]
     for r in results:
         w, h, spp, dz, sid = meta[r.request_id]
         if dz:
             classes.setdefault("%dx%d/%dspp/denoise" % (w, h, spp), []).append(r.latency_ms)
         classes.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.latency_ms)
         queue.setdefault("%dx%d/%dspp" % (w, h, spp), []).append(r.queue_ms)
+    for rid, ms, c in samples:
+        w, h, spp, dz, sid = meta[rid]
+        classes_all.setdefault("%dx%d/%dspp" % (w, h, spp), []).append((ms, c))
     offered = sum(w * h * spp for (w, h, spp, dn, sid) in meta.values())
     line = {"metric": "serving latency p50/p99 (ms) and Mpaths/s", "mode": "serving", "n_gpus": 1,
             "rate_req_per_s": args.rate, "duration_s": args.duration, "requests_submitted": n_req,
             "requests_completed": len(results), "scenes": args.scenes, "scene_build_s": build_s,
             "throughput_mpaths_per_s": paths / elapsed / 1e6, "offered_mpaths_per_s": offered / args.duration / 1e6,
             "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+            "latency_ms_all_submitted": {"p50": pct_c(lat_all, 50), "p99": pct_c(lat_all, 99),
+                                         "censored": len(samples) - len(results)},
             "per_class_latency_ms": {k: {"n": len(v), "p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(classes.items())},
+            "per_class_latency_ms_all_submitted": {
+                k: {"submitted": len(v), "unfinished": sum(1 for _, c in v if c), "p50": pct_c(v, 50),
+                    "p99": pct_c(v, 99)} for k, v in sorted(classes_all.items())},
             "per_class_admission_wait_ms": {k: {"p50": pct(v, 50), "p99": pct(v, 99)} for k, v in sorted(queue.items())},
             "tick_paths": args.tick_paths, "long_tick_paths": args.long_tick_paths,
             "concurrent_ticks": args.concurrent_ticks, "arena_gb": args.arena_gb,
@@ -558,19 +595,6 @@ def run_precision(args, dist):
     print(json.dumps(out), flush=True)
 
 
-def conv_flops_per_pixel():
-    """Forward FLOPs per full-resolution pixel of the denoiser network
-    (2 * 9 * cin * N per output pixel of each convolution, N = MMA width)."""
-    from oracle import denoiser_ref as dr
-    lev = {"x": 0, "a0": 0, "p0": 1, "p1": 2, "p2": 3, "p3": 4, "a4": 4, "u3": 3, "u2": 2, "u1": 1, "u0": 0,
-           "d0": 0, "d0b": 0}
-    tot = 0.0
-    for (_, srcs, cout, _), (ci, co) in zip(dr.LAYERS, dr.layer_shapes()):
-        n = (co + 15) // 16 * 16
-        tot += 2.0 * 9 * ci * n / 4 ** lev[srcs[0][0]]
-    return tot
-
-
 def run_denoise(args, dist):
     """Learned denoiser: data from this tracer, training by the library's own
     tensor-core kernels, then time-to-RMSE at 1920x1080 on held-out variants
@@ -578,15 +602,17 @@ def run_denoise(args, dist):
     import numpy as np
     import helios_gb300 as hx
     from helios_gb300 import denoise_train as T
-    from oracle import denoiser_ref as dr
     ctx = hx.Context(dist.local)
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    peaks = load_peaks()
+    probe = hx.Denoiser(ctx)
+    nparams = probe.num_params
+    probe.close()
     kw = dict(quads=100000, level=6, env=(1024, 512), mask_pool=16, mask_size=256)
     out = {"mode": "denoise", "metric": "time-to-RMSE speed-up vs plain accumulation", "n_gpus": 1,
            "data": "synthetic: seeded variants of the icosphere scene (transforms, materials, lights, masks, sun "
                    "U(10,80) deg, orbit camera); 100k alpha quads, 16 masks 256^2, 1024x512 sky",
            "network": "5-level U-Net, 3x3 convs 32->128 ch, skips; BF16 weights/activations, FP32 accumulate "
-                      "(tcgen05/TMEM); %d parameters" % dr.num_params()}
+                      "(tcgen05/TMEM); %d parameters" % nparams}
     spp_in = [1, 2, 4, 8, 16, 32, 64]
     seeds = list(range(1000, 1000 + args.dn_variants))
     data = T.render_pairs(ctx, seeds, 256, 256, spp_in, args.dn_target_spp, bounces=DEPTH, scene_kw=kw,
@@ -598,7 +624,7 @@ def run_denoise(args, dist):
     nets, out["training"] = {}, {}
     for loss in args.dn_losses:
         dn = hx.Denoiser(ctx)
-        dn.set_params(dr.init_params(0))
+        dn.init_params(0)
         t0 = time.time()
         e0.record()
         if loss == "hybrid":
@@ -615,7 +641,7 @@ def run_denoise(args, dist):
         e1.record()
         ctx.synchronize()
         train_ms = e0.elapsed_ms(e1)
-        step_flops = 3.0 * conv_flops_per_pixel() * 16 * 256 * 256
+        step_flops = 3.0 * hx.denoiser_conv_flops_per_pixel() * 16 * 256 * 256
         out["training"][loss] = {"steps": args.dn_steps, "batch": 16, "adam_lr": [1e-3, 1e-4],
                                  "wall_s": round(time.time() - t0, 1), "ms_per_step": train_ms / args.dn_steps,
                                  "conv_tflops": step_flops / (train_ms / args.dn_steps * 1e-3) / 1e12,
@@ -711,13 +737,13 @@ def run_denoise(args, dist):
         evals.append(res)
         it.close()
         sc.close()
-    flops = conv_flops_per_pixel() * W * ((H + 15) // 16 * 16)
+    flops = hx.denoiser_conv_flops_per_pixel() * W * ((H + 15) // 16 * 16)
     infer_ms = statistics.median(e["infer_ms"] for e in evals)
     out["eval"] = evals
     out["roofline"] = {"bound": "tensor", "kernel": "k_conv (forward, all 13 layers)",
                        "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                        "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
-                       "flops_per_1080p_inference": flops, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
+                       "flops_per_1080p_inference": flops, "peak_source": peaks["source"] + ", bf16 burst"}
     best = None
     for k in nets:
         speed = [e[k]["speedup_vs_plain_256"] for e in evals if e[k]["speedup_vs_plain_256"]]

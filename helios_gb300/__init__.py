@@ -143,7 +143,8 @@ class ProceduralParams(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("num_alpha_quads", C.c_uint32),
                 ("mask_pool", C.c_uint32), ("mask_size", C.c_uint32), ("icosphere_level", C.c_uint32),
                 ("env_width", C.c_uint32), ("env_height", C.c_uint32), ("sun_elevation_deg", C.c_float),
-                ("turbidity", C.c_float), ("terrain_size", C.c_uint32), ("num_spheres", C.c_uint32)]
+                ("turbidity", C.c_float), ("terrain_size", C.c_uint32), ("num_spheres", C.c_uint32),
+                ("ground_albedo", C.c_float)]
 
 
 class ServerDesc(C.Structure):
@@ -167,7 +168,8 @@ class RequestResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("ticks", C.c_uint64), ("requests_done", C.c_uint64),
                 ("requests_pending", C.c_uint64), ("requests_active", C.c_uint64), ("arena_bytes", C.c_uint64),
-                ("arena_used", C.c_uint64), ("seconds", C.c_double), ("requests_denoised", C.c_uint64)]
+                ("arena_used", C.c_uint64), ("seconds", C.c_double), ("requests_denoised", C.c_uint64),
+                ("requests_active_peak", C.c_uint64), ("arena_used_peak", C.c_uint64)]
 
 
 BVH8_NODE_BYTES = 80
@@ -191,6 +193,7 @@ _SIGS = {
     "hx_scene_upload": (C.c_int, [_P, C.POINTER(SceneDesc), C.POINTER(_P)]),
     "hx_scene_destroy": (C.c_int, [_P]),
     "hx_scene_info_get": (C.c_int, [_P, C.POINTER(SceneInfo)]),
+    "hx_scene_set_traversal_stack_limit": (C.c_int, [_P, C.c_uint32]),
     "hx_scene_lights": (C.c_int, [_P, C.POINTER(Light), C.c_uint32, C.POINTER(C.c_uint32)]),
     "hx_scene_export_bvh": (C.c_int, [_P, _P, _P, _P, _P, _P]),
     "hx_scene_trace": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P]),
@@ -227,6 +230,7 @@ _SIGS = {
     "hx_server_submit": (C.c_int, [_P, C.POINTER(RequestDesc), C.POINTER(C.c_uint64)]),
     "hx_server_poll": (C.c_int, [_P, C.POINTER(RequestResult), C.c_uint32, C.POINTER(C.c_uint32), C.c_double]),
     "hx_server_fetch": (C.c_int, [_P, C.c_uint64, _P]),
+    "hx_server_cancel": (C.c_int, [_P, C.c_uint64]),
     "hx_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "hx_server_destroy": (C.c_int, [_P]),
     "hx_integrator_primary_hits": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
@@ -238,6 +242,7 @@ _SIGS = {
     "hx_host_scene_camera": (C.c_int, [_P, C.POINTER(Camera)]),
     "hx_host_scene_destroy": (C.c_int, [_P]),
     "hx_hosek_wilkie_coefficients": (C.c_int, [C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_float)]),
+    "hx_hosek_wilkie_sky": (C.c_int, [_P, C.c_float, C.c_float, C.c_float, _P]),
     "hx_device_alloc": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
     "hx_device_free": (C.c_int, [_P, _P]),
     "hx_device_copy": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_uint32]),
@@ -254,6 +259,8 @@ _SIGS = {
                                          C.POINTER(C.c_float)]),
     "hx_denoiser_infer": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
     "hx_denoiser_check": (C.c_int, [_P]),
+    "hx_denoiser_set_wait_budget": (C.c_int, [_P, C.c_uint64]),
+    "hx_denoiser_init_params": (C.c_int, [_P, C.c_uint64]),
     "hx_denoiser_read_tensor": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, C.c_uint64]),
     "hx_denoiser_read_output": (C.c_int, [_P, C.c_uint32, _P, C.c_uint64]),
     "hx_integrator_features": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
@@ -317,10 +324,10 @@ def frame_desc(camera, width, height):
     return f
 
 
-def hosek_wilkie_coefficients(sun_direction, turbidity=3.0, normalized_sun_y=1.15):
+def hosek_wilkie_coefficients(sun_direction, turbidity=3.0, normalized_sun_y=1.15, albedo=0.1):
     d = (C.c_float * 3)(*sun_direction)
     out = (C.c_float * 40)()
-    check(lib().hx_hosek_wilkie_coefficients(d, turbidity, normalized_sun_y, out))
+    check(lib().hx_hosek_wilkie_sky(d, turbidity, albedo, normalized_sun_y, out))
     return np.array(out[:], dtype=np.float32).reshape(10, 4)[:, :3]
 
 
@@ -473,6 +480,10 @@ class Scene:
         i = SceneInfo()
         check(lib().hx_scene_info_get(self.handle, C.byref(i)))
         return i
+
+    def set_traversal_stack_limit(self, entries):
+        """Diagnostic: stack entries a ray may use (1..32, default 32)."""
+        check(lib().hx_scene_set_traversal_stack_limit(self.handle, entries))
 
     def lights(self):
         n = C.c_uint32()
@@ -684,6 +695,24 @@ DENOISER_TENSORS = [("x", 32, 0), ("a0", 32, 0), ("a0b", 32, 0), ("p0", 32, 1), 
                     ("a2", 64, 2), ("p2", 64, 3), ("a3", 96, 3), ("p3", 96, 4), ("a4", 128, 4), ("a4b", 128, 4),
                     ("u3", 128, 3), ("d3", 96, 3), ("u2", 96, 2), ("d2", 64, 2), ("u1", 64, 1), ("d1", 64, 1),
                     ("u0", 64, 0), ("d0", 32, 0), ("d0b", 32, 0), ("gy", 32, 0)]
+# Denoiser convolutions in network order: (input tensors, output channels)
+DENOISER_LAYERS = [(("x",), 32), (("a0",), 32), (("p0",), 64), (("p1",), 64), (("p2",), 96), (("p3",), 128),
+                   (("a4",), 128), (("u3", "a3"), 96), (("u2", "a2"), 64), (("u1", "a1"), 64), (("u0", "a0b"), 32),
+                   (("d0",), 32), (("d0b",), 3)]
+
+
+def denoiser_conv_flops_per_pixel():
+    """Forward FLOPs of the denoiser per full-resolution pixel: 2 * 9 * cin * N
+    per output pixel of each convolution (N = output channels rounded up to the
+    MMA width of 16), at that convolution's level (1 / 4 per level)."""
+    info = {n: (c, lev) for n, c, lev in DENOISER_TENSORS}
+    tot = 0.0
+    for srcs, cout in DENOISER_LAYERS:
+        cin = sum(info[s][0] for s in srcs)
+        tot += 2.0 * 9 * cin * ((cout + 15) // 16 * 16) / 4 ** info[srcs[0]][1]
+    return tot
+
+
 FEATURE_CHANNELS = 12
 DN_LOSS_L1_LOG, DN_LOSS_L2_LINEAR = 0, 1
 
@@ -703,6 +732,10 @@ class Denoiser:
         check(lib().hx_denoiser_num_params(h, C.byref(n)))
         self.num_params = n.value
         self._shape = {}
+
+    def init_params(self, seed=0):
+        """He-uniform untrained weights, zero biases (hx_denoiser_init_params)."""
+        check(lib().hx_denoiser_init_params(self.handle, seed))
 
     def set_params(self, params):
         p = np.ascontiguousarray(params, dtype=np.float32)
@@ -744,6 +777,10 @@ class Denoiser:
 
     def check(self):
         check(lib().hx_denoiser_check(self.handle))
+
+    def set_wait_budget(self, cycles):
+        """Diagnostic: clock cycles each tensor-core pipeline wait may take (0 = default)."""
+        check(lib().hx_denoiser_set_wait_budget(self.handle, cycles))
 
     def read_tensor(self, name, training=True, gradient=False):
         idx = [t[0] for t in DENOISER_TENSORS].index(name)
@@ -813,6 +850,9 @@ class Server:
         n = C.c_uint32()
         check(lib().hx_server_poll(self.handle, arr, capacity, C.byref(n), wait_seconds))
         return [arr[i] for i in range(n.value)]
+
+    def cancel(self, request_id):
+        check(lib().hx_server_cancel(self.handle, request_id))
 
     def fetch(self, request_id):
         w, h = self.sizes.pop(request_id)

@@ -672,7 +672,8 @@ hx_status hx_build_bvh(hx_context* ctx, hx_scene* s, const float* d_world, uint3
     k_centroid_bounds<<<bnd_blocks, kThreads, 0, st>>>(d_world, n, partial);
     k_bounds_final<<<1, 32, 0, st>>>(partial, bnd_blocks, bounds);
     k_morton<<<blocks_for(n), kThreads, 0, st>>>(d_world, n, bounds, morton, keys, vals);
-    hx_radix_sort_pairs(keys, vals, (uint32_t*)(base + o_keys2), (uint32_t*)(base + o_vals2), n, 30, base + o_sort, st);
+    HX_CUDA(hx_radix_sort_pairs(keys, vals, (uint32_t*)(base + o_keys2), (uint32_t*)(base + o_vals2), n, 30,
+                                base + o_sort, st));
     HX_CUDA(cudaMemcpyAsync(sorted, vals, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
     HX_CUDA(cudaMemsetAsync(pleaf, 0xff, 4 * (size_t)n, st));
     HX_CUDA(cudaMemsetAsync(tot, 0, 16, st));
@@ -828,8 +829,8 @@ extern "C" hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n,
     k_centroid_bounds<<<bnd_blocks, kThreads, 0, st>>>(d_world_tris, n, partial);
     k_bounds_final<<<1, 32, 0, st>>>(partial, bnd_blocks, bounds);
     k_morton<<<blocks_for(n), kThreads, 0, st>>>(d_world_tris, n, bounds, d_morton, keys, vals);
-    hx_radix_sort_pairs(keys, vals, (uint32_t*)(b + kNoAllocOffKeys2), (uint32_t*)(b + kNoAllocOffVals2), n, 30,
-                        b + kNoAllocOffRadix, st);
+    HX_CUDA(hx_radix_sort_pairs(keys, vals, (uint32_t*)(b + kNoAllocOffKeys2), (uint32_t*)(b + kNoAllocOffVals2), n,
+                                30, b + kNoAllocOffRadix, st));
     HX_CUDA(cudaMemcpyAsync(d_sorted, vals, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
     HX_CUDA(cudaGetLastError());
     return HX_OK;

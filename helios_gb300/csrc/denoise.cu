@@ -74,6 +74,7 @@ struct ConvArgs {
     const bf16* resid;         // EPI_LINEAR_F32: network input (32 ch); channels 0-2 are added to the output
     int n_store;               // channels written (EPI_RELU_BF16)
     uint32_t* err;
+    long long wait_cycles;     // budget of each pipeline wait
 };
 
 __device__ __forceinline__ void store16_bf16(bf16* dst, const float (&f)[16]) {
@@ -101,6 +102,22 @@ __device__ __forceinline__ void load16_bf16(const bf16* src, float (&f)[16]) {
 
 __device__ __forceinline__ uint8_t* align1k(uint8_t* p) {
     return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+// Before a CTA frees its TMEM and exits — normally or after a pipeline wait
+// gave up — its own asynchronous work must have landed: the producer waits
+// for the newest load of every stage it filled (older loads of a stage
+// completed before the stage was refilled), the MMA issuer for `done`, which
+// it committed after its last MMA.  These waits use the full budget; on the
+// normal path they find the phases already complete.
+__device__ __forceinline__ void drain(int warp, int lane, int issued, int stages, uint64_t* full, uint64_t* done,
+                                      uint32_t* s_fail) {
+    if (warp == 4 && lane == 0) {
+        for (int i = issued > stages ? issued - stages : 0; i < issued; ++i)
+            if (!tc::mbar_wait(&full[i % stages], (i / stages) & 1)) *s_fail = 1;
+    } else if (warp == 5 && lane == 0) {
+        if (!tc::mbar_wait(done, 0)) *s_fail = 1;
+    }
 }
 
 // Forward / backward-data convolution, one 16x8-pixel tile per CTA.
@@ -142,6 +159,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
 
+    int issued = 0;  // stages loaded by the producer (warp 4, lane 0)
     if (warp == 4) {
         if (lane == 0) {
             tc::tma_prefetch(&src0);
@@ -150,10 +168,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t bytes = kChunkBytes + a.N * 64;
             for (int i = 0; i < iters; ++i) {
                 const int s = i % a.stages;
-                if (i >= a.stages && !tc::mbar_wait(&empty[s], ((i / a.stages) - 1) & 1)) {
+                if (i >= a.stages && !tc::mbar_wait(&empty[s], ((i / a.stages) - 1) & 1, a.wait_cycles)) {
                     s_fail = 1;
                     break;
                 }
+                issued = i + 1;
                 const int tap = i / nch, c = i % nch, ky = tap / 3, kx = tap % 3;
                 tc::mbar_expect_tx(&full[s], bytes);
                 if (c < a.chunks0)
@@ -169,7 +188,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t idesc = tc::idesc_bf16(128, a.N, 0, 0);
             for (int i = 0; i < iters; ++i) {
                 const int s = i % a.stages;
-                if (!tc::mbar_wait(&full[s], (i / a.stages) & 1)) {
+                if (!tc::mbar_wait(&full[s], (i / a.stages) & 1, a.wait_cycles)) {
                     s_fail = 1;
                     break;
                 }
@@ -184,7 +203,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::mma_commit(done);
         }
     } else {
-        bool ok = tc::mbar_wait(done, 0);
+        bool ok = tc::mbar_wait(done, 0, a.wait_cycles);
         ok = __all_sync(0xffffffffu, ok);
         tc::fence_after_sync();
         if (ok) {
@@ -234,6 +253,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             s_fail = 1;
         }
     }
+    drain(warp, lane, issued, a.stages, full, done, &s_fail);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 5) {
@@ -253,6 +273,7 @@ struct WgradArgs {
     float* partial;            // [splits][9][N][cin]
     int cin;
     uint32_t* err;
+    long long wait_cycles;     // budget of each pipeline wait
 };
 
 // Backward-weights: CTA (split, 128-input-channel block, tap) reduces the
@@ -298,6 +319,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
 
+    int issued = 0;  // stages loaded by the producer (warp 4, lane 0)
     if (warp == 4) {
         if (lane == 0) {
             tc::tma_prefetch(&src0);
@@ -306,10 +328,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t bytes = (uint32_t)(qa + a.gchunks) * kChunkBytes;
             for (int i = 0; i < iters; ++i) {
                 const int s = i % a.stages;
-                if (i >= a.stages && !tc::mbar_wait(&empty[s], ((i / a.stages) - 1) & 1)) {
+                if (i >= a.stages && !tc::mbar_wait(&empty[s], ((i / a.stages) - 1) & 1, a.wait_cycles)) {
                     s_fail = 1;
                     break;
                 }
+                issued = i + 1;
                 const int t = t_begin + i, n = t / per_img, rem = t % per_img;
                 const int x0 = (rem % a.tiles_x) * kBX, y0 = (rem / a.tiles_x) * kBY;
                 tc::mbar_expect_tx(&full[s], bytes);
@@ -331,7 +354,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t idesc = tc::idesc_bf16(128, N, 1, 1);
             for (int i = 0; i < iters; ++i) {
                 const int s = i % a.stages;
-                if (!tc::mbar_wait(&full[s], (i / a.stages) & 1)) {
+                if (!tc::mbar_wait(&full[s], (i / a.stages) & 1, a.wait_cycles)) {
                     s_fail = 1;
                     break;
                 }
@@ -347,7 +370,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::mma_commit(done);
         }
     } else {
-        bool ok = tc::mbar_wait(done, 0);
+        bool ok = tc::mbar_wait(done, 0, a.wait_cycles);
         ok = __all_sync(0xffffffffu, ok);
         tc::fence_after_sync();
         if (ok) {
@@ -371,6 +394,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             s_fail = 1;
         }
     }
+    drain(warp, lane, issued, a.stages, full, done, &s_fail);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 5) {
@@ -765,6 +789,7 @@ struct hx_denoiser {
     float* adam_m = nullptr;
     float* adam_v = nullptr;
     uint32_t* err = nullptr;
+    long long wait_cycles = tc::kWaitCycles;  // pipeline-wait budget (hx_denoiser_set_wait_budget)
     int step = 0;
     uint32_t loss_kind = HX_DN_LOSS_L1_LOG;
     std::vector<void*> allocs;
@@ -897,6 +922,7 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
     a.tiles_y = (H + kBY - 1) / kBY;
     a.stages = kConvStages;
     a.err = dn->err;
+    a.wait_cycles = dn->wait_cycles;
     const CUtensorMap *m0, *m1, *wm;
     if (!dgrad) {
         m0 = &p->tm[S.src0];
@@ -972,6 +998,7 @@ hx_status launch_wgrad(hx_denoiser* dn, Plan* p, int l, float scale) {
     a.partial = p->partial;
     a.cin = L.cin;
     a.err = dn->err;
+    a.wait_cycles = dn->wait_cycles;
     HX_CHECK_ARG((size_t)a.splits * 9 * L.cd * L.cin * sizeof(float) <= p->partial_bytes, "wgrad partial overflow");
     const size_t smem = 1024 + a.stages * (a.a_bytes + a.b_bytes) + 256;
     HX_CUDA(cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1087,7 +1114,7 @@ hx_status check_err(hx_denoiser* dn) {
     if (e) {
         HX_CUDA(cudaMemsetAsync(dn->err, 0, sizeof(uint32_t), dn->ctx->stream));
         hx_set_error("denoiser: a tensor-core pipeline wait timed out (status 0x%x)", e);
-        return HX_ERR_DEVICE;
+        return HX_ERR_TIMEOUT;
     }
     return HX_OK;
 }
@@ -1167,6 +1194,29 @@ hx_status hx_denoiser_set_params(hx_denoiser* dn, const float* host, uint64_t n)
     HX_TRY(refresh_weights(dn, false, 0.0f));
     HX_CUDA(cudaStreamSynchronize(dn->ctx->stream));
     return HX_OK;
+}
+
+// He-uniform weights (bound sqrt(6 / fan_in), fan_in = 9 cin) from a
+// SplitMix64 stream of the seed, zero biases; resets the Adam state.
+hx_status hx_denoiser_init_params(hx_denoiser* dn, uint64_t seed) {
+    HX_CHECK_ARG(dn, "null argument");
+    std::vector<float> p(dn->nparams);
+    uint64_t x = seed;
+    auto next = [&]() {  // SplitMix64 (Steele, Lea, Flood 2014)
+        uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    for (int l = 0; l < kNumLayers; ++l) {
+        const Layer& L = dn->layers[l];
+        const double bound = std::sqrt(6.0 / (9.0 * L.cin));
+        float* w = p.data() + L.off;
+        for (size_t k = 0; k < (size_t)9 * L.cout * L.cin; ++k)
+            w[k] = (float)(((double)(next() >> 11) * 0x1.0p-53 * 2.0 - 1.0) * bound);
+        for (int k = 0; k < L.cout; ++k) w[(size_t)9 * L.cout * L.cin + k] = 0.0f;
+    }
+    return hx_denoiser_set_params(dn, p.data(), p.size());
 }
 
 hx_status hx_denoiser_get_params(hx_denoiser* dn, float* host, uint64_t n) {
@@ -1257,6 +1307,13 @@ hx_status hx_denoiser_infer(hx_denoiser* dn, const float* d_features, uint32_t n
 hx_status hx_denoiser_check(hx_denoiser* dn) {
     HX_CHECK_ARG(dn, "null argument");
     return check_err(dn);
+}
+
+hx_status hx_denoiser_set_wait_budget(hx_denoiser* dn, uint64_t cycles) {
+    HX_CHECK_ARG(dn, "null argument");
+    HX_CHECK_ARG(cycles <= (uint64_t)tc::kWaitCycles, "wait budget above the default %lld cycles", tc::kWaitCycles);
+    dn->wait_cycles = cycles ? (long long)cycles : tc::kWaitCycles;
+    return HX_OK;
 }
 
 // Test access to a stored activation of the last forward pass (BF16 bits,

@@ -112,8 +112,12 @@ struct DevEnv {
     uint32_t km, kc;
 };
 
+// Entries of a ray's traversal stack (8-byte node groups, in local memory).
+constexpr uint32_t kTraversalStackEntries = 32;
+
 struct DevScene {
     uint32_t num_prims, num_nodes, num_lights, num_instances;
+    uint32_t stack_limit;        // traversal stack entries a ray may use (<= kStackSize; a diagnostic knob)
     const float4* tri;           // 3 per leaf-ordered triangle: v0.xyz|prim, v1.xyz|flags, v2.xyz|0
     const hx_bvh8_node* nodes;
     const uint4* prim_info;      // per flattened prim: instance, global tri, material, flags
@@ -161,5 +165,5 @@ void hx_scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, void* te
 
 // Stable LSD radix sort of (key, value) pairs on the low `bits` bits.
 size_t hx_radix_temp_bytes(size_t n);
-void hx_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp, size_t n, int bits,
+cudaError_t hx_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp, size_t n, int bits,
                          void* temp, cudaStream_t st);

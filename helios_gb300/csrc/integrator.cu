@@ -111,6 +111,7 @@ struct hx_integrator {
     bool counting = false;
     hx_stats stats{};
     int grid_trace = 0, grid_shade = 0, grid_gen = 0, grid_batched = 0;
+    uint32_t* status_host = nullptr;  // pinned copy of the device status word
 };
 
 static void compute_tiles(hx_integrator* it) {  // path_integrator.cpp:312-336
@@ -182,6 +183,12 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_A(it->hits_host_layout, sizeof(hx_hit) * npix);
     HX_A(it->rgb_tmp, 12 * npix);
 #undef HX_A
+    if (cudaHostAlloc((void**)&it->status_host, 64, cudaHostAllocDefault) != cudaSuccess) {
+        it->status_host = nullptr;
+        hx_set_error("hx_integrator_create: pinned status word allocation failed");
+        return fail(HX_ERR_DEVICE);
+    }
+    *it->status_host = 0;
     cudaStream_t st = ctx->stream;
     HX_CUDA(cudaMemsetAsync(it->acc, 0, 16 * npix, st));
     HX_CUDA(cudaMemsetAsync(it->comp, 0, 16 * npix, st));
@@ -206,15 +213,24 @@ extern "C" hx_status hx_integrator_destroy(hx_integrator* it) {
     if (!it) return HX_OK;
     if (it->ctx) cudaStreamSynchronize(it->ctx->stream);
     for (void* p : it->allocs) hx_free(it->ctx, p);
+    if (it->status_host) cudaFreeHost(it->status_host);
     delete it;
     return HX_OK;
 }
 
-static hx_status check_status(hx_integrator* it) {
-    uint32_t st = 0;
-    HX_CUDA(cudaMemcpyAsync(&st, it->q.status, 4, cudaMemcpyDeviceToHost, it->ctx->stream));
-    HX_CUDA(cudaStreamSynchronize(it->ctx->stream));
+// The device status word: kernels set bit 0 (traversal-stack overflow or a
+// malformed tree) and bit 1 (a shading list that does not cover a bounce's
+// rays).  Calls that synchronise anyway queue a copy of the word into pinned
+// memory before their wait (queue_status) and report it after
+// (report_status), so the production path adds no synchronisation.
+static hx_status queue_status(hx_integrator* it) {
+    HX_CUDA(cudaMemcpyAsync(it->status_host, it->q.status, 4, cudaMemcpyDeviceToHost, it->ctx->stream));
+    return HX_OK;
+}
+static hx_status report_status(hx_integrator* it) {
+    const uint32_t st = *it->status_host;
     if (st & 3u) {
+        *it->status_host = 0;
         hx_set_error((st & 1u) ? "BVH traversal stack overflow (status word 0x%x)"
                                : "shading list does not cover the bounce's rays (status word 0x%x)",
                      st);
@@ -222,6 +238,11 @@ static hx_status check_status(hx_integrator* it) {
         return HX_ERR_DEVICE;
     }
     return HX_OK;
+}
+static hx_status check_status(hx_integrator* it) {
+    HX_TRY(queue_status(it));
+    HX_CUDA(cudaStreamSynchronize(it->ctx->stream));
+    return report_status(it);
 }
 
 struct StageTimer {
@@ -499,7 +520,9 @@ extern "C" hx_status hx_integrator_tonemap(hx_integrator* it, uint32_t op, float
     HX_CUDA(cudaGetLastError());
     if (host_rgba8) {
         HX_CUDA(cudaMemcpyAsync(host_rgba8, it->ldr, 4 * (size_t)W * H, cudaMemcpyDeviceToHost, st));
+        HX_TRY(queue_status(it));
         HX_CUDA(cudaStreamSynchronize(st));
+        return report_status(it);
     }
     return HX_OK;
 }
@@ -512,8 +535,9 @@ extern "C" hx_status hx_integrator_read_accumulation(hx_integrator* it, float* h
     k_resolve<<<it->grid_gen, kGenThreads, 0, st>>>(it->acc, it->count_map, n, kahan ? 1u : 0u, it->resolved);
     HX_CUDA(cudaGetLastError());
     HX_CUDA(cudaMemcpyAsync(host, it->resolved, 16 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    HX_TRY(queue_status(it));
     HX_CUDA(cudaStreamSynchronize(st));
-    return HX_OK;
+    return report_status(it);
 }
 
 // Output-buffer views of Renderer::render_debug_visualization

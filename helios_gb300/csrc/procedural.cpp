@@ -398,7 +398,7 @@ hx_status build_icospheres(hx_host_scene* s, const hx_procedural_params& P) {
     e.sun_direction[0] = (float)(std::cos(el) * std::sin(az));
     e.sun_direction[1] = (float)std::sin(el);
     e.sun_direction[2] = (float)(std::cos(el) * std::cos(az));
-    hx_status st = hx_hosek_wilkie_coefficients(e.sun_direction, P.turbidity, 1.15f, e.coeffs);
+    hx_status st = hx_hosek_wilkie_sky(e.sun_direction, P.turbidity, P.ground_albedo, 1.15f, e.coeffs);
     if (st != HX_OK) return st;
     s->camera = hx_camera{{8.0f, 6.0f, 26.0f}, {0.0f, -3.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, 60.0f, 1.0f, 1000.0f, 8.0f, 0.0f};
     return HX_OK;
@@ -497,7 +497,7 @@ hx_status build_terrain(hx_host_scene* s, const hx_procedural_params& P) {
     e.sun_direction[0] = (float)(std::cos(el) * std::sin(az));
     e.sun_direction[1] = (float)std::sin(el);
     e.sun_direction[2] = (float)(std::cos(el) * std::cos(az));
-    hx_status st = hx_hosek_wilkie_coefficients(e.sun_direction, P.turbidity, 1.15f, e.coeffs);
+    hx_status st = hx_hosek_wilkie_sky(e.sun_direction, P.turbidity, P.ground_albedo, 1.15f, e.coeffs);
     if (st != HX_OK) return st;
     hx_light sun;
     std::memset(&sun, 0, sizeof(sun));
@@ -525,6 +525,7 @@ extern "C" void hx_procedural_defaults(uint32_t kind, hx_procedural_params* p) {
     p->env_height = 1024;
     p->sun_elevation_deg = 30.0f;
     p->turbidity = 3.0f;
+    p->ground_albedo = 0.1f;
     p->terrain_size = 4096;
     p->num_spheres = 200;
     if (kind == HX_SCENE_TERRAIN) p->icosphere_level = 4;
@@ -561,23 +562,45 @@ extern "C" hx_status hx_host_scene_destroy(hx_host_scene* s) {
     return HX_OK;
 }
 
-// Raw coefficients interpolated linearly in the sun zenith angle between the
-// 0.5-degree samples of the table, then the luminance normalisation of
+// Hosek-Wilkie RGB coefficients for any turbidity, ground albedo and sun
+// angle, evaluated the way the reference's evaluate does
+// (hosek_wilkie_sky_model.cpp:48-67): each raw coefficient is a quintic in
+// e = (1 - theta / (pi / 2))^(1/3) per (albedo 0/1, integer turbidity), and
+// the four splines around (turbidity, albedo) blend bilinearly.  The quintic
+// comes from its six samples at e = j / 5 (kHosekNodes) by Lagrange
+// interpolation in double — exact up to rounding, so the FP32 coefficients
+// equal the reference's to an ulp.  Then the luminance normalisation of
 // HosekWilkieSkyModel::update (hosek_wilkie_sky_model.cpp:681-686).
-extern "C" hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], float turbidity, float normalized_sun_y,
-                                                  float out[40]) {
-    if (!sun_direction || !out) { hx_set_error("hx_hosek_wilkie_coefficients: null argument"); return HX_ERR_INVALID_ARG; }
-    int ti = turbidity == 3.0f ? 0 : (turbidity == 4.0f ? 1 : -1);
-    if (ti < 0) { hx_set_error("hx_hosek_wilkie_coefficients: turbidity %g not tabulated (3 or 4)", turbidity); return HX_ERR_UNSUPPORTED; }
-    float theta = std::acos(std::min(std::max(sun_direction[1], 0.0f), 1.0f));
-    double x = (double)theta / (0.5 * 3.14159265358979323846 / 180.0);
-    int k0 = (int)std::floor(x);
-    k0 = std::max(0, std::min(HX_HOSEK_TABLE_STEPS - 2, k0));
-    float f = (float)std::min(1.0, std::max(0.0, x - k0));
+static double hosek_spline(int a, int t, int q, double e) {
+    double v = 0.0;
+    for (int j = 0; j < 6; ++j) {
+        double l = 1.0;
+        for (int m = 0; m < 6; ++m)
+            if (m != j) l *= (e - m / 5.0) / ((j - m) / 5.0);
+        v += kHosekNodes[a][t - 1][j][q] * l;
+    }
+    return v;
+}
+
+extern "C" hx_status hx_hosek_wilkie_sky(const float sun_direction[3], float turbidity, float albedo,
+                                         float normalized_sun_y, float out[40]) {
+    if (!sun_direction || !out) { hx_set_error("hx_hosek_wilkie_sky: null argument"); return HX_ERR_INVALID_ARG; }
+    if (!std::isfinite(turbidity) || !std::isfinite(albedo) || !std::isfinite(normalized_sun_y)) {
+        hx_set_error("hx_hosek_wilkie_sky: non-finite argument");
+        return HX_ERR_INVALID_ARG;
+    }
+    const float theta = std::acos(std::min(std::max(sun_direction[1], 0.0f), 1.0f));
+    const double kPi = 3.14159265358979323846;
+    const double e = std::pow(std::max<float>(0.f, 1.f - theta / (kPi / 2.f)), 1.f / 3.0f);
+    const int t0 = std::min(std::max(static_cast<int>(turbidity), 1), 10);
+    const int t1 = std::min(t0 + 1, 10);
+    const float tk = std::min(std::max(turbidity - t0, 0.f), 1.f);
     float c[30];
     for (int q = 0; q < 30; ++q) {
-        float a = kHosekTable[ti][k0][q], b = kHosekTable[ti][k0 + 1][q];
-        c[q] = f == 0.0f ? a : (f == 1.0f ? b : a + (b - a) * f);
+        const double a0t0 = hosek_spline(0, t0, q, e), a1t0 = hosek_spline(1, t0, q, e);
+        const double a0t1 = hosek_spline(0, t1, q, e), a1t1 = hosek_spline(1, t1, q, e);
+        c[q] = (float)(a0t0 * (1 - albedo) * (1 - tk) + a1t0 * albedo * (1 - tk) + a0t1 * (1 - albedo) * tk +
+                       a1t1 * albedo * tk);
     }
     if (normalized_sun_y != 0.0f) {
         float S[3];
@@ -596,4 +619,10 @@ extern "C" hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], 
     for (int p = 0; p < 10; ++p)
         for (int ch = 0; ch < 3; ++ch) out[4 * p + ch] = c[3 * p + ch];
     return HX_OK;
+}
+
+// Ground albedo 0.1, the reference's default (hosek_wilkie_sky_model.h:33).
+extern "C" hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], float turbidity, float normalized_sun_y,
+                                                  float out[40]) {
+    return hx_hosek_wilkie_sky(sun_direction, turbidity, 0.1f, normalized_sun_y, out);
 }

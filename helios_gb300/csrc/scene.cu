@@ -273,6 +273,7 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
 
     hx_scene* s = new hx_scene();
     s->ctx = ctx;
+    s->d.stack_limit = kTraversalStackEntries;
     cudaStream_t st = ctx->stream;
     // ---- host packing
     std::vector<uint32_t> vbase(desc->num_meshes), tbase(desc->num_meshes);
@@ -479,6 +480,13 @@ extern "C" hx_status hx_scene_destroy(hx_scene* s) {
         for (void* p : s->allocs) hx_free(s->ctx, p);
     }
     delete s;
+    return HX_OK;
+}
+
+extern "C" hx_status hx_scene_set_traversal_stack_limit(hx_scene* s, uint32_t entries) {
+    HX_CHECK_ARG(s && entries >= 1 && entries <= kTraversalStackEntries,
+                 "hx_scene_set_traversal_stack_limit: entries must be in [1, %u]", kTraversalStackEntries);
+    s->d.stack_limit = entries;
     return HX_OK;
 }
 

@@ -183,6 +183,7 @@ struct ServerRequest {
     uint8_t* host_ldr = nullptr;  // pinned
     uint32_t samples_done = 0, pixel_cursor = 0;
     bool in_flight = false, finishing = false, done = false;
+    bool cancel = false;  // hx_server_cancel: ends with HX_ERR_CANCELLED once nothing of it is in flight
     hx_status status = HX_OK;
     uint64_t paths_traced = 0;
 };
@@ -242,6 +243,7 @@ struct hx_server {
     char worker_msg[512] = "";
     // stats
     uint64_t paths_total = 0, ticks_total = 0, requests_done = 0, denoised = 0;
+    uint64_t active_peak = 0, arena_used_peak = 0;
     double t_start = 0, busy_first = 0, busy_last = 0;
     // learned denoiser for requests with denoise set (runs on the context stream)
     hx_denoiser* denoiser = nullptr;
@@ -445,6 +447,48 @@ static void admit(hx_server* s) {
         r->t_admit = now_s();
         s->admitted.push_back(r);
         it = s->pending.erase(it);
+        size_t free_b = 0;
+        for (auto& kv : s->arena_free) free_b += kv.second;
+        s->active_peak = std::max<uint64_t>(s->active_peak, s->admitted.size());
+        s->arena_used_peak = std::max<uint64_t>(s->arena_used_peak, s->arena_bytes - free_b);
+    }
+}
+
+// Result record of a request that ends now (finished or cancelled).
+static void push_result(hx_server* s, ServerRequest* r) {
+    r->done = true;
+    r->t_done = now_s();
+    hx_request_result res{};
+    res.request_id = r->id;
+    res.status = r->status;
+    res.queue_ms = ((r->t_admit > 0 ? r->t_admit : r->t_done) - r->t_submit) * 1000.0;
+    res.latency_ms = (r->t_done - r->t_submit) * 1000.0;
+    res.paths = r->paths_traced;
+    res.user_tag = r->desc.user_tag;
+    s->completed.push_back(res);
+    s->requests_done++;
+}
+
+static uint64_t remaining_work(const ServerRequest* r);
+
+// Ends admitted requests marked for cancellation that have nothing in flight:
+// their slot, device and host arena space are released at once.
+static void retire_cancelled(hx_server* s) {
+    for (size_t k = 0; k < s->admitted.size();) {
+        ServerRequest* r = s->admitted[k];
+        if (!r->cancel || r->in_flight || r->finishing) {
+            ++k;
+            continue;
+        }
+        r->status = HX_ERR_CANCELLED;
+        s->admitted_work -= std::min<uint64_t>(s->admitted_work, remaining_work(r));
+        s->free_slots.push_back(r->slot);
+        r->slot = -1;
+        arena_release(s->arena_free, r->arena_off, r->arena_bytes);
+        arena_release(s->harena_free, r->host_off, r->host_bytes);
+        r->host_bytes = 0;
+        s->admitted.erase(s->admitted.begin() + k);
+        push_result(s, r);
     }
 }
 
@@ -461,7 +505,7 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
     // shortest remaining work first
     std::vector<ServerRequest*> cand;
     for (ServerRequest* r : s->admitted)
-        if (r->desc.scene_id == scene_id && !r->in_flight && !r->finishing && r->samples_done < r->desc.spp &&
+        if (r->desc.scene_id == scene_id && !r->in_flight && !r->finishing && !r->cancel && r->samples_done < r->desc.spp &&
             is_short(s, r) == b->urgent)
             cand.push_back(r);
     if (cand.empty()) return HX_OK;
@@ -573,20 +617,9 @@ static hx_status retire_tick(hx_server* s, SceneBatch* b) {
 }
 
 static void complete_finished(hx_server* s, SceneBatch* b) {
-    double t = now_s();
     for (ServerRequest* r : b->finishing) {
         r->finishing = false;
-        r->done = true;
-        r->t_done = t;
-        hx_request_result res{};
-        res.request_id = r->id;
-        res.status = r->status;
-        res.queue_ms = (r->t_admit - r->t_submit) * 1000.0;
-        res.latency_ms = (r->t_done - r->t_submit) * 1000.0;
-        res.paths = r->paths_traced;
-        res.user_tag = r->desc.user_tag;
-        s->completed.push_back(res);
-        s->requests_done++;
+        push_result(s, r);
         // release the device slot and arena space; the pinned LDR copy stays until fetch
         s->free_slots.push_back(r->slot);
         arena_release(s->arena_free, r->arena_off, r->arena_bytes);
@@ -646,6 +679,7 @@ static void worker_main(hx_server* s) {
                     if (b->urgent) ++urgent;
                 }
             }
+            retire_cancelled(s);
             // start ticks up to the concurrency limit, the lane of the globally
             // smallest remaining request first (shortest remaining work); up to
             // two short-lane ticks may run beyond the limit, and no new long
@@ -654,7 +688,7 @@ static void worker_main(hx_server* s) {
                 int best = -1;
                 uint64_t best_work = ~0ull;
                 for (ServerRequest* r : s->admitted) {
-                    if (r->in_flight || r->finishing || r->samples_done >= r->desc.spp) continue;
+                    if (r->in_flight || r->finishing || r->cancel || r->samples_done >= r->desc.spp) continue;
                     const int lane = 2 * (int)r->desc.scene_id + (is_short(s, r) ? 1 : 0);
                     SceneBatch* b = s->batches[lane];
                     if (b->busy || b->finish_busy) continue;
@@ -828,6 +862,31 @@ extern "C" hx_status hx_server_poll(hx_server* s, hx_request_result* out, uint32
     return HX_OK;
 }
 
+extern "C" hx_status hx_server_cancel(hx_server* s, uint64_t request_id) {
+    HX_CHECK_ARG(s, "hx_server_cancel: null server");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->all.find(request_id);
+        HX_CHECK_ARG(it != s->all.end(), "hx_server_cancel: unknown request %llu", (unsigned long long)request_id);
+        ServerRequest* r = it->second;
+        if (r->done || r->finishing) return HX_OK;  // its image is complete: nothing to cancel
+        if (r->slot < 0) {  // still pending: never admitted, ends now
+            for (auto p = s->pending.begin(); p != s->pending.end(); ++p)
+                if (p->second == r) {
+                    s->pending.erase(p);
+                    break;
+                }
+            r->status = HX_ERR_CANCELLED;
+            r->host_bytes = 0;
+            push_result(s, r);
+        } else {
+            r->cancel = true;  // admitted: the worker ends it once nothing of it is in flight
+        }
+    }
+    s->cv.notify_all();
+    return HX_OK;
+}
+
 extern "C" hx_status hx_server_fetch(hx_server* s, uint64_t request_id, uint8_t* host_rgba8) {
     HX_CHECK_ARG(s, "hx_server_fetch: null server");
     ServerRequest* r = nullptr;
@@ -841,6 +900,11 @@ extern "C" hx_status hx_server_fetch(hx_server* s, uint64_t request_id, uint8_t*
             return HX_ERR_NOT_READY;
         }
         s->all.erase(it);
+        if (r->status == HX_ERR_CANCELLED) {  // no image; its arenas were released when it ended
+            delete r;
+            hx_set_error("hx_server_fetch: request %llu was cancelled", (unsigned long long)request_id);
+            return HX_ERR_CANCELLED;
+        }
     }
     if (host_rgba8) std::memcpy(host_rgba8, r->host_ldr, 4ull * r->desc.width * r->desc.height);
     {
@@ -867,6 +931,8 @@ extern "C" hx_status hx_server_stats_get(hx_server* s, hx_server_stats* out) {
     out->arena_used = s->arena_bytes - free_b;
     out->seconds = now_s() - s->t_start;
     out->requests_denoised = s->denoised;
+    out->requests_active_peak = s->active_peak;
+    out->arena_used_peak = s->arena_used_peak;
     return HX_OK;
 }
 

@@ -157,9 +157,9 @@ size_t hx_radix_temp_bytes(size_t n) {
     return 2 * hist * sizeof(uint32_t) + hx_scan_temp_bytes(hist) + 256;
 }
 
-void hx_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp, size_t n, int bits,
-                         void* temp, cudaStream_t st) {
-    if (n == 0) return;
+cudaError_t hx_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp, size_t n,
+                                int bits, void* temp, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
     uint32_t tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     size_t hist_n = (size_t)256 * tiles;
     uint32_t* hist = (uint32_t*)temp;
@@ -172,11 +172,15 @@ void hx_radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uin
         k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, shift, hist, tiles);
         hx_scan_exclusive_u32(hist, offs, hist_n, scan_tmp, st);
         k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, shift, offs, tiles);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
         std::swap(ka, kb);
         std::swap(va, vb);
     }
-    if (ka != keys) {
-        cudaMemcpyAsync(keys, ka, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    if (ka != keys) {  // an odd number of passes ends in the temporary arrays
+        cudaError_t e = cudaMemcpyAsync(keys, ka, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+        return e;
     }
+    return cudaSuccess;
 }

@@ -33,12 +33,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 // About two seconds at the maximum SM clock: no correct pipeline stage waits
 // anywhere near that long, so running out means the producer side is gone.
+// Pipeline waits take their budget from the launch (default kWaitCycles; a
+// caller may shorten it to exercise the failure path); the drain waits of a
+// failing CTA — for its own TMA copies and MMAs still in flight, before it
+// frees TMEM and exits — always use kWaitCycles.
 constexpr long long kWaitCycles = 4000000000ll;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long budget = kWaitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > budget) return false;
     return true;
 }
 

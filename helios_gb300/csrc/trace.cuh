@@ -203,7 +203,7 @@ HXD bool alpha_pass(const DevScene& s, uint32_t prim, float u, float v) {
     return !(alpha < 0.1f);
 }
 
-constexpr int kStackSize = 32;
+constexpr int kStackSize = (int)kTraversalStackEntries;
 
 HXD uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
@@ -372,7 +372,7 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         const uint32_t slot = (bit - 24u) ^ st.oct_inv;
         const uint32_t child = st.g_base + __popc(st.g_mask & 0xffu & ((1u << slot) - 1u));
         if (st.g_mask > 0x00ffffffu) {
-            if (st.sp < kStackSize) stack[st.sp++] = make_uint2(st.g_base, st.g_mask);
+            if (st.sp < s.stack_limit) stack[st.sp++] = make_uint2(st.g_base, st.g_mask);
             else overflow = true;
         }
         if (st.visits_left-- == 0 || child >= s.num_nodes) {
@@ -454,7 +454,7 @@ HXD uint32_t node_step(TravState& st, uint2* stack, const DevScene& s, float bes
     const uint32_t slot = (bit - 24u) ^ st.oct_inv;
     const uint32_t child = st.g_base + __popc(st.g_mask & 0xffu & ((1u << slot) - 1u));
     if (st.g_mask > 0x00ffffffu) {
-        if (st.sp < kStackSize) stack[st.sp++] = make_uint2(st.g_base, st.g_mask);
+        if (st.sp < s.stack_limit) stack[st.sp++] = make_uint2(st.g_base, st.g_mask);
         else overflow = true;
     }
     if (st.visits_left-- == 0 || child >= s.num_nodes) {

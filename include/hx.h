@@ -387,6 +387,13 @@ typedef struct hx_scene_info {
 } hx_scene_info;
 HX_API hx_status hx_scene_info_get(const hx_scene* scene, hx_scene_info* out);
 
+/* Diagnostic knob (no counterpart in the reference, whose traversal stack
+ * lives in the driver): the number of traversal-stack entries a ray may use,
+ * 1..32 (default 32).  A ray that needs more drops the extra entries and sets
+ * the overflow bit of the device status word, which the next synchronising
+ * call reports as HX_ERR_DEVICE.  Applies to launches issued after the call. */
+HX_API hx_status hx_scene_set_traversal_stack_limit(hx_scene* scene, uint32_t entries);
+
 /* Copies the light list the library derived (reference order, scene.cpp
  * 1111-1119,1269-1309) into out[0..capacity). */
 HX_API hx_status hx_scene_lights(const hx_scene* scene, hx_light* out, uint32_t capacity,
@@ -408,7 +415,13 @@ HX_API hx_status hx_integrator_destroy(hx_integrator* integ);
 
 /* PathIntegrator::render (path_integrator.cpp:48-84) + the accumulation of
  * Renderer::render (renderer.cpp:183-227): traces one progressive frame
- * (1 sample per pixel of the current tile) and accumulates it. */
+ * (1 sample per pixel of the current tile) and accumulates it.
+ * Device-side faults of a frame (traversal-stack overflow, a malformed tree,
+ * a shading list that misses rays) set bits of a device status word; render
+ * itself does not wait, and the next call that synchronises anyway
+ * (tonemap to host memory, read_accumulation, primary_hits,
+ * sample_radiance, render_output, gather_debug_rays) reads the word with its
+ * own copy, returns HX_ERR_DEVICE and clears it. */
 HX_API hx_status hx_integrator_render(hx_integrator* integ, const hx_frame_desc* frame);
 
 /* n consecutive render() calls with the same frame constants, batched into
@@ -560,6 +573,8 @@ typedef struct hx_server_stats {
     uint64_t arena_bytes, arena_used;
     double   seconds;
     uint64_t requests_denoised;
+    uint64_t requests_active_peak;  /* most requests admitted at once        */
+    uint64_t arena_used_peak;       /* most device-arena bytes in use at once */
 } hx_server_stats;
 
 HX_API hx_status hx_server_create(hx_context* ctx, const hx_server_desc* desc, hx_server** out);
@@ -580,6 +595,14 @@ HX_API hx_status hx_server_poll(hx_server* server, hx_request_result* out, uint3
 /* Copies a finished request's RGBA8 image (width*height*4, may be NULL) and
  * releases it. */
 HX_API hx_status hx_server_fetch(hx_server* server, uint64_t request_id, uint8_t* host_rgba8);
+/* Cancels a request (thread-safe, non-blocking; the serving form's own
+ * control, no counterpart in the reference).  A pending request ends at
+ * once; an admitted one ends as soon as none of its samples is on the GPU,
+ * releasing its slot and arena space.  Either way its result reports
+ * HX_ERR_CANCELLED and hx_server_fetch returns HX_ERR_CANCELLED (no image).
+ * A request whose image is already complete is not affected.  Unknown ids:
+ * HX_ERR_INVALID_ARG. */
+HX_API hx_status hx_server_cancel(hx_server* server, uint64_t request_id);
 HX_API hx_status hx_server_stats_get(hx_server* server, hx_server_stats* out);
 HX_API hx_status hx_server_destroy(hx_server* server);
 
@@ -593,11 +616,15 @@ HX_API hx_status hx_server_destroy(hx_server* server);
  * d_sorted[n]: the stable sort order — the same values hx_scene_upload
  * computes (hx_scene_export_bvh).  n must be 1..262144 (2^18); larger n is
  * rejected with HX_ERR_INVALID_ARG.  Scratch is one fixed device array of
- * about 5 MB in the library, held by every GPU that loads it until exit;
- * the first call on a device looks up that array's address (make it before
- * any stream capture).  Work is ordered on cuda_stream (a cudaStream_t,
- * NULL = default stream); calls that overlap on the GPU race on the shared
- * scratch. */
+ * about 5 MB in the library, held by every GPU that loads it until exit.
+ * The first call on a device looks up that array's address and keeps it
+ * for the life of the process; with lazy module loading (the CUDA default)
+ * that first call is also when the array is committed on the device, so a
+ * caller that must not grow its footprint later makes one warm-up call at
+ * start-up, before any stream capture.  The kept address does not survive a
+ * cudaDeviceReset of that device.  Work is ordered on cuda_stream (a
+ * cudaStream_t, NULL = default stream); calls that overlap on the GPU race on
+ * the shared scratch. */
 HX_API hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n, uint32_t* d_morton, uint32_t* d_sorted,
                                       void* cuda_stream);
 
@@ -621,6 +648,7 @@ typedef struct hx_procedural_params {
     float    turbidity;             /* default 3                              */
     uint32_t terrain_size;          /* HX_SCENE_TERRAIN: grid vertices per side (default 4096) */
     uint32_t num_spheres;           /* HX_SCENE_TERRAIN: sphere instances (default 200)        */
+    float    ground_albedo;         /* sky model ground albedo 0..1 (default 0.1)              */
 } hx_procedural_params;
 
 HX_API void      hx_procedural_defaults(uint32_t kind, hx_procedural_params* out);
@@ -639,10 +667,16 @@ HX_API hx_status hx_encode_png(const uint8_t* rgba8, uint32_t width, uint32_t he
                                uint64_t capacity, uint64_t* size);
 HX_API hx_status hx_save_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
 
-/* Hosek-Wilkie RGB coefficients (A..I, Z; 10 x vec4) for the given sun
- * direction, turbidity 3 or 4 and ground albedo 0.1, normalised so the
- * luminance toward the sun is normalized_sun_y
- * (hosek_wilkie_sky_model.cpp:658-686). */
+/* Hosek-Wilkie RGB coefficients (A..I, Z; 10 x vec4): HosekWilkieSkyModel::
+ * update (hosek_wilkie_sky_model.cpp:658-686) for the given sun direction,
+ * turbidity (clamped to 1..10 and blended between integer turbidities) and
+ * ground albedo (blended between 0 and 1), as the reference's evaluate
+ * (hosek_wilkie_sky_model.cpp:48-67) does, normalised so the luminance toward
+ * the sun is normalized_sun_y (0: raw). */
+HX_API hx_status hx_hosek_wilkie_sky(const float sun_direction[3], float turbidity, float albedo,
+                                     float normalized_sun_y, float out[40]);
+/* The same with the reference's default ground albedo 0.1
+ * (hosek_wilkie_sky_model.h:33). */
 HX_API hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], float turbidity,
                                               float normalized_sun_y, float out[40]);
 
@@ -687,6 +721,18 @@ HX_API hx_status hx_denoiser_train_step(hx_denoiser* dn, const float* d_features
 HX_API hx_status hx_denoiser_infer(hx_denoiser* dn, const float* d_features, uint32_t n, uint32_t h, uint32_t w,
                                    float* d_out_rgba);
 HX_API hx_status hx_denoiser_check(hx_denoiser* dn);
+/* Untrained starting point for training: He-uniform weights (bound
+ * sqrt(6 / (9 cin))) from a SplitMix64 stream of `seed`, zero biases; resets
+ * the Adam state. */
+HX_API hx_status hx_denoiser_init_params(hx_denoiser* dn, uint64_t seed);
+/* Diagnostic knob (no counterpart in the reference): the clock-cycle budget
+ * of each tensor-core pipeline wait of later launches (0 = the default, about
+ * two seconds; at most that).  A wait that runs out sets the denoiser's error
+ * word; the CTA still waits (with the default budget) for its own TMA copies
+ * and MMAs in flight, frees its TMEM and exits, and hx_denoiser_check then
+ * returns HX_ERR_TIMEOUT.  A budget of a few cycles makes the waits run out
+ * on purpose, to exercise that path. */
+HX_API hx_status hx_denoiser_set_wait_budget(hx_denoiser* dn, uint64_t cycles);
 /* Test access: a stored BF16 tensor (activation, or its gradient) of the
  * last training (training = 1) or inference pass, by index in network order
  * (x, a0, a0b, p0, a1, p1, a2, p2, a3, p3, a4, a4b, u3, d3, u2, d2, u1, d1,

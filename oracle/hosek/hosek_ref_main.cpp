@@ -11,10 +11,13 @@
 // restatement (restated_evaluate below) bit for bit against it.
 //
 // Outputs (committed; derived data only, no table rows):
-//   helios_gb300/csrc/hosek_table.inc — raw A..I,Z (RGB) for turbidity 3 and 4,
-//       ground albedo 0.1, sun zenith angle theta_k = k * 0.5 deg, k = 0..180;
-//   tests/golden/hosek_coeffs.json — the same coefficients at a few angles
-//       plus the luminance-normalised Z of HosekWilkieSkyModel::update.
+//   helios_gb300/csrc/hosek_table.inc — each raw coefficient's spline A..I,Z
+//       (RGB) sampled at six points of elevation^(1/3), for ground albedo 0
+//       and 1 and turbidity 1..10 (the quintic is exact from six samples);
+//   tests/golden/hosek_coeffs.json — the reference's normalised coefficients
+//       (evaluate + the luminance normalisation of HosekWilkieSkyModel::update)
+//       at on- and off-grid sun elevations, fractional turbidities and
+//       several ground albedos.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -68,56 +71,76 @@ static float hw(float cos_theta, float gamma, float cos_gamma, const float* k, i
     return (1.f + A * expf(B / (cos_theta + 0.01f))) * (C + D * expf(E * gamma) + F * (cos_gamma * cos_gamma) + G * chi + I * sqrtf(std::max(0.f, cos_theta)));
 }
 
+// The spline of one (coefficient, albedo a in {0, 1}, turbidity t in 1..10)
+// sampled at e_j = j / 5, j = 0..5 (e = elevation^(1/3)): six values fix the
+// quintic exactly, so the library evaluates any sun angle from them.
+static double node_value(const double* dataset, size_t stride, int a, int t, int j) {
+    const double* base = dataset + stride * 6 * 10 * a + stride * 6 * (t - 1);
+    return evaluate_spline(base, stride, j / 5.0);
+}
+
 int main(int argc, char** argv) {
     if (argc < 3) { fprintf(stderr, "usage: %s table.inc golden.json\n", argv[0]); return 2; }
-    const float albedo = 0.1f;
-    const float turbs[2] = {3.0f, 4.0f};
-    long mismatches = 0;
+    static const int src[9] = {0, 1, 2, 3, 4, 5, 6, 8, 7};
     FILE* ft = fopen(argv[1], "w");
     fprintf(ft, "// Generated by oracle/hosek/hosek_ref_main.cpp from the Hosek-Wilkie RGB model\n"
-                "// (Hosek & Wilkie 2012): raw A..I,Z (RGB, UBO order) for ground albedo 0.1,\n"
-                "// turbidity {3, 4}, sun zenith angle k * 0.5 degrees, k = 0..180. Derived data.\n"
-                "#define HX_HOSEK_TABLE_STEPS 181\n"
-                "static const float kHosekTable[2][HX_HOSEK_TABLE_STEPS][30] = {\n");
-    for (int ti = 0; ti < 2; ++ti) {
+                "// (Hosek & Wilkie 2012): the quintic spline of each raw coefficient A..I,Z (RGB,\n"
+                "// UBO order) sampled at elevation^(1/3) = j / 5, j = 0..5, for ground albedo\n"
+                "// {0, 1} and turbidity 1..10. Derived data (samples, not the model's table).\n"
+                "static const double kHosekNodes[2][10][6][30] = {\n");
+    for (int a = 0; a < 2; ++a) {
         fprintf(ft, "{\n");
-        for (int k = 0; k <= 180; ++k) {
-            float theta = (float)(k * 0.5 * M_PI / 180.0);
-            float a[30], b[30];
-            coeffs(true, turbs[ti], albedo, theta, a);
-            coeffs(false, turbs[ti], albedo, theta, b);
-            if (memcmp(a, b, sizeof(a)) != 0) ++mismatches;
-            fprintf(ft, "{");
-            for (int q = 0; q < 30; ++q) fprintf(ft, "%.9g%s", a[q], q < 29 ? "," : "");
-            fprintf(ft, "}%s\n", k < 180 ? "," : "");
+        for (int t = 1; t <= 10; ++t) {
+            fprintf(ft, " {\n");
+            for (int j = 0; j <= 5; ++j) {
+                fprintf(ft, "  {");
+                for (int q = 0; q < 30; ++q) {
+                    double v = q < 27 ? node_value(datasetsRGB[q % 3] + src[q / 3], 9, a, t, j)
+                                      : node_value(datasetsRGBRad[q - 27], 1, a, t, j);
+                    fprintf(ft, "%.17g%s", v, q < 29 ? "," : "");
+                }
+                fprintf(ft, "}%s\n", j < 5 ? "," : "");
+            }
+            fprintf(ft, " }%s\n", t < 10 ? "," : "");
         }
-        fprintf(ft, "}%s\n", ti < 1 ? "," : "");
+        fprintf(ft, "}%s\n", a < 1 ? "," : "");
     }
     fprintf(ft, "};\n");
     fclose(ft);
-    // golden: normalised coefficients (HosekWilkieSkyModel::update) at a few sun elevations
+    // golden: the reference's evaluate + update normalisation at on- and
+    // off-grid sun elevations, integer and fractional turbidities, several
+    // ground albedos; also pins the restatement bit for bit on each case
+    long mismatches = 0, cases = 0;
     FILE* fg = fopen(argv[2], "w");
-    fprintf(fg, "{\"source\": \"reference evaluate (hosek_wilkie_sky_model.cpp:41-67) + update normalisation (:658-686)\",\n \"albedo\": 0.1, \"normalized_sun_y\": 1.15, \"cases\": [\n");
-    const float elevs[5] = {10.f, 30.f, 45.f, 60.f, 80.f};
+    fprintf(fg, "{\"source\": \"reference evaluate (hosek_wilkie_sky_model.cpp:41-67) + update normalisation (:658-686)\",\n \"normalized_sun_y\": 1.15, \"cases\": [\n");
+    const float elevs[9] = {0.5f, 10.f, 12.3f, 30.f, 37.77f, 45.f, 61.9f, 80.f, 89.5f};
+    const float turbs[7] = {1.f, 2.5f, 3.f, 4.f, 4.7f, 7.25f, 10.f};
+    const float albs[4] = {0.f, 0.1f, 0.35f, 1.f};
     bool first = true;
-    for (int ti = 0; ti < 2; ++ti)
-        for (float el : elevs) {
-            float e = el * (float)M_PI / 180.f;
-            float dir[3] = {cosf(e) * 0.6f, sinf(e), cosf(e) * 0.8f};
-            float theta = std::acos(std::min(std::max(dir[1], 0.f), 1.f));
-            float k[30];
-            coeffs(true, turbs[ti], albedo, theta, k);
-            float S[3];
-            for (int c = 0; c < 3; ++c) S[c] = hw(std::cos(theta), 0, 1.f, k, c) * k[27 + c];
-            float lum = S[0] * 0.2126f + S[1] * 0.7152f + S[2] * 0.0722f;
-            for (int c = 0; c < 3; ++c) { k[27 + c] /= lum; k[27 + c] *= 1.15f; }
-            fprintf(fg, "%s  {\"turbidity\": %g, \"sun_direction\": [%.9g, %.9g, %.9g], \"coeffs\": [", first ? "" : ",\n", turbs[ti], dir[0], dir[1], dir[2]);
-            for (int q = 0; q < 30; ++q) fprintf(fg, "%.9g%s", k[q], q < 29 ? ", " : "");
-            fprintf(fg, "]}");
-            first = false;
-        }
+    for (float tb : turbs)
+        for (float al : albs)
+            for (float el : elevs) {
+                if (al != 0.1f && (el == 10.f || el == 45.f || el == 80.f)) continue;
+                float e = el * (float)M_PI / 180.f;
+                float dir[3] = {cosf(e) * 0.6f, sinf(e), cosf(e) * 0.8f};
+                float theta = std::acos(std::min(std::max(dir[1], 0.f), 1.f));
+                float k[30], r[30];
+                coeffs(true, tb, al, theta, k);
+                coeffs(false, tb, al, theta, r);
+                if (memcmp(k, r, sizeof(k)) != 0) ++mismatches;
+                ++cases;
+                float S[3];
+                for (int c = 0; c < 3; ++c) S[c] = hw(std::cos(theta), 0, 1.f, k, c) * k[27 + c];
+                float lum = S[0] * 0.2126f + S[1] * 0.7152f + S[2] * 0.0722f;
+                for (int c = 0; c < 3; ++c) { k[27 + c] /= lum; k[27 + c] *= 1.15f; }
+                fprintf(fg, "%s  {\"turbidity\": %.9g, \"albedo\": %.9g, \"elevation_deg\": %.9g, \"sun_direction\": [%.9g, %.9g, %.9g], \"coeffs\": [",
+                        first ? "" : ",\n", tb, al, el, dir[0], dir[1], dir[2]);
+                for (int q = 0; q < 30; ++q) fprintf(fg, "%.9g%s", k[q], q < 29 ? ", " : "");
+                fprintf(fg, "]}");
+                first = false;
+            }
     fprintf(fg, "\n]}\n");
     fclose(fg);
-    printf("restated vs reference evaluate mismatches: %ld of 362 angles\n", mismatches);
+    printf("restated vs reference evaluate mismatches: %ld of %ld cases\n", mismatches, cases);
     return mismatches == 0 ? 0 : 1;
 }

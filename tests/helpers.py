@@ -49,13 +49,11 @@ class TriangleSoupScene:
         tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 3, 3)
         n = tris.shape[0]
         self._verts = (hx.Vertex * (3 * n))()
-        for i in range(n):
-            for c in range(3):
-                v = self._verts[3 * i + c]
-                v.position[0], v.position[1], v.position[2], v.position[3] = (float(tris[i, c, 0]), float(tris[i, c, 1]),
-                                                                              float(tris[i, c, 2]), 0.0)
-                v.normal[1] = 1.0
-        self._idx = (C.c_uint32 * (3 * n))(*range(3 * n))
+        v = np.frombuffer(self._verts, dtype=np.float32).reshape(3 * n, 20)
+        v[:, 0:3] = tris.reshape(-1, 3)
+        v[:, 9] = 1.0  # normal.y
+        self._idx = (C.c_uint32 * (3 * n))()
+        np.frombuffer(self._idx, dtype=np.uint32)[:] = np.arange(3 * n, dtype=np.uint32)
         self._sub = (hx.Submesh * 1)()
         self._sub[0].base_index, self._sub[0].index_count, self._sub[0].material, self._sub[0].flags = 0, 3 * n, 0, 0
         self._mesh = (hx.MeshDesc * 1)()

@@ -87,8 +87,9 @@ def test_results_identical_alone_and_in_the_mix(gpu_ctx, scenes):
 
 def test_admission_by_hbm_budget(gpu_ctx, scenes):
     (box, s_box), _ = scenes
-    # arena for about two 512x512 requests (20 B per pixel each)
-    srv = hx.Server(gpu_ctx, arena_bytes=11 << 20, max_paths_per_tick=1 << 18, max_ray_bounces=4)
+    # arena for two 512x512 requests (20 B per pixel each); each request fits
+    # one tick, so memory alone bounds how many are admitted at once
+    srv = hx.Server(gpu_ctx, arena_bytes=11 << 20, max_paths_per_tick=1 << 21, max_ray_bounces=4)
     sid = srv.add_scene(s_box)
     srv.start()
     with pytest.raises(hx.HxError) as e:
@@ -97,14 +98,65 @@ def test_admission_by_hbm_budget(gpu_ctx, scenes):
     ids = [srv.submit(sid, hx.frame_desc(box.camera(), 512, 512), 512, 512, 8) for _ in range(6)]
     got = {}
     res = _wait_all(srv, ids, images=got)
-    queued = sorted(res[i].queue_ms for i in ids)
-    # at most two fit at a time: later requests waited for memory to free up
-    assert queued[-1] > queued[0]
+    # at most two fit at a time: the server never held more than two of them,
+    # nor more arena bytes than two need
+    st = srv.stats()
+    assert st.requests_active_peak == 2, st.requests_active_peak
+    per_request = 16 * 512 * 512 + 4 * 512 * 512
+    assert 2 * per_request <= st.arena_used_peak <= 11 << 20
     imgs = [got[i] for i in ids]
     for im in imgs[1:]:
         assert np.array_equal(im, imgs[0])
-    st = srv.stats()
     assert st.arena_used == 0
+    srv.close()
+
+
+def test_cancel_pending_and_admitted_requests(gpu_ctx, scenes):
+    """hx_server_cancel: a pending request ends at once, an admitted one as
+    soon as none of its samples is on the GPU; both report HX_ERR_CANCELLED,
+    release their slot and arena space, and the requests around them finish
+    with the same images as alone."""
+    import time
+    (box, s_box), _ = scenes
+    srv = hx.Server(gpu_ctx, arena_bytes=256 << 20, max_paths_per_tick=1 << 16, max_ray_bounces=4)
+    sid = srv.add_scene(s_box)
+    srv.start()
+    f = hx.frame_desc(box.camera(), 256, 256)
+    rid = srv.submit(sid, f, 256, 256, 4)
+    _wait_all(srv, [rid])
+    alone = srv.fetch(rid)
+    # long requests (4,096 ticks each): one is admitted, the others wait behind
+    # the admitted-work cap, and so do the short ones
+    W = 2048
+    long_ids = [srv.submit(sid, hx.frame_desc(box.camera(), W, W), W, W, 64) for _ in range(4)]
+    short_ids = [srv.submit(sid, f, 256, 256, 4) for _ in range(3)]
+    time.sleep(0.05)
+    st = srv.stats()
+    assert st.requests_active >= 1
+    for i in long_ids:
+        srv.cancel(i)
+    with pytest.raises(hx.HxError) as e:
+        srv.cancel(987654321)
+    assert e.value.status == hx.HX_ERR_INVALID_ARG
+    results, imgs = {}, {}
+    t0 = time.time()
+    while len(results) < len(long_ids) + len(short_ids):
+        for r in srv.poll(wait_seconds=0.5):
+            results[r.request_id] = r
+            if r.request_id in short_ids:
+                assert r.status == hx.HX_OK
+                imgs[r.request_id] = srv.fetch(r.request_id)
+        assert time.time() - t0 < 120, "requests did not finish"
+    for i in long_ids:
+        assert results[i].status == hx.HX_ERR_CANCELLED
+        assert results[i].paths < W * W * 64
+        with pytest.raises(hx.HxError) as e:
+            srv.fetch(i)
+        assert e.value.status == hx.HX_ERR_CANCELLED
+    for i in short_ids:
+        assert np.array_equal(imgs[i], alone)
+    st = srv.stats()
+    assert st.arena_used == 0 and st.requests_active == 0 and st.requests_pending == 0
     srv.close()
 
 

@@ -76,11 +76,23 @@ def test_alpha_masks_are_half_cut_out():
 
 
 def test_hosek_coefficients_match_reference_golden():
+    """The reference's own evaluate + normalisation (compiled from its source
+    by oracle/hosek/build_ref.sh) at on- and off-grid sun elevations,
+    fractional turbidities and ground albedos 0..1.  The library builds each
+    quintic from six samples (Lagrange, in double) where the reference sums
+    Bernstein terms, so the FP32 results differ by rounding: within 2e-6 of
+    each coefficient's range over the cases (a few ulps of it; a value that
+    cancels toward zero can differ by more ulps of itself)."""
     g = json.load(open(os.path.join(ROOT, "tests", "golden", "hosek_coeffs.json")))
-    for case in g["cases"]:
-        k = hx.hosek_wilkie_coefficients(case["sun_direction"], case["turbidity"], 1.15)
-        ref = np.array(case["coeffs"], np.float32).reshape(10, 3)
-        assert np.allclose(k, ref, rtol=2e-5, atol=1e-7), case
+    assert len(g["cases"]) > 150
+    assert {round(c["turbidity"], 3) for c in g["cases"]} >= {1.0, 2.5, 4.7, 7.25, 10.0}
+    assert {round(c["albedo"], 3) for c in g["cases"]} >= {0.0, 0.35, 1.0}
+    got = np.array([hx.hosek_wilkie_coefficients(c["sun_direction"], c["turbidity"], 1.15, albedo=c["albedo"])
+                    for c in g["cases"]])
+    ref = np.array([c["coeffs"] for c in g["cases"]], np.float32).reshape(-1, 10, 3)
+    scale = np.abs(ref).max(axis=0)
+    assert (np.abs(got - ref) <= 2e-6 * scale).all(), np.abs((got - ref) / scale).max()
+    assert np.median(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-30)) < 1e-6
 
 
 def test_cpp_driver_builds_and_links():

@@ -8,8 +8,9 @@ test calls it through the C-ABI on buffers the test owns (allocated by
 torch, as a stand-in for the caller's allocator) and checks, on two calls in
 a row, that it returns exactly the Morton codes and stable sort order that
 hx_scene_upload computes for the same triangles (integer outputs: the
-tolerance is bit-exact).  The file sorts last so a stopping run has already
-run every other test.
+tolerance is bit-exact), from the smallest scene up to exactly 2^18
+triangles, where the fixed scratch layout is fullest.  The file sorts last
+so a stopping run has already run every other test.
 """
 import ctypes as C
 
@@ -17,7 +18,7 @@ import numpy as np
 import pytest
 
 import helios_gb300 as hx
-from tests.helpers import small_icosphere_scene
+from tests.helpers import TriangleSoupScene, small_icosphere_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -49,16 +50,30 @@ def _world_tris(hs):
     return np.ascontiguousarray(np.concatenate(out).astype(np.float32))
 
 
-@pytest.mark.parametrize("which", ["box", "ico"])
+def _soup(n, seed=31):
+    """n random world-space triangles (the fullest case of the fixed scratch)."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-50.0, 50.0, (n, 1, 3))
+    return TriangleSoupScene((c + rng.normal(0.0, 0.3, (n, 3, 3))).astype(np.float32))
+
+
+@pytest.mark.parametrize("which", ["box", "ico", "max"])
 def test_lbvh_sort_noalloc_matches_scene_upload(which):
     torch = pytest.importorskip("torch")
     ctx = hx.Context(0)
-    hs = hx.HostScene(hx.SCENE_BOX) if which == "box" else small_icosphere_scene(level=4, quads=5000, pool=4, mask=32)
+    if which == "box":
+        hs = hx.HostScene(hx.SCENE_BOX)
+    elif which == "ico":
+        hs = small_icosphere_scene(level=4, quads=5000, pool=4, mask=32)
+    else:
+        hs = _soup(1 << 18)
     scene = hx.Scene(ctx, hs)
     ref = scene.export_bvh()
     world = _world_tris(hs)
     n = world.shape[0]
     assert n == ref["morton"].size
+    if which == "max":
+        assert n == 1 << 18
     d_world = torch.from_numpy(world).cuda()
     d_morton = torch.zeros(n, dtype=torch.int32, device="cuda")
     d_sorted = torch.zeros(n, dtype=torch.int32, device="cuda")
