@@ -1,22 +1,27 @@
 """Benchmark: Mpaths/s of the wavefront path tracer on the 1M-triangle scene.
 
-Workload (one step = one progressive frame): 12 instances of a level-6
-icosphere (81,920 triangles each) + a 2-triangle ground plane + 100k
-alpha-tested quads (64 distinct 512x512 RGBA8 value-noise masks, 50% cut
-out), Hosek-Wilkie sky (sun elevation 30 deg, turbidity 3) baked to a
-2048x1024 FP16 lat-long map with importance sampling, 4 point lights;
-1920x1080, 1 sample per pixel per frame, max depth 8, reference shading
-policy.  Synthetic, seeded procedural data.
+Workload (config 1; one step = one progressive frame, K steps = the K-frame
+job, 256 by default): 12 instances of a level-6 icosphere (81,920 triangles
+each) + a 2-triangle ground plane + 100k alpha-tested quads (64 distinct
+512x512 RGBA8 value-noise masks, 50% cut out), Hosek-Wilkie sky (sun
+elevation 30 deg, turbidity 3) baked to a 2048x1024 FP16 lat-long map with
+importance sampling, 4 point lights; 1920x1080, 1 sample per pixel per
+frame, max depth 8, reference shading policy.  Synthetic, seeded procedural
+data.
 
-value     = paths / device time of K frames (CUDA events on the library stream)
-e2e       = the same through the C-ABI with the frame constants passed from
-            the host and the tone-mapped RGBA8 frame copied to pinned host
-            memory every step (host wall clock)
-roofline  = traversal kernel (k_extend: one bounce's extension rays + the
-            previous bounce's shadow rays): algorithmic bytes per launch / its
-            mean launch time (bytes = extension rays x (ray 36 B + hit 16 B)
-            + shadow rays x 48 B + node fetches x 80 B + triangle tests x
-            48 B, counted in a separate counting pass of the same frame)
+value     = paths / device time of the K-frame job (hx_integrator_render_frames;
+            --frames-per-wavefront frames traced together, the image equal to
+            K single-frame calls), CUDA events on the library stream
+progressive_one_frame_per_call = the same frame rendered one call at a time
+            (a viewer's loop): Mpaths/s and per-frame latency p50/p99
+e2e       = one frame per C-ABI call with the frame constants passed from the
+            host and the tone-mapped RGBA8 frame copied to pinned host memory
+            every frame (host wall clock)
+roofline  = traversal kernel (k_extend_batched: one bounce's extension rays +
+            the previous bounce's shadow rays): algorithmic bytes per launch /
+            its mean launch time (bytes = extension rays x (ray 36 B + hit
+            16 B) + shadow rays x 48 B + node fetches x 80 B + triangle tests
+            x 48 B, counted in a separate counting pass of the same wavefront)
 
 --impl reference times the oracle's scalar transcription of the reference
 shaders (the reference's Vulkan path cannot run without a graphics stack) on
@@ -42,9 +47,11 @@ METRIC = "Mpaths/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--steps", type=int, default=256, help="frames (config 1: 256 frames of 1 spp)")
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--frames-per-wavefront", type=int, default=8,
+                   help="frames traced together by one wavefront (render_frames batching; same image)")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--serving", action="store_true", help="serving workload (Poisson request stream)")
@@ -57,7 +64,8 @@ def parse():
     p.add_argument("--concurrent-ticks", type=int, default=1)
     p.add_argument("--precision", action="store_true", help="precision-form report (terrain scene)")
     p.add_argument("--terrain-size", type=int, default=4096)
-    p.add_argument("--spp", type=int, default=256)
+    p.add_argument("--spp", type=int, default=4096)
+    p.add_argument("--ref-spp", type=int, default=16384)
     p.add_argument("--ref-pixels", type=int, default=4096)
     p.add_argument("--denoise", action="store_true", help="learned-denoiser training + time-to-RMSE report")
     p.add_argument("--dn-variants", type=int, default=64)
@@ -191,12 +199,14 @@ def load_peaks():
                 "source": "of fallback (MEASURED_PEAKS.json absent)"}
 
 
-def cpu_sample(hs, hx, pol, seconds, threads=0):
+def cpu_sample(hs, hx, pol, seconds, threads=0, osc=None):
     """Oracle (scalar FP32 transcription of the reference shaders) on whole
     image rows of the same frame (wrapping around the frame) until the time
-    budget is used."""
+    budget is used.  osc: the oracle's copy of the scene (built here if None)."""
     from oracle import binding as ob
-    osc = ob.OracleScene(hs)
+    own = osc is None
+    if own:
+        osc = ob.OracleScene(hs)
     d = idesc(hx, pol)
     f = hx.frame_desc(hs.camera(), WIDTH, HEIGHT)
     paths = segs = 0
@@ -217,7 +227,8 @@ def cpu_sample(hs, hx, pol, seconds, threads=0):
         thr = cnt.threads
         rows_done += n
         chunk = min(64, chunk * 2)
-    osc.close()
+    if own:
+        osc.close()
     return {"paths": paths, "segments": segs, "seconds": secs, "threads": thr, "rows": rows_done}
 
 
@@ -235,15 +246,18 @@ def run_reference(args, dist):
     if dist.rank != 0:
         return
     import helios_gb300 as hx
+    from oracle import binding as ob
     hs = make_scene(hx)
     pol = make_policy(hx)
+    osc = ob.OracleScene(hs)
     per_step = []
     total_paths = 0
     total_secs = 0.0
     thr = 0
-    budget = max(1.0, args.cpu_seconds / 4)
+    # bounded sample per step: the whole run stays within about a minute of CPU time
+    budget = min(2.5, max(0.05, 60.0 / (args.warmup + args.steps)))
     for k in range(args.warmup + args.steps):
-        r = cpu_sample(hs, hx, pol, budget)
+        r = cpu_sample(hs, hx, pol, budget, osc=osc)
         if k >= args.warmup:
             per_step.append(r["seconds"] * 1000.0)
             total_paths += r["paths"]
@@ -269,22 +283,25 @@ def run_ours(args, dist):
     scene = hx.Scene(ctx, hs)
     info = scene.info()
     pol = make_policy(hx)
-    it = hx.PathIntegrator(ctx, scene, WIDTH, HEIGHT, max_ray_bounces=DEPTH, max_samples=1 << 30, policy=pol)
+    fpw = max(1, args.frames_per_wavefront)
+    it = hx.PathIntegrator(ctx, scene, WIDTH, HEIGHT, max_ray_bounces=DEPTH, max_samples=1 << 30, policy=pol,
+                           max_paths_in_flight=WIDTH * HEIGHT * fpw)
     frame = hx.frame_desc(hs.camera(), WIDTH, HEIGHT)
     paths_per_step = WIDTH * HEIGHT
 
-    # 1) stage breakdown + segment counts (timing mode syncs per stage: not the timed region)
+    # 1) stage breakdown + segment counts of one wavefront (fpw frames; timing
+    #    mode syncs per stage: not the timed region)
     it.set_timing(True)
-    it.render(frame)
+    it.render(frame, fpw)
     st = it.stats()
-    segs_per_step = st.extension_rays + st.shadow_rays
+    segs_per_step = (st.extension_rays + st.shadow_rays) / fpw
     ms_trace_per_launch = st.ms_trace / max(1, st.trace_launches)
-    stage = {"raygen": st.ms_raygen, "traverse (extension + shadow)": st.ms_trace, "shade": st.ms_shade,
-             "accumulate": st.ms_accumulate}
+    stage = {k: v / fpw for k, v in (("raygen", st.ms_raygen), ("traverse (extension + shadow)", st.ms_trace),
+                                     ("shade", st.ms_shade), ("accumulate", st.ms_accumulate))}
     it.set_timing(False)
     # 2) counting pass: node fetches and triangle tests of the closest-hit launches
     it.set_counting(True)
-    it.render(frame)
+    it.render(frame, fpw)
     ct = it.stats()
     it.set_counting(False)
     ext_rays = ct.extension_rays
@@ -297,32 +314,40 @@ def run_ours(args, dist):
             "warp_tri_steps_per_node_step": ct.warp_tri_steps / max(1, ct.warp_node_steps),
             "alpha_tests_per_segment": ct.alpha_tests / max(1, ext_rays + sh_rays)}
 
-    # 3) warm-up, then K device-timed frames
-    for _ in range(args.warmup):
-        it.render(frame)
+    # 3) the K-frame job (config 1: 1 spp per frame, K frames accumulated), fpw
+    #    frames per wavefront; device-timed with CUDA events on the library stream
+    it.render(frame, max(args.warmup, fpw))
     ctx.synchronize()
-    events = [hx.Event(ctx) for _ in range(args.steps + 1)]
+    e0, e1 = hx.Event(ctx), hx.Event(ctx)
     clocks = Clocks(dist.local)
     dist.barrier()
     ctx.synchronize()
     clocks.start()
-    launches_before = 0
-    events[0].record()
-    launches = 0
-    for k in range(args.steps):
-        it.render(frame)
-        launches += it.stats().kernel_launches
-        events[k + 1].record()
-    frame_ms = [events[k].elapsed_ms(events[k + 1]) for k in range(args.steps)]
+    e0.record()
+    it.render(frame, args.steps)
+    e1.record()
     ctx.synchronize()
     clk = clocks.stop()
-    total_ms = events[0].elapsed_ms(events[-1])
+    launches = it.stats().kernel_launches
+    total_ms = e0.elapsed_ms(e1)
     total_ms = dist.allreduce(total_ms, "max")
     paths_all = dist.allreduce(paths_per_step * args.steps, "sum")
     value = paths_all / (total_ms / 1000.0) / 1e6
     seg_rate = dist.allreduce(segs_per_step * args.steps, "sum") / (total_ms / 1000.0) / 1e6
 
-    # 4) end to end through the C-ABI: frame constants from the host, tone-mapped frame to pinned host memory
+    # 4) progressive display, one frame per call: per-frame device latency, then
+    #    end to end through the C-ABI (frame constants from the host, the
+    #    tone-mapped RGBA8 frame to pinned host memory every frame)
+    prog_frames = min(args.steps, 64)
+    events = [hx.Event(ctx) for _ in range(prog_frames + 1)]
+    ctx.synchronize()
+    events[0].record()
+    for k in range(prog_frames):
+        it.render(frame)
+        events[k + 1].record()
+    ctx.synchronize()
+    frame_ms = [events[k].elapsed_ms(events[k + 1]) for k in range(prog_frames)]
+    prog_value = paths_per_step * prog_frames / (events[0].elapsed_ms(events[-1]) / 1000.0) / 1e6
     out = hx.PinnedBuffer((HEIGHT, WIDTH, 4), np.uint8)
     for _ in range(2):
         it.render(frame)
@@ -337,17 +362,20 @@ def run_ours(args, dist):
     e2e_s = time.perf_counter() - t0
     e2e_s = dist.allreduce(e2e_s, "max")
     e2e_value = paths_all / e2e_s / 1e6
-    launches_e2e = launches + args.steps  # + one tone-map launch per step
+    launches_e2e = it.stats().kernel_launches * args.steps + args.steps  # + one tone-map launch per frame
     out.close()
 
     peaks = load_peaks()
     hbm_peak = peaks["hbm_gbs"]
     achieved = alg_bytes_per_launch / (ms_trace_per_launch / 1000.0) / 1e9
     traffic = None
+    ncu = {}
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "trace_kernel_traffic.json")))
         if prof.get("kernel", "").startswith("k_extend"):
             traffic = prof["dram_bytes_per_segment"] * (ext_rays + sh_rays) / max(1, ct.trace_launches)
+            ncu = {k: prof[k] for k in ("dram_frac_of_peak", "l2_hit_pct", "l1_hit_pct", "issue_active_pct",
+                                        "source") if k in prof}
     except Exception:
         pass
 
@@ -367,19 +395,26 @@ def run_ours(args, dist):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": workload_config(),
                 "parallelism": "replicas" if dist.world > 1 else "single",
+                "frames_per_wavefront": fpw,
                 "mray_segments_per_s": seg_rate,
-                "frame_latency_ms": {"p50": float(np.percentile(fs, 50)), "p99": float(np.percentile(fs, 99)),
-                                     "max": fs[-1]},
+                "progressive_one_frame_per_call": {"mpaths_per_s": prog_value, "frames": prog_frames,
+                                                   "frame_latency_ms": {"p50": float(np.percentile(fs, 50)),
+                                                                        "p99": float(np.percentile(fs, 99)),
+                                                                        "max": fs[-1]}},
                 "segments_per_path": segs_per_step / paths_per_step,
                 "stage_ms_per_frame": stage,
                 "scene": {"triangles": info.num_triangles, "bvh8_nodes": info.num_bvh8_nodes,
                           "build_ms": info.build_ms, "device_mb": info.device_bytes / 2**20},
                 "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 128,
-                        "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
-                "gpu_launches": launches_e2e,
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                             "frac": achieved / hbm_peak, "traffic": traffic,
-                             "kernel": "k_extend (closest hit + shadow)",
+                        "d2h_bytes_per_step": WIDTH * HEIGHT * 4,
+                        "mode": "one frame per C-ABI call, tone-mapped RGBA8 read back every frame"},
+                "gpu_launches": launches,
+                "gpu_launches_e2e": launches_e2e,
+                "roofline": {"bound": "hbm", "limiter": "latency: dependent L1/L2 node and triangle fetches; "
+                                                        "the BVH is cache-resident, DRAM nearly idle",
+                             "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": achieved / hbm_peak, "traffic": traffic, "ncu": ncu,
+                             "kernel": "k_extend_batched (closest hit + shadow)",
                              "peak_source": peaks["source"],
                              "bytes_per_launch": alg_bytes_per_launch, "ms_per_launch": ms_trace_per_launch,
                              "node_fetches_per_segment": ct.node_visits / max(1, ext_rays + sh_rays),
@@ -522,14 +557,16 @@ def run_serving(args, dist):
 
 
 def run_precision(args, dist):
-    """Precision form at scale: 200 spheres + a terrain_size^2 fBm heightfield,
-    1920x1080, 16-bit ray/hit payloads, FP32 traversal, Kahan FP32
-    accumulation to args.spp samples.  Reports throughput, the relative RMSE
-    of the 16-bit-payload and FP32-payload images against the FP64 oracle
-    (the same args.spp-sample sequence, on args.ref_pixels seeded pixels), and
-    the primary hit-ID agreement of rays with 16-bit directions with FP32
-    rays; the quantised 8-bit BVH itself is hit-exact against the unquantised
-    binary tree (bit-exact tests)."""
+    """Precision form at scale (config 2): 200 spheres + a terrain_size^2 fBm
+    heightfield, 1920x1080; 8-bit quantised BVH8 boxes, 16-bit ray/hit
+    payloads, FP32 traversal, Kahan-compensated FP32 accumulation, to args.spp
+    (4096) samples per pixel and on to args.ref_spp (16384).  The FP64
+    oracle renders the same sample sequence to args.ref_spp on args.ref_pixels
+    seeded pixels (and to args.spp, to separate Monte Carlo noise from
+    arithmetic).  Reports throughput, the relative RMSE of each device image
+    against the 16k-spp FP64 oracle with its per-pixel distribution, and the
+    primary hit-ID agreement of the quantised BVH8 with the oracle's
+    unquantised binary tree and of 16-bit with FP32 ray directions."""
     import numpy as np
     import helios_gb300 as hx
     from oracle import binding as ob
@@ -541,54 +578,87 @@ def run_precision(args, dist):
     t_scene = time.time() - t0
     W, H = WIDTH, HEIGHT
     f = hx.frame_desc(hs.camera(), W, H)
+    spp, ref_spp = args.spp, max(args.spp, args.ref_spp)
     out = {"metric": "precision form: relative RMSE vs FP64 oracle", "mode": "precision", "n_gpus": 1,
            "scene": {"triangles": info.num_triangles, "bvh8_nodes": info.num_bvh8_nodes, "build_ms": info.build_ms,
                      "device_mb": info.device_bytes / 2**20, "setup_s": t_scene},
-           "width": W, "height": H, "spp": args.spp, "data": "synthetic"}
+           "width": W, "height": H, "spp": spp, "ref_spp": ref_spp, "data": "synthetic"}
+    pix = np.random.default_rng(11).choice(W * H, size=args.ref_pixels, replace=False).astype(np.uint32)
     imgs = {}
-    for name, fp16, kahan in (("fp16_kahan", True, True), ("fp32", False, False)):
+    for name, fp16, kahan in (("fp16_kahan", True, True), ("fp32_kahan", False, True), ("fp32", False, False)):
         pol = hx.policy_reference()
         pol.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
         pol.payload = hx.PAYLOAD_FP16 if fp16 else hx.PAYLOAD_FP32
         pol.accumulation = hx.ACCUM_KAHAN if kahan else hx.ACCUM_RUNNING_MEAN
-        it = hx.PathIntegrator(ctx, scene, W, H, max_ray_bounces=DEPTH, max_samples=args.spp, policy=pol)
+        it = hx.PathIntegrator(ctx, scene, W, H, max_ray_bounces=DEPTH, max_samples=ref_spp, policy=pol,
+                               max_paths_in_flight=W * H * 4)
         e0, e1 = hx.Event(ctx), hx.Event(ctx)
         ctx.synchronize()
         e0.record()
-        it.render(f, args.spp)
+        it.render(f, spp)
         e1.record()
         ms = e0.elapsed_ms(e1)
-        imgs[name] = it.read_accumulation()[:, :, :3].reshape(-1, 3).astype(np.float64)
-        out[name + "_mpaths_per_s"] = W * H * args.spp / (ms / 1000.0) / 1e6
+        out[name + "_mpaths_per_s"] = W * H * spp / (ms / 1000.0) / 1e6
+        imgs[(name, spp)] = it.read_accumulation()[:, :, :3].reshape(-1, 3).astype(np.float64)
+        if name != "fp32":
+            it.render(f, ref_spp - spp)
+            imgs[(name, ref_spp)] = it.read_accumulation()[:, :, :3].reshape(-1, 3).astype(np.float64)
         it.close()
     # FP64 oracle (FP32-payload semantics, reference policy, the same sample
-    # sequence: spp frames) on a seeded pixel subset, so the difference is
-    # the arithmetic and payload precision, not Monte Carlo noise
+    # sequence) on the seeded pixel subset
     osc = ob.OracleScene(hs)
     d = hx.IntegratorDesc()
     d.width, d.height, d.max_ray_bounces, d.max_samples = W, H, DEPTH, 1 << 30
     d.policy = hx.policy_reference()
     d.policy.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
-    pix = np.random.default_rng(11).choice(W * H, size=args.ref_pixels, replace=False).astype(np.uint32)
     t1 = time.time()
-    ref, cnt = osc.render(d, f, args.spp, precision=64, pixels=pix)
+    ref, cnt = osc.render(d, f, ref_spp, precision=64, pixels=pix)
+    ref_lo, _ = osc.render(d, f, spp, precision=64, pixels=pix)
+    # the oracle's own FP32 evaluation of the same samples: separates what FP32
+    # arithmetic does to the reference's algorithm from what the device does
+    ref32, _ = osc.render(d, f, spp, precision=32, pixels=pix)
     out["oracle_s"] = time.time() - t1
     out["oracle_pixels"] = int(pix.size)
+    out["oracle_threads"] = cnt.threads
 
-    def rr(a):
-        return float(np.linalg.norm(a - ref) / np.linalg.norm(ref))
-    out["rel_rmse_vs_fp64"] = {k: rr(v[pix]) for k, v in imgs.items()}
-    out["rel_rmse_fp16_vs_fp32_full_frame"] = float(np.linalg.norm(imgs["fp16_kahan"] - imgs["fp32"]) /
-                                                    np.linalg.norm(imgs["fp32"]))
-    # primary hit-ID agreement, FP16-direction vs FP32 rays (oracle's bit-exact traversal on a subset)
+    def rr(a, r=ref):
+        return float(np.linalg.norm(a - r) / np.linalg.norm(r))
+
+    def dist_of(a, r=ref):
+        e = np.abs(a - r).sum(1) / max(float(np.abs(r).sum(1).mean()), 1e-30)
+        q = np.percentile(e, [50, 90, 99, 99.9])
+        return {"p50": float(q[0]), "p90": float(q[1]), "p99": float(q[2]), "p99.9": float(q[3]),
+                "share_of_squared_error_top_1pct": float(np.sort(e ** 2)[-max(1, e.size // 100):].sum() /
+                                                         max((e ** 2).sum(), 1e-300))}
+    rel = {}
+    for (name, n), img in imgs.items():
+        rel["%s@%d_vs_fp64@%d" % (name, n, ref_spp)] = {"rel_rmse": rr(img[pix]), "per_pixel_abs_err_over_mean":
+                                                       dist_of(img[pix])}
+    # the Monte Carlo part: the FP64 oracle's own spp-sample image against its ref_spp one
+    rel["fp64@%d_vs_fp64@%d (noise of %d spp)" % (spp, ref_spp, spp)] = {"rel_rmse": rr(ref_lo)}
+    # the arithmetic part at spp: device vs the FP64 oracle at the same spp and sequence
+    for name in ("fp16_kahan", "fp32_kahan", "fp32"):
+        rel["%s@%d_vs_fp64@%d" % (name, spp, spp)] = {"rel_rmse": rr(imgs[(name, spp)][pix], ref_lo)}
+    rel["oracle_fp32@%d_vs_fp64@%d (FP32 arithmetic of the algorithm itself)" % (spp, spp)] = {
+        "rel_rmse": rr(ref32, ref_lo), "per_pixel_abs_err_over_mean": dist_of(ref32, ref_lo)}
+    rel["fp32@%d_vs_oracle_fp32@%d (device vs FP32 oracle)" % (spp, spp)] = {
+        "rel_rmse": rr(imgs[("fp32", spp)][pix], ref32)}
+    out["rel_rmse"] = rel
+    out["rel_rmse_fp16_vs_fp32_full_frame@%d" % spp] = float(
+        np.linalg.norm(imgs[("fp16_kahan", spp)] - imgs[("fp32_kahan", spp)]) /
+        np.linalg.norm(imgs[("fp32_kahan", spp)]))
+    # primary hit IDs: quantised BVH8 (device) vs the oracle's unquantised
+    # binary tree, FP32 rays; and 16-bit-direction rays vs FP32 rays
     d16 = hx.IntegratorDesc()
     d16.width, d16.height, d16.max_ray_bounces, d16.max_samples = W, H, 1, 1
     d16.policy = hx.policy_reference()
     d16.policy.payload = hx.PAYLOAD_FP16
     sub = np.random.default_rng(12).choice(W * H, size=65536, replace=False).astype(np.uint32)
-    _, h16 = osc.sample_radiance(d16, f, 0, precision=32, pixels=sub)
     r32 = ob.primary_rays(d16, f, 0)[sub]
     gh = scene.trace(r32, any_hit=True)
+    oh = osc.trace(r32, any_hit=True)
+    out["primary_hit_agreement_quantised_bvh8_vs_unquantised"] = float((gh["prim"] == oh["prim"]).mean())
+    _, h16 = osc.sample_radiance(d16, f, 0, precision=32, pixels=sub)
     out["primary_hit_agreement_fp16_vs_fp32"] = float((h16["prim"] == gh["prim"]).mean())
     osc.close()
     scene.close()

@@ -149,7 +149,7 @@ extern "C" hx_status hx_save_png(const char* path, const uint8_t* rgba8, uint32_
 namespace {
 
 uint32_t block_bytes(uint32_t fmt) {
-    return (fmt == HX_TEXTURE_BC1_RGB || fmt == HX_TEXTURE_BC1_RGBA || fmt == HX_TEXTURE_BC4) ? 8u : 16u;
+    return (fmt == HX_TEXTURE_BC1_RGB || fmt == HX_TEXTURE_BC1_RGBA || fmt == HX_TEXTURE_BC4) ? 8u : 16u;  // BC2/3/5/7: 16
 }
 
 uint64_t le64(const uint8_t* p) {
@@ -209,11 +209,147 @@ void decode_channel(const uint8_t* b, uint8_t out[16]) {
     for (int t = 0; t < 16; ++t) out[t] = (uint8_t)p[(idx >> (3 * t)) & 7u];
 }
 
+// ---- BC7 (BPTC UNORM; Khronos Data Format Specification, "BC7") -----------
+// Eight modes, chosen by the position of the first set bit of the block.  A
+// mode fixes the number of subsets (1-3), the partition and rotation fields,
+// the endpoint precision (colour / alpha bits, per-endpoint or shared
+// p-bits) and the index precision (one or two index sets).  Endpoints widen
+// to 8 bits by bit replication, interpolate with the 6-bit weights
+// ((64 - w) e0 + w e1 + 32) >> 6; the first index of each subset (its
+// anchor) is stored with one bit less.  A block with no mode bit decodes to
+// zero.
+struct Bc7Mode {
+    int subsets, partition_bits, rotation_bits, index_select_bits;
+    int colour_bits, alpha_bits, endpoint_pbits, shared_pbits, index_bits, index2_bits;
+};
+const Bc7Mode kBc7Modes[8] = {
+    {3, 4, 0, 0, 4, 0, 1, 0, 3, 0}, {2, 6, 0, 0, 6, 0, 0, 1, 3, 0}, {3, 6, 0, 0, 5, 0, 0, 0, 2, 0},
+    {2, 6, 0, 0, 7, 0, 1, 0, 2, 0}, {1, 0, 2, 1, 5, 6, 0, 0, 2, 3}, {1, 0, 2, 0, 7, 8, 0, 0, 2, 2},
+    {1, 0, 0, 0, 7, 7, 1, 0, 4, 0}, {2, 6, 0, 0, 5, 5, 1, 0, 2, 0}};
+// Two-subset partitions: bit t set = texel t in subset 1 (texel t = x + 4 y).
+const uint16_t kBc7Part2[64] = {
+    0xCCCC, 0x8888, 0xEEEE, 0xECC8, 0xC880, 0xFEEC, 0xFEC8, 0xEC80, 0xC800, 0xFFEC, 0xFE80, 0xE800, 0xFFE8,
+    0xFF00, 0xFFF0, 0xF000, 0xF710, 0x008E, 0x7100, 0x08CE, 0x008C, 0x7310, 0x3100, 0x8CCE, 0x088C, 0x3110,
+    0x6666, 0x366C, 0x17E8, 0x0FF0, 0x718E, 0x399C, 0xAAAA, 0xF0F0, 0x5A5A, 0x33CC, 0x3C3C, 0x55AA, 0x9696,
+    0xA55A, 0x73CE, 0x13C8, 0x324C, 0x3BDC, 0x6996, 0xC33C, 0x9966, 0x0660, 0x0272, 0x04E4, 0x4E40, 0x2720,
+    0xC936, 0x936C, 0x39C6, 0x639C, 0x9336, 0x9CC6, 0x817E, 0xE718, 0xCCF0, 0x0FCC, 0x7744, 0xEE22};
+// Three-subset partitions: two bits per texel (texel t at bits 2t).
+const uint32_t kBc7Part3[64] = {
+    0xAA685050, 0x6A5A5040, 0x5A5A4200, 0x5450A0A8, 0xA5A50000, 0xA0A05050, 0x5555A0A0, 0x5A5A5050,
+    0xAA550000, 0xAA555500, 0xAAAA5500, 0x90909090, 0x94949494, 0xA4A4A4A4, 0xA9A59450, 0x2A0A4250,
+    0xA5945040, 0x0A425054, 0xA5A5A500, 0x55A0A0A0, 0xA8A85454, 0x6A6A4040, 0xA4A45000, 0x1A1A0500,
+    0x0050A4A4, 0xAAA59090, 0x14696914, 0x69691400, 0xA08585A0, 0xAA821414, 0x50A4A450, 0x6A5A0200,
+    0xA9A58000, 0x5090A0A8, 0xA8A09050, 0x24242424, 0x00AA5500, 0x24924924, 0x24499224, 0x50A50A50,
+    0x500AA550, 0xAAAA4444, 0x66660000, 0xA5A0A5A0, 0x50A050A0, 0x69286928, 0x44AAAA44, 0x66666600,
+    0xAA444444, 0x54A854A8, 0x95809580, 0x96969600, 0xA85454A8, 0x80959580, 0xAA141414, 0x96960000,
+    0xAAAA1414, 0xA05050A0, 0xA0A5A5A0, 0x96000000, 0x40804080, 0xA9A8A9A8, 0xAAAAAA44, 0x2A4A5254};
+// Anchor texel of subset 1 (two subsets), of subsets 1 and 2 (three subsets).
+const uint8_t kBc7Anchor2[64] = {15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 2,  8,  2,  2,  8,
+                                 8,  15, 2,  8,  2,  2,  8,  8,  2,  2,  15, 15, 6,  8,  2,  8,  15, 15, 2,  8,  2,  2,
+                                 2,  15, 15, 6,  6,  2,  6,  8,  15, 15, 2,  2,  15, 15, 15, 15, 15, 2,  2,  15};
+const uint8_t kBc7Anchor3a[64] = {3,  3,  15, 15, 8,  3,  15, 15, 8,  8,  6,  6,  6,  5,  3,  3,  3,  3,  8,  15, 3,  3,
+                                  6,  10, 5,  8,  8,  6,  8,  5,  15, 15, 8,  15, 3,  5,  6,  10, 8,  15, 15, 3,  15, 5,
+                                  15, 15, 15, 15, 3,  15, 5,  5,  5,  8,  5,  10, 5,  10, 8,  13, 15, 12, 3,  3};
+const uint8_t kBc7Anchor3b[64] = {15, 8,  8,  3,  15, 15, 3,  8,  15, 15, 15, 15, 15, 15, 15, 8,  15, 8,  15, 3,  15, 8,
+                                  15, 8,  3,  15, 6,  10, 15, 15, 10, 8,  15, 3,  15, 10, 10, 8,  9,  10, 6,  15, 8,  15,
+                                  3,  6,  6,  8,  15, 3,  15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 3,  15, 15, 8};
+const uint8_t kBc7W2[4] = {0, 21, 43, 64};
+const uint8_t kBc7W3[8] = {0, 9, 18, 27, 37, 46, 55, 64};
+const uint8_t kBc7W4[16] = {0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64};
+
+struct BitReader {
+    const uint8_t* b;
+    int pos = 0;
+    uint32_t get(int n) {
+        uint32_t v = 0;
+        for (int k = 0; k < n; ++k, ++pos) v |= (uint32_t)((b[pos >> 3] >> (pos & 7)) & 1u) << k;
+        return v;
+    }
+};
+
+uint32_t bc7_interp(uint32_t e0, uint32_t e1, uint32_t idx, int bits) {
+    const uint8_t* w = bits == 2 ? kBc7W2 : (bits == 3 ? kBc7W3 : kBc7W4);
+    return ((64u - w[idx]) * e0 + w[idx] * e1 + 32u) >> 6;
+}
+
+void decode_bc7(const uint8_t* blk, uint8_t out[16][4]) {
+    int mode = 0;
+    while (mode < 8 && !(blk[0] & (1u << mode))) ++mode;
+    if (mode == 8) {
+        for (int t = 0; t < 16; ++t) out[t][0] = out[t][1] = out[t][2] = out[t][3] = 0;
+        return;
+    }
+    const Bc7Mode& M = kBc7Modes[mode];
+    BitReader br{blk};
+    br.get(mode + 1);
+    const uint32_t part = br.get(M.partition_bits);
+    const uint32_t rot = br.get(M.rotation_bits);
+    const uint32_t isel = br.get(M.index_select_bits);
+    const int ne = 2 * M.subsets;
+    uint32_t e[6][4];
+    for (int ch = 0; ch < 3; ++ch)
+        for (int k = 0; k < ne; ++k) e[k][ch] = br.get(M.colour_bits);
+    for (int k = 0; k < ne; ++k) e[k][3] = M.alpha_bits ? br.get(M.alpha_bits) : 255u;
+    int cbits = M.colour_bits, abits = M.alpha_bits;
+    if (M.endpoint_pbits || M.shared_pbits) {
+        uint32_t pb[6];
+        if (M.endpoint_pbits)
+            for (int k = 0; k < ne; ++k) pb[k] = br.get(1);
+        else
+            for (int s = 0; s < M.subsets; ++s) pb[2 * s] = pb[2 * s + 1] = br.get(1);
+        for (int k = 0; k < ne; ++k) {
+            for (int ch = 0; ch < 3; ++ch) e[k][ch] = (e[k][ch] << 1) | pb[k];
+            if (abits) e[k][3] = (e[k][3] << 1) | pb[k];
+        }
+        ++cbits;
+        if (abits) ++abits;
+    }
+    for (int k = 0; k < ne; ++k) {
+        for (int ch = 0; ch < 3; ++ch) e[k][ch] = (e[k][ch] << (8 - cbits)) | (e[k][ch] >> (2 * cbits - 8));
+        if (abits) e[k][3] = (e[k][3] << (8 - abits)) | (e[k][3] >> (2 * abits - 8));
+    }
+    uint32_t subset[16], anchor[3] = {0, 0, 0};
+    for (int t = 0; t < 16; ++t)
+        subset[t] = M.subsets == 1 ? 0u : (M.subsets == 2 ? (kBc7Part2[part] >> t) & 1u : (kBc7Part3[part] >> (2 * t)) & 3u);
+    if (M.subsets == 2) anchor[1] = kBc7Anchor2[part];
+    if (M.subsets == 3) {
+        anchor[1] = kBc7Anchor3a[part];
+        anchor[2] = kBc7Anchor3b[part];
+    }
+    auto is_anchor = [&](int t) {
+        for (int s = 0; s < M.subsets; ++s)
+            if ((uint32_t)t == anchor[s]) return true;
+        return false;
+    };
+    uint32_t idx1[16], idx2[16];
+    for (int t = 0; t < 16; ++t) idx1[t] = br.get(M.index_bits - (is_anchor(t) ? 1 : 0));
+    if (M.index2_bits)
+        for (int t = 0; t < 16; ++t) idx2[t] = br.get(M.index2_bits - (t == 0 ? 1 : 0));
+    for (int t = 0; t < 16; ++t) {
+        const uint32_t s = subset[t];
+        const uint32_t* e0 = e[2 * s];
+        const uint32_t* e1 = e[2 * s + 1];
+        uint32_t c[4];
+        if (M.index2_bits) {
+            // modes 4 and 5: colour from one index set, alpha from the other
+            // (mode 4 swaps the sets when its selection bit is set)
+            const uint32_t ci = isel ? idx2[t] : idx1[t], ai = isel ? idx1[t] : idx2[t];
+            const int cb = isel ? M.index2_bits : M.index_bits, ab = isel ? M.index_bits : M.index2_bits;
+            for (int ch = 0; ch < 3; ++ch) c[ch] = bc7_interp(e0[ch], e1[ch], ci, cb);
+            c[3] = bc7_interp(e0[3], e1[3], ai, ab);
+        } else {
+            for (int ch = 0; ch < 4; ++ch) c[ch] = bc7_interp(e0[ch], e1[ch], idx1[t], M.index_bits);
+        }
+        if (rot) std::swap(c[3], c[rot - 1]);  // 1: swap A,R; 2: A,G; 3: A,B
+        for (int ch = 0; ch < 4; ++ch) out[t][ch] = (uint8_t)c[ch];
+    }
+}
+
 }  // namespace
 
 extern "C" hx_status hx_texture_decode(const hx_texture_desc* tex, uint8_t* out) {
     HX_CHECK_ARG(tex && out && tex->rgba8 && tex->width > 0 && tex->height > 0, "hx_texture_decode: null argument or empty texture");
-    HX_CHECK_ARG(tex->format <= HX_TEXTURE_BC5, "hx_texture_decode: unknown format %u", tex->format);
+    HX_CHECK_ARG(tex->format <= HX_TEXTURE_BC7, "hx_texture_decode: unknown format %u", tex->format);
     const uint32_t W = tex->width, H = tex->height;
     if (tex->format == HX_TEXTURE_RGBA8) {
         std::copy(tex->rgba8, tex->rgba8 + (size_t)W * H * 4, out);
@@ -241,6 +377,7 @@ extern "C" hx_status hx_texture_decode(const hx_texture_desc* tex, uint8_t* out)
                     decode_channel(b, ch);
                     for (int t = 0; t < 16; ++t) { px[t][0] = ch[t]; px[t][1] = px[t][2] = 0; px[t][3] = 255; }
                     break;
+                case HX_TEXTURE_BC7: decode_bc7(b, px); break;
                 default:  // BC5
                     decode_channel(b, ch);
                     for (int t = 0; t < 16; ++t) { px[t][0] = ch[t]; px[t][2] = 0; px[t][3] = 255; }

@@ -4,7 +4,7 @@
 // (path_trace_rgen.glsl:217-248, tone_map.frag).
 //
 // One progressive frame = one sample per pixel of the current tile.  Several
-// frames can share one wavefront (paths p = frame * npix + pixel); the
+// frames can share one wavefront (paths p = pixel * nframes + frame); the
 // accumulation then replays them in frame order, so the image is identical
 // to frame-by-frame rendering.
 //
@@ -298,9 +298,11 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             k_raygen_debug<<<it->grid_gen, kGenThreads, 0, st>>>(f, dbg->px, dbg->py, it->desc.width, it->desc.height, dbg->n,
                                                                  frame0, P.rng, it->q);
         else if (fp16)
-            k_raygen<true><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, 0, total, P.rng, it->q);
+            k_raygen<true><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, 0,
+                                                                 total, P.rng, it->q);
         else
-            k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, 0, total, P.rng, it->q);
+            k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(f, rect, it->desc.width, it->desc.height, frame0, nframes, 0,
+                                                                  total, P.rng, it->q);
         it->stats.kernel_launches++;
     }
     {
@@ -766,7 +768,7 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     HX_CHECK_ARG((uint64_t)W * H <= it->capacity, "frame exceeds wavefront capacity");
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
-    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 0, W * H, P.rng, it->q);
+    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, 0, W * H, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));
     launch_primary_trace(it, st);
     uint32_t n = W * H;
@@ -794,7 +796,7 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     }
     Rect r{0, 0, W, H};
     Policy P = make_policy(it->desc.policy);
-    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 0, W * H, P.rng, it->q);
+    k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, 0, W * H, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));
     launch_primary_trace(it, st);
     k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, n, d_features);

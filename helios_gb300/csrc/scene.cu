@@ -262,7 +262,7 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
     for (uint32_t t = 0; t < desc->num_textures; ++t) {
         HX_CHECK_ARG(desc->textures[t].rgba8 && desc->textures[t].width > 0 && desc->textures[t].height > 0,
                      "texture %u: empty", t);
-        HX_CHECK_ARG(desc->textures[t].format <= HX_TEXTURE_BC5, "texture %u: unknown format %u", t,
+        HX_CHECK_ARG(desc->textures[t].format <= HX_TEXTURE_BC7, "texture %u: unknown format %u", t,
                      desc->textures[t].format);
     }
     for (uint32_t l = 0; l < desc->num_punctual_lights; ++l) {

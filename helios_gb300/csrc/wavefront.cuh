@@ -140,16 +140,21 @@ HXD uint32_t half2_bits(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
+// Path p of a wavefront over nframes frames of a rect: the frames interleave
+// per pixel (p = pixel * nframes + frame), so the lanes of a warp carry the
+// samples of a few neighbouring pixels (near-identical camera rays: coherent
+// node fetches in the first bounce).  Results do not depend on the order.
+HXD uint32_t path_index(uint32_t pix, uint32_t fr, uint32_t nframes) { return pix * nframes + fr; }
+
 // Camera rays of paths [path_base, path_base + path_count) of the rect's
-// nframes frames (path p = frame * npix + pixel); path p goes to ray-queue
-// slot p - path_base, its state (T, L, rng) stays indexed by p.
+// nframes frames (path_index); path p goes to ray-queue slot p - path_base,
+// its state (T, L, rng) stays indexed by p.
 template <bool FP16>
-__global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uint32_t frame0, uint32_t path_base,
-                         uint32_t path_count, uint32_t kind, Queues q) {
-    uint32_t npix = rect.w * rect.h;
+__global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uint32_t frame0, uint32_t nframes,
+                         uint32_t path_base, uint32_t path_count, uint32_t kind, Queues q) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < path_count; k += gridDim.x * blockDim.x) {
         const uint32_t p = path_base + k;
-        uint32_t fr = p / npix, pix = p - fr * npix;
+        const uint32_t pix = p / nframes, fr = p - pix * nframes;
         uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
         Rng rng = rng_init(kind, x, y, W, frame0 + fr);
         V3 o, d;
@@ -626,7 +631,7 @@ __global__ void k_accumulate(Rect rect, uint32_t W, uint32_t frame0, uint32_t nf
         float4 a = acc[idx];
         float4 cp = kahan ? comp[idx] : make_float4(0, 0, 0, 0);
         for (uint32_t f = 0; f < nframes; ++f) {
-            float4 l = L[(size_t)f * npix + pix];
+            float4 l = L[path_index(pix, f, nframes)];
             float c[3] = {l.x, l.y, l.z};
             if (clampv > 0.0f)
                 for (int k = 0; k < 3; ++k) c[k] = gmin(c[k], clampv);
@@ -755,7 +760,7 @@ __global__ void k_aov_accumulate(DevScene s, Rect rect, uint32_t frame0, uint32_
         const size_t o = (size_t)y * W + x;
         float4 a = aov_a[o], nn = aov_n[o];
         for (uint32_t fr = 0; fr < nframes; ++fr) {
-            const uint32_t p = fr * npix + pix;
+            const uint32_t p = path_index(pix, fr, nframes);
             uint32_t prim;
             float t, u, v;
             if (FP16) {

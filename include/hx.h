@@ -160,6 +160,7 @@ typedef struct hx_instance {
 #define HX_TEXTURE_BC3      4u  /* 16-byte blocks: interpolated alpha + colour        */
 #define HX_TEXTURE_BC4      5u  /* 8-byte blocks: R (G = B = 0, A = 255)              */
 #define HX_TEXTURE_BC5      6u  /* 16-byte blocks: R, G (B = 0, A = 255)              */
+#define HX_TEXTURE_BC7      7u  /* 16-byte blocks: BPTC RGBA, 8 modes, 1-3 subsets     */
 typedef struct hx_texture_desc {
     const uint8_t* rgba8;
     uint32_t       width;
@@ -173,7 +174,10 @@ typedef struct hx_texture_desc {
  * bit replication; interpolated palette entries round to nearest:
  * (2a + b + 1) / 3 and (a + b + 1) / 2 for colour, ((8 - k) a + (k - 1) b + 3) / 7
  * and ((6 - k) a + (k - 1) b + 2) / 5 for BC4-style channels; BC2 alpha is
- * a4 * 17.  The 3-colour mode (c0 <= c1) exists in BC1 blocks only. */
+ * a4 * 17.  The 3-colour mode (c0 <= c1) exists in BC1 blocks only.  BC7
+ * follows the BPTC specification exactly (its interpolation is integer:
+ * ((64 - w) e0 + w e1 + 32) >> 6); a block with a reserved mode decodes to
+ * zero.  BC6H (HDR) is not supported (the texture path is 8-bit). */
 HX_API hx_status hx_texture_decode(const hx_texture_desc* texture, uint8_t* rgba8_out);
 
 #define HX_ENV_NONE          0u  /* black environment                        */
@@ -252,7 +256,9 @@ typedef struct hx_integrator_desc {
     uint32_t  max_samples;         /* default 5000, path_integrator.h:48            */
     float     shadow_ray_bias;     /* default 0, path_integrator.h:51               */
     uint32_t  tiled;               /* 128x128 tiles, path_integrator.cpp:7,312-336  */
-    uint32_t  max_paths_in_flight; /* wavefront capacity (0 = width*height)         */
+    uint32_t  max_paths_in_flight; /* wavefront capacity in paths (0 = max(width*height,
+                                      2^22)); k*width*height lets render_frames trace
+                                      k frames per wavefront (same result)         */
     uint32_t  reserved;
     hx_policy policy;
 } hx_integrator_desc;

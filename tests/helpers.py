@@ -210,6 +210,17 @@ def bump_normal_map(size=64, freq=3, amp=0.35):
     return rgba
 
 
+def random_bc7_blocks(n, seed=0):
+    """n random BC7 blocks (16 bytes each) cycling through all eight modes:
+    the low bits of byte 0 select the mode, every other bit is random."""
+    rng = np.random.default_rng(seed)
+    blocks = rng.integers(0, 256, size=(n, 16), dtype=np.uint8)
+    for i in range(n):
+        m = i % 8
+        blocks[i, 0] = (int(blocks[i, 0]) & ~((1 << (m + 1)) - 1) & 0xFF) | (1 << m)
+    return blocks
+
+
 def checker_texture(size=32, a=(200, 180, 150), b=(40, 60, 90)):
     y, x = np.mgrid[0:size, 0:size]
     sel = ((x // 4 + y // 4) % 2 == 0)[..., None]

@@ -77,7 +77,7 @@ def test_normal_map_and_srgb_change_the_result(gpu_ctx):
     assert rel_rmse(out["nmap"][0], out["plain"][0]) > 0.01
 
 
-@pytest.mark.parametrize("fmt", [hx.TEXTURE_BC1_RGB, hx.TEXTURE_BC3, hx.TEXTURE_BC5])
+@pytest.mark.parametrize("fmt", [hx.TEXTURE_BC1_RGB, hx.TEXTURE_BC3, hx.TEXTURE_BC5, hx.TEXTURE_BC7])
 def test_block_compressed_albedo_renders_like_its_decoded_texels(gpu_ctx, fmt):
     """A BCn albedo texture (decoded at upload) gives the same accumulated
     image and albedo view, bit for bit, as uploading its RGBA8 decode."""
@@ -100,3 +100,40 @@ def test_block_compressed_albedo_renders_like_its_decoded_texels(gpu_ctx, fmt):
         sc.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert np.any(out[0][1][..., :3] != 0)
+
+
+def _texture_unit_bc7():
+    """tests/hw/bc7_texture_unit.cu built for sm_103a into a temporary library:
+    BC7 blocks decoded by the GPU's own texture unit."""
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+    import tempfile
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "hw", "bc7_texture_unit.cu")
+    out = os.path.join(tempfile.mkdtemp(), "libbc7tu.so")
+    nvcc = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-shared", "-Xcompiler", "-fPIC",
+                    "-o", out, src], check=True, capture_output=True)
+    lib = ctypes.CDLL(out)
+    lib.bc7_texture_unit_decode.restype = ctypes.c_int
+    lib.bc7_texture_unit_decode.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    return lib
+
+
+def test_bc7_decode_matches_the_texture_unit(gpu_ctx):
+    """The library's BC7 decoder (hx_texture_decode) against the GPU's
+    texture unit on 4,096 random blocks of all eight modes (every partition,
+    rotation and index-selection value occurs): identical RGBA8 texels.  The
+    format's interpolation is exact integer arithmetic, so any mismatch is a
+    decoding error (a table entry, a bit field)."""
+    from tests.helpers import random_bc7_blocks
+    lib = _texture_unit_bc7()
+    blocks = np.ascontiguousarray(random_bc7_blocks(64 * 64, seed=3))
+    got = hx.texture_decode(blocks.reshape(-1), 256, 256, hx.TEXTURE_BC7)
+    hw = np.zeros((256, 256, 4), np.uint8)
+    rc = lib.bc7_texture_unit_decode(blocks.ctypes.data, 64, 64, hw.ctypes.data)
+    assert rc == 0, "CUDA error %d" % rc
+    bad = np.nonzero((got != hw).any(-1).reshape(64, 4, 64, 4).any(axis=(1, 3)).reshape(-1))[0]
+    info = [(int(b), int(b % 8), blocks[b].tobytes().hex()) for b in bad[:8]]
+    assert bad.size == 0, (bad.size, info)

@@ -146,3 +146,39 @@ def test_block_compressed_texture_decode_matches_restatement():
     out2 = hx.texture_decode(blk2, 4, 4, hx.TEXTURE_BC1_RGBA).reshape(-1, 4)
     assert (out2[:8] == np.array([128, 0, 128, 255], np.uint8)).all()
     assert (out2[8:] == 0).all()
+
+
+def test_bc7_decode_matches_restatement():
+    """BC7 (BPTC): hx_texture_decode equals the restatement of the published
+    format on random blocks of all eight modes (and the reserved all-zero
+    mode byte), and a hand-computed mode-6 block.  The GPU's own texture
+    unit checks the same decoder in tests/test_gpu_textures.py."""
+    from oracle import texture_ref as tr
+    from tests.helpers import random_bc7_blocks
+    blocks = random_bc7_blocks(4096, seed=7)
+    blocks[5, 0] = 0  # reserved: decodes to zero
+    data = blocks.reshape(-1)
+    w, h = 4 * 64, 4 * 64
+    got = hx.texture_decode(data, w, h, hx.TEXTURE_BC7)
+    ref = tr.decode(data, w, h, tr.BC7)
+    assert np.array_equal(got, ref)
+    assert (got[0:4, 20:24] == 0).all()
+    assert np.array_equal(hx.texture_decode(data[:16 * 12], 13, 7, hx.TEXTURE_BC7), tr.decode(data[:16 * 12], 13, 7, tr.BC7))
+    # mode 6 (bit 6 of byte 0), RGBA 7+7 bits with per-endpoint p-bits, 4-bit
+    # indices: e0 = (0, 127, 254, 1) p 0 -> (0, 254, 252, 2), e1 = (127, 0, 0, 127)
+    # p 1 -> (255, 1, 1, 255) after 8-bit widening; every index 15 except the
+    # anchor (3 bits, value 7); weights 64 -> e1, 30 (index 7) ->
+    # ((64 - 30) e0 + 30 e1 + 32) >> 6
+    bits = 1 << 6
+    pos = 7
+    fields = [(0, 7), (127, 7), (127, 7), (0, 7), (254 >> 1, 7), (0, 7), (1, 7), (127, 7), (0, 1), (1, 1), (7, 3)]
+    fields += [(15, 4)] * 15
+    for v, nb in fields:
+        bits |= v << pos
+        pos += nb
+    blk = np.frombuffer(bits.to_bytes(16, "little"), np.uint8)
+    px = hx.texture_decode(blk, 4, 4, hx.TEXTURE_BC7).reshape(16, 4)
+    e0 = np.array([0, 254, 254, 2])
+    e1 = np.array([255, 1, 1, 255])
+    assert (px[1:] == e1).all(), px[1]
+    assert (px[0] == ((64 - 30) * e0 + 30 * e1 + 32) >> 6).all(), px[0]
