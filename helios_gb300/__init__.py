@@ -25,6 +25,7 @@ ENV_SAMPLE_COSINE, ENV_SAMPLE_IMPORTANCE = 0, 1
 PAYLOAD_FP32, PAYLOAD_FP16 = 0, 1
 TONEMAP_ACES, TONEMAP_REINHARD, TONEMAP_NONE = 0, 1, 2
 TEXTURE_RGBA8, TEXTURE_BC1_RGB, TEXTURE_BC1_RGBA, TEXTURE_BC2, TEXTURE_BC3, TEXTURE_BC4, TEXTURE_BC5, TEXTURE_BC7 = range(8)
+TEXTURE_BC6H_SF16, TEXTURE_BC6H_UF16, TEXTURE_RGBA16F = 8, 9, 10
 OUTPUT_ALBEDO, OUTPUT_NORMALS, OUTPUT_ROUGHNESS, OUTPUT_METALLIC, OUTPUT_EMISSIVE, OUTPUT_FINAL = 0, 1, 2, 3, 4, 5
 SCENE_BOX, SCENE_ICOSPHERES, SCENE_TERRAIN = 0, 1, 2
 SUBMESH_NON_OPAQUE = 1
@@ -210,6 +211,9 @@ _SIGS = {
     "hx_integrator_progress": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "hx_integrator_tonemap": (C.c_int, [_P, C.c_uint32, C.c_float, _P]),
     "hx_integrator_read_accumulation": (C.c_int, [_P, _P]),
+    "hx_integrator_checkpoint_size": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
+    "hx_integrator_save_checkpoint": (C.c_int, [_P, _P, C.c_size_t]),
+    "hx_integrator_load_checkpoint": (C.c_int, [_P, _P, C.c_size_t]),
     "hx_integrator_render_output": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, _P]),
     "hx_integrator_gather_debug_rays": (C.c_int, [_P, C.POINTER(FrameDesc), C.c_uint32, C.c_uint32, C.c_uint32, _P,
                                                   C.c_uint32, C.POINTER(C.c_uint32)]),
@@ -272,6 +276,7 @@ _SIGS = {
     "hx_encode_png": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "hx_save_png": (C.c_int, [C.c_char_p, _P, C.c_uint32, C.c_uint32]),
     "hx_texture_decode": (C.c_int, [C.POINTER(TextureDesc), _P]),
+    "hx_texture_decode_hdr": (C.c_int, [C.POINTER(TextureDesc), _P]),
 }
 
 _lib_handle = None
@@ -351,6 +356,17 @@ def texture_decode(data, width, height, fmt):
     out = np.zeros((height, width, 4), np.uint8)
     check(lib().hx_texture_decode(C.byref(t), _ptr(out)))
     return out
+
+
+def texture_decode_hdr(data, width, height, fmt):
+    """RGBA16F (height, width, 4) float16 of a half-float texture (TEXTURE_BC6H_SF16/_UF16/RGBA16F)."""
+    buf = np.ascontiguousarray(np.frombuffer(np.ascontiguousarray(data).tobytes(), np.uint8))
+    t = TextureDesc()
+    t.rgba8 = buf.ctypes.data_as(C.POINTER(C.c_uint8))
+    t.width, t.height, t.format = width, height, fmt
+    out = np.zeros((height, width, 4), np.uint16)
+    check(lib().hx_texture_decode_hdr(C.byref(t), _ptr(out)))
+    return out.view(np.float16)
 
 
 def save_png(path, rgba8):
@@ -579,6 +595,19 @@ class PathIntegrator:
         out = np.zeros((self.height, self.width, 4), np.float32)
         check(lib().hx_integrator_read_accumulation(self.handle, _ptr(out)))
         return out
+
+    def save_checkpoint(self):
+        """The progressive bake state (header + images) as bytes."""
+        n = C.c_size_t()
+        check(lib().hx_integrator_checkpoint_size(self.handle, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        check(lib().hx_integrator_save_checkpoint(self.handle, _ptr(buf), buf.size))
+        return buf.tobytes()
+
+    def load_checkpoint(self, data):
+        """Restore a state written by save_checkpoint (same size, max_samples, tiling, accumulation mode)."""
+        buf = np.frombuffer(bytes(data), np.uint8)
+        check(lib().hx_integrator_load_checkpoint(self.handle, _ptr(buf), buf.size))
 
     def render_output(self, frame, output_buffer):
         """Renderer output buffer (OUTPUT_ALBEDO .. OUTPUT_FINAL): (H, W, 4) float32, display row order."""

@@ -18,7 +18,6 @@
 #include "hx_internal.h"
 
 #include <algorithm>
-#include <mutex>
 
 namespace {
 
@@ -788,10 +787,6 @@ constexpr size_t kNoAllocScratchBytes = kNoAllocOffRadix + kNoAllocRadixBytes;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
 }  // namespace
 
 extern "C" hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n, uint32_t* d_morton,
@@ -801,23 +796,15 @@ extern "C" hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n,
                  "hx_lbvh_sort_noalloc: %u triangles; this entry point handles 1..%u (its scratch is a fixed %zu-byte "
                  "device array)", n, kNoAllocMaxTriangles, (size_t)kNoAllocScratchBytes);
     HX_CHECK_ARG(hx_radix_temp_bytes(n) <= kNoAllocRadixBytes, "hx_lbvh_sort_noalloc: radix scratch too small");
-    int dev = 0;
-    HX_CUDA(cudaGetDevice(&dev));
-    HX_CHECK_ARG(dev >= 0 && dev < kNoAllocMaxDevices, "hx_lbvh_sort_noalloc: device %d out of range", dev);
+    // the array's address on the current device, looked up on every call (a host-side table lookup, no
+    // allocation) so that it stays right after a cudaDeviceReset reloads the module
     void* base = nullptr;
     {
-        // once per device, with that device current: the device address of the array
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess) {
-                hx_set_error("hx_lbvh_sort_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-                return HX_ERR_DEVICE;
-            }
-            g_noalloc_ptr[dev] = p;
+        cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            hx_set_error("hx_lbvh_sort_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            return HX_ERR_DEVICE;
         }
-        base = g_noalloc_ptr[dev];
     }
     cudaStream_t st = (cudaStream_t)cuda_stream;
     char* b = (char*)base;

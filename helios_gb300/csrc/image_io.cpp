@@ -345,11 +345,213 @@ void decode_bc7(const uint8_t* blk, uint8_t out[16][4]) {
     }
 }
 
+// ---- BC6H (BPTC half-float RGB; Khronos Data Format Specification, "BC6H") -
+// Fourteen modes, chosen by the low two bits of the block (00, 01) or, when
+// those are 10 or 11, by its low five bits (four five-bit codes are
+// reserved).  A mode fixes one or two regions (the two-region partitions are
+// the first 32 of BC7's), the endpoint precision, and whether endpoints 1-3
+// are stored as signed deltas from endpoint 0 ("transformed", with the delta
+// widths of the mode).  The mode's header bits scatter the endpoint fields; a
+// layout below lists them in stored order as <channel><endpoint><hi>[:<lo>]
+// (endpoints w, x = region 0, y, z = region 1), the bits of a field stored
+// from <lo> towards <hi>, so "rw10:11" stores bit 11 first.  Endpoints widen
+// to 16 bits (unquantisation), interpolate with the BC7 weights and scale to
+// the half-float bit pattern (x 31/64 unsigned, x 31/32 signed magnitude).
+struct Bc6Mode {
+    int regions;
+    bool transformed;
+    int epb;       // endpoint precision (bits)
+    int delta[3];  // stored widths of endpoints 1-3 per channel
+    const char* layout;
+};
+const Bc6Mode kBc6Modes[14] = {
+    {2, true, 10, {5, 5, 5},
+     "gy4 by4 bz4 rw9:0 gw9:0 bw9:0 rx4:0 gz4 gy3:0 gx4:0 bz0 gz3:0 bx4:0 bz1 by3:0 ry4:0 bz2 rz4:0 bz3"},
+    {2, true, 7, {6, 6, 6},
+     "gy5 gz4 gz5 rw6:0 bz0 bz1 by4 gw6:0 by5 bz2 gy4 bw6:0 bz3 bz5 bz4 rx5:0 gy3:0 gx5:0 gz3:0 bx5:0 by3:0 ry5:0 "
+     "rz5:0"},
+    {2, true, 11, {5, 4, 4},
+     "rw9:0 gw9:0 bw9:0 rx4:0 rw10 gy3:0 gx3:0 gw10 bz0 gz3:0 bx3:0 bw10 bz1 by3:0 ry4:0 bz2 rz4:0 bz3"},
+    {2, true, 11, {4, 5, 4},
+     "rw9:0 gw9:0 bw9:0 rx3:0 rw10 gz4 gy3:0 gx4:0 gw10 gz3:0 bx3:0 bw10 bz1 by3:0 ry3:0 bz0 bz2 rz3:0 gy4 bz3"},
+    {2, true, 11, {4, 4, 5},
+     "rw9:0 gw9:0 bw9:0 rx3:0 rw10 by4 gy3:0 gx3:0 gw10 bz0 gz3:0 bx4:0 bw10 by3:0 ry3:0 bz1 bz2 rz3:0 bz4 bz3"},
+    {2, true, 9, {5, 5, 5},
+     "rw8:0 by4 gw8:0 gy4 bw8:0 bz4 rx4:0 gz4 gy3:0 gx4:0 bz0 gz3:0 bx4:0 bz1 by3:0 ry4:0 bz2 rz4:0 bz3"},
+    {2, true, 8, {6, 5, 5},
+     "rw7:0 gz4 by4 gw7:0 bz2 gy4 bw7:0 bz3 bz4 rx5:0 gy3:0 gx4:0 bz0 gz3:0 bx4:0 bz1 by3:0 ry5:0 rz5:0"},
+    {2, true, 8, {5, 6, 5},
+     "rw7:0 bz0 by4 gw7:0 gy5 gy4 bw7:0 gz5 bz4 rx4:0 gz4 gy3:0 gx5:0 gz3:0 bx4:0 bz1 by3:0 ry4:0 bz2 rz4:0 bz3"},
+    {2, true, 8, {5, 5, 6},
+     "rw7:0 bz1 by4 gw7:0 by5 gy4 bw7:0 bz5 bz4 rx4:0 gz4 gy3:0 gx4:0 bz0 gz3:0 bx5:0 by3:0 ry4:0 bz2 rz4:0 bz3"},
+    {2, false, 6, {6, 6, 6},
+     "rw5:0 gz4 bz0 bz1 by4 gw5:0 gy5 by5 bz2 gy4 bw5:0 gz5 bz3 bz5 bz4 rx5:0 gy3:0 gx5:0 gz3:0 bx5:0 by3:0 ry5:0 "
+     "rz5:0"},
+    {1, false, 10, {10, 10, 10}, "rw9:0 gw9:0 bw9:0 rx9:0 gx9:0 bx9:0"},
+    {1, true, 11, {9, 9, 9}, "rw9:0 gw9:0 bw9:0 rx8:0 rw10 gx8:0 gw10 bx8:0 bw10"},
+    {1, true, 12, {8, 8, 8}, "rw9:0 gw9:0 bw9:0 rx7:0 rw10:11 gx7:0 gw10:11 bx7:0 bw10:11"},
+    {1, true, 16, {4, 4, 4}, "rw9:0 gw9:0 bw9:0 rx3:0 rw10:15 gx3:0 gw10:15 bx3:0 bw10:15"},
+};
+
+// Mode index of a block, -1 for the reserved codes.
+int bc6_mode(const uint8_t* blk) {
+    const uint32_t m2 = blk[0] & 3u;
+    if (m2 < 2) return (int)m2;
+    switch (blk[0] & 31u) {
+        case 2: return 2;
+        case 6: return 3;
+        case 10: return 4;
+        case 14: return 5;
+        case 18: return 6;
+        case 22: return 7;
+        case 26: return 8;
+        case 30: return 9;
+        case 3: return 10;
+        case 7: return 11;
+        case 11: return 12;
+        case 15: return 13;
+        default: return -1;
+    }
+}
+
+// Reads the endpoint fields of a mode's layout: e[endpoint][channel], raw bits.
+void bc6_read_endpoints(const char* layout, BitReader& br, int32_t e[4][3]) {
+    for (const char* p = layout; *p;) {
+        while (*p == ' ') ++p;
+        if (!*p) break;
+        const int ch = *p == 'r' ? 0 : (*p == 'g' ? 1 : 2);
+        ++p;
+        const int ep = *p - 'w';  // w x y z -> 0 1 2 3
+        ++p;
+        int hi = 0, lo;
+        while (*p >= '0' && *p <= '9') hi = 10 * hi + (*p++ - '0');
+        lo = hi;
+        if (*p == ':') {
+            ++p;
+            lo = 0;
+            while (*p >= '0' && *p <= '9') lo = 10 * lo + (*p++ - '0');
+        }
+        const int step = hi >= lo ? 1 : -1;
+        for (int b = lo;; b += step) {
+            e[ep][ch] |= (int32_t)br.get(1) << b;
+            if (b == hi) break;
+        }
+    }
+}
+
+int32_t sign_extend(int32_t v, int bits) {
+    const int32_t m = 1 << (bits - 1);
+    v &= (1 << bits) - 1;
+    return (v ^ m) - m;
+}
+
+int32_t bc6_unquantize(int32_t c, int epb, bool is_signed) {
+    if (!is_signed) {
+        if (epb >= 15) return c;
+        if (c == 0) return 0;
+        if (c == (1 << epb) - 1) return 0xFFFF;
+        return ((c << 16) + 0x8000) >> epb;
+    }
+    if (epb >= 16) return c;
+    const bool neg = c < 0;
+    int32_t m = neg ? -c : c, u;
+    if (m == 0) u = 0;
+    else if (m >= (1 << (epb - 1)) - 1) u = 0x7FFF;
+    else u = ((m << 15) + 0x4000) >> (epb - 1);
+    return neg ? -u : u;
+}
+
+// floor(v / 64) for any sign
+int32_t floor_div64(int32_t v) { return v >= 0 ? v >> 6 : -((-v + 63) >> 6); }
+
+uint16_t bc6_finish(int32_t c, bool is_signed) {
+    if (!is_signed) return (uint16_t)((c * 31) >> 6);
+    if (c < 0) {
+        const int32_t m = ((-c) * 31) >> 5;
+        return (uint16_t)(m ? (0x8000 | m) : 0);
+    }
+    return (uint16_t)((c * 31) >> 5);
+}
+
+// One BC6H block to 16 RGBA half-float texels (alpha 1.0); a reserved mode
+// decodes to zero colour.
+void decode_bc6h(const uint8_t* blk, bool is_signed, uint16_t out[16][4]) {
+    const int mi = bc6_mode(blk);
+    if (mi < 0) {
+        for (int t = 0; t < 16; ++t) {
+            out[t][0] = out[t][1] = out[t][2] = 0;
+            out[t][3] = 0x3C00;
+        }
+        return;
+    }
+    const Bc6Mode& M = kBc6Modes[mi];
+    BitReader br{blk};
+    br.get(mi < 2 ? 2 : 5);
+    int32_t e[4][3] = {};
+    bc6_read_endpoints(M.layout, br, e);
+    const uint32_t part = M.regions == 2 ? br.get(5) : 0u;
+    const int ne = 2 * M.regions;
+    for (int c = 0; c < 3; ++c) {
+        if (is_signed) e[0][c] = sign_extend(e[0][c], M.epb);
+        for (int k = 1; k < ne; ++k) {
+            if (M.transformed) {
+                const int32_t d = sign_extend(e[k][c], M.delta[c]);
+                e[k][c] = (e[0][c] + d) & ((1 << M.epb) - 1);
+                if (is_signed) e[k][c] = sign_extend(e[k][c], M.epb);
+            } else if (is_signed) {
+                e[k][c] = sign_extend(e[k][c], M.epb);
+            }
+        }
+        for (int k = 0; k < ne; ++k) e[k][c] = bc6_unquantize(e[k][c], M.epb, is_signed);
+    }
+    const int ib = M.regions == 2 ? 3 : 4;
+    const uint32_t anchor1 = M.regions == 2 ? kBc7Anchor2[part] : 0u;
+    const uint8_t* w = ib == 3 ? kBc7W3 : kBc7W4;
+    for (int t = 0; t < 16; ++t) {
+        const bool anchor = t == 0 || (M.regions == 2 && (uint32_t)t == anchor1);
+        const uint32_t idx = br.get(ib - (anchor ? 1 : 0));
+        const uint32_t s = M.regions == 2 ? (kBc7Part2[part] >> t) & 1u : 0u;
+        for (int c = 0; c < 3; ++c) {
+            const int32_t v = floor_div64(e[2 * s][c] * (64 - (int32_t)w[idx]) + e[2 * s + 1][c] * (int32_t)w[idx] + 32);
+            out[t][c] = bc6_finish(v, is_signed);
+        }
+        out[t][3] = 0x3C00;
+    }
+}
+
 }  // namespace
+
+extern "C" hx_status hx_texture_decode_hdr(const hx_texture_desc* tex, uint16_t* out) {
+    HX_CHECK_ARG(tex && out && tex->rgba8 && tex->width > 0 && tex->height > 0,
+                 "hx_texture_decode_hdr: null argument or empty texture");
+    HX_CHECK_ARG(tex->format >= HX_TEXTURE_BC6H_SF16 && tex->format <= HX_TEXTURE_RGBA16F,
+                 "hx_texture_decode_hdr: format %u is not a half-float format (8-bit formats: hx_texture_decode)",
+                 tex->format);
+    const uint32_t W = tex->width, H = tex->height;
+    if (tex->format == HX_TEXTURE_RGBA16F) {
+        const uint8_t* src = tex->rgba8;
+        for (size_t i = 0; i < (size_t)W * H * 4; ++i) out[i] = (uint16_t)(src[2 * i] | (src[2 * i + 1] << 8));
+        return HX_OK;
+    }
+    const bool is_signed = tex->format == HX_TEXTURE_BC6H_SF16;
+    const uint32_t bw = (W + 3) / 4, bh = (H + 3) / 4;
+    for (uint32_t by = 0; by < bh; ++by)
+        for (uint32_t bx = 0; bx < bw; ++bx) {
+            uint16_t px[16][4];
+            decode_bc6h(tex->rgba8 + ((size_t)by * bw + bx) * 16, is_signed, px);
+            for (uint32_t t = 0; t < 16; ++t) {
+                const uint32_t x = bx * 4 + (t & 3), y = by * 4 + (t >> 2);
+                if (x < W && y < H) std::copy(px[t], px[t] + 4, out + ((size_t)y * W + x) * 4);
+            }
+        }
+    return HX_OK;
+}
 
 extern "C" hx_status hx_texture_decode(const hx_texture_desc* tex, uint8_t* out) {
     HX_CHECK_ARG(tex && out && tex->rgba8 && tex->width > 0 && tex->height > 0, "hx_texture_decode: null argument or empty texture");
-    HX_CHECK_ARG(tex->format <= HX_TEXTURE_BC7, "hx_texture_decode: unknown format %u", tex->format);
+    HX_CHECK_ARG(tex->format <= HX_TEXTURE_BC7,
+                 "hx_texture_decode: format %u is not an 8-bit format (half-float formats: hx_texture_decode_hdr)",
+                 tex->format);
     const uint32_t W = tex->width, H = tex->height;
     if (tex->format == HX_TEXTURE_RGBA8) {
         std::copy(tex->rgba8, tex->rgba8 + (size_t)W * H * 4, out);

@@ -542,6 +542,134 @@ extern "C" hx_status hx_integrator_read_accumulation(hx_integrator* it, float* h
     return report_status(it);
 }
 
+// ---------------------------------------------------------------------------
+// Bake checkpoint / resume: the progressive state (path_integrator.h:46-53 —
+// the accumulation image, num_accumulated_samples, tile_idx) to host memory and
+// back.  The next frame's seeds come from `accumulated` (frame0 of
+// run_wavefront), so a restored integrator continues the same sample sequence.
+// ---------------------------------------------------------------------------
+static_assert(sizeof(hx_bake_checkpoint) == 64, "checkpoint header is 64 bytes");
+
+// 64-bit payload hash: four independent lanes (h = rotl(h ^ w * K2, 31) * K1 per
+// little-endian 8-byte word, lanes strided by 32 bytes), the tail bytes packed
+// into a last word, the lanes and the length folded through the SplitMix64
+// finaliser (Steele, Lea, Flood 2014).
+static uint64_t checkpoint_hash(const unsigned char* p, size_t n) {
+    const uint64_t K1 = 0x9E3779B97F4A7C15ull, K2 = 0xBF58476D1CE4E5B9ull;
+    auto rotl = [](uint64_t x, int r) { return (x << r) | (x >> (64 - r)); };
+    auto fin = [](uint64_t z) {
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    uint64_t h[4] = {K1, K2, ~K1, ~K2};
+    size_t i = 0;
+    for (; i + 32 <= n; i += 32)
+        for (int l = 0; l < 4; ++l) {
+            uint64_t w;
+            std::memcpy(&w, p + i + 8 * l, 8);
+            h[l] = rotl(h[l] ^ (w * K2), 31) * K1;
+        }
+    uint64_t tail = 0;
+    for (size_t k = 0; i + k < n; ++k) tail |= (uint64_t)p[i + k] << (8 * (k & 7));
+    uint64_t r = fin(n ^ tail);
+    for (int l = 0; l < 4; ++l) r = fin(r ^ h[l]);
+    return r;
+}
+
+static size_t checkpoint_payload_bytes(uint32_t w, uint32_t h, bool aov) {
+    const size_t npix = (size_t)w * h;
+    return npix * (16 + 16 + 4) + (aov ? npix * 32 : 0);
+}
+
+extern "C" hx_status hx_integrator_checkpoint_size(const hx_integrator* it, size_t* bytes) {
+    HX_CHECK_ARG(it && bytes, "hx_integrator_checkpoint_size: null argument");
+    *bytes = sizeof(hx_bake_checkpoint) + checkpoint_payload_bytes(it->desc.width, it->desc.height, it->aov);
+    return HX_OK;
+}
+
+extern "C" hx_status hx_integrator_save_checkpoint(hx_integrator* it, void* host, size_t bytes) {
+    HX_CHECK_ARG(it && host, "hx_integrator_save_checkpoint: null argument");
+    const size_t payload = checkpoint_payload_bytes(it->desc.width, it->desc.height, it->aov);
+    HX_CHECK_ARG(bytes >= sizeof(hx_bake_checkpoint) + payload,
+                 "hx_integrator_save_checkpoint: %zu bytes given, %zu needed", bytes,
+                 sizeof(hx_bake_checkpoint) + payload);
+    HX_CUDA(cudaSetDevice(it->ctx->device));
+    const size_t npix = (size_t)it->desc.width * it->desc.height;
+    unsigned char* out = (unsigned char*)host;
+    unsigned char* d = out + sizeof(hx_bake_checkpoint);
+    cudaStream_t st = it->ctx->stream;
+    HX_CUDA(cudaMemcpyAsync(d, it->acc, 16 * npix, cudaMemcpyDeviceToHost, st));
+    HX_CUDA(cudaMemcpyAsync(d + 16 * npix, it->comp, 16 * npix, cudaMemcpyDeviceToHost, st));
+    HX_CUDA(cudaMemcpyAsync(d + 32 * npix, it->count_map, 4 * npix, cudaMemcpyDeviceToHost, st));
+    if (it->aov) {
+        HX_CUDA(cudaMemcpyAsync(d + 36 * npix, it->aov_a, 16 * npix, cudaMemcpyDeviceToHost, st));
+        HX_CUDA(cudaMemcpyAsync(d + 52 * npix, it->aov_n, 16 * npix, cudaMemcpyDeviceToHost, st));
+    }
+    HX_TRY(queue_status(it));
+    HX_CUDA(cudaStreamSynchronize(st));
+    HX_TRY(report_status(it));
+    hx_bake_checkpoint hdr{};
+    hdr.magic = HX_BAKE_CHECKPOINT_MAGIC;
+    hdr.version = HX_BAKE_CHECKPOINT_VERSION;
+    hdr.width = it->desc.width;
+    hdr.height = it->desc.height;
+    hdr.max_samples = it->desc.max_samples;
+    hdr.tiled = it->desc.tiled;
+    hdr.accumulation = it->desc.policy.accumulation;
+    hdr.accumulated = it->accumulated;
+    hdr.tile_idx = it->tile_idx;
+    hdr.aov = it->aov ? 1u : 0u;
+    hdr.aov_frames = it->aov_frames;
+    hdr.payload_bytes = payload;
+    hdr.checksum = checkpoint_hash(d, payload);
+    std::memcpy(out, &hdr, sizeof(hdr));
+    return HX_OK;
+}
+
+extern "C" hx_status hx_integrator_load_checkpoint(hx_integrator* it, const void* host, size_t bytes) {
+    HX_CHECK_ARG(it && host, "hx_integrator_load_checkpoint: null argument");
+    HX_CHECK_ARG(bytes >= sizeof(hx_bake_checkpoint), "hx_integrator_load_checkpoint: %zu bytes, shorter than the header",
+                 bytes);
+    hx_bake_checkpoint hdr;
+    std::memcpy(&hdr, host, sizeof(hdr));
+    HX_CHECK_ARG(hdr.magic == HX_BAKE_CHECKPOINT_MAGIC && hdr.version == HX_BAKE_CHECKPOINT_VERSION,
+                 "hx_integrator_load_checkpoint: not a version-%u bake checkpoint (magic 0x%08x, version %u)",
+                 HX_BAKE_CHECKPOINT_VERSION, hdr.magic, hdr.version);
+    HX_CHECK_ARG(hdr.width == it->desc.width && hdr.height == it->desc.height,
+                 "hx_integrator_load_checkpoint: checkpoint is %ux%u, integrator %ux%u", hdr.width, hdr.height,
+                 it->desc.width, it->desc.height);
+    HX_CHECK_ARG(hdr.max_samples == it->desc.max_samples && hdr.tiled == it->desc.tiled &&
+                     hdr.accumulation == it->desc.policy.accumulation,
+                 "hx_integrator_load_checkpoint: max_samples/tiled/accumulation %u/%u/%u differ from the integrator's "
+                 "%u/%u/%u", hdr.max_samples, hdr.tiled, hdr.accumulation, it->desc.max_samples, it->desc.tiled,
+                 it->desc.policy.accumulation);
+    HX_CHECK_ARG(hdr.aov <= 1 && hdr.tile_idx <= it->tiles.size() && hdr.accumulated < hdr.max_samples,
+                 "hx_integrator_load_checkpoint: progress fields out of range");
+    const size_t payload = checkpoint_payload_bytes(hdr.width, hdr.height, hdr.aov != 0);
+    HX_CHECK_ARG(hdr.payload_bytes == payload && bytes >= sizeof(hdr) + payload,
+                 "hx_integrator_load_checkpoint: payload %llu bytes recorded, %zu expected, %zu available",
+                 (unsigned long long)hdr.payload_bytes, payload, bytes - sizeof(hdr));
+    const unsigned char* d = (const unsigned char*)host + sizeof(hdr);
+    HX_CHECK_ARG(checkpoint_hash(d, payload) == hdr.checksum, "hx_integrator_load_checkpoint: checksum mismatch");
+    HX_CUDA(cudaSetDevice(it->ctx->device));
+    HX_TRY(hx_integrator_set_aov_accumulation(it, hdr.aov));
+    const size_t npix = (size_t)hdr.width * hdr.height;
+    cudaStream_t st = it->ctx->stream;
+    HX_CUDA(cudaMemcpyAsync(it->acc, d, 16 * npix, cudaMemcpyHostToDevice, st));
+    HX_CUDA(cudaMemcpyAsync(it->comp, d + 16 * npix, 16 * npix, cudaMemcpyHostToDevice, st));
+    HX_CUDA(cudaMemcpyAsync(it->count_map, d + 32 * npix, 4 * npix, cudaMemcpyHostToDevice, st));
+    if (hdr.aov) {
+        HX_CUDA(cudaMemcpyAsync(it->aov_a, d + 36 * npix, 16 * npix, cudaMemcpyHostToDevice, st));
+        HX_CUDA(cudaMemcpyAsync(it->aov_n, d + 52 * npix, 16 * npix, cudaMemcpyHostToDevice, st));
+    }
+    HX_CUDA(cudaStreamSynchronize(st));  // the caller's buffer may go away after the return
+    it->accumulated = hdr.accumulated;
+    it->tile_idx = hdr.tile_idx;
+    it->aov_frames = hdr.aov_frames;
+    return HX_OK;
+}
+
 // Output-buffer views of Renderer::render_debug_visualization
 // (renderer.cpp:491-545; debug_visualization.vert:54-64,
 // debug_visualization.frag:71-161), rendered headless by ray casting: per

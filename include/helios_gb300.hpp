@@ -89,6 +89,17 @@ public:
     uint32_t tile_idx() const { return progress(1); }
     uint32_t num_target_samples() const { return progress(2); }
     void restart_bake() { hx_check(hx_integrator_restart_bake(m_it)); }
+    // Bake checkpoint / resume (progressive state to host memory and back).
+    std::vector<uint8_t> save_checkpoint() {
+        size_t n = 0;
+        hx_check(hx_integrator_checkpoint_size(m_it, &n));
+        std::vector<uint8_t> buf(n);
+        hx_check(hx_integrator_save_checkpoint(m_it, buf.data(), buf.size()));
+        return buf;
+    }
+    void load_checkpoint(const std::vector<uint8_t>& buf) {
+        hx_check(hx_integrator_load_checkpoint(m_it, buf.data(), buf.size()));
+    }
     void set_max_ray_bounces(const uint32_t& n) { hx_check(hx_integrator_set_max_ray_bounces(m_it, n)); }
     void set_max_samples(const uint32_t& n) { hx_check(hx_integrator_set_max_samples(m_it, n)); }
     void set_shadow_ray_bias(const float& b) { hx_check(hx_integrator_set_shadow_ray_bias(m_it, b)); }

@@ -152,7 +152,11 @@ typedef struct hx_instance {
  * block-compressed formats of the reference's assets
  * (kCompressedFormats, resource_manager.cpp:14-30), then rgba8 points at
  * ceil(width / 4) * ceil(height / 4) blocks in row-major block order; they
- * are decoded to RGBA8 at upload (hx_texture_decode). */
+ * are decoded to RGBA8 at upload (hx_texture_decode).  The half-float
+ * formats (BC6H, the reference's VK_FORMAT_BC6H_SFLOAT_BLOCK, and
+ * uncompressed RGBA16F, its R16G16B16A16_SFLOAT for FLOAT16 images) are kept
+ * as RGBA16F texels on the device (hx_texture_decode_hdr) and sampled in
+ * FP32; they take srgb = 0 (the reference has no sRGB variant of them). */
 #define HX_TEXTURE_RGBA8    0u
 #define HX_TEXTURE_BC1_RGB  1u  /* 8-byte blocks, alpha 255                          */
 #define HX_TEXTURE_BC1_RGBA 2u  /* 8-byte blocks, 1-bit alpha in the 3-colour mode   */
@@ -161,6 +165,9 @@ typedef struct hx_instance {
 #define HX_TEXTURE_BC4      5u  /* 8-byte blocks: R (G = B = 0, A = 255)              */
 #define HX_TEXTURE_BC5      6u  /* 16-byte blocks: R, G (B = 0, A = 255)              */
 #define HX_TEXTURE_BC7      7u  /* 16-byte blocks: BPTC RGBA, 8 modes, 1-3 subsets     */
+#define HX_TEXTURE_BC6H_SF16 8u /* 16-byte blocks: BPTC signed half-float RGB (A = 1)  */
+#define HX_TEXTURE_BC6H_UF16 9u /* 16-byte blocks: BPTC unsigned half-float RGB (A = 1) */
+#define HX_TEXTURE_RGBA16F 10u  /* width * height * 4 IEEE half floats (little-endian) */
 typedef struct hx_texture_desc {
     const uint8_t* rgba8;
     uint32_t       width;
@@ -177,8 +184,17 @@ typedef struct hx_texture_desc {
  * a4 * 17.  The 3-colour mode (c0 <= c1) exists in BC1 blocks only.  BC7
  * follows the BPTC specification exactly (its interpolation is integer:
  * ((64 - w) e0 + w e1 + 32) >> 6); a block with a reserved mode decodes to
- * zero.  BC6H (HDR) is not supported (the texture path is 8-bit). */
+ * zero.  Half-float formats are refused (hx_texture_decode_hdr). */
 HX_API hx_status hx_texture_decode(const hx_texture_desc* texture, uint8_t* rgba8_out);
+
+/* Host-only: decodes a half-float texture (HX_TEXTURE_BC6H_SF16 / _UF16 /
+ * RGBA16F) to width * height RGBA16F texels (IEEE half bit patterns, rows top
+ * to bottom).  BC6H follows the BPTC specification exactly: endpoints
+ * unquantised to 16 bits, interpolated with the 6-bit weights in integers
+ * (floor((64 - w) e0 + w e1 + 32) / 64), scaled to the half pattern (x 31/64
+ * unsigned; signed: magnitude x 31/32 with the sign bit); alpha is 1.0; a
+ * block with a reserved mode decodes to zero colour. */
+HX_API hx_status hx_texture_decode_hdr(const hx_texture_desc* texture, uint16_t* rgba16f_out);
 
 #define HX_ENV_NONE          0u  /* black environment                        */
 #define HX_ENV_EQUIRECT      1u  /* caller-supplied RGBA32F lat-long map     */
@@ -458,6 +474,52 @@ HX_API hx_status hx_integrator_tonemap(hx_integrator* integ, uint32_t op, float 
  * renderer.cpp:1483-1506) into width*height*4 floats. */
 HX_API hx_status hx_integrator_read_accumulation(hx_integrator* integ, float* host_rgba32f);
 
+/* Bake checkpoint / resume.  The reference keeps its progressive state (the
+ * accumulation image, num_accumulated_samples, tile_idx of
+ * path_integrator.h:46-53) only for the life of the process; these calls
+ * serialise it to host memory and restore it into an integrator of the same
+ * size, so a bake can stop and continue (another process, another GPU) with a
+ * result bit-identical to an uninterrupted one: the next frame's samples are
+ * seeded from the restored sample count, like the reference's frame index.
+ * Layout: one hx_bake_checkpoint header, then the payload — the accumulation
+ * image (RGBA32F, the running mean or the Kahan sum), the Kahan compensation
+ * image (RGBA32F), the per-pixel sample counts (uint32), and with AOV
+ * accumulation on the first-hit albedo+depth and normal images (RGBA32F each),
+ * every image width*height in launch-grid order.  checksum is a 64-bit hash of
+ * the payload (four multiply-rotate lanes over little-endian 8-byte words,
+ * folded through the SplitMix64 finaliser). */
+#define HX_BAKE_CHECKPOINT_MAGIC   0x4B425848u  /* "HXBK" */
+#define HX_BAKE_CHECKPOINT_VERSION 1u
+typedef struct hx_bake_checkpoint {
+    uint32_t magic, version;
+    uint32_t width, height;
+    uint32_t max_samples;      /* samples per tile */
+    uint32_t tiled;
+    uint32_t accumulation;     /* HX_ACCUM_* */
+    uint32_t accumulated;      /* samples of the current tile */
+    uint32_t tile_idx;
+    uint32_t aov;              /* 1: the two AOV images follow the counts */
+    uint32_t aov_frames;
+    uint32_t reserved;
+    uint64_t payload_bytes;
+    uint64_t checksum;
+} hx_bake_checkpoint;          /* 64 bytes */
+
+/* Bytes hx_integrator_save_checkpoint writes for the integrator's current
+ * state (header included). */
+HX_API hx_status hx_integrator_checkpoint_size(const hx_integrator* integ, size_t* bytes);
+/* Waits for the integrator's queued work, then writes the checkpoint into
+ * host[0 .. checkpoint_size); HX_ERR_INVALID_ARG if `bytes` is smaller, and
+ * HX_ERR_DEVICE (no checkpoint) if the device status word is set. */
+HX_API hx_status hx_integrator_save_checkpoint(hx_integrator* integ, void* host, size_t bytes);
+/* Restores a checkpoint.  HX_ERR_INVALID_ARG, with the state unchanged, when
+ * the magic, version, sizes or checksum do not match or when its width,
+ * height, max_samples, tiled flag or accumulation mode differ from the
+ * integrator's; AOV accumulation is switched to the checkpoint's setting.
+ * Other parameters (bounces, bias, RNG kind) are the caller's to keep equal
+ * for a bit-identical continuation. */
+HX_API hx_status hx_integrator_load_checkpoint(hx_integrator* integ, const void* host, size_t bytes);
+
 /* Output buffers of Renderer::set_current_output_buffer (renderer.h:27-35,
  * 85) and its debug-visualization pass (renderer.cpp:491-545,
  * debug_visualization.frag:71-161).  Rendered headless: one camera ray
@@ -623,12 +685,11 @@ HX_API hx_status hx_server_destroy(hx_server* server);
  * computes (hx_scene_export_bvh).  n must be 1..262144 (2^18); larger n is
  * rejected with HX_ERR_INVALID_ARG.  Scratch is one fixed device array of
  * about 5 MB in the library, held by every GPU that loads it until exit.
- * The first call on a device looks up that array's address and keeps it
- * for the life of the process; with lazy module loading (the CUDA default)
- * that first call is also when the array is committed on the device, so a
+ * Every call looks up that array's address on the current device (valid
+ * again after a cudaDeviceReset); with lazy module loading (the CUDA default)
+ * the first call on a device is also when the array is committed there, so a
  * caller that must not grow its footprint later makes one warm-up call at
- * start-up, before any stream capture.  The kept address does not survive a
- * cudaDeviceReset of that device.  Work is ordered on cuda_stream (a
+ * start-up, before any stream capture.  Work is ordered on cuda_stream (a
  * cudaStream_t, NULL = default stream); calls that overlap on the GPU race on
  * the shared scratch. */
 HX_API hx_status hx_lbvh_sort_noalloc(const float* d_world_tris, uint32_t n, uint32_t* d_morton, uint32_t* d_sorted,
