@@ -25,7 +25,7 @@ ENV_SAMPLE_COSINE, ENV_SAMPLE_IMPORTANCE = 0, 1
 PAYLOAD_FP32, PAYLOAD_FP16 = 0, 1
 TONEMAP_ACES, TONEMAP_REINHARD, TONEMAP_NONE = 0, 1, 2
 TEXTURE_RGBA8, TEXTURE_BC1_RGB, TEXTURE_BC1_RGBA, TEXTURE_BC2, TEXTURE_BC3, TEXTURE_BC4, TEXTURE_BC5, TEXTURE_BC7 = range(8)
-TEXTURE_BC6H_SF16, TEXTURE_BC6H_UF16, TEXTURE_RGBA16F = 8, 9, 10
+TEXTURE_BC6H_SF16, TEXTURE_BC6H_UF16, TEXTURE_RGBA16F, TEXTURE_RGBA8_SNORM = 8, 9, 10, 11
 OUTPUT_ALBEDO, OUTPUT_NORMALS, OUTPUT_ROUGHNESS, OUTPUT_METALLIC, OUTPUT_EMISSIVE, OUTPUT_FINAL = 0, 1, 2, 3, 4, 5
 SCENE_BOX, SCENE_ICOSPHERES, SCENE_TERRAIN = 0, 1, 2
 SUBMESH_NON_OPAQUE = 1

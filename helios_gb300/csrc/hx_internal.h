@@ -118,6 +118,7 @@ constexpr uint32_t kTraversalStackEntries = 32;
 struct DevScene {
     uint32_t num_prims, num_nodes, num_lights, num_instances;
     uint32_t stack_limit;        // traversal stack entries a ray may use (<= kStackSize; a diagnostic knob)
+    uint32_t wide_alpha;         // 1: some alpha-tested albedo texture is RGBA16F / SNORM (traversal's WA kernels)
     const float4* tri;           // 3 per leaf-ordered triangle: v0.xyz|prim, v1.xyz|flags, v2.xyz|0
     const hx_bvh8_node* nodes;
     const uint4* prim_info;      // per flattened prim: instance, global tri, material, flags

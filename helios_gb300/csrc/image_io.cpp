@@ -549,11 +549,11 @@ extern "C" hx_status hx_texture_decode_hdr(const hx_texture_desc* tex, uint16_t*
 
 extern "C" hx_status hx_texture_decode(const hx_texture_desc* tex, uint8_t* out) {
     HX_CHECK_ARG(tex && out && tex->rgba8 && tex->width > 0 && tex->height > 0, "hx_texture_decode: null argument or empty texture");
-    HX_CHECK_ARG(tex->format <= HX_TEXTURE_BC7,
+    HX_CHECK_ARG(tex->format <= HX_TEXTURE_BC7 || tex->format == HX_TEXTURE_RGBA8_SNORM,
                  "hx_texture_decode: format %u is not an 8-bit format (half-float formats: hx_texture_decode_hdr)",
                  tex->format);
     const uint32_t W = tex->width, H = tex->height;
-    if (tex->format == HX_TEXTURE_RGBA8) {
+    if (tex->format == HX_TEXTURE_RGBA8 || tex->format == HX_TEXTURE_RGBA8_SNORM) {  // the bytes as they are
         std::copy(tex->rgba8, tex->rgba8 + (size_t)W * H * 4, out);
         return HX_OK;
     }

@@ -201,7 +201,8 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
     it->grid_shade = std::max(1, per_sm) * ctx->num_sms;
     it->grid_gen = ctx->num_sms * 8;
-    HX_CUDA(set_carveouts(k_extend_batched<false>, k_extend_batched<true>));
+    HX_CUDA(set_carveouts(k_extend_batched<false, false>, k_extend_batched<true, false>, k_extend_batched<false, true>,
+                          k_extend_batched<true, true>));
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_batched<false>, kTraceThreads, 0));
     it->grid_batched = std::max(1, per_sm) * ctx->num_sms;
     compute_tiles(it);
@@ -313,17 +314,9 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             {
                 StageTimer t(it, &it->stats.ms_trace);
                 HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));  // fetch cursor, miss / hit counts
-#define HX_EXTEND(COUNT, FP16)                                                                                      \
-    do {                                                                                                            \
-        if (!FP16 && s.num_prims < (1u << 27))                                                                      \
-            k_extend_batched<COUNT><<<it->grid_batched, kTraceThreads, 0, st>>>(                                    \
-                s, qs, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.counters + cur, it->q.counters + 4,        \
-                kFlushTris, kFlushParked);                                                                          \
-        else                                                                                                        \
-            k_extend<COUNT, FP16><<<it->grid_trace, kTraceThreads, 0, st>>>(                                        \
-                s, qs, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], it->q.p[cur], it->q.counters + cur,              \
-                it->q.counters + 4);                                                                                \
-    } while (0)
+#define HX_EXTEND(COUNT, FP16)                                                                                 \
+    launch_extend<COUNT, FP16>(s, qs, it->grid_batched, it->grid_trace, st, it->q.o[cur], it->q.r0[cur], it->q.r1[cur], \
+                               it->q.p[cur], it->q.counters + cur, it->q.counters + 4)
                 if (it->counting) {
                     if (fp16) HX_EXTEND(true, true);
                     else HX_EXTEND(true, false);
@@ -707,7 +700,7 @@ __global__ void k_output_view(DevScene s, hx_frame_desc f, uint32_t W, uint32_t 
         uint2 stack[kStackSize];
         bool overflow = false;
         trav_init(st, s, cam, d, 0.001f, 10000.0f, false);
-        while (!trav_step<false>(st, stack, s, overflow, nullptr)) {
+        while (!trav_step<false, true>(st, stack, s, overflow, nullptr)) {
         }
         if (overflow) atomicOr(status, 1u);
         float4 c = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
@@ -879,13 +872,8 @@ extern "C" hx_status hx_integrator_stats(const hx_integrator* it, hx_stats* out)
 // kernel a frame's first bounce uses (no shadow rays are queued).
 static void launch_primary_trace(hx_integrator* it, cudaStream_t st) {
     const DevScene& s = it->scene->d;
-    if (s.num_prims < (1u << 27))
-        k_extend_batched<false><<<it->grid_batched, kTraceThreads, 0, st>>>(s, it->q, it->q.o[0], it->q.r0[0], it->q.r1[0],
-                                                                            it->q.counters, it->q.counters + 4, kFlushTris,
-                                                                            kFlushParked);
-    else
-        k_extend<false, false><<<it->grid_trace, kTraceThreads, 0, st>>>(s, it->q, it->q.o[0], it->q.r0[0], it->q.r1[0],
-                                                                         it->q.p[0], it->q.counters, it->q.counters + 4);
+    launch_extend<false, false>(s, it->q, it->grid_batched, it->grid_trace, st, it->q.o[0], it->q.r0[0], it->q.r1[0],
+                                it->q.p[0], it->q.counters, it->q.counters + 4);
 }
 
 extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_frame_desc* f, uint32_t frame_index,
@@ -1006,12 +994,7 @@ extern "C" hx_status hx_scene_trace(const hx_scene* scene, const float* host_ray
     k_ray_records<<<ctx->num_sms * 4, 256, 0, st>>>(d_rays, n, any_hit, q.o[0], q.r0[0], q.r1[0], q.counters);
     const DevScene& s = scene->d;
     const int grid = ctx->num_sms * kTraceMinBlocks;
-    if (s.num_prims < (1u << 27))
-        k_extend_batched<false><<<grid, kTraceThreads, 0, st>>>(s, q, q.o[0], q.r0[0], q.r1[0], q.counters, q.counters + 4,
-                                                               kFlushTris, kFlushParked);
-    else
-        k_extend<false, false><<<grid, kTraceThreads, 0, st>>>(s, q, q.o[0], q.r0[0], q.r1[0], nullptr, q.counters,
-                                                              q.counters + 4);
+    launch_extend<false, false>(s, q, grid, grid, st, q.o[0], q.r0[0], q.r1[0], nullptr, q.counters, q.counters + 4);
     k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(q.hit, n, d_hits);
     HX_CUDA(cudaGetLastError());
     uint32_t status = 0;

@@ -262,8 +262,10 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
     for (uint32_t t = 0; t < desc->num_textures; ++t) {
         HX_CHECK_ARG(desc->textures[t].rgba8 && desc->textures[t].width > 0 && desc->textures[t].height > 0,
                      "texture %u: empty", t);
-        HX_CHECK_ARG(desc->textures[t].format <= HX_TEXTURE_BC7, "texture %u: unknown format %u", t,
+        HX_CHECK_ARG(desc->textures[t].format <= HX_TEXTURE_RGBA8_SNORM, "texture %u: unknown format %u", t,
                      desc->textures[t].format);
+        HX_CHECK_ARG((desc->textures[t].format < HX_TEXTURE_BC6H_SF16) || !desc->textures[t].srgb,
+                     "texture %u: half-float and SNORM formats have no sRGB variant", t);
     }
     for (uint32_t l = 0; l < desc->num_punctual_lights; ++l) {
         uint32_t ty = (uint32_t)desc->punctual_lights[l].data0[0];
@@ -274,6 +276,7 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
     hx_scene* s = new hx_scene();
     s->ctx = ctx;
     s->d.stack_limit = kTraversalStackEntries;
+    s->d.wide_alpha = 0;
     cudaStream_t st = ctx->stream;
     // ---- host packing
     std::vector<uint32_t> vbase(desc->num_meshes), tbase(desc->num_meshes);
@@ -333,7 +336,15 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
                 const hx_vertex& a = md.vertices[md.indices[3 * mp]];
                 const hx_vertex& b = md.vertices[md.indices[3 * mp + 1]];
                 const hx_vertex& c = md.vertices[md.indices[3 * mp + 2]];
-                uint32_t tex = mt.texture_indices0[0] >= 0 ? (uint32_t)mt.texture_indices0[0] : 0xffffffffu;
+                // albedo texture index for the any-hit test; bit 31 marks an
+                // RGBA16F / SNORM texture (alpha read without the A8 copy)
+                uint32_t tex = 0xffffffffu;
+                if (mt.texture_indices0[0] >= 0) {
+                    const uint32_t f = desc->textures[mt.texture_indices0[0]].format;
+                    const bool wide = f >= HX_TEXTURE_BC6H_SF16;
+                    tex = (uint32_t)mt.texture_indices0[0] | (wide ? 0x80000000u : 0u);
+                    if (wide && flags) s->d.wide_alpha = 1u;  // an alpha-tested triangle reads it
+                }
                 float tex_f;
                 std::memcpy(&tex_f, &tex, 4);
                 hauv[2 * p] = make_float4(a.tex_coord[0], a.tex_coord[1], b.tex_coord[0], b.tex_coord[1]);
@@ -376,15 +387,20 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
             for (uint32_t l = 0; l < desc->num_punctual_lights; ++l)
                 if ((uint32_t)desc->punctual_lights[l].data0[0] == type) s->lights_host.push_back(desc->punctual_lights[l]);
     }
-    // textures
+    // textures: one 32-bit word per RGBA8 texel, two per RGBA16F texel (at an
+    // even word offset); flags in tex_desc.w (bit 0 sRGB, bit 1 half-float)
     std::vector<uint4> htd(desc->num_textures);
-    size_t ntexels = 0;
+    size_t nwords = 0;
     for (uint32_t t = 0; t < desc->num_textures; ++t) {
-        htd[t] = make_uint4((uint32_t)ntexels, desc->textures[t].width, desc->textures[t].height,
-                            desc->textures[t].srgb ? 1u : 0u);
-        ntexels += (size_t)desc->textures[t].width * desc->textures[t].height;
+        const uint32_t fmt = desc->textures[t].format;
+        const bool half = fmt >= HX_TEXTURE_BC6H_SF16 && fmt <= HX_TEXTURE_RGBA16F;
+        if (half) nwords = (nwords + 1) & ~(size_t)1;
+        htd[t] = make_uint4((uint32_t)nwords, desc->textures[t].width, desc->textures[t].height,
+                            (desc->textures[t].srgb ? 1u : 0u) | (half ? 2u : 0u) |
+                                (fmt == HX_TEXTURE_RGBA8_SNORM ? 4u : 0u));
+        nwords += (size_t)desc->textures[t].width * desc->textures[t].height * (half ? 2 : 1);
     }
-    HX_CHECK_ARG(ntexels < 0xffffffffull, "textures too large");
+    HX_CHECK_ARG(nwords < 0xffffffffull, "textures too large");
 
     // ---- device upload
     auto up = [&](void** dptr, const void* src, size_t bytes) -> hx_status {
@@ -419,27 +435,37 @@ extern "C" hx_status hx_scene_upload(hx_context* ctx, const hx_scene_desc* desc,
         std::vector<hx_material> mats(desc->materials, desc->materials + desc->num_materials);
         if ((rc = up((void**)&s->d.materials, mats.data(), mats.size() * sizeof(hx_material))) != HX_OK) return scene_fail(s, rc);
     }
-    if (ntexels) {
+    if (nwords) {
         uint32_t* texels;
-        if ((rc = hx_alloc_t(ctx, &texels, ntexels)) != HX_OK) return scene_fail(s, rc);
+        if ((rc = hx_alloc_t(ctx, &texels, nwords)) != HX_OK) return scene_fail(s, rc);
         s->allocs.push_back(texels);
-        // block-compressed textures are decoded to RGBA8 on the host first
+        // block-compressed textures are decoded on the host first (8-bit
+        // formats to RGBA8, half-float formats to RGBA16F)
         std::vector<std::vector<uint8_t>> decoded;
         for (uint32_t t = 0; t < desc->num_textures; ++t) {
-            size_t cnt = (size_t)desc->textures[t].width * desc->textures[t].height;
-            const uint8_t* src = desc->textures[t].rgba8;
-            if (desc->textures[t].format != HX_TEXTURE_RGBA8) {
+            const hx_texture_desc& td = desc->textures[t];
+            size_t cnt = (size_t)td.width * td.height;
+            const uint8_t* src = td.rgba8;
+            const bool half = td.format >= HX_TEXTURE_BC6H_SF16 && td.format <= HX_TEXTURE_RGBA16F;
+            if (half) {
+                decoded.emplace_back(8 * cnt);
+                if ((rc = hx_texture_decode_hdr(&td, reinterpret_cast<uint16_t*>(decoded.back().data()))) != HX_OK)
+                    return scene_fail(s, rc);
+                src = decoded.back().data();
+            } else if (td.format != HX_TEXTURE_RGBA8 && td.format != HX_TEXTURE_RGBA8_SNORM) {
                 decoded.emplace_back(4 * cnt);
-                if ((rc = hx_texture_decode(&desc->textures[t], decoded.back().data())) != HX_OK) return scene_fail(s, rc);
+                if ((rc = hx_texture_decode(&td, decoded.back().data())) != HX_OK) return scene_fail(s, rc);
                 src = decoded.back().data();
             }
-            HX_CUDA(cudaMemcpyAsync(texels + htd[t].x, src, 4 * cnt, cudaMemcpyHostToDevice, st));
+            HX_CUDA(cudaMemcpyAsync(texels + htd[t].x, src, (half ? 8 : 4) * cnt, cudaMemcpyHostToDevice, st));
         }
         if (!decoded.empty()) HX_CUDA(cudaStreamSynchronize(st));
+        // the A8 copy shares the word offsets (the entries of half-float and
+        // SNORM textures are unused: their alpha test goes through tex_bilinear)
         uint8_t* alpha8;
-        if ((rc = hx_alloc_t(ctx, &alpha8, ntexels)) != HX_OK) return scene_fail(s, rc);
+        if ((rc = hx_alloc_t(ctx, &alpha8, nwords)) != HX_OK) return scene_fail(s, rc);
         s->allocs.push_back(alpha8);
-        k_alpha8<<<ctx->num_sms * 4, 256, 0, st>>>(texels, ntexels, alpha8);
+        k_alpha8<<<ctx->num_sms * 4, 256, 0, st>>>(texels, nwords, alpha8);
         HX_CUDA(cudaGetLastError());
         s->d.texels = texels;
         s->d.alpha8 = alpha8;

@@ -347,7 +347,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     int per_sm = 0;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend<false, false>, kTraceThreads, 0));
     const int grid_trace = std::max(1, per_sm) * ctx->num_sms;
-    HX_CUDA(set_carveouts(k_extend_batched<false>, k_extend_batched<false>));
+    HX_CUDA(set_carveouts(k_extend_batched<false, false>, k_extend_batched<false, true>));
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_batched<false>, kTraceThreads, 0));
     const int grid_batched = std::max(1, per_sm) * ctx->num_sms;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, kShadeThreads, 0));
@@ -366,13 +366,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     for (uint32_t bo = 0; bo <= s->desc.max_ray_bounces; ++bo) {
         int cur = bo & 1;
         cudaMemsetAsync(b->q.counters + 4, 0, 24, st);  // fetch cursor, miss / hit counts
-        if (sc.num_prims < (1u << 27))
-            k_extend_batched<false><<<grid_batched, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.r0[cur], b->q.r1[cur],
-                                                                            b->q.counters + cur, b->q.counters + 4,
-                                                                            kFlushTris, kFlushParked);
-        else
-            k_extend<false, false><<<grid_trace, kTraceThreads, 0, st>>>(sc, b->q, b->q.o[cur], b->q.r0[cur], b->q.r1[cur], b->q.p[cur],
-                                                                         b->q.counters + cur, b->q.counters + 4);
+        launch_extend<false, false>(sc, b->q, grid_batched, grid_trace, st, b->q.o[cur], b->q.r0[cur], b->q.r1[cur],
+                                    b->q.p[cur], b->q.counters + cur, b->q.counters + 4);
         if (bo == s->desc.max_ray_bounces) break;
         if (bo == 0)
             k_aov_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, sc, b->q.hit);

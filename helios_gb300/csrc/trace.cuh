@@ -83,19 +83,30 @@ HXD float unorm8(uint32_t q) {
     return __fmaf_rn(e, c, r);
 }
 
-// Texel channel value: q / 255, or for an sRGB texture's RGB the decoded
-// linear value (alpha is never sRGB-encoded).
-HXD float texel_value(const DevScene& s, uint32_t q, bool srgb) { return srgb ? __ldg(s.srgb_lut + q) : unorm8(q); }
+// SNORM byte: max(int8(q) / 127, -1), the IEEE quotient (*_SNORM texels).
+HXD float snorm8(uint32_t q) { return fmaxf(__fdiv_rn((float)(int8_t)(uint8_t)q, 127.0f), -1.0f); }
 
-// Software bilinear RGBA8 fetch, REPEAT addressing, level 0; channel c.
-// Power-of-two sizes wrap with a mask (the same integers as the modulo).
-// sRGB textures decode texels before filtering, as sampled *_SRGB images do.
-HXD float tex_bilinear(const DevScene& s, uint32_t tex, float u, float v, int c) {
-    uint4 td = s.tex_desc[tex];
+// Texel channel value of an 8-bit texel by encoding: 0 UNORM q / 255, 1 the
+// sRGB-decoded linear value (an sRGB texture's RGB; alpha is never
+// sRGB-encoded), 2 SNORM (every channel).
+HXD float texel_value(const DevScene& s, uint32_t q, uint32_t enc) {
+    return enc == 1u ? __ldg(s.srgb_lut + q) : (enc ? snorm8(q) : unorm8(q));
+}
+
+// Bilinear taps with REPEAT addressing at level 0: the four texel indices
+// (row-major within the texture) and the fractional weights.  Power-of-two
+// sizes wrap with a mask (the same integers as the modulo).
+struct TexTaps {
+    int i00, i10, i01, i11;
+    float fx, fy;
+};
+HXD TexTaps tex_taps(uint4 td, float u, float v) {
     int W = (int)td.y, H = (int)td.z;
     float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
     float x0 = floorf(x), y0 = floorf(y);
-    float fx = x - x0, fy = y - y0;
+    TexTaps r;
+    r.fx = x - x0;
+    r.fy = y - y0;
     int ix0, iy0, ix1, iy1;
     if (((W & (W - 1)) | (H & (H - 1))) == 0) {
         ix0 = (int)x0 & (W - 1);
@@ -108,57 +119,97 @@ HXD float tex_bilinear(const DevScene& s, uint32_t tex, float u, float v, int c)
         ix1 = ix0 + 1 == W ? 0 : ix0 + 1;
         iy1 = iy0 + 1 == H ? 0 : iy0 + 1;
     }
+    r.i00 = iy0 * W + ix0;
+    r.i10 = iy0 * W + ix1;
+    r.i01 = iy1 * W + ix0;
+    r.i11 = iy1 * W + ix1;
+    return r;
+}
+
+HXD float bilerp(const TexTaps& k, float a00, float a10, float a01, float a11) {
+    float top = a00 + (a10 - a00) * k.fx;
+    float bot = a01 + (a11 - a01) * k.fx;
+    return top + (bot - top) * k.fy;
+}
+
+// Channel c of an RGBA16F texel (two 32-bit words: R | G << 16, B | A << 16).
+HXD float half_channel(uint2 q, int c) {
+    const uint32_t w = c < 2 ? q.x : q.y;
+    return __half2float(__ushort_as_half((unsigned short)((c & 1) ? (w >> 16) : (w & 0xffffu))));
+}
+
+// Texture flag bits (tex_desc.w): bit 0 sRGB-encoded RGB, bit 1 RGBA16F texels
+// (half-float formats; two words per texel at an even word offset), bit 2
+// SNORM RGBA8 texels.
+constexpr uint32_t kTexSrgb = 1u, kTexHalf = 2u, kTexSnorm = 4u;
+
+// Software bilinear fetch, REPEAT addressing, level 0; channel c.  RGBA8
+// textures: q / 255 per texel, sRGB textures decode texels before filtering,
+// as sampled *_SRGB images do, SNORM textures max(int8 / 127, -1); RGBA16F
+// textures: the half values.
+HXD float tex_bilinear(const DevScene& s, uint32_t tex, float u, float v, int c) {
+    const uint4 td = s.tex_desc[tex];
+    const TexTaps k = tex_taps(td, u, v);
+    if (td.w & kTexHalf) {
+        const uint2* t = reinterpret_cast<const uint2*>(s.texels + td.x);
+        return bilerp(k, half_channel(__ldg(t + k.i00), c), half_channel(__ldg(t + k.i10), c),
+                      half_channel(__ldg(t + k.i01), c), half_channel(__ldg(t + k.i11), c));
+    }
     const uint32_t* t = s.texels + td.x;
     int sh = 8 * c;
-    const bool srgb = (td.w & 1u) && c < 3;
-    float a00 = texel_value(s, (__ldg(t + iy0 * W + ix0) >> sh) & 0xffu, srgb);
-    float a10 = texel_value(s, (__ldg(t + iy0 * W + ix1) >> sh) & 0xffu, srgb);
-    float a01 = texel_value(s, (__ldg(t + iy1 * W + ix0) >> sh) & 0xffu, srgb);
-    float a11 = texel_value(s, (__ldg(t + iy1 * W + ix1) >> sh) & 0xffu, srgb);
-    float top = a00 + (a10 - a00) * fx;
-    float bot = a01 + (a11 - a01) * fx;
-    return top + (bot - top) * fy;
+    const uint32_t enc = (td.w & kTexSnorm) ? 2u : (((td.w & kTexSrgb) && c < 3) ? 1u : 0u);
+    float a00 = texel_value(s, (__ldg(t + k.i00) >> sh) & 0xffu, enc);
+    float a10 = texel_value(s, (__ldg(t + k.i10) >> sh) & 0xffu, enc);
+    float a01 = texel_value(s, (__ldg(t + k.i01) >> sh) & 0xffu, enc);
+    float a11 = texel_value(s, (__ldg(t + k.i11) >> sh) & 0xffu, enc);
+    return bilerp(k, a00, a10, a01, a11);
 }
 
 // tex_bilinear for channels 0, 1, 2 at once: one address computation and one
 // fetch of the four texels, the same per-channel arithmetic.
 HXD V3 tex_bilinear_rgb(const DevScene& s, uint32_t tex, float u, float v) {
-    uint4 td = s.tex_desc[tex];
-    int W = (int)td.y, H = (int)td.z;
-    float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
-    float x0 = floorf(x), y0 = floorf(y);
-    float fx = x - x0, fy = y - y0;
-    int ix0, iy0, ix1, iy1;
-    if (((W & (W - 1)) | (H & (H - 1))) == 0) {
-        ix0 = (int)x0 & (W - 1);
-        iy0 = (int)y0 & (H - 1);
-        ix1 = (ix0 + 1) & (W - 1);
-        iy1 = (iy0 + 1) & (H - 1);
-    } else {
-        ix0 = (((int)x0 % W) + W) % W;
-        iy0 = (((int)y0 % H) + H) % H;
-        ix1 = ix0 + 1 == W ? 0 : ix0 + 1;
-        iy1 = iy0 + 1 == H ? 0 : iy0 + 1;
+    const uint4 td = s.tex_desc[tex];
+    const TexTaps k = tex_taps(td, u, v);
+    float r[3];
+    if (td.w & kTexHalf) {
+        const uint2* t = reinterpret_cast<const uint2*>(s.texels + td.x);
+        const uint2 t00 = __ldg(t + k.i00), t10 = __ldg(t + k.i10), t01 = __ldg(t + k.i01), t11 = __ldg(t + k.i11);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            r[c] = bilerp(k, half_channel(t00, c), half_channel(t10, c), half_channel(t01, c), half_channel(t11, c));
+        return v3(r[0], r[1], r[2]);
     }
     const uint32_t* t = s.texels + td.x;
-    const uint32_t t00 = __ldg(t + iy0 * W + ix0), t10 = __ldg(t + iy0 * W + ix1);
-    const uint32_t t01 = __ldg(t + iy1 * W + ix0), t11 = __ldg(t + iy1 * W + ix1);
-    const bool srgb = td.w & 1u;
-    float r[3];
+    const uint32_t t00 = __ldg(t + k.i00), t10 = __ldg(t + k.i10);
+    const uint32_t t01 = __ldg(t + k.i01), t11 = __ldg(t + k.i11);
+    const uint32_t enc = (td.w & kTexSnorm) ? 2u : ((td.w & kTexSrgb) ? 1u : 0u);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int sh = 8 * c;
-        float a00 = texel_value(s, (t00 >> sh) & 0xffu, srgb), a10 = texel_value(s, (t10 >> sh) & 0xffu, srgb);
-        float a01 = texel_value(s, (t01 >> sh) & 0xffu, srgb), a11 = texel_value(s, (t11 >> sh) & 0xffu, srgb);
-        float top = a00 + (a10 - a00) * fx;
-        float bot = a01 + (a11 - a01) * fx;
-        r[c] = top + (bot - top) * fy;
+        float a00 = texel_value(s, (t00 >> sh) & 0xffu, enc), a10 = texel_value(s, (t10 >> sh) & 0xffu, enc);
+        float a01 = texel_value(s, (t01 >> sh) & 0xffu, enc), a11 = texel_value(s, (t11 >> sh) & 0xffu, enc);
+        r[c] = bilerp(k, a00, a10, a01, a11);
     }
     return v3(r[0], r[1], r[2]);
 }
 
-// Bilinear alpha from the scene's A8 copy of the textures: the same texel
-// bytes and arithmetic as tex_bilinear(..., 3).
+// Bilinear alpha of an RGBA16F or SNORM texture, out of line: the any-hit test
+// inside the traversal loop carries only the A8 path's code.
+static __device__ __noinline__ float tex_alpha_wide(const uint32_t* __restrict__ texels, uint4 td, float u, float v) {
+    const TexTaps k = tex_taps(td, u, v);
+    if (td.w & kTexHalf) {
+        const uint2* t = reinterpret_cast<const uint2*>(texels + td.x);
+        return bilerp(k, half_channel(__ldg(t + k.i00), 3), half_channel(__ldg(t + k.i10), 3),
+                      half_channel(__ldg(t + k.i01), 3), half_channel(__ldg(t + k.i11), 3));
+    }
+    const uint32_t* t = texels + td.x;  // SNORM
+    return bilerp(k, snorm8(__ldg(t + k.i00) >> 24), snorm8(__ldg(t + k.i10) >> 24), snorm8(__ldg(t + k.i01) >> 24),
+                  snorm8(__ldg(t + k.i11) >> 24));
+}
+
+// Bilinear alpha of a UNORM/sRGB RGBA8 texture from the scene's A8 copy (the
+// same texel bytes and arithmetic as tex_bilinear(..., 3), a quarter of the
+// cache footprint).
 HXD float tex_alpha_bilinear(const DevScene& s, uint32_t tex, float u, float v) {
     uint4 td = s.tex_desc[tex];
     int W = (int)td.y, H = (int)td.z;
@@ -187,13 +238,23 @@ HXD float tex_alpha_bilinear(const DevScene& s, uint32_t tex, float u, float v) 
     return top + (bot - top) * fy;
 }
 
-// Any-hit alpha test: interpolated UV, albedo alpha, reject below 0.1.
+// Any-hit alpha test: interpolated UV, albedo alpha, reject below 0.1.  The
+// record's texture word is the albedo texture index, 0xffffffff for none, or
+// the index | 0x80000000 for an RGBA16F / SNORM texture ("wide" alpha, read
+// without the A8 copy).  Only scenes with such records (DevScene::wide_alpha)
+// run the WA instantiation; the others carry no code for it.
+template <bool WA>
 HXD bool alpha_pass(const DevScene& s, uint32_t prim, float u, float v) {
     float4 a = __ldg(&s.alpha_uv[2 * (size_t)prim]);
     float4 b = __ldg(&s.alpha_uv[2 * (size_t)prim + 1]);
     uint32_t tex = __float_as_uint(b.z);
     float alpha;
-    if (tex == 0xffffffffu) alpha = b.w;
+    if (WA && (int32_t)tex < 0 && tex != 0xffffffffu) {
+        float b0 = 1.0f - u - v;
+        float tu = a.x * b0 + a.z * u + b.x * v;
+        float tv = a.y * b0 + a.w * u + b.y * v;
+        alpha = tex_alpha_wide(s.texels, s.tex_desc[tex & 0x7fffffffu], tu, tv);
+    } else if (tex == 0xffffffffu) alpha = b.w;
     else {
         float b0 = 1.0f - u - v;
         float tu = a.x * b0 + a.z * u + b.x * v;
@@ -364,7 +425,7 @@ HXD void trav_init_record(TravState& st, const DevScene& s, float4 o_tmin, float
 // One step of a lane's traversal: visits one node and tests the triangles it
 // exposed.  Returns true when the ray is finished (traversal exhausted, or
 // the first accepted hit of a shadow ray, st.shadow).
-template <bool COUNT>
+template <bool COUNT, bool WA>
 HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflow, TraverseCount* tc) {
     if (st.g_mask > 0x00ffffffu) {
         const uint32_t bit = 31u - __clz(st.g_mask);
@@ -417,7 +478,7 @@ HXD bool trav_step(TravState& st, uint2* stack, const DevScene& s, bool& overflo
         if (!(t < st.best_t || (t == st.best_t && prim < st.best))) continue;
         if (st.any_hit && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE)) {
             if (COUNT) tc->alpha++;
-            if (!alpha_pass(s, prim, u, v)) continue;
+            if (!alpha_pass<WA>(s, prim, u, v)) continue;
         }
         st.best_t = t; st.bu = u; st.bv = v; st.best = prim;
         if (st.shadow) return true;
@@ -502,7 +563,7 @@ struct WarpTris {
 
 // Tests the first n queued triangles, one per lane and round (all 32 lanes
 // call it together); accepted hits lower their ray's key.
-template <bool COUNT>
+template <bool COUNT, bool WA>
 HXD void warp_test_tris(WarpTris& w, uint32_t lane, uint32_t n, const DevScene& s, const float4* __restrict__ qo,
                         const float4* __restrict__ qr1, const float4* __restrict__ so, const float4* __restrict__ sr1,
                         bool& overflow, TraverseCount* tc) {
@@ -545,7 +606,7 @@ HXD void warp_test_tris(WarpTris& w, uint32_t lane, uint32_t n, const DevScene& 
                         bool pass = true;
                         if ((bits & (1u << 9)) && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE)) {
                             if (COUNT) tc->alpha++;
-                            pass = alpha_pass(s, prim, u, v);
+                            pass = alpha_pass<WA>(s, prim, u, v);
                         }
                         if (pass) {
                             cand = ((unsigned long long)__float_as_uint(t) << 32) | prim;

@@ -27,10 +27,11 @@ constexpr int kBatchedCarveoutPct = 10;
 
 // Applies the carve-out preferences to this translation unit's traversal
 // and shading kernels (each unit has its own instances).
-template <typename F1, typename F2>
-static inline cudaError_t set_carveouts(F1 batched0, F2 batched1) {
-    cudaError_t e = cudaFuncSetAttribute(batched0, cudaFuncAttributePreferredSharedMemoryCarveout, kBatchedCarveoutPct);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(batched1, cudaFuncAttributePreferredSharedMemoryCarveout, kBatchedCarveoutPct);
+template <typename... F>
+static inline cudaError_t set_carveouts(F... kernels) {
+    cudaError_t e = cudaSuccess;
+    for (const void* k : {reinterpret_cast<const void*>(kernels)...})
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, kBatchedCarveoutPct);
     return e;
 }
 constexpr int kShadeThreads = 128;
@@ -370,7 +371,7 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevSce
 // visits, [3] triangle tests, [4] warp node steps, [5] warp triangle steps,
 // [6] warp loop iterations, [7] lane loop iterations with a ray, [8] alpha
 // tests.
-template <bool COUNT, bool FP16>
+template <bool COUNT, bool FP16, bool WA = false>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevScene s, Queues q, const float4* __restrict__ qo,
                                                                            const float4* __restrict__ qr0,
                                                                            const float4* __restrict__ qr1,
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
             if (ray != kNoHit) loop_busy++;
         }
         if (ray != kNoHit) {
-            if (trav_step<COUNT>(st, stack, s, overflow, &cnt)) {
+            if (trav_step<COUNT, WA>(st, stack, s, overflow, &cnt)) {
                 if (st.shadow) {
                     if (st.best == kNoHit) {
                         const float4 c = q.sc[ray];
@@ -480,7 +481,7 @@ constexpr uint32_t kNodeSteps = 3;
 // keeps them and visits no node until they do.  A ray is finished when it
 // has no node left and no pending triangle (or, for a shadow ray, as soon as
 // a flush accepted a hit).  Same queues, results and counters as k_extend.
-template <bool COUNT>
+template <bool COUNT, bool WA = false>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
     k_extend_batched(DevScene s, Queues q, const float4* __restrict__ qo, const float4* __restrict__ qr0,
                      const float4* __restrict__ qr1, const uint32_t* __restrict__ count, uint32_t* fetch,
@@ -576,7 +577,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
         const uint32_t walking = __ballot_sync(0xffffffffu, has_node && tmask == 0);
         const uint32_t carried = __ballot_sync(0xffffffffu, tmask != 0);
         if (qn >= flush_tris || (uint32_t)__popc(parked) >= flush_parked || carried != 0 || (qn > 0 && walking == 0)) {
-            warp_test_tris<COUNT>(w, lane, qn, s, qo, qr1, q.so, q.sr1, overflow, &cnt);
+            warp_test_tris<COUNT, WA>(w, lane, qn, s, qo, qr1, q.so, q.sr1, overflow, &cnt);
             qn = 0;
             queued = false;
         }
@@ -614,6 +615,28 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
         atomicAdd(&q.stats[8], (unsigned long long)cnt.alpha);
     }
     if (overflow) atomicOr(q.status, 1u);
+}
+
+// One traversal launch: the batched kernel for scenes under 2^27 triangles
+// with FP32 payloads, else the per-lane one; the WA instantiations (wide-alpha
+// any-hit path) only for scenes that need them.
+template <bool COUNT, bool FP16>
+static inline void launch_extend(const DevScene& s, const Queues& q, int grid_batched, int grid_trace, cudaStream_t st,
+                                 const float4* qo, const float4* qr0, const float4* qr1, const uint32_t* qp,
+                                 const uint32_t* count, uint32_t* fetch) {
+    if (!FP16 && s.num_prims < (1u << 27)) {
+        if (s.wide_alpha)
+            k_extend_batched<COUNT, true><<<grid_batched, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, count, fetch,
+                                                                                  kFlushTris, kFlushParked);
+        else
+            k_extend_batched<COUNT, false><<<grid_batched, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, count, fetch,
+                                                                                   kFlushTris, kFlushParked);
+    } else {
+        if (s.wide_alpha)
+            k_extend<COUNT, FP16, true><<<grid_trace, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, qp, count, fetch);
+        else
+            k_extend<COUNT, FP16, false><<<grid_trace, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, qp, count, fetch);
+    }
 }
 
 // Accumulation (path_trace_rgen.glsl:217-248): clamp, then running mean

@@ -156,7 +156,10 @@ typedef struct hx_instance {
  * formats (BC6H, the reference's VK_FORMAT_BC6H_SFLOAT_BLOCK, and
  * uncompressed RGBA16F, its R16G16B16A16_SFLOAT for FLOAT16 images) are kept
  * as RGBA16F texels on the device (hx_texture_decode_hdr) and sampled in
- * FP32; they take srgb = 0 (the reference has no sRGB variant of them). */
+ * FP32; they take srgb = 0 (the reference has no sRGB variant of them).
+ * HX_TEXTURE_RGBA8_SNORM is how the reference creates uncompressed 8-bit
+ * images that are not sRGB (kNonSRGBFormats, resource_manager.cpp:32-36, 64:
+ * R8G8B8A8_SNORM): each channel reads max(int8 / 127, -1), srgb = 0. */
 #define HX_TEXTURE_RGBA8    0u
 #define HX_TEXTURE_BC1_RGB  1u  /* 8-byte blocks, alpha 255                          */
 #define HX_TEXTURE_BC1_RGBA 2u  /* 8-byte blocks, 1-bit alpha in the 3-colour mode   */
@@ -168,6 +171,7 @@ typedef struct hx_instance {
 #define HX_TEXTURE_BC6H_SF16 8u /* 16-byte blocks: BPTC signed half-float RGB (A = 1)  */
 #define HX_TEXTURE_BC6H_UF16 9u /* 16-byte blocks: BPTC unsigned half-float RGB (A = 1) */
 #define HX_TEXTURE_RGBA16F 10u  /* width * height * 4 IEEE half floats (little-endian) */
+#define HX_TEXTURE_RGBA8_SNORM 11u /* width * height * 4 signed bytes: max(c / 127, -1)  */
 typedef struct hx_texture_desc {
     const uint8_t* rgba8;
     uint32_t       width;
@@ -176,8 +180,9 @@ typedef struct hx_texture_desc {
     uint32_t       format;  /* HX_TEXTURE_* */
 } hx_texture_desc;
 
-/* Host-only: decodes a texture of any HX_TEXTURE_* format to width * height
- * RGBA8 texels (rows top to bottom).  Colour endpoints expand from RGB565 by
+/* Host-only: decodes a texture of an 8-bit HX_TEXTURE_* format to width *
+ * height RGBA8 texels (rows top to bottom; RGBA8 and RGBA8_SNORM bytes are
+ * returned as they are).  Colour endpoints expand from RGB565 by
  * bit replication; interpolated palette entries round to nearest:
  * (2a + b + 1) / 3 and (a + b + 1) / 2 for colour, ((8 - k) a + (k - 1) b + 3) / 7
  * and ((6 - k) a + (k - 1) b + 2) / 5 for BC4-style channels; BC2 alpha is

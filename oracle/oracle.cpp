@@ -46,8 +46,10 @@ struct PrimInfo {
 };
 struct Tex {
     std::vector<uint8_t> rgba;
+    std::vector<float> hdr;  // RGBA16F textures: the half values as floats (then rgba is empty)
     uint32_t w = 0, h = 0;
-    bool srgb = false;  // RGB sRGB-encoded (resource_manager.cpp:48-67)
+    bool srgb = false;   // RGB sRGB-encoded (resource_manager.cpp:48-67)
+    bool snorm = false;  // *_SNORM bytes (kNonSRGBFormats, resource_manager.cpp:32-36, 64)
 };
 
 struct Bvh {
@@ -744,7 +746,8 @@ static inline uint8_t tex_fetch(const Tex& t, long x, long y, int c) { return t.
 // A texel channel as a value in [0, 1]: q / 255, or for the RGB of an sRGB
 // texture the sRGB transfer function (IEC 61966-2-1, the decode of *_SRGB
 // formats), applied before filtering; in FP32 the exact value rounded once.
-template <typename R> static R texel_value(uint8_t q, bool srgb) {
+template <typename R> static R texel_value(uint8_t q, bool srgb, bool snorm = false) {
+    if (snorm) return R(std::max((int)(int8_t)q / 127.0, -1.0));  // Vulkan SNORM: max(c / 127, -1)
     if (!srgb) return R(q) / R(255);
     const double c = q / 255.0;
     return R(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
@@ -759,8 +762,15 @@ template <typename R> static R tex_bilinear(const Tex& t, R u, R v, int c) {
     long ix0 = (((long)x0 % W) + W) % W, iy0 = (((long)y0 % H) + H) % H;
     long ix1 = (ix0 + 1) % W, iy1 = (iy0 + 1) % H;
     const bool srgb = t.srgb && c < 3;
-    R a00 = texel_value<R>(tex_fetch(t, ix0, iy0, c), srgb), a10 = texel_value<R>(tex_fetch(t, ix1, iy0, c), srgb);
-    R a01 = texel_value<R>(tex_fetch(t, ix0, iy1, c), srgb), a11 = texel_value<R>(tex_fetch(t, ix1, iy1, c), srgb);
+    R a00, a10, a01, a11;
+    if (!t.hdr.empty()) {  // half-float texels: their values (the formats have no sRGB variant)
+        auto hv = [&](long x, long y) { return R(t.hdr[((size_t)y * t.w + x) * 4 + c]); };
+        a00 = hv(ix0, iy0), a10 = hv(ix1, iy0), a01 = hv(ix0, iy1), a11 = hv(ix1, iy1);
+    } else {
+        const bool sn = t.snorm;
+        a00 = texel_value<R>(tex_fetch(t, ix0, iy0, c), srgb, sn), a10 = texel_value<R>(tex_fetch(t, ix1, iy0, c), srgb, sn);
+        a01 = texel_value<R>(tex_fetch(t, ix0, iy1, c), srgb, sn), a11 = texel_value<R>(tex_fetch(t, ix1, iy1, c), srgb, sn);
+    }
     R top = a00 + (a10 - a00) * fx;
     R bot = a01 + (a11 - a01) * fx;
     return top + (bot - top) * fy;
@@ -1391,11 +1401,14 @@ struct oracle_counters {
     int threads;
 };
 
-// Textures must be RGBA8 (the oracle does not restate the block decoders;
-// those are pinned by oracle/texture_ref.py): NULL otherwise.
+// Textures must be RGBA8 (UNORM, sRGB or SNORM) or RGBA16F (the oracle does
+// not restate the block decoders; those are pinned by oracle/texture_ref.py):
+// NULL otherwise.
 void* oracle_scene_create(const hx_scene_desc* d) {
     for (uint32_t t = 0; t < d->num_textures; ++t)
-        if (d->textures[t].format != HX_TEXTURE_RGBA8) return nullptr;
+        if (d->textures[t].format != HX_TEXTURE_RGBA8 && d->textures[t].format != HX_TEXTURE_RGBA16F &&
+            d->textures[t].format != HX_TEXTURE_RGBA8_SNORM)
+            return nullptr;
     Scene* s = new Scene();
     for (uint32_t m = 0; m < d->num_meshes; ++m) {
         const hx_mesh_desc& md = d->meshes[m];
@@ -1409,8 +1422,15 @@ void* oracle_scene_create(const hx_scene_desc* d) {
         Tex tx;
         tx.w = d->textures[t].width;
         tx.h = d->textures[t].height;
-        tx.rgba.assign(d->textures[t].rgba8, d->textures[t].rgba8 + (size_t)tx.w * tx.h * 4);
+        if (d->textures[t].format == HX_TEXTURE_RGBA16F) {
+            const uint8_t* b = d->textures[t].rgba8;
+            tx.hdr.resize((size_t)tx.w * tx.h * 4);
+            for (size_t i = 0; i < tx.hdr.size(); ++i) tx.hdr[i] = half_to_float((uint16_t)(b[2 * i] | (b[2 * i + 1] << 8)));
+        } else {
+            tx.rgba.assign(d->textures[t].rgba8, d->textures[t].rgba8 + (size_t)tx.w * tx.h * 4);
+        }
         tx.srgb = d->textures[t].srgb != 0;
+        tx.snorm = d->textures[t].format == HX_TEXTURE_RGBA8_SNORM;
         s->textures.push_back(std::move(tx));
     }
     s->punctual.assign(d->punctual_lights, d->punctual_lights + d->num_punctual_lights);

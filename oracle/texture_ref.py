@@ -19,6 +19,14 @@ Data Format Specification (S3TC and RGTC sections):
   replication, anchor indices one bit shorter, interpolation
   ((64 - w) e0 + w e1 + 32) >> 6 with the 2/3/4-bit weight tables, optional
   channel rotation and a second index set (modes 4 and 5).
+* BC6H (BPTC half float): fourteen modes chosen by the low two bits (00, 01)
+  or low five bits of the block; one or two regions (the two-region
+  partitions are BC7's first 32); endpoint fields scattered through the
+  header in a per-mode order; endpoints 1-3 optionally stored as signed
+  deltas from endpoint 0; endpoints unquantised to 16 bits, interpolated
+  with BC7's 3- or 4-bit weights in integers, then scaled to the half-float
+  bit pattern (x 31/64, or for the signed format the magnitude x 31/32 with
+  the sign bit).  Reserved mode codes decode to zero colour; alpha is 1.0.
 
 The specification leaves the rounding of interpolated entries to the
 implementation; this library rounds to nearest in integers and so does
@@ -27,6 +35,7 @@ this restatement.
 import numpy as np
 
 BC1_RGB, BC1_RGBA, BC2, BC3, BC4, BC5, BC7 = 1, 2, 3, 4, 5, 6, 7
+BC6H_SF16, BC6H_UF16 = 8, 9
 BLOCK_BYTES = {BC1_RGB: 8, BC1_RGBA: 8, BC2: 16, BC3: 16, BC4: 8, BC5: 16, BC7: 16}
 
 # BC7 (BPTC), Khronos Data Format Specification: per mode (subsets,
@@ -135,6 +144,174 @@ def decode_bc7_block(block):
             c[3], c[rot - 1] = c[rot - 1], c[3]
         out.append(c)
     return out
+
+
+def _bits(field, *spec):
+    """Storage-order bit list of one endpoint field: spec items are value-bit
+    numbers or (lo, hi) runs stored from lo to hi (hi < lo: stored reversed)."""
+    out = []
+    for s in spec:
+        if isinstance(s, tuple):
+            lo, hi = s
+            step = 1 if hi >= lo else -1
+            out += [(field, b) for b in range(lo, hi + step, step)]
+        else:
+            out.append((field, s))
+    return out
+
+
+def _layout(*items):
+    return [fb for it in items for fb in it]
+
+
+R = _bits
+# per mode code: (mode bits, regions, transformed, endpoint bits, delta bits (r, g, b), header layout after the
+# mode bits as (field, value bit) in storage order; fields r/g/b + endpoint w, x (region 0), y, z (region 1))
+BC6H_MODES = {
+    0b00: (2, 2, True, 10, (5, 5, 5), _layout(
+        R("gy", 4), R("by", 4), R("bz", 4), R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 4)),
+        R("gz", 4), R("gy", (0, 3)), R("gx", (0, 4)), R("bz", 0), R("gz", (0, 3)), R("bx", (0, 4)), R("bz", 1),
+        R("by", (0, 3)), R("ry", (0, 4)), R("bz", 2), R("rz", (0, 4)), R("bz", 3))),
+    0b01: (2, 2, True, 7, (6, 6, 6), _layout(
+        R("gy", 5), R("gz", 4, 5), R("rw", (0, 6)), R("bz", 0, 1), R("by", 4), R("gw", (0, 6)), R("by", 5),
+        R("bz", 2), R("gy", 4), R("bw", (0, 6)), R("bz", 3, 5, 4), R("rx", (0, 5)), R("gy", (0, 3)),
+        R("gx", (0, 5)), R("gz", (0, 3)), R("bx", (0, 5)), R("by", (0, 3)), R("ry", (0, 5)), R("rz", (0, 5)))),
+    0b00010: (5, 2, True, 11, (5, 4, 4), _layout(
+        R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 4)), R("rw", 10), R("gy", (0, 3)),
+        R("gx", (0, 3)), R("gw", 10), R("bz", 0), R("gz", (0, 3)), R("bx", (0, 3)), R("bw", 10), R("bz", 1),
+        R("by", (0, 3)), R("ry", (0, 4)), R("bz", 2), R("rz", (0, 4)), R("bz", 3))),
+    0b00110: (5, 2, True, 11, (4, 5, 4), _layout(
+        R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 3)), R("rw", 10), R("gz", 4),
+        R("gy", (0, 3)), R("gx", (0, 4)), R("gw", 10), R("gz", (0, 3)), R("bx", (0, 3)), R("bw", 10), R("bz", 1),
+        R("by", (0, 3)), R("ry", (0, 3)), R("bz", 0, 2), R("rz", (0, 3)), R("gy", 4), R("bz", 3))),
+    0b01010: (5, 2, True, 11, (4, 4, 5), _layout(
+        R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 3)), R("rw", 10), R("by", 4),
+        R("gy", (0, 3)), R("gx", (0, 3)), R("gw", 10), R("bz", 0), R("gz", (0, 3)), R("bx", (0, 4)), R("bw", 10),
+        R("by", (0, 3)), R("ry", (0, 3)), R("bz", 1, 2), R("rz", (0, 3)), R("bz", 4, 3))),
+    0b01110: (5, 2, True, 9, (5, 5, 5), _layout(
+        R("rw", (0, 8)), R("by", 4), R("gw", (0, 8)), R("gy", 4), R("bw", (0, 8)), R("bz", 4), R("rx", (0, 4)),
+        R("gz", 4), R("gy", (0, 3)), R("gx", (0, 4)), R("bz", 0), R("gz", (0, 3)), R("bx", (0, 4)), R("bz", 1),
+        R("by", (0, 3)), R("ry", (0, 4)), R("bz", 2), R("rz", (0, 4)), R("bz", 3))),
+    0b10010: (5, 2, True, 8, (6, 5, 5), _layout(
+        R("rw", (0, 7)), R("gz", 4), R("by", 4), R("gw", (0, 7)), R("bz", 2), R("gy", 4), R("bw", (0, 7)),
+        R("bz", 3, 4), R("rx", (0, 5)), R("gy", (0, 3)), R("gx", (0, 4)), R("bz", 0), R("gz", (0, 3)),
+        R("bx", (0, 4)), R("bz", 1), R("by", (0, 3)), R("ry", (0, 5)), R("rz", (0, 5)))),
+    0b10110: (5, 2, True, 8, (5, 6, 5), _layout(
+        R("rw", (0, 7)), R("bz", 0), R("by", 4), R("gw", (0, 7)), R("gy", 5, 4), R("bw", (0, 7)), R("gz", 5),
+        R("bz", 4), R("rx", (0, 4)), R("gz", 4), R("gy", (0, 3)), R("gx", (0, 5)), R("gz", (0, 3)),
+        R("bx", (0, 4)), R("bz", 1), R("by", (0, 3)), R("ry", (0, 4)), R("bz", 2), R("rz", (0, 4)), R("bz", 3))),
+    0b11010: (5, 2, True, 8, (5, 5, 6), _layout(
+        R("rw", (0, 7)), R("bz", 1), R("by", 4), R("gw", (0, 7)), R("by", 5), R("gy", 4), R("bw", (0, 7)),
+        R("bz", 5, 4), R("rx", (0, 4)), R("gz", 4), R("gy", (0, 3)), R("gx", (0, 4)), R("bz", 0),
+        R("gz", (0, 3)), R("bx", (0, 5)), R("by", (0, 3)), R("ry", (0, 4)), R("bz", 2), R("rz", (0, 4)),
+        R("bz", 3))),
+    0b11110: (5, 2, False, 6, (6, 6, 6), _layout(
+        R("rw", (0, 5)), R("gz", 4), R("bz", 0, 1), R("by", 4), R("gw", (0, 5)), R("gy", 5), R("by", 5),
+        R("bz", 2), R("gy", 4), R("bw", (0, 5)), R("gz", 5), R("bz", 3, 5, 4), R("rx", (0, 5)), R("gy", (0, 3)),
+        R("gx", (0, 5)), R("gz", (0, 3)), R("bx", (0, 5)), R("by", (0, 3)), R("ry", (0, 5)), R("rz", (0, 5)))),
+    0b00011: (5, 1, False, 10, (10, 10, 10), _layout(
+        R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 9)), R("gx", (0, 9)), R("bx", (0, 9)))),
+    0b00111: (5, 1, True, 11, (9, 9, 9), _layout(
+        R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 8)), R("rw", 10), R("gx", (0, 8)),
+        R("gw", 10), R("bx", (0, 8)), R("bw", 10))),
+    0b01011: (5, 1, True, 12, (8, 8, 8), _layout(
+        R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 7)), R("rw", (11, 10)), R("gx", (0, 7)),
+        R("gw", (11, 10)), R("bx", (0, 7)), R("bw", (11, 10)))),
+    0b01111: (5, 1, True, 16, (4, 4, 4), _layout(
+        R("rw", (0, 9)), R("gw", (0, 9)), R("bw", (0, 9)), R("rx", (0, 3)), R("rw", (15, 10)), R("gx", (0, 3)),
+        R("gw", (15, 10)), R("bx", (0, 3)), R("bw", (15, 10)))),
+}
+del R
+
+
+def _sext(v, n):
+    v &= (1 << n) - 1
+    return v - (1 << n) if v >> (n - 1) else v
+
+
+def _bc6_unq(c, epb, signed):
+    if not signed:
+        if epb >= 15:
+            return c
+        if c == 0:
+            return 0
+        if c == (1 << epb) - 1:
+            return 0xFFFF
+        return ((c << 16) + 0x8000) >> epb
+    if epb >= 16:
+        return c
+    m = abs(c)
+    if m == 0:
+        u = 0
+    elif m >= (1 << (epb - 1)) - 1:
+        u = 0x7FFF
+    else:
+        u = ((m << 15) + 0x4000) >> (epb - 1)
+    return -u if c < 0 else u
+
+
+def _bc6_half(c, signed):
+    if not signed:
+        return (c * 31) >> 6
+    m = (abs(c) * 31) >> 5
+    return (0x8000 | m) if (c < 0 and m) else m
+
+
+def decode_bc6h_block(block, signed):
+    """16 RGBA half-float bit patterns of one 16-byte BC6H block (texel t = x + 4 y)."""
+    bits = int.from_bytes(bytes(block), "little")
+    code = bits & 3 if (bits & 3) < 2 else bits & 31
+    if code not in BC6H_MODES:
+        return [[0, 0, 0, 0x3C00] for _ in range(16)]
+    nmode, regions, transformed, epb, delta, layout = BC6H_MODES[code]
+    pos = nmode
+    ep = {f + e: 0 for f in "rgb" for e in "wxyz"}
+    for field, b in layout:
+        ep[field] |= ((bits >> pos) & 1) << b
+        pos += 1
+    part = 0
+    if regions == 2:
+        part = (bits >> pos) & 31
+        pos += 5
+    names = "wxyz"[: 2 * regions]
+    ends = {}
+    for ci, ch in enumerate("rgb"):
+        w = ep[ch + "w"]
+        if signed:
+            w = _sext(w, epb)
+        vals = [w]
+        for e in names[1:]:
+            v = ep[ch + e]
+            if transformed:
+                v = (w + _sext(v, delta[ci])) & ((1 << epb) - 1)
+                if signed:
+                    v = _sext(v, epb)
+            elif signed:
+                v = _sext(v, epb)
+            vals.append(v)
+        ends[ch] = [_bc6_unq(v, epb, signed) for v in vals]
+    nbits = 3 if regions == 2 else 4
+    subset = [int(c) for c in BC7_PART2[part]] if regions == 2 else [0] * 16
+    anchors = {0, BC7_ANCHOR2[part]} if regions == 2 else {0}
+    wts = BC7_WEIGHTS[nbits]
+    out = []
+    for t in range(16):
+        n = nbits - (1 if t in anchors else 0)
+        idx = (bits >> pos) & ((1 << n) - 1)
+        pos += n
+        s, w = subset[t], wts[idx]
+        px = [_bc6_half((ends[ch][2 * s] * (64 - w) + ends[ch][2 * s + 1] * w + 32) >> 6, signed) for ch in "rgb"]
+        out.append(px + [0x3C00])
+    return out
+
+
+def decode_hdr(data, width, height, fmt):
+    """(height, width, 4) uint16 half-float bit patterns of width x height BC6H data (row-major blocks)."""
+    bw, bh = (width + 3) // 4, (height + 3) // 4
+    blocks = np.frombuffer(bytes(data), np.uint8)[: bw * bh * 16].reshape(bw * bh, 16)
+    px = np.array([decode_bc6h_block(b, fmt == BC6H_SF16) for b in blocks], np.int64).reshape(bh, bw, 4, 4, 4)
+    img = px.transpose(0, 2, 1, 3, 4).reshape(bh * 4, bw * 4, 4)
+    return img[:height, :width].astype(np.uint16)
 
 
 def _le(blocks, off, n):

@@ -121,9 +121,13 @@ class TexturedQuadScene:
     point light above; no environment.  .desc points at its hx_scene_desc,
     .camera() looks down at the quad."""
 
-    def __init__(self, albedo, albedo_srgb=True, normal_map=None, roughness=0.5, albedo_format=0, albedo_wh=None):
-        # albedo: (H, W, 4) RGBA8, or block-compressed bytes with albedo_format / albedo_wh = (W, H)
-        self._tex_data = [np.ascontiguousarray(albedo, np.uint8)]
+    def __init__(self, albedo, albedo_srgb=True, normal_map=None, roughness=0.5, albedo_format=0, albedo_wh=None,
+                 non_opaque=False, roughness_channel=None):
+        # albedo: (H, W, 4) RGBA8, or the bytes of another format (block-compressed, RGBA16F) with
+        # albedo_format / albedo_wh = (W, H); non_opaque: alpha-tested submesh; roughness_channel: roughness
+        # read from that channel of the albedo texture
+        a = np.ascontiguousarray(albedo)
+        self._tex_data = [a if a.dtype == np.uint8 else a.view(np.uint8)]
         if normal_map is not None:
             self._tex_data.append(np.ascontiguousarray(normal_map, np.uint8))
         pos = [(-1, 0, -1), (1, 0, -1), (1, 0, 1), (-1, 0, 1)]
@@ -138,7 +142,8 @@ class TexturedQuadScene:
             v.bitangent[2] = 1.0
         self._idx = (C.c_uint32 * 6)(0, 2, 1, 0, 3, 2)
         self._sub = (hx.Submesh * 1)()
-        self._sub[0].base_index, self._sub[0].index_count, self._sub[0].material, self._sub[0].flags = 0, 6, 0, 0
+        self._sub[0].base_index, self._sub[0].index_count, self._sub[0].material = 0, 6, 0
+        self._sub[0].flags = HX_NON_OPAQUE if non_opaque else 0
         self._mesh = (hx.MeshDesc * 1)()
         m = self._mesh[0]
         m.vertices, m.num_vertices = self._verts, 4
@@ -154,6 +159,8 @@ class TexturedQuadScene:
             mat.texture_indices0[1] = 1
         mat.albedo[0] = mat.albedo[1] = mat.albedo[2] = mat.albedo[3] = 1.0
         mat.roughness_metallic[0] = roughness
+        if roughness_channel is not None:
+            mat.texture_indices0[2], mat.texture_indices1[2] = 0, roughness_channel
         self._tex = (hx.TextureDesc * len(self._tex_data))()
         for k, t in enumerate(self._tex_data):
             self._tex[k].rgba8 = t.ctypes.data_as(C.POINTER(C.c_uint8))
@@ -219,6 +226,46 @@ def random_bc7_blocks(n, seed=0):
         m = i % 8
         blocks[i, 0] = (int(blocks[i, 0]) & ~((1 << (m + 1)) - 1) & 0xFF) | (1 << m)
     return blocks
+
+
+BC6H_MODE_CODES = [0b00, 0b01, 0b00010, 0b00110, 0b01010, 0b01110, 0b10010, 0b10110, 0b11010, 0b11110, 0b00011,
+                   0b00111, 0b01011, 0b01111]
+BC6H_RESERVED_CODES = [0b10011, 0b10111, 0b11011, 0b11111]
+
+
+def random_bc6h_blocks(n, seed=0, reserved=True):
+    """n random BC6H blocks (16 bytes each) cycling through the fourteen mode
+    codes (and the four reserved codes when `reserved`): the low two or five
+    bits of byte 0 set the code, every other bit is random."""
+    rng = np.random.default_rng(seed)
+    blocks = rng.integers(0, 256, size=(n, 16), dtype=np.uint8)
+    codes = BC6H_MODE_CODES + (BC6H_RESERVED_CODES if reserved else [])
+    for i in range(n):
+        c = codes[i % len(codes)]
+        nb = 2 if c < 2 else 5
+        blocks[i, 0] = (int(blocks[i, 0]) & ~((1 << nb) - 1) & 0xFF) | c
+    return blocks
+
+
+def bc6h_mode11_blocks(n, lo=0, hi=256, seed=0):
+    """n BC6H blocks of the one-region, untransformed mode (code 00011) with
+    every 10-bit endpoint channel drawn from [lo, hi) and random 4-bit indices:
+    with hi <= 512 the signed format decodes them to moderate positive values
+    (endpoint 248 is about 1.0)."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n, 16), np.uint8)
+    for i in range(n):
+        bits = 0b00011
+        pos = 5
+        for _ in range(6):
+            bits |= int(rng.integers(lo, hi)) << pos
+            pos += 10
+        for t in range(16):
+            nb = 3 if t == 0 else 4
+            bits |= int(rng.integers(0, 1 << nb)) << pos
+            pos += nb
+        out[i] = np.frombuffer(bits.to_bytes(16, "little"), np.uint8)
+    return out
 
 
 def checker_texture(size=32, a=(200, 180, 150), b=(40, 60, 90)):

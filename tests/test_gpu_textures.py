@@ -137,3 +137,137 @@ def test_bc7_decode_matches_the_texture_unit(gpu_ctx):
     bad = np.nonzero((got != hw).any(-1).reshape(64, 4, 64, 4).any(axis=(1, 3)).reshape(-1))[0]
     info = [(int(b), int(b % 8), blocks[b].tobytes().hex()) for b in bad[:8]]
     assert bad.size == 0, (bad.size, info)
+
+
+def _texture_unit_bc6h():
+    """tests/hw/bc6h_texture_unit.cu built for sm_103a into a temporary
+    library: BC6H blocks decoded by the GPU's own texture unit."""
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+    import tempfile
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "hw", "bc6h_texture_unit.cu")
+    out = os.path.join(tempfile.mkdtemp(), "libbc6tu.so")
+    nvcc = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-shared", "-Xcompiler", "-fPIC",
+                    "-o", out, src], check=True, capture_output=True)
+    lib = ctypes.CDLL(out)
+    lib.bc6h_texture_unit_decode.restype = ctypes.c_int
+    lib.bc6h_texture_unit_decode.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_void_p]
+    return lib
+
+
+@pytest.mark.parametrize("fmt", [hx.TEXTURE_BC6H_SF16, hx.TEXTURE_BC6H_UF16])
+def test_bc6h_decode_matches_the_texture_unit(gpu_ctx, fmt):
+    """The library's BC6H decoder (hx_texture_decode_hdr) against the GPU's
+    texture unit on 4,096 random blocks cycling through the fourteen modes
+    (every partition and index value occurs): identical half-float bit
+    patterns, signed and unsigned.  The format's arithmetic is exact
+    integers, so any mismatch is a decoding error (a bit field of a mode's
+    header, a table entry, a rounding step)."""
+    from tests.helpers import random_bc6h_blocks
+    lib = _texture_unit_bc6h()
+    blocks = np.ascontiguousarray(random_bc6h_blocks(64 * 64, seed=11 + fmt, reserved=False))
+    got = hx.texture_decode_hdr(blocks.reshape(-1), 256, 256, fmt).view(np.uint16)
+    hw = np.zeros((256, 256, 4), np.uint16)
+    rc = lib.bc6h_texture_unit_decode(blocks.ctypes.data, 64, 64, 1 if fmt == hx.TEXTURE_BC6H_SF16 else 0,
+                                      hw.ctypes.data)
+    assert rc == 0, "CUDA error %d" % rc
+    bad = np.nonzero((got[..., :3] != hw[..., :3]).any(-1).reshape(64, 4, 64, 4).any(axis=(1, 3)).reshape(-1))[0]
+    info = [(int(b), int(b % 14), blocks[b].tobytes().hex()) for b in bad[:8]]
+    assert bad.size == 0, (bad.size, info)
+
+
+def _hdr_quad(gpu_ctx, **kw):
+    qs = TexturedQuadScene(albedo_srgb=False, normal_map=bump_normal_map(), **kw)
+    return qs, hx.Scene(gpu_ctx, qs)
+
+
+@pytest.mark.parametrize("case", ["bc6h_sf16", "rgba16f_alpha_roughness", "rgba8_snorm_alpha_roughness"])
+def test_half_float_and_snorm_textures_match_oracle(gpu_ctx, case):
+    """Per-sample radiance with a half-float or SNORM albedo texture against
+    the oracle's FP32 restatement, which samples the same texel values: a
+    BC6H (signed, the reference's format) texture given to the device as
+    blocks and to the oracle as the restatement's decode
+    (oracle/texture_ref.py); an uncompressed RGBA16F texture; and an RGBA8
+    SNORM texture (the reference's format for uncompressed 8-bit images that
+    are not sRGB: bytes 128-255 read negative).  In the last two the alpha
+    (cut out below 0.1 on an alpha-tested quad) and the green channel (the
+    roughness channel) vary."""
+    from oracle import texture_ref as tr
+    from tests.helpers import bc6h_mode11_blocks
+    w, h = 24, 20
+    if case == "bc6h_sf16":
+        blocks = bc6h_mode11_blocks(((w + 3) // 4) * ((h + 3) // 4), seed=5)
+        texels = tr.decode_hdr(blocks.reshape(-1).tobytes(), w, h, tr.BC6H_SF16).view(np.float16)
+        dev = dict(albedo=blocks.reshape(-1), albedo_format=hx.TEXTURE_BC6H_SF16, albedo_wh=(w, h))
+        extra = {}
+    else:
+        rng = np.random.default_rng(8)
+        texels = rng.uniform(0.0, 1.6, (h, w, 4)).astype(np.float16)
+        texels[..., 1] = rng.uniform(0.05, 0.95, (h, w)).astype(np.float16)
+        texels[..., 3] = np.where(rng.uniform(0, 1, (h, w)) < 0.3, 0.02, 1.0).astype(np.float16)
+        dev = dict(albedo=texels, albedo_format=hx.TEXTURE_RGBA16F, albedo_wh=(w, h))
+        extra = dict(non_opaque=True, roughness_channel=1)
+    if case == "rgba8_snorm_alpha_roughness":
+        rng = np.random.default_rng(12)
+        texels = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+        texels[..., 1] = rng.integers(6, 127, (h, w))
+        texels[..., 3] = rng.choice(np.array([127, 200, 5], np.uint8), (h, w), p=[0.7, 0.15, 0.15])
+        dev = dict(albedo=texels, albedo_format=hx.TEXTURE_RGBA8_SNORM, albedo_wh=(w, h))
+    qs, sc = _hdr_quad(gpu_ctx, **dev, **extra)
+    ofmt = hx.TEXTURE_RGBA8_SNORM if case == "rgba8_snorm_alpha_roughness" else hx.TEXTURE_RGBA16F
+    oq = TexturedQuadScene(texels, albedo_srgb=False, normal_map=bump_normal_map(), albedo_format=ofmt,
+                           albedo_wh=(w, h), **extra)
+    osc = ob.OracleScene(oq)
+    W, H = 96, 64
+    d = integrator_desc(W, H, bounces=4, policy="reference")
+    f = hx.frame_desc(qs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=4, policy=d.policy)
+    for frame in (0, 5):
+        g = it.sample_radiance(f, frame)
+        o, _ = osc.sample_radiance(d, f, frame, precision=32)
+        close = np.all(np.abs(g - o) <= 1e-4 * (1 + np.abs(o)), axis=1)
+        info = (frame, rel_rmse(g, o), int((~close).sum()))
+        assert close.mean() > 0.995, info
+        assert rel_rmse(g, o) < 1e-3, info
+        assert np.abs(g).max() > 0.0
+    a = it.render_output(f, hx.OUTPUT_ALBEDO)
+    assert np.max(np.abs(a - osc.output_view(f, W, H, hx.OUTPUT_ALBEDO))) <= 2e-6
+    if case == "rgba8_snorm_alpha_roughness":
+        assert a[..., :3].min() < 0.0  # negative SNORM texels reach the albedo view
+    if case != "bc6h_sf16":
+        r = it.render_output(f, hx.OUTPUT_ROUGHNESS)
+        assert np.max(np.abs(r - osc.output_view(f, W, H, hx.OUTPUT_ROUGHNESS))) <= 2e-6
+    it.close()
+    sc.close()
+
+
+def test_bc6h_renders_like_its_rgba16f_texels(gpu_ctx):
+    """A BC6H albedo texture (decoded at upload) gives the same accumulated
+    image and albedo view, bit for bit, as uploading its RGBA16F decode; a
+    half-float texture flagged sRGB is refused (the reference has no sRGB
+    BC6H format)."""
+    from tests.helpers import bc6h_mode11_blocks
+    w, h = 30, 22
+    blocks = bc6h_mode11_blocks(((w + 3) // 4) * ((h + 3) // 4), seed=9).reshape(-1)
+    texels = hx.texture_decode_hdr(blocks, w, h, hx.TEXTURE_BC6H_SF16)
+    W, H = 64, 48
+    out = []
+    for kw in (dict(albedo=blocks, albedo_format=hx.TEXTURE_BC6H_SF16, albedo_wh=(w, h)),
+               dict(albedo=texels, albedo_format=hx.TEXTURE_RGBA16F, albedo_wh=(w, h))):
+        qs, sc = _hdr_quad(gpu_ctx, **kw)
+        f = hx.frame_desc(qs.camera(), W, H)
+        it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=3)
+        it.render(f, 4)
+        out.append((it.read_accumulation(), it.render_output(f, hx.OUTPUT_ALBEDO)))
+        it.close()
+        sc.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert np.any(out[0][1][..., :3] > 0)
+    qs = TexturedQuadScene(blocks, albedo_srgb=True, albedo_format=hx.TEXTURE_BC6H_SF16, albedo_wh=(w, h))
+    with pytest.raises(hx.HxError) as e:
+        hx.Scene(gpu_ctx, qs)
+    assert e.value.status == hx.HX_ERR_INVALID_ARG and "sRGB" in str(e.value)

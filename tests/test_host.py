@@ -7,6 +7,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 import helios_gb300 as hx
 from tests.helpers import decode_png
@@ -182,3 +183,82 @@ def test_bc7_decode_matches_restatement():
     e1 = np.array([255, 1, 1, 255])
     assert (px[1:] == e1).all(), px[1]
     assert (px[0] == ((64 - 30) * e0 + 30 * e1 + 32) >> 6).all(), px[0]
+
+
+def _bc6h_block(code, fields, indices):
+    """A BC6H block from its mode code, (value, bits) endpoint fields in stored
+    order and the per-texel index values (texel 0 one bit shorter)."""
+    bits, pos = code, (2 if code < 2 else 5)
+    for v, nb in fields:
+        bits |= (v & ((1 << nb) - 1)) << pos
+        pos += nb
+    for t, v in enumerate(indices):
+        nb = 3 if t == 0 else 4
+        bits |= v << pos
+        pos += nb
+    assert pos == 128
+    return np.frombuffer(bits.to_bytes(16, "little"), np.uint8)
+
+
+def test_bc6h_decode_matches_restatement():
+    """BC6H (BPTC half float, the reference's VK_FORMAT_BC6H_SFLOAT_BLOCK, and
+    the unsigned variant): hx_texture_decode_hdr equals the restatement of the
+    published format on random blocks of all fourteen modes and the four
+    reserved codes (half bit patterns, bit-exact), also for sizes that are
+    not multiples of 4.  The GPU's texture unit checks the same decoder in
+    tests/test_gpu_textures.py."""
+    from oracle import texture_ref as tr
+    from tests.helpers import random_bc6h_blocks
+    for fmt in (hx.TEXTURE_BC6H_SF16, hx.TEXTURE_BC6H_UF16):
+        blocks = random_bc6h_blocks(48 * 48, seed=fmt)
+        data = blocks.reshape(-1)
+        got = hx.texture_decode_hdr(data, 192, 192, fmt).view(np.uint16)
+        ref = tr.decode_hdr(data, 192, 192, fmt)
+        assert np.array_equal(got, ref), fmt
+        assert (got[..., 3] == 0x3C00).all()
+        small = hx.texture_decode_hdr(data[:16 * 8], 13, 6, fmt).view(np.uint16)
+        assert np.array_equal(small, tr.decode_hdr(data[:16 * 8], 13, 6, fmt))
+        # reserved code 10011 (block 14 of the cycle): zero colour
+        assert (got[0:4, 56:60, :3] == 0).all()
+
+
+def test_bc6h_hand_computed_blocks():
+    """Mode 11 (code 00011: one region, 10-bit endpoints, no transform, 4-bit
+    indices) worked by hand from the format's arithmetic."""
+    # unsigned: e0 = (1023, 512, 0), e1 = (0, 1023, 1023); unquantised
+    # 1023 -> 0xFFFF, 512 -> ((512 << 16) + 0x8000) >> 10 = 32800, 0 -> 0;
+    # texel 0 index 0 (e0), texel 1 index 15 (e1), texel 2 index 8 (weight 34):
+    #   R: (65535 * 30 + 0 * 34 + 32) >> 6 = 30720 -> 30720 * 31 >> 6 = 14880
+    #   G: (32800 * 30 + 65535 * 34 + 32) >> 6 = 50190 -> 24310
+    #   B: (0 * 30 + 65535 * 34 + 32) >> 6 = 34815 -> 16863
+    # and e0 -> (65535 * 31 >> 6, 32800 * 31 >> 6, 0) = (31743, 15887, 0)
+    blk = _bc6h_block(0b00011, [(1023, 10), (512, 10), (0, 10), (0, 10), (1023, 10), (1023, 10)],
+                      [0, 15, 8] + [0] * 13)
+    px = hx.texture_decode_hdr(blk, 4, 4, hx.TEXTURE_BC6H_UF16).view(np.uint16).reshape(16, 4)
+    assert px[0].tolist() == [31743, 15887, 0, 0x3C00]
+    assert px[1].tolist() == [0, 31743, 31743, 0x3C00]
+    assert px[2].tolist() == [14880, 24310, 16863, 0x3C00]
+    assert (px[3:] == px[0]).all()
+    # signed: e0 = (0x3FF, 0x1FF, 0x200) sign-extends to (-1, 511, -512);
+    # unquantised: -1 -> -(((1 << 15) + 0x4000) >> 9) = -96, 511 and -512 clamp
+    # to +-0x7FFF; index 0 everywhere: floor((64 e0 + 32) / 64) = e0, then the
+    # magnitude * 31 >> 5 with the sign bit: 96 -> 93 (0x805D), 32767 -> 31743
+    blk = _bc6h_block(0b00011, [(0x3FF, 10), (0x1FF, 10), (0x200, 10), (0, 10), (0, 10), (0, 10)], [0] * 16)
+    px = hx.texture_decode_hdr(blk, 4, 4, hx.TEXTURE_BC6H_SF16).view(np.uint16).reshape(16, 4)
+    assert (px == np.array([0x805D, 31743, 0x8000 | 31743, 0x3C00])).all(), px[0]
+    assert float(px[0].view(np.float16)[0]) == -93 * 2.0 ** -24  # a subnormal half
+
+
+def test_half_float_formats_host_checks():
+    """RGBA16F passes through hx_texture_decode_hdr unchanged; each decoder
+    refuses the other family's formats."""
+    rng = np.random.default_rng(3)
+    tex = rng.normal(0, 4, (5, 7, 4)).astype(np.float16)
+    assert np.array_equal(hx.texture_decode_hdr(tex.view(np.uint8), 7, 5, hx.TEXTURE_RGBA16F).view(np.uint16),
+                          tex.view(np.uint16))
+    with pytest.raises(hx.HxError) as e:
+        hx.texture_decode(np.zeros(16, np.uint8), 4, 4, hx.TEXTURE_BC6H_SF16)
+    assert e.value.status == hx.HX_ERR_INVALID_ARG and "hdr" in str(e.value)
+    with pytest.raises(hx.HxError) as e:
+        hx.texture_decode_hdr(np.zeros(16, np.uint8), 4, 4, hx.TEXTURE_BC7)
+    assert e.value.status == hx.HX_ERR_INVALID_ARG
