@@ -50,8 +50,9 @@ def parse():
     p.add_argument("--steps", type=int, default=256, help="frames (config 1: 256 frames of 1 spp)")
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--frames-per-wavefront", type=int, default=8,
-                   help="frames traced together by one wavefront (render_frames batching; same image)")
+    p.add_argument("--frames-per-wavefront", type=int, default=64,
+                   help="frames traced together by one wavefront (render_frames batching; same image; 64: 34 GB "
+                        "of path state)")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--serving", action="store_true", help="serving workload (Poisson request stream)")

@@ -172,6 +172,7 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_A(it->q.rng, 8 * cap);
     HX_A(it->q.shade_list, 4 * cap);
     it->q.shade_cap = (uint32_t)cap;
+    HX_A(it->q.part, 4 * (size_t)kPartBlocks);
     HX_A(it->q.counters, 64);
     HX_A(it->q.stats, 128);
     HX_A(it->q.status, 64);
@@ -287,11 +288,9 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
     uint32_t npix = rect.w * rect.h;
     uint32_t total = npix * nframes;
     const bool fp16 = it->desc.policy.payload == HX_PAYLOAD_FP16;
-    // the traversal and shading launches' queues: the 16-bit payload form
-    // shades in queue order (its lane-local traversal finishes rays too
-    // scattered for the shading list: -10 % on the terrain scene)
     Queues qs = it->q;
-    if (fp16) qs.shade_list = nullptr;
+    qs.list_mode = shade_list_mode(total, fp16);
+    if (qs.list_mode == 0u) qs.shade_list = nullptr;  // shade in queue order
     it->stats.paths += total;
     {
         StageTimer t(it, &it->stats.ms_raygen);
@@ -343,6 +342,8 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
             HX_CUDA(cudaMemsetAsync(it->q.counters + 2, 0, 4, st));
             {
                 StageTimer t(it, &it->stats.ms_shade);
+                it->stats.kernel_launches += fp16 ? launch_shade_partition<true>(qs, cur, st)
+                                                  : launch_shade_partition<false>(qs, cur, st);
                 if (dbg)
                     k_shade<false, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces,
                                                                                    it->desc.shadow_ray_bias, cur, qs);

@@ -325,6 +325,9 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
     HX_TRY(A((void**)&b->q.rng, 8ull * cap));
     HX_TRY(A((void**)&b->q.shade_list, 4ull * cap));
     b->q.shade_cap = cap;
+    HX_TRY(A((void**)&b->q.part, 4ull * kPartBlocks));
+    b->q.list_mode = shade_list_mode(cap, false);
+
     HX_TRY(A((void**)&b->q.counters, 64));
     HX_TRY(A((void**)&b->q.stats, 64));
     HX_TRY(A((void**)&b->q.status, 64));
@@ -373,6 +376,7 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
             k_aov_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, sc, b->q.hit);
         cudaMemsetAsync(b->q.counters + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(b->q.counters + 2, 0, 4, st);
+        launch_shade_partition<false>(b->q, cur, st);
         k_shade<false><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
     }
     k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp,
