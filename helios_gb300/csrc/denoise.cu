@@ -53,6 +53,7 @@ constexpr int kChunk = 32;                // channels per K step (64-byte rows)
 constexpr int kChunkBytes = 128 * 64;     // one 128-row x 64-byte operand tile
 constexpr int kThreads = 192;
 constexpr int kConvStages = 4;
+constexpr bool kConvHalo = true;          // forward / backward-data through k_conv_halo
 constexpr int kWgradStages = 3;
 
 enum Epi : int { EPI_RELU_BF16 = 0, EPI_LINEAR_F32 = 1, EPI_DGRAD = 2 };
@@ -254,6 +255,204 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     }
     drain(warp, lane, issued, a.stages, full, done, &s_fail);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 5) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, a.tmem_cols);
+    }
+    if (threadIdx.x == 0 && s_fail) atomicOr(a.err, 1u);
+}
+
+// Forward / backward-data convolution over a halo: one CTA = two 8x16-pixel
+// tiles stacked vertically (8 x 32 pixels, two 128-row accumulators in TMEM).
+// Per 32-channel chunk ONE TMA box of the tiles and their one-pixel halo
+// (32 ch x 10 x 34 pixels, 64-byte swizzle: 340 rows of 64 B) is loaded, and
+// the nine taps are nine descriptor start offsets into it: tap (ky, kx) of
+// tile m reads rows (m*16 + py + ky) * 10 + kx + px, i.e. 8-row groups one
+// halo row (640 B) apart, K-major within each 64-byte row.  Each weight tile
+// (one tap, one chunk) feeds both accumulators.  Activation bytes per pixel
+// and chunk fall from 9 x 64 B to 340 x 64 / 256 B, weight bytes by half.
+constexpr int kHX = 8, kHY = 16, kHMT = 2;                      // tile, tiles per CTA
+constexpr int kHaloW = kHX + 2, kHaloH = kHMT * kHY + 2;
+constexpr uint32_t kHaloBytes = kHaloW * kHaloH * 64;            // 21,760
+constexpr uint32_t kHaloStride = (kHaloBytes + 1023) / 1024 * 1024;
+constexpr uint32_t kHaloRowBytes = kHaloW * 64;                  // 640: stride of 8-row groups
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_conv_halo(const __grid_constant__ CUtensorMap src0, const __grid_constant__ CUtensorMap src1,
+                const __grid_constant__ CUtensorMap wmap, ConvArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = align1k(smem_raw);
+    uint8_t* As = smem;                              // two halo buffers (double-buffered over chunks)
+    uint8_t* Bs = smem + 2 * kHaloStride;            // weight stages
+    uint64_t* a_full = reinterpret_cast<uint64_t*>(Bs + a.stages * a.b_bytes);
+    uint64_t* a_empty = a_full + 2;
+    uint64_t* b_full = a_empty + 2;
+    uint64_t* b_empty = b_full + a.stages;
+    uint64_t* done = b_empty + a.stages;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+    __shared__ uint32_t s_fail;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int per_img = a.tiles_x * a.tiles_y;
+    const int n = blockIdx.x / per_img, rem = blockIdx.x % per_img;
+    const int x0 = (rem % a.tiles_x) * kHX, y0 = (rem / a.tiles_x) * (kHMT * kHY);
+    const int nch = a.chunks0 + a.chunks1;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2; ++s) {
+            tc::mbar_init(&a_full[s], 1);
+            tc::mbar_init(&a_empty[s], 1);
+        }
+        for (int s = 0; s < a.stages; ++s) {
+            tc::mbar_init(&b_full[s], 1);
+            tc::mbar_init(&b_empty[s], 1);
+        }
+        tc::mbar_init(done, 1);
+        tc::fence_mbar_init();
+        s_fail = 0;
+    }
+    if (warp == 5) {
+        tc::tmem_alloc(tslot, a.tmem_cols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    int issued_a = 0, issued_b = 0;  // halo and weight loads issued by the producer (warp 4, lane 0)
+    if (warp == 4) {
+        if (lane == 0) {
+            tc::tma_prefetch(&src0);
+            if (a.chunks1) tc::tma_prefetch(&src1);
+            tc::tma_prefetch(&wmap);
+            const uint32_t wbytes = a.N * 64;
+            bool stop = false;
+            for (int c = 0; c < nch && !stop; ++c) {
+                const int hb = c & 1;
+                if (c >= 2 && !tc::mbar_wait(&a_empty[hb], ((c >> 1) - 1) & 1, a.wait_cycles)) {
+                    s_fail = 1;
+                    break;
+                }
+                issued_a = c + 1;
+                tc::mbar_expect_tx(&a_full[hb], kHaloBytes);
+                if (c < a.chunks0)
+                    tc::tma_load_4d(As + hb * kHaloStride, &src0, &a_full[hb], c * kChunk, x0 - 1, y0 - 1, n);
+                else
+                    tc::tma_load_4d(As + hb * kHaloStride, &src1, &a_full[hb], (c - a.chunks0) * kChunk, x0 - 1,
+                                    y0 - 1, n);
+                for (int t = 0; t < 9; ++t) {
+                    const int i = c * 9 + t, s = i % a.stages;
+                    if (i >= a.stages && !tc::mbar_wait(&b_empty[s], ((i / a.stages) - 1) & 1, a.wait_cycles)) {
+                        s_fail = 1;
+                        stop = true;
+                        break;
+                    }
+                    issued_b = i + 1;
+                    tc::mbar_expect_tx(&b_full[s], wbytes);
+                    tc::tma_load_3d(Bs + s * a.b_bytes, &wmap, &b_full[s], c * kChunk, 0, t);
+                }
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, a.N, 0, 0);
+            bool ok = true;
+            for (int c = 0; c < nch && ok; ++c) {
+                const int hb = c & 1;
+                if (!tc::mbar_wait(&a_full[hb], (c >> 1) & 1, a.wait_cycles)) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t ab = tc::smem_u32(As + hb * kHaloStride);
+                for (int t = 0; t < 9; ++t) {
+                    const int i = c * 9 + t, s = i % a.stages;
+                    if (!tc::mbar_wait(&b_full[s], (i / a.stages) & 1, a.wait_cycles)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const int ky = t / 3, kx = t % 3;
+                    const uint32_t bb = tc::smem_u32(Bs + s * a.b_bytes);
+#pragma unroll
+                    for (int m = 0; m < kHMT; ++m)
+#pragma unroll
+                        for (int k = 0; k < 2; ++k) {
+                            const uint32_t aa = ab + (uint32_t)(m * kHY + ky) * kHaloRowBytes + kx * 64 + 32 * k;
+                            tc::mma_bf16(tmem + (uint32_t)(m * a.N), tc::smem_desc(aa, 16, kHaloRowBytes, tc::kSwizzle64B),
+                                         tc::smem_desc(bb + 32 * k, 16, 512, tc::kSwizzle64B), idesc, (c | t | k) != 0);
+                        }
+                    tc::mma_commit(&b_empty[s]);
+                }
+                if (ok) tc::mma_commit(&a_empty[hb]);
+            }
+            if (!ok) s_fail = 1;
+            tc::mma_commit(done);
+        }
+    } else {
+        bool ok = tc::mbar_wait(done, 0, a.wait_cycles);
+        ok = __all_sync(0xffffffffu, ok);
+        tc::fence_after_sync();
+        if (ok) {
+            const int r = warp * 32 + lane;
+            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+            for (int m = 0; m < kHMT; ++m) {
+                const int x = x0 + (r & (kHX - 1)), y = y0 + m * kHY + r / kHX;
+                const bool inb = x < a.W && y < a.H;
+                const size_t pix = ((size_t)n * a.H + y) * a.W + x;
+                for (int col = 0; col < a.N; col += 16) {
+                    uint32_t v[16];
+                    __syncwarp();
+                    tc::tmem_ld16(trow + (uint32_t)(m * a.N + col), v);
+                    tc::tmem_wait_ld();
+                    float f[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) f[j] = __uint_as_float(v[j]);
+                    if (!inb) continue;
+                    if (a.mode == EPI_RELU_BF16) {
+                        if (col < a.n_store) {
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) f[j] = fmaxf(f[j] + a.bias[col + j], 0.0f);
+                            store16_bf16(reinterpret_cast<bf16*>(a.out0) + pix * a.och0 + col, f);
+                        }
+                    } else if (a.mode == EPI_LINEAR_F32) {
+                        if (col == 0) {
+                            const __nv_bfloat162 r01 = *reinterpret_cast<const __nv_bfloat162*>(a.resid + pix * 32);
+                            const float r2 = __bfloat162float(a.resid[pix * 32 + 2]);
+                            reinterpret_cast<float4*>(a.out0)[pix] =
+                                make_float4((f[0] + a.bias[0]) + __low2float(r01), (f[1] + a.bias[1]) + __high2float(r01),
+                                            (f[2] + a.bias[2]) + r2, 0.0f);
+                        }
+                    } else {
+                        const bool hi = col >= a.och0;
+                        const int och = hi ? a.och1 : a.och0, lc = hi ? col - a.och0 : col;
+                        const bf16* mk = hi ? a.mask1 : a.mask0;
+                        if (mk) {
+                            float mv[16];
+                            load16_bf16(mk + pix * och + lc, mv);
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) f[j] = mv[j] > 0.0f ? f[j] : 0.0f;
+                        }
+                        store16_bf16(reinterpret_cast<bf16*>(hi ? a.out1 : a.out0) + pix * och + lc, f);
+                    }
+                }
+            }
+        } else if (lane == 0) {
+            s_fail = 1;
+        }
+    }
+    // drain: the producer's newest halo and weight loads, the MMA issuer's `done`
+    if (warp == 4 && lane == 0) {
+        for (int c = issued_a > 2 ? issued_a - 2 : 0; c < issued_a; ++c)
+            if (!tc::mbar_wait(&a_full[c & 1], (c >> 1) & 1)) s_fail = 1;
+        for (int i = issued_b > a.stages ? issued_b - a.stages : 0; i < issued_b; ++i)
+            if (!tc::mbar_wait(&b_full[i % a.stages], (i / a.stages) & 1)) s_fail = 1;
+    } else if (warp == 5 && lane == 0) {
+        if (!tc::mbar_wait(done, 0)) s_fail = 1;
+    }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 5) {
@@ -710,6 +909,23 @@ hx_status make_act_map(CUtensorMap* m, const bf16* p, int C, int W, int H, int n
     }
     return HX_OK;
 }
+// The same tensor for k_conv_halo: box (32, 10, 34, 1) — two 8x16 tiles and
+// their one-pixel halo; out-of-range pixels read as zero.
+hx_status make_halo_map(CUtensorMap* m, const bf16* p, int C, int W, int H, int n) {
+    HX_TRY(get_encode());
+    cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)n};
+    cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)C * 2 * W, (cuuint64_t)C * 2 * W * H};
+    cuuint32_t box[4] = {kChunk, kHaloW, kHaloH, 1};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)p, dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        hx_set_error("cuTensorMapEncodeTiled (halo C=%d W=%d H=%d n=%d) failed: %d", C, W, H, n, (int)r);
+        return HX_ERR_DEVICE;
+    }
+    return HX_OK;
+}
 // Weights [9][rows][K] BF16: 3-D map (K, rows, 9), box (32, rows, 1).
 hx_status make_w_map(CUtensorMap* m, const bf16* p, int K, int rows) {
     HX_TRY(get_encode());
@@ -770,6 +986,7 @@ struct Plan {
     bf16* t[NT] = {};
     bf16* g[NT] = {};
     CUtensorMap tm[NT], gm[NT];
+    CUtensorMap hm[NT], hgm[NT];  // halo boxes of the same tensors (k_conv_halo)
     float4* y = nullptr;
     float* partial = nullptr;
     size_t partial_bytes = 0;
@@ -827,10 +1044,12 @@ hx_status build_plan(hx_denoiser* dn, Plan* p, int n, int H, int W, bool train) 
         if (i != GYT) {
             HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->t[i], bytes));
             HX_TRY(make_act_map(&p->tm[i], p->t[i], C, w, h, n));
+            HX_TRY(make_halo_map(&p->hm[i], p->t[i], C, w, h, n));
         }
         if (train && i != X) {
             HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->g[i], bytes));
             HX_TRY(make_act_map(&p->gm[i], p->g[i], C, w, h, n));
+            HX_TRY(make_halo_map(&p->hgm[i], p->g[i], C, w, h, n));
         }
     }
     HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->y, (size_t)n * H * W * sizeof(float4)));
@@ -918,15 +1137,18 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
     a.W = W;
     a.H = H;
     a.nimg = p->n;
-    a.tiles_x = (W + kBX - 1) / kBX;
-    a.tiles_y = (H + kBY - 1) / kBY;
+    const bool halo = kConvHalo;
+    a.tiles_x = halo ? (W + kHX - 1) / kHX : (W + kBX - 1) / kBX;
+    a.tiles_y = halo ? (H + kHMT * kHY - 1) / (kHMT * kHY) : (H + kBY - 1) / kBY;
     a.stages = kConvStages;
     a.err = dn->err;
     a.wait_cycles = dn->wait_cycles;
     const CUtensorMap *m0, *m1, *wm;
+    const CUtensorMap* act = halo ? p->hm : p->tm;
+    const CUtensorMap* gact = halo ? p->hgm : p->gm;
     if (!dgrad) {
-        m0 = &p->tm[S.src0];
-        m1 = S.src1 >= 0 ? &p->tm[S.src1] : m0;
+        m0 = &act[S.src0];
+        m1 = S.src1 >= 0 ? &act[S.src1] : m0;
         wm = &L.wf_map;
         a.chunks0 = kTensors[S.src0].C / kChunk;
         a.chunks1 = S.src1 >= 0 ? kTensors[S.src1].C / kChunk : 0;
@@ -945,7 +1167,7 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
         }
     } else {
         const int gout = S.out >= 0 ? S.out : GYT;
-        m0 = &p->gm[gout];
+        m0 = &gact[gout];
         m1 = m0;
         wm = &L.wd_map;
         a.chunks0 = L.cd / kChunk;
@@ -964,11 +1186,18 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
     }
     HX_CHECK_ARG(a.N % 16 == 0 && a.N >= 16 && a.N <= 256, "conv N=%d out of range", a.N);
     a.b_bytes = (uint32_t)round_up(a.N * 64, 1024);
-    a.tmem_cols = pow2_cols(a.N);
-    const size_t smem = conv_smem(a.stages, a.b_bytes);
-    HX_CUDA(cudaFuncSetAttribute(k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = a.tiles_x * a.tiles_y * p->n;
-    k_conv<<<grid, kThreads, smem, ctx->stream>>>(*m0, *m1, *wm, a);
+    if (halo) {
+        a.tmem_cols = pow2_cols(kHMT * a.N);
+        const size_t smem = 1024 + 2 * (size_t)kHaloStride + a.stages * (size_t)a.b_bytes + 256;
+        HX_CUDA(cudaFuncSetAttribute(k_conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_conv_halo<<<grid, kThreads, smem, ctx->stream>>>(*m0, *m1, *wm, a);
+    } else {
+        a.tmem_cols = pow2_cols(a.N);
+        const size_t smem = conv_smem(a.stages, a.b_bytes);
+        HX_CUDA(cudaFuncSetAttribute(k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_conv<<<grid, kThreads, smem, ctx->stream>>>(*m0, *m1, *wm, a);
+    }
     HX_CUDA(cudaGetLastError());
     return HX_OK;
 }
