@@ -279,13 +279,14 @@ constexpr uint32_t kHaloBytes = kHaloW * kHaloH * 64;            // 21,760
 constexpr uint32_t kHaloStride = (kHaloBytes + 1023) / 1024 * 1024;
 constexpr uint32_t kHaloRowBytes = kHaloW * 64;                  // 640: stride of 8-row groups
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 6)
     k_conv_halo(const __grid_constant__ CUtensorMap src0, const __grid_constant__ CUtensorMap src1,
                 const __grid_constant__ CUtensorMap wmap, ConvArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = align1k(smem_raw);
-    uint8_t* As = smem;                              // two halo buffers (double-buffered over chunks)
-    uint8_t* Bs = smem + 2 * kHaloStride;            // weight stages
+    const int nch = a.chunks0 + a.chunks1;
+    uint8_t* As = smem;                              // halo buffers: two (double-buffered over chunks), one
+    uint8_t* Bs = smem + (nch > 1 ? 2 : 1) * kHaloStride;  // for a single chunk; then the weight stages
     uint64_t* a_full = reinterpret_cast<uint64_t*>(Bs + a.stages * a.b_bytes);
     uint64_t* a_empty = a_full + 2;
     uint64_t* b_full = a_empty + 2;
@@ -298,7 +299,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int per_img = a.tiles_x * a.tiles_y;
     const int n = blockIdx.x / per_img, rem = blockIdx.x % per_img;
     const int x0 = (rem % a.tiles_x) * kHX, y0 = (rem / a.tiles_x) * (kHMT * kHY);
-    const int nch = a.chunks0 + a.chunks1;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < 2; ++s) {
@@ -616,31 +616,54 @@ __global__ void k_wgrad_reduce(const float* __restrict__ partial, int splits, in
     }
 }
 
-// Per-channel sums of a [P][C] BF16 tensor in two fixed-order passes.
-constexpr int kColBlocks = 128;
-__global__ void k_colsum_partial(const bf16* __restrict__ g, size_t P, int C, float* __restrict__ part) {
-    __shared__ float acc[256];
-    const int groups = blockDim.x / C;  // pixel lanes per block
-    const int c = threadIdx.x % C, lanep = threadIdx.x / C;
+// Per-channel sums of a [P][C] BF16 tensor (C a multiple of 8, at most 128) in
+// two fixed-order passes: each of kColBlocks blocks sums its contiguous pixel
+// range, every thread 8 channels of a pixel per 16-byte load, the block's
+// lanes combined in lane order; then one block per channel sums the blocks'
+// partials (fixed per-thread subsets, a fixed-order tree).
+constexpr int kColBlocks = 1024, kColThreads = 256;
+__global__ void __launch_bounds__(kColThreads) k_colsum_partial(const bf16* __restrict__ g, size_t P, int C,
+                                                                float* __restrict__ part) {
+    __shared__ float acc[kColThreads][8];
+    const int ncg = C / 8;                  // 8-channel groups of a pixel
+    const int lanes = kColThreads / ncg;    // pixel lanes of the block
+    const int cg = threadIdx.x % ncg, lanep = threadIdx.x / ncg;
     const size_t p0 = P * blockIdx.x / gridDim.x, p1 = P * (blockIdx.x + 1) / gridDim.x;
-    float s = 0.0f;
-    if (lanep < groups)
-        for (size_t p = p0 + lanep; p < p1; p += groups) s += __bfloat162float(g[p * C + c]);
-    acc[threadIdx.x] = s;
+    float s[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (lanep < lanes)
+        for (size_t p = p0 + lanep; p < p1; p += lanes) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(g + p * C) + cg);
+            const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&w[j]);
+                s[2 * j] += __low2float(h);
+                s[2 * j + 1] += __high2float(h);
+            }
+        }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[threadIdx.x][j] = s[j];
     __syncthreads();
     if (threadIdx.x < C) {
+        const int c = threadIdx.x;
         float t = 0.0f;
-        for (int k = 0; k < groups; ++k) t += acc[k * C + threadIdx.x];
-        part[(size_t)blockIdx.x * C + threadIdx.x] = t;
+        for (int k = 0; k < lanes; ++k) t += acc[k * ncg + c / 8][c % 8];
+        part[(size_t)blockIdx.x * C + c] = t;
     }
 }
-__global__ void k_colsum_final(const float* __restrict__ part, int blocks, int C, int cout, float scale,
-                               float* __restrict__ out) {
-    const int c = threadIdx.x;
-    if (c >= cout) return;
+__global__ void __launch_bounds__(kColThreads) k_colsum_final(const float* __restrict__ part, int blocks, int C,
+                                                              float scale, float* __restrict__ out) {
+    __shared__ float red[kColThreads];
+    const int c = blockIdx.x;
     float t = 0.0f;
-    for (int k = 0; k < blocks; ++k) t += part[(size_t)k * C + c];
-    out[c] = t * scale;
+    for (int k = threadIdx.x; k < blocks; k += kColThreads) t += part[(size_t)k * C + c];
+    red[threadIdx.x] = t;
+    __syncthreads();
+    for (int h = kColThreads / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = red[0] * scale;
 }
 
 // 8-channel vector helpers
@@ -1189,7 +1212,9 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
     const int grid = a.tiles_x * a.tiles_y * p->n;
     if (halo) {
         a.tmem_cols = pow2_cols(kHMT * a.N);
-        const size_t smem = 1024 + 2 * (size_t)kHaloStride + a.stages * (size_t)a.b_bytes + 256;
+        // one halo buffer for a single 32-channel chunk (more resident CTAs for the 32-channel layers)
+        const int nhalo = a.chunks0 + a.chunks1 > 1 ? 2 : 1;
+        const size_t smem = 1024 + nhalo * (size_t)kHaloStride + a.stages * (size_t)a.b_bytes + 256;
         HX_CUDA(cudaFuncSetAttribute(k_conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_conv_halo<<<grid, kThreads, smem, ctx->stream>>>(*m0, *m1, *wm, a);
     } else {
@@ -1244,8 +1269,8 @@ hx_status launch_wgrad(hx_denoiser* dn, Plan* p, int l, float scale) {
     const int C = kTensors[gout].C;
     const int lev_o = S.out >= 0 ? kTensors[S.out].level : 0;
     const size_t P = (size_t)p->n * level_dim(p->H, lev_o) * level_dim(p->W, lev_o);
-    k_colsum_partial<<<kColBlocks, 256, 0, ctx->stream>>>(p->g[gout], P, C, p->colpart);
-    k_colsum_final<<<1, 128, 0, ctx->stream>>>(p->colpart, kColBlocks, C, L.cout, scale, gw + total);
+    k_colsum_partial<<<kColBlocks, kColThreads, 0, ctx->stream>>>(p->g[gout], P, C, p->colpart);
+    k_colsum_final<<<L.cout, kColThreads, 0, ctx->stream>>>(p->colpart, kColBlocks, C, scale, gw + total);
     HX_CUDA(cudaGetLastError());
     return HX_OK;
 }
