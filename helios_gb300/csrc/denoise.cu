@@ -603,6 +603,158 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (threadIdx.x == 0 && s_fail) atomicOr(a.err, 1u);
 }
 
+// Backward-weights over a halo: CTA (split, 128-input-channel block, group of
+// consecutive taps) walks the split's 8x16-pixel tiles; per tile it loads each
+// input chunk ONCE as a tile + one-pixel-halo box (32 ch x 10 x 18, 64-byte
+// swizzle) and the output gradient once (32 ch x 8 x 16), and every tap of
+// the group reads its shifted input view from the halo box by descriptor
+// offset (pixel rows 640 B apart) into its own TMEM accumulator D_t[ci][co]
+// (the group's taps x N columns).  Both operands MN-major, as in k_wgrad.
+constexpr uint32_t kWHaloBytes = kHaloW * (kHY + 2) * 64;                  // 11,520
+constexpr uint32_t kWHaloStride = (kWHaloBytes + 1023) / 1024 * 1024;      // 12 KB
+
+struct WgradHaloArgs {
+    int W, H, tiles_x, tiles_y, ntiles;
+    int chunks0, chunks1, gchunks;
+    int splits, stages, taps;  // taps per CTA (grid.z groups)
+    uint32_t a_bytes, b_bytes, tmem_cols;
+    float* partial;            // [splits][9][N][cin]
+    int cin;
+    uint32_t* err;
+    long long wait_cycles;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_wgrad_halo(const __grid_constant__ CUtensorMap src0, const __grid_constant__ CUtensorMap src1,
+                 const __grid_constant__ CUtensorMap gmap, WgradHaloArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = align1k(smem_raw);
+    uint8_t* As = smem;
+    uint8_t* Bs = smem + a.stages * a.a_bytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(Bs + a.stages * a.b_bytes);
+    uint64_t* empty = full + a.stages;
+    uint64_t* done = empty + a.stages;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+    __shared__ uint32_t s_fail;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sp = blockIdx.x, mb = blockIdx.y;
+    const int tap0 = blockIdx.z * a.taps, ntap = min(a.taps, 9 - tap0);
+    const int t_begin = (int)((long long)a.ntiles * sp / a.splits);
+    const int t_end = (int)((long long)a.ntiles * (sp + 1) / a.splits);
+    const int iters = t_end - t_begin;
+    const int nch = a.chunks0 + a.chunks1;
+    const int qa = min(4, nch - mb * 4);
+    const int N = 32 * a.gchunks;
+    const int per_img = a.tiles_x * a.tiles_y;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < a.stages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(done, 1);
+        tc::fence_mbar_init();
+        s_fail = 0;
+    }
+    if (warp == 5) {
+        tc::tmem_alloc(tslot, a.tmem_cols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    int issued = 0;  // stages loaded by the producer (warp 4, lane 0)
+    if (warp == 4) {
+        if (lane == 0) {
+            tc::tma_prefetch(&src0);
+            if (a.chunks1) tc::tma_prefetch(&src1);
+            tc::tma_prefetch(&gmap);
+            const uint32_t bytes = (uint32_t)qa * kWHaloBytes + (uint32_t)a.gchunks * kChunkBytes;
+            for (int i = 0; i < iters; ++i) {
+                const int s = i % a.stages;
+                if (i >= a.stages && !tc::mbar_wait(&empty[s], ((i / a.stages) - 1) & 1, a.wait_cycles)) {
+                    s_fail = 1;
+                    break;
+                }
+                issued = i + 1;
+                const int t = t_begin + i, n = t / per_img, rem = t % per_img;
+                const int x0 = (rem % a.tiles_x) * kHX, y0 = (rem / a.tiles_x) * kHY;
+                tc::mbar_expect_tx(&full[s], bytes);
+                for (int q = 0; q < qa; ++q) {
+                    const int c = mb * 4 + q;
+                    uint8_t* dst = As + s * a.a_bytes + q * kWHaloStride;
+                    if (c < a.chunks0)
+                        tc::tma_load_4d(dst, &src0, &full[s], c * kChunk, x0 - 1, y0 - 1, n);
+                    else
+                        tc::tma_load_4d(dst, &src1, &full[s], (c - a.chunks0) * kChunk, x0 - 1, y0 - 1, n);
+                }
+                for (int q = 0; q < a.gchunks; ++q)
+                    tc::tma_load_4d(Bs + s * a.b_bytes + q * kChunkBytes, &gmap, &full[s], q * kChunk, x0, y0, n);
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, N, 1, 1);
+            for (int i = 0; i < iters; ++i) {
+                const int s = i % a.stages;
+                if (!tc::mbar_wait(&full[s], (i / a.stages) & 1, a.wait_cycles)) {
+                    s_fail = 1;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t ab = tc::smem_u32(As + s * a.a_bytes), bb = tc::smem_u32(Bs + s * a.b_bytes);
+                for (int j = 0; j < ntap; ++j) {
+                    const int tap = tap0 + j, ky = tap / 3, kx = tap % 3;
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)  // 16 pixels = tile rows 2k, 2k + 1
+                        tc::mma_bf16(tmem + (uint32_t)(j * N),
+                                     tc::smem_desc(ab + (uint32_t)((2 * k + ky) * kHaloW + kx) * 64, kWHaloStride,
+                                                   kHaloRowBytes, tc::kSwizzle64B),
+                                     tc::smem_desc(bb + 1024 * k, kChunkBytes, 512, tc::kSwizzle64B), idesc,
+                                     (i | k) != 0);
+                }
+                tc::mma_commit(&empty[s]);
+            }
+            tc::mma_commit(done);
+        }
+    } else {
+        bool ok = tc::mbar_wait(done, 0, a.wait_cycles);
+        ok = __all_sync(0xffffffffu, ok);
+        tc::fence_after_sync();
+        if (ok) {
+            const int ci = mb * 128 + warp * 32 + lane;
+            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+            for (int j = 0; j < ntap; ++j) {
+                float* dst = a.partial + ((size_t)sp * 9 + tap0 + j) * N * a.cin;
+                for (int col = 0; col < N; col += 16) {
+                    uint32_t v[16];
+                    __syncwarp();
+                    tc::tmem_ld16(trow + (uint32_t)(j * N + col), v);
+                    tc::tmem_wait_ld();
+                    if (ci < a.cin) {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e)
+                            dst[(size_t)(col + e) * a.cin + ci] = iters > 0 ? __uint_as_float(v[e]) : 0.0f;
+                    }
+                }
+            }
+        } else if (lane == 0) {
+            s_fail = 1;
+        }
+    }
+    drain(warp, lane, issued, a.stages, full, done, &s_fail);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 5) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, a.tmem_cols);
+    }
+    if (threadIdx.x == 0 && s_fail) atomicOr(a.err, 1u);
+}
+
 // grad[tap][co][ci] = scale * sum_split partial[split][tap][co][ci], co < cout.
 __global__ void k_wgrad_reduce(const float* __restrict__ partial, int splits, int N, int cout, int cin, float scale,
                                float* __restrict__ grad) {
@@ -932,13 +1084,16 @@ hx_status make_act_map(CUtensorMap* m, const bf16* p, int C, int W, int H, int n
     }
     return HX_OK;
 }
-// The same tensor for k_conv_halo: box (32, 10, 34, 1) — two 8x16 tiles and
-// their one-pixel halo; out-of-range pixels read as zero.
-hx_status make_halo_map(CUtensorMap* m, const bf16* p, int C, int W, int H, int n) {
+// The same tensor with a box of bx x by pixels: (10, 34) for k_conv_halo (two
+// 8x16 tiles and their one-pixel halo), (10, 18) and (8, 16) for
+// k_wgrad_halo's input halo and output-gradient tile; out-of-range pixels
+// read as zero.
+hx_status make_halo_map(CUtensorMap* m, const bf16* p, int C, int W, int H, int n, int bx = kHaloW,
+                        int by = kHaloH) {
     HX_TRY(get_encode());
     cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)n};
     cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)C * 2 * W, (cuuint64_t)C * 2 * W * H};
-    cuuint32_t box[4] = {kChunk, kHaloW, kHaloH, 1};
+    cuuint32_t box[4] = {kChunk, (cuuint32_t)bx, (cuuint32_t)by, 1};
     cuuint32_t es[4] = {1, 1, 1, 1};
     CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)p, dims, strides, box, es,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1003,6 +1158,29 @@ struct Layer {
     CUtensorMap wf_map, wd_map;
 };
 
+// Work split of a layer's backward-weights pass (k_wgrad_halo): 8x16-pixel
+// tiles; taps per CTA so the taps' accumulators (taps x N columns) fit 256
+// TMEM columns, spread evenly over the groups; pixel-tile splits for about
+// two CTAs per SM.
+struct WgradPlan {
+    int tiles_x, tiles_y, ntiles, mblocks, taps, groups, splits;
+};
+WgradPlan wgrad_plan(const Layer& L, int W, int H, int n, int sms) {
+    WgradPlan w{};
+    w.tiles_x = (W + kHX - 1) / kHX;
+    w.tiles_y = (H + kHY - 1) / kHY;
+    w.ntiles = w.tiles_x * w.tiles_y * n;
+    w.mblocks = (L.cin + 127) / 128;
+    const int fit = std::max(1, std::min(9, 256 / L.cd));
+    w.groups = (9 + fit - 1) / fit;
+    w.taps = (9 + w.groups - 1) / w.groups;
+    w.groups = (9 + w.taps - 1) / w.taps;
+    const int per = w.mblocks * w.groups;
+    w.splits = std::max(1, std::min(w.ntiles, (2 * sms + per - 1) / per));
+    return w;
+}
+
+
 struct Plan {
     int n = 0, H = 0, W = 0;  // padded network size (multiple of 16)
     bool train = false;
@@ -1010,6 +1188,7 @@ struct Plan {
     bf16* g[NT] = {};
     CUtensorMap tm[NT], gm[NT];
     CUtensorMap hm[NT], hgm[NT];  // halo boxes of the same tensors (k_conv_halo)
+    CUtensorMap wxm[NT], wgm[NT]; // k_wgrad_halo: input halo (10 x 18), output-gradient tile (8 x 16)
     float4* y = nullptr;
     float* partial = nullptr;
     size_t partial_bytes = 0;
@@ -1068,11 +1247,13 @@ hx_status build_plan(hx_denoiser* dn, Plan* p, int n, int H, int W, bool train) 
             HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->t[i], bytes));
             HX_TRY(make_act_map(&p->tm[i], p->t[i], C, w, h, n));
             HX_TRY(make_halo_map(&p->hm[i], p->t[i], C, w, h, n));
+            if (train) HX_TRY(make_halo_map(&p->wxm[i], p->t[i], C, w, h, n, kHaloW, kHY + 2));
         }
         if (train && i != X) {
             HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->g[i], bytes));
             HX_TRY(make_act_map(&p->gm[i], p->g[i], C, w, h, n));
             HX_TRY(make_halo_map(&p->hgm[i], p->g[i], C, w, h, n));
+            HX_TRY(make_halo_map(&p->wgm[i], p->g[i], C, w, h, n, kHX, kHY));
         }
     }
     HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->y, (size_t)n * H * W * sizeof(float4)));
@@ -1081,10 +1262,8 @@ hx_status build_plan(hx_denoiser* dn, Plan* p, int n, int H, int W, bool train) 
         for (int l = 0; l < kNumLayers; ++l) {
             const Layer& L = dn->layers[l];
             const int lev = kTensors[kLayers[l].src0].level;
-            const int ntiles = n * ((level_dim(W, lev) + kBX - 1) / kBX) * ((level_dim(H, lev) + kBY - 1) / kBY);
-            const int mblocks = (L.cin + 127) / 128;
-            const int splits = std::max(1, std::min(ntiles, (2 * ctx->num_sms + 9 * mblocks - 1) / (9 * mblocks)));
-            mx = std::max(mx, (size_t)splits * 9 * L.cd * L.cin * sizeof(float));
+            const WgradPlan wp = wgrad_plan(L, level_dim(W, lev), level_dim(H, lev), n, ctx->num_sms);
+            mx = std::max(mx, (size_t)wp.splits * 9 * L.cd * L.cin * sizeof(float));
         }
         p->partial_bytes = mx;
         HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->partial, mx));
@@ -1234,31 +1413,37 @@ hx_status launch_wgrad(hx_denoiser* dn, Plan* p, int l, float scale) {
     const int lev = kTensors[S.src0].level;
     const int H = level_dim(p->H, lev), W = level_dim(p->W, lev);
     const int gout = S.out >= 0 ? S.out : GYT;
-    WgradArgs a{};
+    const WgradPlan wp = wgrad_plan(L, W, H, p->n, ctx->num_sms);
+    WgradHaloArgs a{};
     a.W = W;
     a.H = H;
-    a.tiles_x = (W + kBX - 1) / kBX;
-    a.tiles_y = (H + kBY - 1) / kBY;
-    a.ntiles = a.tiles_x * a.tiles_y * p->n;
+    a.tiles_x = wp.tiles_x;
+    a.tiles_y = wp.tiles_y;
+    a.ntiles = wp.ntiles;
     a.chunks0 = kTensors[S.src0].C / kChunk;
     a.chunks1 = S.src1 >= 0 ? kTensors[S.src1].C / kChunk : 0;
     a.gchunks = L.cd / kChunk;
-    const int mblocks = (L.cin + 127) / 128;
-    a.splits = std::max(1, std::min(a.ntiles, (2 * ctx->num_sms + 9 * mblocks - 1) / (9 * mblocks)));
-    a.stages = kWgradStages;
-    a.a_bytes = 4 * kChunkBytes;
+    a.splits = wp.splits;
+    a.taps = wp.taps;
+    const int qmax = std::min(4, a.chunks0 + a.chunks1);
+    a.a_bytes = (uint32_t)qmax * kWHaloStride;
     a.b_bytes = a.gchunks * kChunkBytes;
-    a.tmem_cols = pow2_cols(L.cd);
+    a.stages = a.a_bytes + a.b_bytes <= 40u * 1024 ? 3 : 2;
+    a.tmem_cols = pow2_cols(wp.taps * L.cd);
     a.partial = p->partial;
     a.cin = L.cin;
     a.err = dn->err;
     a.wait_cycles = dn->wait_cycles;
     HX_CHECK_ARG((size_t)a.splits * 9 * L.cd * L.cin * sizeof(float) <= p->partial_bytes, "wgrad partial overflow");
-    const size_t smem = 1024 + a.stages * (a.a_bytes + a.b_bytes) + 256;
-    HX_CUDA(cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const CUtensorMap* m0 = &p->tm[S.src0];
-    const CUtensorMap* m1 = S.src1 >= 0 ? &p->tm[S.src1] : m0;
-    k_wgrad<<<dim3(a.splits, mblocks, 9), kThreads, smem, ctx->stream>>>(*m0, *m1, p->gm[gout], a);
+    // the MMA's M = 128 input channels reads four chunk slots at kWHaloStride
+    // apart even when a block has fewer chunks: cover the last stage's reach
+    const size_t body = std::max<size_t>((size_t)a.stages * (a.a_bytes + a.b_bytes),
+                                         (size_t)(a.stages - 1) * a.a_bytes + 4 * (size_t)kWHaloStride);
+    const size_t smem = 1024 + body + 256;
+    HX_CUDA(cudaFuncSetAttribute(k_wgrad_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const CUtensorMap* m0 = &p->wxm[S.src0];
+    const CUtensorMap* m1 = S.src1 >= 0 ? &p->wxm[S.src1] : m0;
+    k_wgrad_halo<<<dim3(a.splits, wp.mblocks, wp.groups), kThreads, smem, ctx->stream>>>(*m0, *m1, p->wgm[gout], a);
     HX_CUDA(cudaGetLastError());
     float* gw = dn->grads + L.off;
     const size_t total = (size_t)9 * L.cout * L.cin;
