@@ -784,7 +784,7 @@ def run_denoise(args, dist):
         # plain spp reaching a given error: log-log interpolation of the
         # measured curve, extrapolated past 256 spp with its last slope
         cs = sorted(plain)
-        lx, ly = np.log([float(c) for c in cs]), np.log([plain[c] for c in cs])
+        lx, ly = np.log([float(c) for c in cs]), np.log(np.maximum([plain[c] for c in cs], 1e-30))
 
         def plain_spp_for(err):
             le = np.log(err)
@@ -811,7 +811,7 @@ def run_denoise(args, dist):
     flops = hx.denoiser_conv_flops_per_pixel() * W * ((H + 15) // 16 * 16)
     infer_ms = statistics.median(e["infer_ms"] for e in evals)
     out["eval"] = evals
-    out["roofline"] = {"bound": "tensor", "kernel": "k_conv (forward, all 13 layers)",
+    out["roofline"] = {"bound": "tensor", "kernel": "k_conv_halo (forward, all 13 layers)",
                        "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                        "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
                        "flops_per_1080p_inference": flops, "peak_source": peaks["source"] + ", bf16 burst"}

@@ -10,16 +10,20 @@
 // accumulator in TMEM and BF16 operands staged in shared memory by TMA:
 //
 //   forward / backward-data   D[128 px][N ch] += A[128 px][32 ch] * B[N][32]^T
-//       A: a 16x8-pixel tile of an NHWC activation tensor shifted by the tap,
-//          loaded as one 4-D TMA box whose out-of-range pixels read as zero
-//          (that is the convolution's zero padding); K-major, 64-byte swizzle.
-//       B: the tap's weights [N][32 ch], K-major.  Backward-data runs the
-//          same kernel on the output gradient with the weights transposed and
-//          the taps mirrored.
+//       A: an 8x16-pixel tile of an NHWC activation tensor shifted by the
+//          tap — a descriptor offset into ONE 4-D TMA box per 32-channel
+//          chunk that holds two tiles and their one-pixel halo; out-of-range
+//          pixels read as zero (that is the convolution's zero padding);
+//          K-major, 64-byte swizzle (k_conv_halo).
+//       B: the tap's weights [N][32 ch], K-major, shared by the two tiles'
+//          accumulators.  Backward-data runs the same kernel on the output
+//          gradient with the weights transposed and the taps mirrored.
 //   backward-weights          D[128 ci][N co] += X[px][ci]^T * G[px][co]
-//       both operands MN-major straight from the same NHWC boxes; each CTA
-//       reduces over a split of the pixel tiles into TMEM and writes a
-//       partial, and a second kernel sums the partials in a fixed order.
+//       both operands MN-major straight from NHWC boxes — X as a halo box,
+//          each tap of a group of taps reading its shifted view by
+//          descriptor offset into its own accumulator (k_wgrad_halo); each
+//          CTA reduces over a split of the pixel tiles and writes partials,
+//          and a second kernel sums the partials in a fixed order.
 //
 // One CTA = 6 warps: warps 0-3 drain TMEM (tcgen05.ld, one TMEM lane quarter
 // each) and run the fused epilogue (bias, ReLU, ReLU-mask of the gradient,
@@ -48,13 +52,10 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-constexpr int kBX = 16, kBY = 8;          // pixel tile = 128 rows of the MMA
 constexpr int kChunk = 32;                // channels per K step (64-byte rows)
 constexpr int kChunkBytes = 128 * 64;     // one 128-row x 64-byte operand tile
 constexpr int kThreads = 192;
 constexpr int kConvStages = 4;
-constexpr bool kConvHalo = true;          // forward / backward-data through k_conv_halo
-constexpr int kWgradStages = 3;
 
 enum Epi : int { EPI_RELU_BF16 = 0, EPI_LINEAR_F32 = 1, EPI_DGRAD = 2 };
 
@@ -119,149 +120,6 @@ __device__ __forceinline__ void drain(int warp, int lane, int issued, int stages
     } else if (warp == 5 && lane == 0) {
         if (!tc::mbar_wait(done, 0)) *s_fail = 1;
     }
-}
-
-// Forward / backward-data convolution, one 16x8-pixel tile per CTA.
-__global__ void __launch_bounds__(kThreads, 1)
-    k_conv(const __grid_constant__ CUtensorMap src0, const __grid_constant__ CUtensorMap src1,
-           const __grid_constant__ CUtensorMap wmap, ConvArgs a) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = align1k(smem_raw);
-    uint8_t* As = smem;
-    uint8_t* Bs = smem + a.stages * kChunkBytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(Bs + a.stages * a.b_bytes);
-    uint64_t* empty = full + a.stages;
-    uint64_t* done = empty + a.stages;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
-    __shared__ uint32_t s_fail;
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_img = a.tiles_x * a.tiles_y;
-    const int n = blockIdx.x / per_img, rem = blockIdx.x % per_img;
-    const int x0 = (rem % a.tiles_x) * kBX, y0 = (rem / a.tiles_x) * kBY;
-    const int nch = a.chunks0 + a.chunks1;
-    const int iters = 9 * nch;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < a.stages; ++s) {
-            tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
-        }
-        tc::mbar_init(done, 1);
-        tc::fence_mbar_init();
-        s_fail = 0;
-    }
-    if (warp == 5) {
-        tc::tmem_alloc(tslot, a.tmem_cols);
-        tc::tmem_relinquish();
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tmem = *tslot;
-
-    int issued = 0;  // stages loaded by the producer (warp 4, lane 0)
-    if (warp == 4) {
-        if (lane == 0) {
-            tc::tma_prefetch(&src0);
-            if (a.chunks1) tc::tma_prefetch(&src1);
-            tc::tma_prefetch(&wmap);
-            const uint32_t bytes = kChunkBytes + a.N * 64;
-            for (int i = 0; i < iters; ++i) {
-                const int s = i % a.stages;
-                if (i >= a.stages && !tc::mbar_wait(&empty[s], ((i / a.stages) - 1) & 1, a.wait_cycles)) {
-                    s_fail = 1;
-                    break;
-                }
-                issued = i + 1;
-                const int tap = i / nch, c = i % nch, ky = tap / 3, kx = tap % 3;
-                tc::mbar_expect_tx(&full[s], bytes);
-                if (c < a.chunks0)
-                    tc::tma_load_4d(As + s * kChunkBytes, &src0, &full[s], c * kChunk, x0 + kx - 1, y0 + ky - 1, n);
-                else
-                    tc::tma_load_4d(As + s * kChunkBytes, &src1, &full[s], (c - a.chunks0) * kChunk, x0 + kx - 1,
-                                    y0 + ky - 1, n);
-                tc::tma_load_3d(Bs + s * a.b_bytes, &wmap, &full[s], c * kChunk, 0, tap);
-            }
-        }
-    } else if (warp == 5) {
-        if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16(128, a.N, 0, 0);
-            for (int i = 0; i < iters; ++i) {
-                const int s = i % a.stages;
-                if (!tc::mbar_wait(&full[s], (i / a.stages) & 1, a.wait_cycles)) {
-                    s_fail = 1;
-                    break;
-                }
-                tc::fence_after_sync();
-                const uint32_t ab = tc::smem_u32(As + s * kChunkBytes), bb = tc::smem_u32(Bs + s * a.b_bytes);
-#pragma unroll
-                for (int k = 0; k < 2; ++k)
-                    tc::mma_bf16(tmem, tc::smem_desc(ab + 32 * k, 16, 512, tc::kSwizzle64B),
-                                 tc::smem_desc(bb + 32 * k, 16, 512, tc::kSwizzle64B), idesc, (i | k) != 0);
-                tc::mma_commit(&empty[s]);
-            }
-            tc::mma_commit(done);
-        }
-    } else {
-        bool ok = tc::mbar_wait(done, 0, a.wait_cycles);
-        ok = __all_sync(0xffffffffu, ok);
-        tc::fence_after_sync();
-        if (ok) {
-            const int r = warp * 32 + lane;
-            const int x = x0 + (r & (kBX - 1)), y = y0 + r / kBX;
-            const bool inb = x < a.W && y < a.H;
-            const size_t pix = ((size_t)n * a.H + y) * a.W + x;
-            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-            for (int col = 0; col < a.N; col += 16) {
-                uint32_t v[16];
-                __syncwarp();
-                tc::tmem_ld16(trow + col, v);
-                tc::tmem_wait_ld();
-                float f[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) f[j] = __uint_as_float(v[j]);
-                if (!inb) continue;
-                if (a.mode == EPI_RELU_BF16) {
-                    if (col < a.n_store) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) f[j] = fmaxf(f[j] + a.bias[col + j], 0.0f);
-                        store16_bf16(reinterpret_cast<bf16*>(a.out0) + pix * a.och0 + col, f);
-                    }
-                } else if (a.mode == EPI_LINEAR_F32) {
-                    if (col == 0) {
-                        // residual output: the input's log1p radiance + the predicted correction
-                        const __nv_bfloat162 r01 = *reinterpret_cast<const __nv_bfloat162*>(a.resid + pix * 32);
-                        const float r2 = __bfloat162float(a.resid[pix * 32 + 2]);
-                        reinterpret_cast<float4*>(a.out0)[pix] =
-                            make_float4((f[0] + a.bias[0]) + __low2float(r01), (f[1] + a.bias[1]) + __high2float(r01),
-                                        (f[2] + a.bias[2]) + r2, 0.0f);
-                    }
-                } else {
-                    const bool hi = col >= a.och0;
-                    const int och = hi ? a.och1 : a.och0, lc = hi ? col - a.och0 : col;
-                    const bf16* m = hi ? a.mask1 : a.mask0;
-                    if (m) {
-                        float mv[16];
-                        load16_bf16(m + pix * och + lc, mv);
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) f[j] = mv[j] > 0.0f ? f[j] : 0.0f;
-                    }
-                    store16_bf16(reinterpret_cast<bf16*>(hi ? a.out1 : a.out0) + pix * och + lc, f);
-                }
-            }
-        } else if (lane == 0) {
-            s_fail = 1;
-        }
-    }
-    drain(warp, lane, issued, a.stages, full, done, &s_fail);
-    tc::fence_before_sync();
-    __syncthreads();
-    if (warp == 5) {
-        tc::fence_after_sync();
-        tc::tmem_dealloc(tmem, a.tmem_cols);
-    }
-    if (threadIdx.x == 0 && s_fail) atomicOr(a.err, 1u);
 }
 
 // Forward / backward-data convolution over a halo: one CTA = two 8x16-pixel
@@ -453,147 +311,6 @@ __global__ void __launch_bounds__(kThreads, 6)
     } else if (warp == 5 && lane == 0) {
         if (!tc::mbar_wait(done, 0)) s_fail = 1;
     }
-    tc::fence_before_sync();
-    __syncthreads();
-    if (warp == 5) {
-        tc::fence_after_sync();
-        tc::tmem_dealloc(tmem, a.tmem_cols);
-    }
-    if (threadIdx.x == 0 && s_fail) atomicOr(a.err, 1u);
-}
-
-struct WgradArgs {
-    int W, H, tiles_x, tiles_y, ntiles;
-    int chunks0, chunks1;      // input-activation chunks (M side, 4 per CTA)
-    int gchunks;               // output-gradient chunks (N = 32 * gchunks)
-    int splits, stages;
-    uint32_t a_bytes, b_bytes; // per-stage operand bytes
-    uint32_t tmem_cols;
-    float* partial;            // [splits][9][N][cin]
-    int cin;
-    uint32_t* err;
-    long long wait_cycles;     // budget of each pipeline wait
-};
-
-// Backward-weights: CTA (split, 128-input-channel block, tap) reduces the
-// split's pixel tiles into D[ci][co] in TMEM and writes its partial.
-__global__ void __launch_bounds__(kThreads, 1)
-    k_wgrad(const __grid_constant__ CUtensorMap src0, const __grid_constant__ CUtensorMap src1,
-            const __grid_constant__ CUtensorMap gmap, WgradArgs a) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = align1k(smem_raw);
-    uint8_t* As = smem;
-    uint8_t* Bs = smem + a.stages * a.a_bytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(Bs + a.stages * a.b_bytes);
-    uint64_t* empty = full + a.stages;
-    uint64_t* done = empty + a.stages;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
-    __shared__ uint32_t s_fail;
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sp = blockIdx.x, mb = blockIdx.y, tap = blockIdx.z, ky = tap / 3, kx = tap % 3;
-    const int t_begin = (int)((long long)a.ntiles * sp / a.splits);
-    const int t_end = (int)((long long)a.ntiles * (sp + 1) / a.splits);
-    const int iters = t_end - t_begin;
-    const int nch = a.chunks0 + a.chunks1;
-    const int qa = min(4, nch - mb * 4);
-    const int N = 32 * a.gchunks;
-    const int per_img = a.tiles_x * a.tiles_y;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < a.stages; ++s) {
-            tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
-        }
-        tc::mbar_init(done, 1);
-        tc::fence_mbar_init();
-        s_fail = 0;
-    }
-    if (warp == 5) {
-        tc::tmem_alloc(tslot, a.tmem_cols);
-        tc::tmem_relinquish();
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tmem = *tslot;
-
-    int issued = 0;  // stages loaded by the producer (warp 4, lane 0)
-    if (warp == 4) {
-        if (lane == 0) {
-            tc::tma_prefetch(&src0);
-            if (a.chunks1) tc::tma_prefetch(&src1);
-            tc::tma_prefetch(&gmap);
-            const uint32_t bytes = (uint32_t)(qa + a.gchunks) * kChunkBytes;
-            for (int i = 0; i < iters; ++i) {
-                const int s = i % a.stages;
-                if (i >= a.stages && !tc::mbar_wait(&empty[s], ((i / a.stages) - 1) & 1, a.wait_cycles)) {
-                    s_fail = 1;
-                    break;
-                }
-                issued = i + 1;
-                const int t = t_begin + i, n = t / per_img, rem = t % per_img;
-                const int x0 = (rem % a.tiles_x) * kBX, y0 = (rem / a.tiles_x) * kBY;
-                tc::mbar_expect_tx(&full[s], bytes);
-                for (int q = 0; q < qa; ++q) {
-                    const int c = mb * 4 + q;
-                    if (c < a.chunks0)
-                        tc::tma_load_4d(As + s * a.a_bytes + q * kChunkBytes, &src0, &full[s], c * kChunk,
-                                        x0 + kx - 1, y0 + ky - 1, n);
-                    else
-                        tc::tma_load_4d(As + s * a.a_bytes + q * kChunkBytes, &src1, &full[s],
-                                        (c - a.chunks0) * kChunk, x0 + kx - 1, y0 + ky - 1, n);
-                }
-                for (int q = 0; q < a.gchunks; ++q)
-                    tc::tma_load_4d(Bs + s * a.b_bytes + q * kChunkBytes, &gmap, &full[s], q * kChunk, x0, y0, n);
-            }
-        }
-    } else if (warp == 5) {
-        if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16(128, N, 1, 1);
-            for (int i = 0; i < iters; ++i) {
-                const int s = i % a.stages;
-                if (!tc::mbar_wait(&full[s], (i / a.stages) & 1, a.wait_cycles)) {
-                    s_fail = 1;
-                    break;
-                }
-                tc::fence_after_sync();
-                const uint32_t ab = tc::smem_u32(As + s * a.a_bytes), bb = tc::smem_u32(Bs + s * a.b_bytes);
-#pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    tc::mma_bf16(tmem, tc::smem_desc(ab + 1024 * k, kChunkBytes, 512, tc::kSwizzle64B),
-                                 tc::smem_desc(bb + 1024 * k, kChunkBytes, 512, tc::kSwizzle64B), idesc,
-                                 (i | k) != 0);
-                tc::mma_commit(&empty[s]);
-            }
-            tc::mma_commit(done);
-        }
-    } else {
-        bool ok = tc::mbar_wait(done, 0, a.wait_cycles);
-        ok = __all_sync(0xffffffffu, ok);
-        tc::fence_after_sync();
-        if (ok) {
-            const int ci = mb * 128 + warp * 32 + lane;
-            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-            float* dst = a.partial + ((size_t)sp * 9 + tap) * N * a.cin;
-            for (int col = 0; col < N; col += 16) {
-                uint32_t v[16];
-                __syncwarp();
-                tc::tmem_ld16(trow + col, v);
-                tc::tmem_wait_ld();
-                if (ci < a.cin && iters > 0) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) dst[(size_t)(col + j) * a.cin + ci] = __uint_as_float(v[j]);
-                } else if (ci < a.cin) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) dst[(size_t)(col + j) * a.cin + ci] = 0.0f;
-                }
-            }
-        } else if (lane == 0) {
-            s_fail = 1;
-        }
-    }
-    drain(warp, lane, issued, a.stages, full, done, &s_fail);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 5) {
@@ -1068,23 +785,8 @@ hx_status get_encode() {
     return HX_OK;
 }
 
-// NHWC BF16 activation: 4-D map (C, W, H, n), box (32, 16, 8, 1), 64-byte swizzle.
-hx_status make_act_map(CUtensorMap* m, const bf16* p, int C, int W, int H, int n) {
-    HX_TRY(get_encode());
-    cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)n};
-    cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)C * 2 * W, (cuuint64_t)C * 2 * W * H};
-    cuuint32_t box[4] = {kChunk, kBX, kBY, 1};
-    cuuint32_t es[4] = {1, 1, 1, 1};
-    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)p, dims, strides, box, es,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        hx_set_error("cuTensorMapEncodeTiled (activation C=%d W=%d H=%d n=%d) failed: %d", C, W, H, n, (int)r);
-        return HX_ERR_DEVICE;
-    }
-    return HX_OK;
-}
-// The same tensor with a box of bx x by pixels: (10, 34) for k_conv_halo (two
+// NHWC BF16 activation: 4-D map (C, W, H, n), a box of 32 channels x bx x by pixels,
+// 64-byte swizzle: (10, 34) for k_conv_halo (two
 // 8x16 tiles and their one-pixel halo), (10, 18) and (8, 16) for
 // k_wgrad_halo's input halo and output-gradient tile; out-of-range pixels
 // read as zero.
@@ -1186,8 +888,7 @@ struct Plan {
     bool train = false;
     bf16* t[NT] = {};
     bf16* g[NT] = {};
-    CUtensorMap tm[NT], gm[NT];
-    CUtensorMap hm[NT], hgm[NT];  // halo boxes of the same tensors (k_conv_halo)
+    CUtensorMap hm[NT], hgm[NT];  // k_conv_halo: two 8x16 tiles + halo (10 x 34) of activations / gradients
     CUtensorMap wxm[NT], wgm[NT]; // k_wgrad_halo: input halo (10 x 18), output-gradient tile (8 x 16)
     float4* y = nullptr;
     float* partial = nullptr;
@@ -1245,13 +946,11 @@ hx_status build_plan(hx_denoiser* dn, Plan* p, int n, int H, int W, bool train) 
         const size_t bytes = (size_t)n * h * w * C * sizeof(bf16);
         if (i != GYT) {
             HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->t[i], bytes));
-            HX_TRY(make_act_map(&p->tm[i], p->t[i], C, w, h, n));
             HX_TRY(make_halo_map(&p->hm[i], p->t[i], C, w, h, n));
             if (train) HX_TRY(make_halo_map(&p->wxm[i], p->t[i], C, w, h, n, kHaloW, kHY + 2));
         }
         if (train && i != X) {
             HX_TRY(dn_alloc(ctx, p->allocs, (void**)&p->g[i], bytes));
-            HX_TRY(make_act_map(&p->gm[i], p->g[i], C, w, h, n));
             HX_TRY(make_halo_map(&p->hgm[i], p->g[i], C, w, h, n));
             HX_TRY(make_halo_map(&p->wgm[i], p->g[i], C, w, h, n, kHX, kHY));
         }
@@ -1321,7 +1020,6 @@ hx_status get_plan(hx_denoiser* dn, int n, int H, int W, bool train, Plan** out)
     return HX_OK;
 }
 
-size_t conv_smem(int stages, uint32_t b_bytes) { return 1024 + stages * (kChunkBytes + b_bytes) + 256; }
 
 int grid_for(size_t total, int threads, int sms) {
     return (int)std::max<size_t>(1, std::min<size_t>((total + threads - 1) / threads, (size_t)sms * 8));
@@ -1339,15 +1037,14 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
     a.W = W;
     a.H = H;
     a.nimg = p->n;
-    const bool halo = kConvHalo;
-    a.tiles_x = halo ? (W + kHX - 1) / kHX : (W + kBX - 1) / kBX;
-    a.tiles_y = halo ? (H + kHMT * kHY - 1) / (kHMT * kHY) : (H + kBY - 1) / kBY;
+    a.tiles_x = (W + kHX - 1) / kHX;
+    a.tiles_y = (H + kHMT * kHY - 1) / (kHMT * kHY);
     a.stages = kConvStages;
     a.err = dn->err;
     a.wait_cycles = dn->wait_cycles;
     const CUtensorMap *m0, *m1, *wm;
-    const CUtensorMap* act = halo ? p->hm : p->tm;
-    const CUtensorMap* gact = halo ? p->hgm : p->gm;
+    const CUtensorMap* act = p->hm;
+    const CUtensorMap* gact = p->hgm;
     if (!dgrad) {
         m0 = &act[S.src0];
         m1 = S.src1 >= 0 ? &act[S.src1] : m0;
@@ -1389,19 +1086,12 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
     HX_CHECK_ARG(a.N % 16 == 0 && a.N >= 16 && a.N <= 256, "conv N=%d out of range", a.N);
     a.b_bytes = (uint32_t)round_up(a.N * 64, 1024);
     const int grid = a.tiles_x * a.tiles_y * p->n;
-    if (halo) {
-        a.tmem_cols = pow2_cols(kHMT * a.N);
-        // one halo buffer for a single 32-channel chunk (more resident CTAs for the 32-channel layers)
-        const int nhalo = a.chunks0 + a.chunks1 > 1 ? 2 : 1;
-        const size_t smem = 1024 + nhalo * (size_t)kHaloStride + a.stages * (size_t)a.b_bytes + 256;
-        HX_CUDA(cudaFuncSetAttribute(k_conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_conv_halo<<<grid, kThreads, smem, ctx->stream>>>(*m0, *m1, *wm, a);
-    } else {
-        a.tmem_cols = pow2_cols(a.N);
-        const size_t smem = conv_smem(a.stages, a.b_bytes);
-        HX_CUDA(cudaFuncSetAttribute(k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_conv<<<grid, kThreads, smem, ctx->stream>>>(*m0, *m1, *wm, a);
-    }
+    a.tmem_cols = pow2_cols(kHMT * a.N);
+    // one halo buffer for a single 32-channel chunk (more resident CTAs for the 32-channel layers)
+    const int nhalo = a.chunks0 + a.chunks1 > 1 ? 2 : 1;
+    const size_t smem = 1024 + nhalo * (size_t)kHaloStride + a.stages * (size_t)a.b_bytes + 256;
+    HX_CUDA(cudaFuncSetAttribute(k_conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_conv_halo<<<grid, kThreads, smem, ctx->stream>>>(*m0, *m1, *wm, a);
     HX_CUDA(cudaGetLastError());
     return HX_OK;
 }
