@@ -555,83 +555,92 @@ __device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
     return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
+// The resampling kernels below run one block row per image row of the
+// half-resolution grid (grid.y = n * h) and one thread per 8-channel group of
+// a half-resolution pixel (grid.x covers w * C / 8): 32-bit indices, one
+// division per thread, each thread handling the pixel's 2x2 full-resolution
+// block.  Sizes are checked on the host (n * h, w * C / 8 < 2^31).
+struct RowIdx {
+    int n, y, x, g;
+    bool ok;
+};
+__device__ __forceinline__ RowIdx row_idx(int h, int w, int cg) {
+    RowIdx r;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    r.ok = j < w * cg;
+    r.x = j / cg;
+    r.g = j - r.x * cg;
+    r.n = blockIdx.y / h;
+    r.y = blockIdx.y - r.n * h;
+    return r;
+}
+
 // 2x2 average pool: out [n][H/2][W/2][C] from in [n][H][W][C].
 __global__ void k_pool(const bf16* __restrict__ in, int H, int W, int C, int nimg, bf16* __restrict__ out) {
     const int h = H / 2, w = W / 2, cg = C / 8;
-    const size_t total = (size_t)nimg * h * w * cg;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int g = (int)(i % cg);
-        const size_t p = i / cg;
-        const int x = (int)(p % w), y = (int)((p / w) % h);
-        const size_t n = p / ((size_t)w * h);
-        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int dy = 0; dy < 2; ++dy)
-            for (int dx = 0; dx < 2; ++dx) {
-                float f[8];
-                unpack8(reinterpret_cast<const uint4*>(in + (((n * H + 2 * y + dy) * W) + 2 * x + dx) * C)[g], f);
+    const RowIdx r = row_idx(h, w, cg);
+    if (!r.ok) return;
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+            float f[8];
+            const size_t q = ((size_t)(r.n * H + 2 * r.y + dy) * W + 2 * r.x + dx) * C;
+            unpack8(reinterpret_cast<const uint4*>(in + q)[r.g], f);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) s[j] += f[j];
-            }
+            for (int j = 0; j < 8; ++j) s[j] += f[j];
+        }
 #pragma unroll
-        for (int j = 0; j < 8; ++j) s[j] *= 0.25f;
-        reinterpret_cast<uint4*>(out + p * C)[g] = pack8(s);
-    }
+    for (int j = 0; j < 8; ++j) s[j] *= 0.25f;
+    reinterpret_cast<uint4*>(out + ((size_t)(r.n * h + r.y) * w + r.x) * C)[r.g] = pack8(s);
 }
 
 // g_a += (a > 0) * g_p / 4 spread over each 2x2 block (pool backward into a
 // ReLU output that also feeds a skip connection).
 __global__ void k_pool_bwd_add(const bf16* __restrict__ gp, const bf16* __restrict__ act, int H, int W, int C,
                                int nimg, bf16* __restrict__ ga) {
-    const int cg = C / 8;
-    const size_t total = (size_t)nimg * H * W * cg;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int g = (int)(i % cg);
-        const size_t p = i / cg;
-        const int x = (int)(p % W), y = (int)((p / W) % H);
-        const size_t n = p / ((size_t)W * H);
-        float fa[8], fg[8], fp[8];
-        unpack8(reinterpret_cast<const uint4*>(act + p * C)[g], fa);
-        unpack8(reinterpret_cast<const uint4*>(ga + p * C)[g], fg);
-        unpack8(reinterpret_cast<const uint4*>(gp + (((n * (H / 2) + y / 2) * (W / 2)) + x / 2) * C)[g], fp);
+    const int h = H / 2, w = W / 2, cg = C / 8;
+    const RowIdx r = row_idx(h, w, cg);
+    if (!r.ok) return;
+    float fp[8];
+    unpack8(reinterpret_cast<const uint4*>(gp + ((size_t)(r.n * h + r.y) * w + r.x) * C)[r.g], fp);
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+            const size_t q = ((size_t)(r.n * H + 2 * r.y + dy) * W + 2 * r.x + dx) * C;
+            float fa[8], fg[8];
+            unpack8(reinterpret_cast<const uint4*>(act + q)[r.g], fa);
+            unpack8(reinterpret_cast<const uint4*>(ga + q)[r.g], fg);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) fg[j] = fg[j] + (fa[j] > 0.0f ? 0.25f * fp[j] : 0.0f);
-        reinterpret_cast<uint4*>(ga + p * C)[g] = pack8(fg);
-    }
+            for (int j = 0; j < 8; ++j) fg[j] = fg[j] + (fa[j] > 0.0f ? 0.25f * fp[j] : 0.0f);
+            reinterpret_cast<uint4*>(ga + q)[r.g] = pack8(fg);
+        }
 }
 
 // Nearest 2x upsampling: out [n][2h][2w][C].
 __global__ void k_up(const bf16* __restrict__ in, int h, int w, int C, int nimg, bf16* __restrict__ out) {
     const int H = 2 * h, W = 2 * w, cg = C / 8;
-    const size_t total = (size_t)nimg * H * W * cg;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int g = (int)(i % cg);
-        const size_t p = i / cg;
-        const int x = (int)(p % W), y = (int)((p / W) % H);
-        const size_t n = p / ((size_t)W * H);
-        reinterpret_cast<uint4*>(out + p * C)[g] =
-            reinterpret_cast<const uint4*>(in + (((n * h + y / 2) * w) + x / 2) * C)[g];
-    }
+    const RowIdx r = row_idx(h, w, cg);
+    if (!r.ok) return;
+    const uint4 v = reinterpret_cast<const uint4*>(in + ((size_t)(r.n * h + r.y) * w + r.x) * C)[r.g];
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx)
+            reinterpret_cast<uint4*>(out + ((size_t)(r.n * H + 2 * r.y + dy) * W + 2 * r.x + dx) * C)[r.g] = v;
 }
 
 // Upsampling backward: sum of the 2x2 gradient block.
 __global__ void k_up_bwd(const bf16* __restrict__ gin, int h, int w, int C, int nimg, bf16* __restrict__ gout) {
     const int H = 2 * h, W = 2 * w, cg = C / 8;
-    const size_t total = (size_t)nimg * h * w * cg;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int g = (int)(i % cg);
-        const size_t p = i / cg;
-        const int x = (int)(p % w), y = (int)((p / w) % h);
-        const size_t n = p / ((size_t)w * h);
-        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int dy = 0; dy < 2; ++dy)
-            for (int dx = 0; dx < 2; ++dx) {
-                float f[8];
-                unpack8(reinterpret_cast<const uint4*>(gin + (((n * H + 2 * y + dy) * W) + 2 * x + dx) * C)[g], f);
+    const RowIdx r = row_idx(h, w, cg);
+    if (!r.ok) return;
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+            float f[8];
+            const size_t q = ((size_t)(r.n * H + 2 * r.y + dy) * W + 2 * r.x + dx) * C;
+            unpack8(reinterpret_cast<const uint4*>(gin + q)[r.g], f);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) s[j] += f[j];
-            }
-        reinterpret_cast<uint4*>(gout + p * C)[g] = pack8(s);
-    }
+            for (int j = 0; j < 8; ++j) s[j] += f[j];
+        }
+    reinterpret_cast<uint4*>(gout + ((size_t)(r.n * h + r.y) * w + r.x) * C)[r.g] = pack8(s);
 }
 
 // Features [n][h][w][12] (radiance rgb, -, albedo rgb, depth, normal xyz, -)
@@ -1150,19 +1159,29 @@ hx_status launch_wgrad(hx_denoiser* dn, Plan* p, int l, float scale) {
     return HX_OK;
 }
 
+// Launch grid of the resampling kernels over an h x w half-resolution grid.
+hx_status row_grid(int n, int h, int w, int C, dim3* g) {
+    HX_CHECK_ARG((long long)n * h <= 65535 && (long long)w * (C / 8) < (1ll << 31), "resampling grid %d x %d x %d too large",
+                 n, h, w);
+    *g = dim3((unsigned)((w * (C / 8) + 255) / 256), (unsigned)(n * h));
+    return HX_OK;
+}
+
 hx_status elementwise_pool(hx_denoiser* dn, Plan* p, int src, int dst) {
     const int lev = kTensors[src].level, C = kTensors[src].C;
     const int H = level_dim(p->H, lev), W = level_dim(p->W, lev);
-    const size_t total = (size_t)p->n * (H / 2) * (W / 2) * (C / 8);
-    k_pool<<<grid_for(total, 256, dn->ctx->num_sms), 256, 0, dn->ctx->stream>>>(p->t[src], H, W, C, p->n, p->t[dst]);
+    dim3 g;
+    HX_TRY(row_grid(p->n, H / 2, W / 2, C, &g));
+    k_pool<<<g, 256, 0, dn->ctx->stream>>>(p->t[src], H, W, C, p->n, p->t[dst]);
     HX_CUDA(cudaGetLastError());
     return HX_OK;
 }
 hx_status elementwise_up(hx_denoiser* dn, Plan* p, int src, int dst) {
     const int lev = kTensors[src].level, C = kTensors[src].C;
     const int h = level_dim(p->H, lev), w = level_dim(p->W, lev);
-    const size_t total = (size_t)p->n * (2 * h) * (2 * w) * (C / 8);
-    k_up<<<grid_for(total, 256, dn->ctx->num_sms), 256, 0, dn->ctx->stream>>>(p->t[src], h, w, C, p->n, p->t[dst]);
+    dim3 g;
+    HX_TRY(row_grid(p->n, h, w, C, &g));
+    k_up<<<g, 256, 0, dn->ctx->stream>>>(p->t[src], h, w, C, p->n, p->t[dst]);
     HX_CUDA(cudaGetLastError());
     return HX_OK;
 }
@@ -1193,16 +1212,16 @@ hx_status run_backward(hx_denoiser* dn, Plan* p, float scale) {
             const int H = level_dim(p->H, lev), W = level_dim(p->W, lev);
             if (s == U3 || s == U2 || s == U1 || s == U0) {
                 const int dst = s == U3 ? A4B : s == U2 ? D3 : s == U1 ? D2 : D1;
-                const size_t total = (size_t)p->n * (H / 2) * (W / 2) * (C / 8);
-                k_up_bwd<<<grid_for(total, 256, ctx->num_sms), 256, 0, ctx->stream>>>(p->g[s], H / 2, W / 2, C, p->n,
-                                                                                      p->g[dst]);
+                dim3 g;
+                HX_TRY(row_grid(p->n, H / 2, W / 2, C, &g));
+                k_up_bwd<<<g, 256, 0, ctx->stream>>>(p->g[s], H / 2, W / 2, C, p->n, p->g[dst]);
                 HX_CUDA(cudaGetLastError());
             } else if (s == P0 || s == P1 || s == P2 || s == P3) {
                 const int a = s == P0 ? A0B : s == P1 ? A1 : s == P2 ? A2 : A3;
                 const int Ha = 2 * H, Wa = 2 * W;
-                const size_t total = (size_t)p->n * Ha * Wa * (C / 8);
-                k_pool_bwd_add<<<grid_for(total, 256, ctx->num_sms), 256, 0, ctx->stream>>>(p->g[s], p->t[a], Ha, Wa,
-                                                                                           C, p->n, p->g[a]);
+                dim3 g;
+                HX_TRY(row_grid(p->n, H, W, C, &g));
+                k_pool_bwd_add<<<g, 256, 0, ctx->stream>>>(p->g[s], p->t[a], Ha, Wa, C, p->n, p->g[a]);
                 HX_CUDA(cudaGetLastError());
             }
         }
