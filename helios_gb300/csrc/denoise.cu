@@ -137,6 +137,54 @@ constexpr uint32_t kHaloBytes = kHaloW * kHaloH * 64;            // 21,760
 constexpr uint32_t kHaloStride = (kHaloBytes + 1023) / 1024 * 1024;
 constexpr uint32_t kHaloRowBytes = kHaloW * 64;                  // 640: stride of 8-row groups
 
+// Epilogue of one halo-kernel CTA tile pair: TMEM lane r (pixel (r % 8,
+// r / 8) of tile m) from the accumulator at column col0 + m * N, bias + ReLU /
+// residual / gradient mask, stores.  Called by warps 0-3 (TMEM lane quarters).
+__device__ __forceinline__ void halo_epilogue(const ConvArgs& a, uint32_t trow, uint32_t col0, int x0, int y0, int n,
+                                              int r) {
+    for (int m = 0; m < kHMT; ++m) {
+        const int x = x0 + (r & (kHX - 1)), y = y0 + m * kHY + r / kHX;
+        const bool inb = x < a.W && y < a.H;
+        const size_t pix = ((size_t)n * a.H + y) * a.W + x;
+        for (int col = 0; col < a.N; col += 16) {
+            uint32_t v[16];
+            __syncwarp();
+            tc::tmem_ld16(trow + col0 + (uint32_t)(m * a.N + col), v);
+            tc::tmem_wait_ld();
+            float f[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) f[j] = __uint_as_float(v[j]);
+            if (!inb) continue;
+            if (a.mode == EPI_RELU_BF16) {
+                if (col < a.n_store) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) f[j] = fmaxf(f[j] + a.bias[col + j], 0.0f);
+                    store16_bf16(reinterpret_cast<bf16*>(a.out0) + pix * a.och0 + col, f);
+                }
+            } else if (a.mode == EPI_LINEAR_F32) {
+                if (col == 0) {
+                    const __nv_bfloat162 r01 = *reinterpret_cast<const __nv_bfloat162*>(a.resid + pix * 32);
+                    const float r2 = __bfloat162float(a.resid[pix * 32 + 2]);
+                    reinterpret_cast<float4*>(a.out0)[pix] =
+                        make_float4((f[0] + a.bias[0]) + __low2float(r01), (f[1] + a.bias[1]) + __high2float(r01),
+                                    (f[2] + a.bias[2]) + r2, 0.0f);
+                }
+            } else {
+                const bool hi = col >= a.och0;
+                const int och = hi ? a.och1 : a.och0, lc = hi ? col - a.och0 : col;
+                const bf16* mk = hi ? a.mask1 : a.mask0;
+                if (mk) {
+                    float mv[16];
+                    load16_bf16(mk + pix * och + lc, mv);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) f[j] = mv[j] > 0.0f ? f[j] : 0.0f;
+                }
+                store16_bf16(reinterpret_cast<bf16*>(hi ? a.out1 : a.out0) + pix * och + lc, f);
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 6)
     k_conv_halo(const __grid_constant__ CUtensorMap src0, const __grid_constant__ CUtensorMap src1,
                 const __grid_constant__ CUtensorMap wmap, ConvArgs a) {
@@ -255,49 +303,7 @@ __global__ void __launch_bounds__(kThreads, 6)
         ok = __all_sync(0xffffffffu, ok);
         tc::fence_after_sync();
         if (ok) {
-            const int r = warp * 32 + lane;
-            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-            for (int m = 0; m < kHMT; ++m) {
-                const int x = x0 + (r & (kHX - 1)), y = y0 + m * kHY + r / kHX;
-                const bool inb = x < a.W && y < a.H;
-                const size_t pix = ((size_t)n * a.H + y) * a.W + x;
-                for (int col = 0; col < a.N; col += 16) {
-                    uint32_t v[16];
-                    __syncwarp();
-                    tc::tmem_ld16(trow + (uint32_t)(m * a.N + col), v);
-                    tc::tmem_wait_ld();
-                    float f[16];
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) f[j] = __uint_as_float(v[j]);
-                    if (!inb) continue;
-                    if (a.mode == EPI_RELU_BF16) {
-                        if (col < a.n_store) {
-#pragma unroll
-                            for (int j = 0; j < 16; ++j) f[j] = fmaxf(f[j] + a.bias[col + j], 0.0f);
-                            store16_bf16(reinterpret_cast<bf16*>(a.out0) + pix * a.och0 + col, f);
-                        }
-                    } else if (a.mode == EPI_LINEAR_F32) {
-                        if (col == 0) {
-                            const __nv_bfloat162 r01 = *reinterpret_cast<const __nv_bfloat162*>(a.resid + pix * 32);
-                            const float r2 = __bfloat162float(a.resid[pix * 32 + 2]);
-                            reinterpret_cast<float4*>(a.out0)[pix] =
-                                make_float4((f[0] + a.bias[0]) + __low2float(r01), (f[1] + a.bias[1]) + __high2float(r01),
-                                            (f[2] + a.bias[2]) + r2, 0.0f);
-                        }
-                    } else {
-                        const bool hi = col >= a.och0;
-                        const int och = hi ? a.och1 : a.och0, lc = hi ? col - a.och0 : col;
-                        const bf16* mk = hi ? a.mask1 : a.mask0;
-                        if (mk) {
-                            float mv[16];
-                            load16_bf16(mk + pix * och + lc, mv);
-#pragma unroll
-                            for (int j = 0; j < 16; ++j) f[j] = mv[j] > 0.0f ? f[j] : 0.0f;
-                        }
-                        store16_bf16(reinterpret_cast<bf16*>(hi ? a.out1 : a.out0) + pix * och + lc, f);
-                    }
-                }
-            }
+            halo_epilogue(a, tmem + ((uint32_t)(warp * 32) << 16), 0u, x0, y0, n, warp * 32 + lane);
         } else if (lane == 0) {
             s_fail = 1;
         }
@@ -308,6 +314,151 @@ __global__ void __launch_bounds__(kThreads, 6)
             if (!tc::mbar_wait(&a_full[c & 1], (c >> 1) & 1)) s_fail = 1;
         for (int i = issued_b > a.stages ? issued_b - a.stages : 0; i < issued_b; ++i)
             if (!tc::mbar_wait(&b_full[i % a.stages], (i / a.stages) & 1)) s_fail = 1;
+    } else if (warp == 5 && lane == 0) {
+        if (!tc::mbar_wait(done, 0)) s_fail = 1;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 5) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, a.tmem_cols);
+    }
+    if (threadIdx.x == 0 && s_fail) atomicOr(a.err, 1u);
+}
+
+// Persistent form of k_conv_halo for single-chunk layers (32 input channels,
+// N <= 64: the full-resolution layers): a CTA per SM slot loads the layer's
+// nine weight tiles once, then walks tile pairs (blockIdx.x, + gridDim.x, ...)
+// through a kPHaloStages-deep halo ring; two TMEM accumulator sets let the
+// epilogue warps drain pair i while the MMAs of pair i + 1 run.  Barriers:
+// w_full (weights), h_full / h_empty (halo ring), acc_full (MMA -> epilogue,
+// one commit per pair) and acc_empty (epilogue -> MMA, one arrival per
+// epilogue warp).
+constexpr int kPHaloStages = 3;
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_conv_halo_p(const __grid_constant__ CUtensorMap src0, const __grid_constant__ CUtensorMap wmap, ConvArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = align1k(smem_raw);
+    uint8_t* Ws = smem;                                    // nine weight tiles
+    uint8_t* Hs = smem + 9 * a.b_bytes;                    // halo ring
+    uint64_t* w_full = reinterpret_cast<uint64_t*>(Hs + kPHaloStages * kHaloStride);
+    uint64_t* h_full = w_full + 1;
+    uint64_t* h_empty = h_full + kPHaloStages;
+    uint64_t* acc_full = h_empty + kPHaloStages;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* done = acc_empty + 2;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+    __shared__ uint32_t s_fail;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int per_img = a.tiles_x * a.tiles_y;
+    const int ntiles = per_img * a.nimg;
+    const uint32_t acc_cols = (uint32_t)(kHMT * a.N);  // one accumulator set (both tiles of a pair)
+
+    if (threadIdx.x == 0) {
+        tc::mbar_init(w_full, 1);
+        for (int s = 0; s < kPHaloStages; ++s) {
+            tc::mbar_init(&h_full[s], 1);
+            tc::mbar_init(&h_empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], 4);
+        }
+        tc::mbar_init(done, 1);
+        tc::fence_mbar_init();
+        s_fail = 0;
+    }
+    if (warp == 5) {
+        tc::tmem_alloc(tslot, a.tmem_cols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    int issued = 0;  // halo loads issued by the producer (warp 4, lane 0)
+    if (warp == 4) {
+        if (lane == 0) {
+            tc::tma_prefetch(&src0);
+            tc::tma_prefetch(&wmap);
+            tc::mbar_expect_tx(w_full, 9u * a.N * 64);
+            for (int t = 0; t < 9; ++t) tc::tma_load_3d(Ws + t * a.b_bytes, &wmap, w_full, 0, 0, t);
+            int i = 0;
+            for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+                const int s = i % kPHaloStages;
+                if (i >= kPHaloStages &&
+                    !tc::mbar_wait(&h_empty[s], ((i / kPHaloStages) - 1) & 1, a.wait_cycles)) {
+                    s_fail = 1;
+                    break;
+                }
+                issued = i + 1;
+                const int n = tile / per_img, rem = tile % per_img;
+                const int x0 = (rem % a.tiles_x) * kHX, y0 = (rem / a.tiles_x) * (kHMT * kHY);
+                tc::mbar_expect_tx(&h_full[s], kHaloBytes);
+                tc::tma_load_4d(Hs + s * kHaloStride, &src0, &h_full[s], 0, x0 - 1, y0 - 1, n);
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, a.N, 0, 0);
+            bool ok = tc::mbar_wait(w_full, 0, a.wait_cycles);
+            const uint32_t wb = tc::smem_u32(Ws);
+            int i = 0;
+            for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x, ++i) {
+                const int s = i % kPHaloStages, b = i & 1;
+                if (!tc::mbar_wait(&h_full[s], (i / kPHaloStages) & 1, a.wait_cycles) ||
+                    (i >= 2 && !tc::mbar_wait(&acc_empty[b], ((i >> 1) - 1) & 1, a.wait_cycles))) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t hb = tc::smem_u32(Hs + s * kHaloStride);
+                const uint32_t d = tmem + (uint32_t)b * acc_cols;
+                for (int t = 0; t < 9; ++t) {
+                    const int ky = t / 3, kx = t % 3;
+                    const uint32_t bb = wb + (uint32_t)t * a.b_bytes;
+#pragma unroll
+                    for (int m = 0; m < kHMT; ++m)
+#pragma unroll
+                        for (int k = 0; k < 2; ++k) {
+                            const uint32_t aa = hb + (uint32_t)(m * kHY + ky) * kHaloRowBytes + kx * 64 + 32 * k;
+                            tc::mma_bf16(d + (uint32_t)(m * a.N), tc::smem_desc(aa, 16, kHaloRowBytes, tc::kSwizzle64B),
+                                         tc::smem_desc(bb + 32 * k, 16, 512, tc::kSwizzle64B), idesc, (t | k) != 0);
+                        }
+                }
+                tc::mma_commit(&h_empty[s]);
+                tc::mma_commit(&acc_full[b]);
+            }
+            if (!ok) s_fail = 1;
+            tc::mma_commit(done);
+        }
+    } else {
+        int i = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            const int b = i & 1;
+            bool ok = tc::mbar_wait(&acc_full[b], (i >> 1) & 1, a.wait_cycles);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                if (lane == 0) s_fail = 1;
+                break;
+            }
+            tc::fence_after_sync();
+            const int n = tile / per_img, rem = tile % per_img;
+            const int x0 = (rem % a.tiles_x) * kHX, y0 = (rem / a.tiles_x) * (kHMT * kHY);
+            halo_epilogue(a, tmem + ((uint32_t)(warp * 32) << 16), (uint32_t)b * acc_cols, x0, y0, n, warp * 32 + lane);
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+        }
+    }
+    // drain: the producer's weight load and newest halo loads, the MMA issuer's `done`
+    if (warp == 4 && lane == 0) {
+        if (!tc::mbar_wait(w_full, 0)) s_fail = 1;
+        for (int i = issued > kPHaloStages ? issued - kPHaloStages : 0; i < issued; ++i)
+            if (!tc::mbar_wait(&h_full[i % kPHaloStages], (i / kPHaloStages) & 1)) s_fail = 1;
     } else if (warp == 5 && lane == 0) {
         if (!tc::mbar_wait(done, 0)) s_fail = 1;
     }
@@ -1095,6 +1246,17 @@ hx_status launch_conv(hx_denoiser* dn, Plan* p, int l, bool dgrad) {
     HX_CHECK_ARG(a.N % 16 == 0 && a.N >= 16 && a.N <= 256, "conv N=%d out of range", a.N);
     a.b_bytes = (uint32_t)round_up(a.N * 64, 1024);
     const int grid = a.tiles_x * a.tiles_y * p->n;
+    if (a.chunks0 + a.chunks1 == 1 && a.N <= 64) {
+        // single-chunk layer: the persistent kernel (weights resident, halo ring,
+        // two accumulator sets), two CTAs per SM
+        a.tmem_cols = pow2_cols(2 * kHMT * a.N);
+        const size_t smem = 1024 + 9 * (size_t)a.b_bytes + kPHaloStages * (size_t)kHaloStride + 256;
+        HX_CUDA(cudaFuncSetAttribute(k_conv_halo_p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int pgrid = std::min(grid, 2 * ctx->num_sms);
+        k_conv_halo_p<<<pgrid, kThreads, smem, ctx->stream>>>(*m0, *wm, a);
+        HX_CUDA(cudaGetLastError());
+        return HX_OK;
+    }
     a.tmem_cols = pow2_cols(kHMT * a.N);
     // one halo buffer for a single 32-channel chunk (more resident CTAs for the 32-channel layers)
     const int nhalo = a.chunks0 + a.chunks1 > 1 ? 2 : 1;
