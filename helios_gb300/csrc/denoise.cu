@@ -624,15 +624,30 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // grad[tap][co][ci] = scale * sum_split partial[split][tap][co][ci], co < cout.
-__global__ void k_wgrad_reduce(const float* __restrict__ partial, int splits, int N, int cout, int cin, float scale,
-                               float* __restrict__ grad) {
+// A block = 32 consecutive outputs (lanes) x 8 split groups (warps): warp j
+// sums splits j, j + 8, ... in order, then the eight group sums are added in
+// warp order — a fixed order, so the result is deterministic.
+constexpr int kReduceGroups = 8;
+__global__ void __launch_bounds__(32 * kReduceGroups) k_wgrad_reduce(const float* __restrict__ partial, int splits, int N,
+                                                                      int cout, int cin, float scale,
+                                                                      float* __restrict__ grad) {
+    __shared__ float red[kReduceGroups][33];
+    const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
     const size_t total = (size_t)9 * cout * cin;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = (size_t)blockIdx.x * 32 + lane;
+    float s = 0.0f;
+    if (i < total) {
         const size_t tap = i / ((size_t)cout * cin), rem = i % ((size_t)cout * cin);
         const size_t co = rem / cin, ci = rem % cin;
-        float s = 0.0f;
-        for (int k = 0; k < splits; ++k) s += partial[(((size_t)k * 9 + tap) * N + co) * cin + ci];
-        grad[i] = s * scale;
+        for (int k = j; k < splits; k += kReduceGroups) s += partial[(((size_t)k * 9 + tap) * N + co) * cin + ci];
+    }
+    red[j][lane] = s;
+    __syncthreads();
+    if (j == 0 && i < total) {
+        float t = 0.0f;
+#pragma unroll
+        for (int q = 0; q < kReduceGroups; ++q) t += red[q][lane];
+        grad[i] = t * scale;
     }
 }
 
@@ -1308,8 +1323,8 @@ hx_status launch_wgrad(hx_denoiser* dn, Plan* p, int l, float scale) {
     HX_CUDA(cudaGetLastError());
     float* gw = dn->grads + L.off;
     const size_t total = (size_t)9 * L.cout * L.cin;
-    k_wgrad_reduce<<<grid_for(total, 256, ctx->num_sms), 256, 0, ctx->stream>>>(p->partial, a.splits, L.cd, L.cout,
-                                                                               L.cin, scale, gw);
+    k_wgrad_reduce<<<(unsigned)((total + 31) / 32), 32 * kReduceGroups, 0, ctx->stream>>>(p->partial, a.splits, L.cd,
+                                                                                           L.cout, L.cin, scale, gw);
     HX_CUDA(cudaGetLastError());
     // bias gradient
     const int C = kTensors[gout].C;
