@@ -69,6 +69,9 @@ def parse():
     p.add_argument("--ref-spp", type=int, default=16384)
     p.add_argument("--ref-pixels", type=int, default=4096)
     p.add_argument("--denoise", action="store_true", help="learned-denoiser training + time-to-RMSE report")
+    p.add_argument("--denoise-kernels", action="store_true",
+                   help="denoiser kernel timing: 1080p inference and a 16 x 256^2 training step (random network)")
+    p.add_argument("--dn-iters", type=int, default=20, help="timed iterations of --denoise-kernels")
     p.add_argument("--dn-variants", type=int, default=64)
     p.add_argument("--dn-target-spp", type=int, default=4096)
     p.add_argument("--dn-steps", type=int, default=3000)
@@ -831,11 +834,61 @@ def run_denoise(args, dist):
     print(json.dumps(out), flush=True)
 
 
+def run_denoise_kernels(args, dist):
+    """The denoiser's kernels alone, on seeded random inputs and a network from
+    the library's initialiser: CUDA-event time of a 1080p inference and of a
+    training step on 16 x 256^2 crops, with the convolutions' FLOP rates."""
+    import numpy as np
+    import helios_gb300 as hx
+    ctx = hx.Context(dist.local)
+    dn = hx.Denoiser(ctx)
+    dn.init_params(3)
+    rng = np.random.default_rng(1)
+    feats = np.zeros((1, HEIGHT, WIDTH, 12), np.float32)
+    feats[..., 0:3] = rng.exponential(0.5, (1, HEIGHT, WIDTH, 3))
+    feats[..., 4:7] = rng.uniform(0, 1, (1, HEIGHT, WIDTH, 3))
+    feats[..., 8:11] = 0.577
+    fb = hx.DeviceBuffer(ctx, feats.nbytes)
+    fb.upload(feats)
+    ob = hx.DeviceBuffer(ctx, HEIGHT * WIDTH * 16)
+    n, h, w = 16, 256, 256
+    f2 = np.zeros((n, h, w, 12), np.float32)
+    f2[..., 0:3] = rng.exponential(0.5, (n, h, w, 3))
+    f2[..., 4:7] = 0.5
+    f2[..., 8:11] = 0.577
+    fb2 = hx.DeviceBuffer(ctx, f2.nbytes)
+    fb2.upload(f2)
+    tb2 = hx.DeviceBuffer(ctx, n * h * w * 16)
+    tb2.upload(np.ones((n, h, w, 4), np.float32))
+    e0, e1 = hx.Event(ctx), hx.Event(ctx)
+    out = {"mode": "denoise-kernels", "n_gpus": 1, "data": "synthetic (seeded random features; random network)"}
+    for name, run, flops in (
+            ("inference_1080p", lambda: dn.infer(fb, 1, HEIGHT, WIDTH, ob),
+             hx.denoiser_conv_flops_per_pixel() * WIDTH * ((HEIGHT + 15) // 16 * 16)),
+            ("train_step_16x256x256", lambda: dn.train_step(fb2, tb2, n, h, w, 1e-4, want_loss=False),
+             3 * hx.denoiser_conv_flops_per_pixel() * n * h * w)):
+        for _ in range(3):
+            run()
+        dn.check()
+        ctx.synchronize()
+        e0.record()
+        for _ in range(max(1, args.dn_iters)):
+            run()
+        e1.record()
+        ms = e0.elapsed_ms(e1) / max(1, args.dn_iters)
+        dn.check()
+        out[name] = {"ms": ms, "conv_tflops": flops / ms / 1e9}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.denoise:
+        if args.denoise_kernels:
+            if dist.rank == 0:
+                run_denoise_kernels(args, dist)
+        elif args.denoise:
             if dist.rank == 0:
                 run_denoise(args, dist)
         elif args.precision:
