@@ -59,20 +59,25 @@ __global__ void k_rng_streams(uint32_t kind, const uint32_t* seeds, uint32_t n, 
     for (uint32_t k = 0; k < draws; ++k) out[(size_t)i * draws + k] = rng_next_k(kind, r);
 }
 
-__global__ void k_hits_to_host_layout(const float4* __restrict__ hits, uint32_t n, hx_hit* out) {
+// Hits / radiance of one W x H frame's paths (slot = path = pix in the
+// rect's tiled pixel order, pix_xy) to row-major pixel order.  Caller-supplied
+// rays pass W = n, H = 1, for which the order is the identity.
+__global__ void k_hits_to_host_layout(const float4* __restrict__ hits, uint32_t W, uint32_t H, hx_hit* out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 h = hits[i];
+    if (i >= W * H) return;
+    const Rect rect{0, 0, W, H};
+    const float4 h = hits[pix_of_xy(rect, i % W, i / W)];
     out[i].t = h.x;
     out[i].prim = __float_as_uint(h.y);
     out[i].u = h.z;
     out[i].v = h.w;
 }
 
-__global__ void k_radiance_out(const float4* __restrict__ L, uint32_t n, float* out) {
+__global__ void k_radiance_out(const float4* __restrict__ L, uint32_t W, uint32_t H, float* out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 l = L[i];
+    if (i >= W * H) return;
+    const Rect rect{0, 0, W, H};
+    const float4 l = L[pix_of_xy(rect, i % W, i / W)];
     out[3 * (size_t)i] = l.x;
     out[3 * (size_t)i + 1] = l.y;
     out[3 * (size_t)i + 2] = l.z;
@@ -889,7 +894,7 @@ extern "C" hx_status hx_integrator_primary_hits(hx_integrator* it, const hx_fram
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));
     launch_primary_trace(it, st);
     uint32_t n = W * H;
-    k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(it->q.hit, n, it->hits_host_layout);
+    k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(it->q.hit, W, H, it->hits_host_layout);
     HX_CUDA(cudaGetLastError());
     HX_CUDA(cudaMemcpyAsync(host, it->hits_host_layout, sizeof(hx_hit) * n, cudaMemcpyDeviceToHost, st));
     HX_TRY(check_status(it));
@@ -916,7 +921,7 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, 0, W * H, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));
     launch_primary_trace(it, st);
-    k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, n, d_features);
+    k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, W, H, d_features);
     HX_CUDA(cudaGetLastError());
     HX_TRY(check_status(it));
     return HX_OK;
@@ -962,7 +967,7 @@ extern "C" hx_status hx_integrator_sample_radiance(hx_integrator* it, const hx_f
     HX_TRY(run_wavefront(it, *f, r, frame_index, 1, false));
     uint32_t n = W * H;
     cudaStream_t st = it->ctx->stream;
-    k_radiance_out<<<(n + 255) / 256, 256, 0, st>>>(it->q.L, n, it->rgb_tmp);
+    k_radiance_out<<<(n + 255) / 256, 256, 0, st>>>(it->q.L, W, H, it->rgb_tmp);
     HX_CUDA(cudaGetLastError());
     HX_CUDA(cudaMemcpyAsync(host_rgb, it->rgb_tmp, 12 * (size_t)n, cudaMemcpyDeviceToHost, st));
     HX_TRY(check_status(it));
@@ -996,7 +1001,7 @@ extern "C" hx_status hx_scene_trace(const hx_scene* scene, const float* host_ray
     const DevScene& s = scene->d;
     const int grid = ctx->num_sms * kTraceMinBlocks;
     launch_extend<false, false>(s, q, grid, grid, st, q.o[0], q.r0[0], q.r1[0], nullptr, q.counters, q.counters + 4);
-    k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(q.hit, n, d_hits);
+    k_hits_to_host_layout<<<(n + 255) / 256, 256, 0, st>>>(q.hit, n, 1, d_hits);
     HX_CUDA(cudaGetLastError());
     uint32_t status = 0;
     HX_CUDA(cudaMemcpyAsync(host_hits, d_hits, sizeof(hx_hit) * N, cudaMemcpyDeviceToHost, st));

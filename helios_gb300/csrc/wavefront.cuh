@@ -273,6 +273,45 @@ HXD uint32_t half2_bits(float a, float b) {
 // node fetches in the first bounce).  Results do not depend on the order.
 HXD uint32_t path_index(uint32_t pix, uint32_t fr, uint32_t nframes) { return pix * nframes + fr; }
 
+// Pixel order of a rect's paths (`pix`): 8 x 4-pixel tiles first — a warp's
+// 32 single-frame paths cover one compact tile instead of a 32 x 1 strip —
+// then the right remainder (rows of the tiled height), then the bottom
+// remainder rows.  pix_xy and pix_of_xy are inverse bijections on the rect.
+constexpr uint32_t kPixTileW = 8, kPixTileH = 4;
+HXD void pix_xy(const Rect& r, uint32_t pix, uint32_t& x, uint32_t& y) {
+    const uint32_t tw = r.w / kPixTileW, fx = tw * kPixTileW, fy = (r.h / kPixTileH) * kPixTileH;
+    const uint32_t nfull = fx * fy;
+    if (pix < nfull) {
+        const uint32_t t = pix / (kPixTileW * kPixTileH), k = pix % (kPixTileW * kPixTileH);
+        x = (t % tw) * kPixTileW + k % kPixTileW;
+        y = (t / tw) * kPixTileH + k / kPixTileW;
+    } else {
+        uint32_t q = pix - nfull;
+        const uint32_t rw = r.w - fx, rs = rw * fy;
+        if (q < rs) {
+            x = fx + q % rw;
+            y = q / rw;
+        } else {
+            q -= rs;
+            x = q % r.w;
+            y = fy + q / r.w;
+        }
+    }
+    x += r.x0;
+    y += r.y0;
+}
+HXD uint32_t pix_of_xy(const Rect& r, uint32_t x, uint32_t y) {
+    x -= r.x0;
+    y -= r.y0;
+    const uint32_t tw = r.w / kPixTileW, fx = tw * kPixTileW, fy = (r.h / kPixTileH) * kPixTileH;
+    if (x < fx && y < fy)
+        return ((y / kPixTileH) * tw + x / kPixTileW) * (kPixTileW * kPixTileH) + (y % kPixTileH) * kPixTileW +
+               x % kPixTileW;
+    const uint32_t nfull = fx * fy, rw = r.w - fx;
+    if (y < fy) return nfull + y * rw + (x - fx);
+    return nfull + rw * fy + (y - fy) * r.w + x;
+}
+
 // Camera rays of paths [path_base, path_base + path_count) of the rect's
 // nframes frames (path_index); path p goes to ray-queue slot p - path_base,
 // its state (T, L, rng) stays indexed by p.
@@ -282,7 +321,8 @@ __global__ void k_raygen(hx_frame_desc f, Rect rect, uint32_t W, uint32_t H, uin
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < path_count; k += gridDim.x * blockDim.x) {
         const uint32_t p = path_base + k;
         const uint32_t pix = p / nframes, fr = p - pix * nframes;
-        uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        uint32_t x, y;
+        pix_xy(rect, pix, x, y);
         Rng rng = rng_init(kind, x, y, W, frame0 + fr);
         V3 o, d;
         generate_ray(f, kind, x, y, W, H, rng, o, d);
@@ -775,7 +815,8 @@ __global__ void k_accumulate(Rect rect, uint32_t W, uint32_t frame0, uint32_t nf
                              float4* __restrict__ comp) {
     uint32_t npix = rect.w * rect.h;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
-        uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        uint32_t x, y;
+        pix_xy(rect, pix, x, y);
         size_t idx = (size_t)y * W + x;
         float4 a = acc[idx];
         float4 cp = kahan ? comp[idx] : make_float4(0, 0, 0, 0);
@@ -853,7 +894,8 @@ __global__ void k_resolve(const float4* __restrict__ acc, const uint32_t* __rest
 __global__ void k_count_add(Rect rect, uint32_t W, uint32_t add, uint32_t* __restrict__ count_map) {
     uint32_t npix = rect.w * rect.h;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
-        uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        uint32_t x, y;
+        pix_xy(rect, pix, x, y);
         count_map[(size_t)y * W + x] += add;
     }
 }
@@ -875,10 +917,13 @@ Policy make_policy(const hx_policy& p) {
 // depth feature log1p(t)/8, shading normal xyz, 0 — first-hit AOVs as the
 // reference's debug views define them (debug_visualization.frag:142-161:
 // base colour, shading normal); zeros on a miss.
-__global__ void k_features(DevScene s, const float4* __restrict__ hit, const float4* __restrict__ img, uint32_t n,
-                           float* __restrict__ feat) {
+__global__ void k_features(DevScene s, const float4* __restrict__ hit, const float4* __restrict__ img, uint32_t W,
+                           uint32_t H, float* __restrict__ feat) {
+    const Rect rect{0, 0, W, H};
+    const uint32_t n = W * H;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 h = hit[i], r = img[i];
+        // pixel i (row-major) was traced as path pix_of_xy (one frame)
+        const float4 h = hit[pix_of_xy(rect, i % W, i / W)], r = img[i];
         const uint32_t prim = __float_as_uint(h.y);
         V3 alb = v3(0.0f), nrm = v3(0.0f);
         float depth = 0.0f;
@@ -905,7 +950,8 @@ __global__ void k_aov_accumulate(DevScene s, Rect rect, uint32_t frame0, uint32_
                                  float4* __restrict__ aov_a, float4* __restrict__ aov_n, uint32_t W) {
     const uint32_t npix = rect.w * rect.h;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
-        const uint32_t x = rect.x0 + pix % rect.w, y = rect.y0 + pix / rect.w;
+        uint32_t x, y;
+        pix_xy(rect, pix, x, y);
         const size_t o = (size_t)y * W + x;
         float4 a = aov_a[o], nn = aov_n[o];
         for (uint32_t fr = 0; fr < nframes; ++fr) {
