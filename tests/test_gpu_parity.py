@@ -125,6 +125,26 @@ def test_primary_hit_ids_bit_exact(which, policy, gpu_ctx, box, ico):
     it.close()
 
 
+@pytest.mark.parametrize("W,H", [(97, 53), (7, 3), (1, 1)])
+def test_primary_hit_ids_bit_exact_ragged_frames(W, H, gpu_ctx, ico):
+    """Frames whose sides are not multiples of the 8 x 4-pixel tile the paths
+    are traced in (the right and bottom remainders take the row-major part of
+    the pixel order): hits still land on their own pixels, bit-exact, and the
+    per-sample radiance of the remainders matches the oracle."""
+    hs, sc, osc = ico
+    d = integrator_desc(W, H, bounces=4, policy="reference")
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=4, policy=d.policy)
+    g = it.primary_hits(f, 2)
+    o = osc.trace(ob.primary_rays(d, f, 2), any_hit=True)
+    assert np.array_equal(g["prim"], o["prim"]) and np.array_equal(g["t"], o["t"])
+    gr = it.sample_radiance(f, 1)
+    orad, _ = osc.sample_radiance(d, f, 1, precision=32)
+    close = np.all(np.abs(gr - orad) <= 1e-4 * (1 + np.abs(orad)), axis=1)
+    assert close.mean() > 0.99 or close.sum() >= close.size - 1, (W, H, rel_rmse(gr, orad))
+    it.close()
+
+
 @pytest.mark.parametrize("which,policy", [("box", "spec"), ("box", "reference"), ("ico", "reference"), ("ico", "spec")])
 def test_sample_radiance_matches_oracle(which, policy, gpu_ctx, box, ico):
     """Per-sample radiance of one frame, FP32 device vs FP32 oracle: the same
