@@ -224,13 +224,16 @@ def test_trained_denoiser_beats_plain_accumulation(gpu_ctx):
 
 
 
-def test_accumulated_aovs_are_the_mean_of_per_sample_aovs(gpu_ctx):
+@pytest.mark.parametrize("W,H", [(96, 64), (90, 61)])
+def test_accumulated_aovs_are_the_mean_of_per_sample_aovs(gpu_ctx, W, H):
     """AOV accumulation: the features' albedo / depth / normal after N frames
-    equal the mean of the N per-sample primary-hit AOVs (same jitter)."""
+    equal the mean of the N per-sample primary-hit AOVs (same jitter); the
+    90 x 61 frame has right and bottom remainders of the 8 x 4 tile order the
+    paths are traced in."""
     from tests.helpers import small_icosphere_scene
     hs = small_icosphere_scene(level=3, quads=2000, pool=4, mask=64, env=(128, 64))
     sc = hx.Scene(gpu_ctx, hs)
-    W, H, N = 96, 64, 4
+    N = 4
     f = hx.frame_desc(hs.camera(), W, H)
     pol = hx.policy_reference()
     a = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=4, policy=pol)
