@@ -570,7 +570,9 @@ def run_precision(args, dist):
     arithmetic).  Reports throughput, the relative RMSE of each device image
     against the 16k-spp FP64 oracle with its per-pixel distribution, and the
     primary hit-ID agreement of the quantised BVH8 with the oracle's
-    unquantised binary tree and of 16-bit with FP32 ray directions."""
+    unquantised binary tree and of 16-bit with FP32 ray directions.  The
+    "_offset" images use HX_RAY_OFFSET_SCALED ray origins and are compared
+    with the oracle under the same policy."""
     import numpy as np
     import helios_gb300 as hx
     from oracle import binding as ob
@@ -589,11 +591,14 @@ def run_precision(args, dist):
            "width": W, "height": H, "spp": spp, "ref_spp": ref_spp, "data": "synthetic"}
     pix = np.random.default_rng(11).choice(W * H, size=args.ref_pixels, replace=False).astype(np.uint32)
     imgs = {}
-    for name, fp16, kahan in (("fp16_kahan", True, True), ("fp32_kahan", False, True), ("fp32", False, False)):
+    runs = (("fp16_kahan", True, True, False), ("fp32_kahan", False, True, False), ("fp32", False, False, False),
+            ("fp16_kahan_offset", True, True, True), ("fp32_kahan_offset", False, True, True))
+    for name, fp16, kahan, offset in runs:
         pol = hx.policy_reference()
         pol.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
         pol.payload = hx.PAYLOAD_FP16 if fp16 else hx.PAYLOAD_FP32
         pol.accumulation = hx.ACCUM_KAHAN if kahan else hx.ACCUM_RUNNING_MEAN
+        pol.ray_offset = hx.RAY_OFFSET_SCALED if offset else hx.RAY_OFFSET_REFERENCE
         it = hx.PathIntegrator(ctx, scene, W, H, max_ray_bounces=DEPTH, max_samples=ref_spp, policy=pol,
                                max_paths_in_flight=W * H * 4)
         e0, e1 = hx.Event(ctx), hx.Event(ctx)
@@ -621,6 +626,11 @@ def run_precision(args, dist):
     # the oracle's own FP32 evaluation of the same samples: separates what FP32
     # arithmetic does to the reference's algorithm from what the device does
     ref32, _ = osc.render(d, f, spp, precision=32, pixels=pix)
+    # the same three under scaled ray origins
+    d.policy.ray_offset = hx.RAY_OFFSET_SCALED
+    ref_off, _ = osc.render(d, f, ref_spp, precision=64, pixels=pix)
+    ref_off_lo, _ = osc.render(d, f, spp, precision=64, pixels=pix)
+    ref32_off, _ = osc.render(d, f, spp, precision=32, pixels=pix)
     out["oracle_s"] = time.time() - t1
     out["oracle_pixels"] = int(pix.size)
     out["oracle_threads"] = cnt.threads
@@ -636,8 +646,17 @@ def run_precision(args, dist):
                                                          max((e ** 2).sum(), 1e-300))}
     rel = {}
     for (name, n), img in imgs.items():
-        rel["%s@%d_vs_fp64@%d" % (name, n, ref_spp)] = {"rel_rmse": rr(img[pix]), "per_pixel_abs_err_over_mean":
-                                                       dist_of(img[pix])}
+        if name.endswith("_offset"):
+            rel["%s@%d_vs_fp64_offset@%d" % (name, n, ref_spp)] = {
+                "rel_rmse": rr(img[pix], ref_off), "per_pixel_abs_err_over_mean": dist_of(img[pix], ref_off)}
+        else:
+            rel["%s@%d_vs_fp64@%d" % (name, n, ref_spp)] = {"rel_rmse": rr(img[pix]), "per_pixel_abs_err_over_mean":
+                                                           dist_of(img[pix])}
+    for name in ("fp16_kahan_offset", "fp32_kahan_offset"):
+        rel["%s@%d_vs_fp64_offset@%d" % (name, spp, spp)] = {"rel_rmse": rr(imgs[(name, spp)][pix], ref_off_lo)}
+    rel["oracle_fp32_offset@%d_vs_fp64_offset@%d" % (spp, spp)] = {"rel_rmse": rr(ref32_off, ref_off_lo)}
+    rel["fp64_offset@%d_vs_fp64_offset@%d (noise of %d spp)" % (spp, ref_spp, spp)] = {"rel_rmse": rr(ref_off_lo, ref_off)}
+    rel["fp64_offset@%d_vs_fp64@%d (what the offset changes)" % (ref_spp, ref_spp)] = {"rel_rmse": rr(ref_off)}
     # the Monte Carlo part: the FP64 oracle's own spp-sample image against its ref_spp one
     rel["fp64@%d_vs_fp64@%d (noise of %d spp)" % (spp, ref_spp, spp)] = {"rel_rmse": rr(ref_lo)}
     # the arithmetic part at spp: device vs the FP64 oracle at the same spp and sequence

@@ -23,6 +23,7 @@ RNG_XOROSHIRO64STAR, RNG_PCG = 0, 1
 ACCUM_RUNNING_MEAN, ACCUM_KAHAN = 0, 1
 ENV_SAMPLE_COSINE, ENV_SAMPLE_IMPORTANCE = 0, 1
 PAYLOAD_FP32, PAYLOAD_FP16 = 0, 1
+RAY_OFFSET_REFERENCE, RAY_OFFSET_SCALED = 0, 1
 TONEMAP_ACES, TONEMAP_REINHARD, TONEMAP_NONE = 0, 1, 2
 TEXTURE_RGBA8, TEXTURE_BC1_RGB, TEXTURE_BC1_RGBA, TEXTURE_BC2, TEXTURE_BC3, TEXTURE_BC4, TEXTURE_BC5, TEXTURE_BC7 = range(8)
 TEXTURE_BC6H_SF16, TEXTURE_BC6H_UF16, TEXTURE_RGBA16F, TEXTURE_RGBA8_SNORM = 8, 9, 10, 11
@@ -95,7 +96,7 @@ class Policy(C.Structure):
     _fields_ = [("rng", C.c_uint32), ("rr_start_depth", C.c_uint32), ("rr_clamp", C.c_uint32),
                 ("radiance_clamp", C.c_float), ("accumulation", C.c_uint32), ("area_count_from_x", C.c_uint32),
                 ("area_w_one", C.c_uint32), ("env_sampling", C.c_uint32), ("payload", C.c_uint32),
-                ("visualize_nans", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("visualize_nans", C.c_uint32), ("ray_offset", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class IntegratorDesc(C.Structure):

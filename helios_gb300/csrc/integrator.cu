@@ -139,7 +139,8 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     HX_CHECK_ARG(ctx && scene && desc && out, "hx_integrator_create: null argument");
     HX_CHECK_ARG(desc->width > 0 && desc->height > 0 && desc->width <= 16384 && desc->height <= 16384,
                  "hx_integrator_create: bad extents %ux%u", desc->width, desc->height);
-    HX_CHECK_ARG(desc->policy.rng <= 1 && desc->policy.accumulation <= 1, "hx_integrator_create: bad policy");
+    HX_CHECK_ARG(desc->policy.rng <= 1 && desc->policy.accumulation <= 1 && desc->policy.ray_offset <= 1,
+                 "hx_integrator_create: bad policy");
     HX_CHECK_ARG(!(desc->policy.visualize_nans && desc->policy.accumulation == HX_ACCUM_KAHAN),
                  "hx_integrator_create: visualize_nans needs running-mean accumulation");
     HX_CUDA(cudaSetDevice(ctx->device));
@@ -349,13 +350,15 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
                 StageTimer t(it, &it->stats.ms_shade);
                 it->stats.kernel_launches += fp16 ? launch_shade_partition<true>(qs, cur, st)
                                                   : launch_shade_partition<false>(qs, cur, st);
-                if (dbg)
-                    k_shade<false, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces,
-                                                                                   it->desc.shadow_ray_bias, cur, qs);
-                else if (fp16)
-                    k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, qs);
-                else
-                    k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, it->desc.max_ray_bounces, it->desc.shadow_ray_bias, cur, qs);
+                const float bias = it->desc.shadow_ray_bias;
+                const uint32_t nb = it->desc.max_ray_bounces;
+                if (P.ray_offset) {
+                    if (dbg) k_shade<false, true, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, nb, bias, cur, qs);
+                    else if (fp16) k_shade<true, false, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, nb, bias, cur, qs);
+                    else k_shade<false, false, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, nb, bias, cur, qs);
+                } else if (dbg) k_shade<false, true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, nb, bias, cur, qs);
+                else if (fp16) k_shade<true><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, nb, bias, cur, qs);
+                else k_shade<false><<<it->grid_shade, kShadeThreads, 0, st>>>(s, P, nb, bias, cur, qs);
                 it->stats.kernel_launches++;
             }
         }
@@ -493,7 +496,8 @@ extern "C" hx_status hx_integrator_set_tiled(hx_integrator* it, uint32_t tiled) 
     return HX_OK;
 }
 extern "C" hx_status hx_integrator_set_policy(hx_integrator* it, const hx_policy* p) {
-    HX_CHECK_ARG(it && p && p->rng <= 1 && p->accumulation <= 1, "hx_integrator_set_policy: bad policy");
+    HX_CHECK_ARG(it && p && p->rng <= 1 && p->accumulation <= 1 && p->ray_offset <= 1,
+                 "hx_integrator_set_policy: bad policy");
     HX_CHECK_ARG(!(p->visualize_nans && p->accumulation == HX_ACCUM_KAHAN),
                  "hx_integrator_set_policy: visualize_nans needs running-mean accumulation");
     it->desc.policy = *p;

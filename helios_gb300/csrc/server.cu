@@ -377,7 +377,8 @@ static hx_status batch_init(hx_server* s, SceneBatch* b) {
         cudaMemsetAsync(b->q.counters + (cur ^ 1), 0, 4, st);
         cudaMemsetAsync(b->q.counters + 2, 0, 4, st);
         launch_shade_partition<false>(b->q, cur, st);
-        k_shade<false><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
+        if (P.ray_offset) k_shade<false, false, true><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
+        else k_shade<false><<<grid_shade, kShadeThreads, 0, st>>>(sc, P, s->desc.max_ray_bounces, 0.0f, cur, b->q);
     }
     k_accumulate_multi<<<grid_gen, kGenThreads, 0, st>>>(b->d_hdr, b->d_chunks, s->d_slots, s->desc.policy.radiance_clamp,
                                                          s->desc.policy.visualize_nans ? 1u : 0u, b->q.L);
@@ -727,6 +728,7 @@ extern "C" hx_status hx_server_create(hx_context* ctx, const hx_server_desc* des
     HX_CHECK_ARG(desc->max_paths_per_tick >= 1024 && desc->max_ray_bounces >= 1 && desc->max_ray_bounces <= 64,
                  "hx_server_create: bad parameters");
     HX_CHECK_ARG(desc->request_arena_bytes >= (1u << 20), "hx_server_create: request arena too small");
+    HX_CHECK_ARG(desc->policy.rng <= 1 && desc->policy.ray_offset <= 1, "hx_server_create: bad policy");
     HX_CUDA(cudaSetDevice(ctx->device));
     hx_server* s = new hx_server();
     s->ctx = ctx;

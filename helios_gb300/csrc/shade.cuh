@@ -15,6 +15,7 @@ struct Surface {
 struct Policy {
     uint32_t rng, rr_start, rr_clamp, area_count_x, area_w_one, env_importance;
     float clampv;
+    uint32_t ray_offset;  // 1: HX_RAY_OFFSET_SCALED
 };
 
 HXD V3 rot_mul(V3 z, V3 t) {  // make_rotation_matrix(z) * t, sampling.glsl:28-36
@@ -86,6 +87,33 @@ HXD V3 sample_uber(uint32_t kind, const Surface& p, V3 Wo, Rng rng, V3& Wi, floa
     }
     pdf = pdf_uber(p, Wh, Wi);
     return evaluate_uber(p, Wo, Wh, Wi);
+}
+
+// Geometric normal of a hit triangle in world space: the object-space edge
+// cross product through the instance's normal matrix, normalised.
+HXD V3 geo_normal(const DevScene& s, uint32_t prim) {
+    const uint4 pi = __ldg(&s.prim_info[prim]);
+    const DevInstance& inst = s.inst[pi.x];
+    const uint32_t i0 = __ldg(&s.indices[3 * pi.y]), i1 = __ldg(&s.indices[3 * pi.y + 1]),
+                   i2 = __ldg(&s.indices[3 * pi.y + 2]);
+    const float4 p0 = __ldg(&s.vtx[2 * (size_t)i0]), p1 = __ldg(&s.vtx[2 * (size_t)i1]), p2 = __ldg(&s.vtx[2 * (size_t)i2]);
+    const V3 e1 = v3(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z);
+    const V3 e2 = v3(p2.x - p0.x, p2.y - p0.y, p2.z - p0.z);
+    return normalize(mat3_mul(inst.normal, cross(e1, e2)));
+}
+
+// HX_RAY_OFFSET_SCALED: the origin p moved off the surface along the
+// geometric normal ng, to the side of the outgoing direction, by
+// n_i (2^-15 |p_i| + 2^-16) in each coordinate — a continuous form of the
+// per-coordinate integer-ulp offset of Waechter and Binder ("A Fast and Robust
+// Method for Avoiding Self-Intersection", Ray Tracing Gems, 2019): 2^-15 |p_i|
+// is 128-256 ulps of p_i, well above the rounding of an interpolated,
+// instance-transformed FP32 hit position.
+HXD V3 offset_origin(V3 p, V3 ng, V3 dir) {
+    const V3 n = dot(ng, dir) < 0.0f ? -ng : ng;
+    return v3(p.x + n.x * (fabsf(p.x) * 3.0517578125e-5f + 1.52587890625e-5f),
+              p.y + n.y * (fabsf(p.y) * 3.0517578125e-5f + 1.52587890625e-5f),
+              p.z + n.z * (fabsf(p.z) * 3.0517578125e-5f + 1.52587890625e-5f));
 }
 
 // Surface properties at a hit (path_trace_rchit.glsl:256-280).

@@ -385,8 +385,10 @@ __global__ void k_raygen_debug(hx_frame_desc f, uint32_t px, uint32_t py, uint32
 // DEBUG: also records each hit of a ray after the camera ray as a segment
 // (ray origin, hit point; the path's colour) in q.dbg_verts
 // (path_trace_rchit.glsl:548-567); the order of segments is the order their
-// hits are shaded.
-template <bool FP16, bool DEBUG = false>
+// hits are shaded.  OFFSET: the policy's HX_RAY_OFFSET_SCALED origins (an
+// instantiation of its own, so the reference-origin kernel carries no code
+// for them).
+template <bool FP16, bool DEBUG = false, bool OFFSET = false>
 __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevScene s, Policy P, uint32_t max_bounces, float bias, int cur,
                                                          Queues q) {
     // with a shading list: misses [0, n_miss) then hits, else queue order
@@ -469,6 +471,13 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevSce
                         if (pdf != 0.0f) c = c / pdf;
                         c = c * (float)num_lights;
                         V3 o = p.position + p.normal * bias;
+                        if (OFFSET) {
+                            // the shadow ray starts closer to the light by at
+                            // most the offset's length: shorten it by that
+                            const V3 oo = offset_origin(o, geo_normal(s, prim), Wi);
+                            stmax = stmax - (fabsf(oo.x - o.x) + fabsf(oo.y - o.y) + fabsf(oo.z - o.z));
+                            o = oo;
+                        }
                         so = make_float4(o.x, o.y, o.z, 0.0001f);
                         ray_record(Wi, stmax, depth == 0, sr0, sr1);
                         sc = make_float4(c.x, c.y, c.z, __uint_as_float(path));
@@ -490,10 +499,11 @@ __global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) k_shade(DevSce
                     }
                     if (alive) {
                         q.T[path] = make_float4(Tn.x, Tn.y, Tn.z, __uint_as_float(depth + 1));
+                        const V3 o = OFFSET ? offset_origin(p.position, geo_normal(s, prim), Wi) : p.position;
                         if (FP16) {
-                            no = make_float4(p.position.x, p.position.y, p.position.z, __uint_as_float(oct_encode(Wi)));
+                            no = make_float4(o.x, o.y, o.z, __uint_as_float(oct_encode(Wi)));
                         } else {
-                            no = make_float4(p.position.x, p.position.y, p.position.z, 0.0001f);
+                            no = make_float4(o.x, o.y, o.z, 0.0001f);
                             nd = make_float4(Wi.x, Wi.y, Wi.z, 10000.0f);
                             ray_record(Wi, 10000.0f, false, nr0, nr1);
                         }
@@ -909,6 +919,7 @@ Policy make_policy(const hx_policy& p) {
     P.area_w_one = p.area_w_one;
     P.env_importance = p.env_sampling == HX_ENV_SAMPLE_IMPORTANCE;
     P.clampv = p.radiance_clamp;
+    P.ray_offset = p.ray_offset == HX_RAY_OFFSET_SCALED ? 1u : 0u;
     return P;
 }
 

@@ -244,6 +244,22 @@ typedef struct hx_scene_desc {
 #define HX_PAYLOAD_FP16 1u          /* 16-bit ray / hit payloads (precision form):
                                        direction = two snorm16 octahedral coords,
                                        barycentrics = FP16; traversal stays FP32 */
+/* Origins of the rays a hit spawns (the next bounce's ray and the shadow ray). */
+#define HX_RAY_OFFSET_REFERENCE 0u  /* the reference's: the interpolated hit position
+                                       (+ shading normal * shadow_ray_bias for shadow
+                                       rays), tmin 1e-4 (path_trace_rchit.glsl:293-295,
+                                       518-520)                                      */
+#define HX_RAY_OFFSET_SCALED 1u     /* that origin moved off the surface along the
+                                       geometric normal, to the side the ray leaves
+                                       on, by n_i * (2^-15 |p_i| + 2^-16) in each
+                                       coordinate (a continuous form of Waechter and
+                                       Binder's self-intersection offset, Ray Tracing
+                                       Gems ch. 6, 2019); shadow-ray tmax shortened by
+                                       the offset's L1 length.  The fixed tmin of 1e-4
+                                       is below the FP32 rounding of hit positions far
+                                       from the origin (ulp(2048) = 2.4e-4), so rays
+                                       re-hit the surface they leave there; this
+                                       removes that bias and keeps tmin as it is     */
 
 typedef struct hx_policy {
     uint32_t rng;                 /* HX_RNG_*                                              */
@@ -258,7 +274,8 @@ typedef struct hx_policy {
     uint32_t visualize_nans;      /* 1: a sample whose radiance has a NaN stores (1, 0, 0)
                                      in its pixel (VISUALIZE_NANS, path_trace_rgen.glsl:
                                      225-244); running-mean accumulation only             */
-    uint32_t reserved[2];
+    uint32_t ray_offset;          /* HX_RAY_OFFSET_*                                       */
+    uint32_t reserved;
 } hx_policy;
 
 /* Reference-faithful policy (every reference quirk reproduced). */

@@ -1094,6 +1094,31 @@ template <typename R> static Surface<R> populate(const Scene& s, uint32_t prim, 
     return p;
 }
 
+// HX_RAY_OFFSET_SCALED (the library's own policy, not the reference's): the
+// world-space geometric normal of a hit triangle (object-space edge cross
+// product through the normal matrix) and the ray origin moved off the surface
+// along it, to the side of the outgoing direction, by n_i (2^-15 |p_i| + 2^-16)
+// per coordinate — a continuous form of Waechter and Binder's self-intersection
+// offset (Ray Tracing Gems, 2019, ch. 6).  Same operation order as the device.
+template <typename R> static V3<R> geo_normal(const Scene& s, uint32_t prim) {
+    const PrimInfo& pi = s.prims[prim];
+    const hx_instance& inst = s.instances[pi.instance];
+    const hx_vertex& a = mesh_vertex<R>(s, inst.mesh_index, pi.mesh_prim, 0);
+    const hx_vertex& b = mesh_vertex<R>(s, inst.mesh_index, pi.mesh_prim, 1);
+    const hx_vertex& c = mesh_vertex<R>(s, inst.mesh_index, pi.mesh_prim, 2);
+    V3<R> e1(R(b.position[0]) - R(a.position[0]), R(b.position[1]) - R(a.position[1]), R(b.position[2]) - R(a.position[2]));
+    V3<R> e2(R(c.position[0]) - R(a.position[0]), R(c.position[1]) - R(a.position[1]), R(c.position[2]) - R(a.position[2]));
+    R N[16];
+    for (int k = 0; k < 16; ++k) N[k] = inst.normal_matrix[k];
+    return normalize(mat3_mul(N, cross(e1, e2)));
+}
+template <typename R> static V3<R> offset_origin(V3<R> p, V3<R> ng, V3<R> dir) {
+    const V3<R> n = dot(ng, dir) < R(0) ? -ng : ng;
+    const R rel = R(3.0517578125e-5f), ab = R(1.52587890625e-5f);  // 2^-15, 2^-16
+    return V3<R>(p.x + n.x * (std::fabs(p.x) * rel + ab), p.y + n.y * (std::fabs(p.y) * rel + ab),
+                 p.z + n.z * (std::fabs(p.z) * rel + ab));
+}
+
 struct Params {
     uint32_t width, height, max_bounces;
     float shadow_bias;
@@ -1340,6 +1365,11 @@ static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f,
                 V3<R> brdf = evaluate_uber(p, Wo, Wh, Wi);
                 R cos_theta = gclamp(dot(p.normal, Wi), R(0), R(1));
                 V3<R> so = p.position + p.normal * R(P.shadow_bias);
+                if (P.pol.ray_offset == HX_RAY_OFFSET_SCALED) {
+                    const V3<R> oo = offset_origin(so, geo_normal<R>(s, prim), Wi);
+                    stmax = stmax - (std::fabs(oo.x - so.x) + std::fabs(oo.y - so.y) + std::fabs(oo.z - so.z));
+                    so = oo;
+                }
                 R st, su, sv;
                 uint32_t sp;
                 cnt.shadow++;
@@ -1366,7 +1396,7 @@ static V3<R> trace_path(const Scene& s, const Params& P, const hx_frame_desc& f,
         }
         T = Tn;
         depth++;
-        o = p.position;
+        o = P.pol.ray_offset == HX_RAY_OFFSET_SCALED ? offset_origin(p.position, geo_normal<R>(s, prim), Wi) : p.position;
         d = fp16 ? payload_dir(Wi) : Wi;
         tmin = R(0.0001f);
         tmax = R(10000.0f);

@@ -57,6 +57,63 @@ def test_fp16_payload_samples_match_oracle(which, gpu_ctx, terrain):
     it.close()
 
 
+@pytest.mark.parametrize("which,fp16", [("box", False), ("terrain", False), ("terrain", True)])
+def test_scaled_ray_offset_samples_match_oracle(which, fp16, gpu_ctx, terrain):
+    """HX_RAY_OFFSET_SCALED origins (geometric normal, position-relative
+    offset; shadow rays shortened by the offset): per-sample radiance, device
+    vs the oracle's FP32 evaluation of the same policy.  The box has an area
+    light (shadow rays end 1e-4 before it, so the shortening matters); the
+    terrain's coordinates reach 2048."""
+    if which == "box":
+        hs = hx.HostScene(hx.SCENE_BOX)
+        sc, osc, pol, W, H, b = hx.Scene(gpu_ctx, hs), None, _policy("spec", fp16=fp16), 64, 64, 5
+    else:
+        hs, sc, osc = terrain
+        pol, W, H, b = _policy("reference", fp16=fp16), 96, 54, 8
+    pol.ray_offset = hx.RAY_OFFSET_SCALED
+    osc = osc or ob.OracleScene(hs)
+    d = integrator_desc(W, H, bounces=b)
+    d.policy = pol
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=b, policy=pol)
+    for frame in (0, 5):
+        g = it.sample_radiance(f, frame)
+        o, _ = osc.sample_radiance(d, f, frame, precision=32)
+        close = np.all(np.abs(g - o) <= 1e-4 * (1 + np.abs(o)), axis=1)
+        info = (frame, rel_rmse(g, o), int((~close).sum()))
+        assert close.mean() > 0.995, info
+        assert rel_rmse(g, o) < 1e-2, info
+    it.close()
+
+
+def test_scaled_ray_offset_converges_to_fp64(gpu_ctx, terrain):
+    """Terrain at world scale (coordinates to 2048), 1024 spp: the device's
+    FP32 image against the FP64 oracle's image of the same samples, with the
+    reference's ray origins and with HX_RAY_OFFSET_SCALED.  The reference's
+    fixed tmin of 1e-4 is below the FP32 rounding of hit positions there, so
+    FP32 re-hits surfaces that FP64 leaves (a bias); scaled origins remove it
+    and leave the noise of paths that diverge by rounding."""
+    hs, sc, osc = terrain
+    W, H, spp = 1920, 1080, 1024
+    f = hx.frame_desc(hs.camera(), W, H)
+    pix = np.random.default_rng(12).choice(W * H, size=1024, replace=False).astype(np.uint32)
+    err = {}
+    for off in (hx.RAY_OFFSET_REFERENCE, hx.RAY_OFFSET_SCALED):
+        pol = _policy("reference", fp16=False)
+        pol.ray_offset = off
+        d = integrator_desc(W, H, bounces=8, max_samples=1 << 30)
+        d.policy = pol
+        ref, _ = osc.render(d, f, spp, precision=64, pixels=pix)
+        it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=8, max_samples=spp, policy=pol)
+        it.render(f, spp)
+        img = it.read_accumulation()[:, :, :3].reshape(-1, 3)
+        it.close()
+        err[off] = rel_rmse(img[pix], ref)
+    print("device FP32 vs FP64 oracle (reference origins, scaled origins):", err)
+    assert err[hx.RAY_OFFSET_SCALED] < 0.5 * err[hx.RAY_OFFSET_REFERENCE], err
+    assert err[hx.RAY_OFFSET_SCALED] < 2e-3, err
+
+
 def test_fp16_primary_hit_agreement(gpu_ctx, terrain):
     """Hit-ID agreement of primary rays whose directions went through the
     16-bit octahedral payload with FP32 rays.  The quantised BVH itself never

@@ -147,6 +147,36 @@ def test_fp32_matches_fp64_oracle():
     assert rel_rmse(a, b) < 1e-4
 
 
+def test_scaled_ray_offset_removes_the_fp32_bias_at_world_scale():
+    """The terrain spans 4096 units: FP32 hit positions there carry rounding
+    above the reference's fixed tmin of 1e-4 (ulp(2048) = 2.4e-4), so in FP32
+    some secondary and shadow rays re-hit the surface they leave — a bias
+    against the FP64 evaluation of the same samples that does not shrink with
+    more samples.  HX_RAY_OFFSET_SCALED moves the origins off the surface by a
+    position-relative amount; what is left between FP32 and FP64 is the noise
+    of paths that diverge by rounding (it falls with the sample count).
+    Measured here: 3.1e-3 with the reference's origins, 0.9e-3 with scaled
+    ones; FP64 images with and without the offset differ by 1.0e-4 (the
+    offset moves origins by at most 2^-15 of their coordinates)."""
+    hs = hx.HostScene(hx.SCENE_TERRAIN, terrain_size=256, num_spheres=40, env_width=256, env_height=128)
+    osc = ob.OracleScene(hs)
+    W, H = 1920, 1080
+    f = hx.frame_desc(hs.camera(), W, H)
+    pix = np.random.default_rng(11).choice(W * H, size=1024, replace=False).astype(np.uint32)
+    err, img64 = {}, {}
+    for off in (hx.RAY_OFFSET_REFERENCE, hx.RAY_OFFSET_SCALED):
+        d = integrator_desc(W, H, bounces=8, policy="reference", max_samples=1 << 30)
+        d.policy.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
+        d.policy.ray_offset = off
+        img64[off], _ = osc.render(d, f, 1024, precision=64, pixels=pix)
+        r32, _ = osc.render(d, f, 1024, precision=32, pixels=pix)
+        err[off] = rel_rmse(r32, img64[off])
+    print("FP32 vs FP64 relative RMSE (reference origins, scaled origins):", err)
+    assert err[hx.RAY_OFFSET_SCALED] < 0.4 * err[hx.RAY_OFFSET_REFERENCE], err
+    assert err[hx.RAY_OFFSET_SCALED] < 1.5e-3, err
+    assert rel_rmse(img64[hx.RAY_OFFSET_SCALED], img64[hx.RAY_OFFSET_REFERENCE]) < 5e-4
+
+
 def test_light_list_reference_order():
     hs = small_icosphere_scene()
     osc = ob.OracleScene(hs)
