@@ -209,7 +209,9 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
     it->grid_shade = std::max(1, per_sm) * ctx->num_sms;
     it->grid_gen = ctx->num_sms * 8;
     HX_CUDA(set_carveouts(k_extend_batched<false, false>, k_extend_batched<true, false>, k_extend_batched<false, true>,
-                          k_extend_batched<true, true>));
+                          k_extend_batched<true, true>, k_extend_batched<false, false, true>,
+                          k_extend_batched<true, false, true>, k_extend_batched<false, true, true>,
+                          k_extend_batched<true, true, true>));
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend_batched<false>, kTraceThreads, 0));
     it->grid_batched = std::max(1, per_sm) * ctx->num_sms;
     compute_tiles(it);

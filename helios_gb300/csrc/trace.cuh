@@ -625,3 +625,70 @@ HXD void warp_test_tris(WarpTris& w, uint32_t lane, uint32_t n, const DevScene& 
         __syncwarp();
     }
 }
+
+// The same tests for 16-bit payloads, whose extension rays carry no traversal
+// record in memory: the testing lane takes the owner's origin, tmin, shear and
+// flags from the owner's registers (warp shuffles of its TravState, which
+// trav_init_record filled with exactly the record's values).
+template <bool COUNT, bool WA>
+HXD void warp_test_tris_shfl(WarpTris& w, uint32_t lane, uint32_t n, const DevScene& s, const TravState& st,
+                             bool& overflow, TraverseCount* tc) {
+    const uint32_t my_bits = (uint32_t)st.r.kx | ((uint32_t)st.r.ky << 2) | ((uint32_t)st.r.kz << 4) |
+                             (st.any_hit ? 1u << 9 : 0u);
+    for (uint32_t b0 = 0; b0 < n; b0 += 32u) {
+        const uint32_t e = b0 + lane;
+        const uint32_t ent = e < n ? w.tri[e] : 0u;
+        const uint32_t own = ent >> 27;
+        RayPre r;
+        r.o = v3(__shfl_sync(0xffffffffu, st.r.o.x, own), __shfl_sync(0xffffffffu, st.r.o.y, own),
+                 __shfl_sync(0xffffffffu, st.r.o.z, own));
+        const float tmin = __shfl_sync(0xffffffffu, st.tmin, own);
+        r.sx = __shfl_sync(0xffffffffu, st.r.sx, own);
+        r.sy = __shfl_sync(0xffffffffu, st.r.sy, own);
+        r.sz = __shfl_sync(0xffffffffu, st.r.sz, own);
+        const uint32_t bits = __shfl_sync(0xffffffffu, my_bits, own);
+        r.kx = (int)(bits & 3u);
+        r.ky = (int)((bits >> 2) & 3u);
+        r.kz = (int)((bits >> 4) & 3u);
+        r.ix = r.iy = r.iz = 0.0f;
+        unsigned long long cand = ~0ull;
+        float cu = 0.0f, cv = 0.0f;
+        if (e < n) {
+            const uint32_t k = ent & 0x07ffffffu;
+            if (COUNT) {
+                tc->tris++;
+                if (lowest_active_lane()) tc->warp_tris++;
+            }
+            if (k < s.num_prims) {
+                const float4 a = __ldg(&s.tri[3 * (size_t)k]);
+                const float4 bb = __ldg(&s.tri[3 * (size_t)k + 1]);
+                const float4 cc = __ldg(&s.tri[3 * (size_t)k + 2]);
+                const unsigned long long key = w.key[own];
+                const float best_t = __uint_as_float((uint32_t)(key >> 32));
+                const uint32_t best = (uint32_t)key;
+                float t, u, v;
+                if (intersect_tri(r, v3(a), v3(bb), v3(cc), tmin, best_t, t, u, v)) {
+                    const uint32_t prim = __float_as_uint(a.w);
+                    if (t < best_t || (t == best_t && prim < best)) {
+                        bool pass = true;
+                        if ((bits & (1u << 9)) && (__float_as_uint(bb.w) & HX_TRI_NONOPAQUE)) {
+                            if (COUNT) tc->alpha++;
+                            pass = alpha_pass<WA>(s, prim, u, v);
+                        }
+                        if (pass) {
+                            cand = ((unsigned long long)__float_as_uint(t) << 32) | prim;
+                            atomicMin(&w.key[own], cand);
+                            cu = u;
+                            cv = v;
+                        }
+                    }
+                }
+            } else {
+                overflow = true;
+            }
+        }
+        __syncwarp();
+        if (cand != ~0ull && w.key[own] == cand) w.uv[own] = make_float2(cu, cv);
+        __syncwarp();
+    }
+}

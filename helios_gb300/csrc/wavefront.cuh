@@ -636,9 +636,11 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_extend(DevSc
     if (overflow) atomicOr(q.status, 1u);
 }
 
-// Batched triangle tests run every bounce of the FP32-payload path (with
-// three node visits per iteration they also beat the lane-local k_extend on
-// the small late launches: +0.7%); k_extend serves the 16-bit payload form.
+// Batched triangle tests run every bounce (with three node visits per
+// iteration they also beat the lane-local k_extend on the small late
+// launches: +0.7%), for both payload forms (16-bit payloads on the 34.5 M-
+// triangle terrain: 845 Mpaths/s batched, 674 lane-local; FP32 885); k_extend
+// serves scenes of 2^27 triangles or more.
 // Flush after 24 queued triangles or 4 waiting lanes (measured on the
 // 1.18 M-triangle scene at 1080p: 16-24 queued and 2-4 waiting lanes within
 // 0.2 % of each other, 12 queued -0.8 %, 32 queued -1.5 %).
@@ -657,11 +659,15 @@ constexpr uint32_t kNodeSteps = 3;
 // keeps them and visits no node until they do.  A ray is finished when it
 // has no node left and no pending triangle (or, for a shadow ray, as soon as
 // a flush accepted a hit).  Same queues, results and counters as k_extend.
-template <bool COUNT, bool WA = false>
+// FP16: 16-bit payloads (qo = origin + octahedral direction, qp = path |
+// any-hit flag, 8-byte hit records): a lane builds its ray's traversal record
+// at refill, and the triangle testers take it from the owner's registers
+// (warp_test_tris_shfl).
+template <bool COUNT, bool WA = false, bool FP16 = false>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
     k_extend_batched(DevScene s, Queues q, const float4* __restrict__ qo, const float4* __restrict__ qr0,
                      const float4* __restrict__ qr1, const uint32_t* __restrict__ count, uint32_t* fetch,
-                     uint32_t flush_tris, uint32_t flush_parked) {
+                     uint32_t flush_tris, uint32_t flush_parked, const uint32_t* __restrict__ qp) {
     __shared__ WarpTris warp_tris[kTraceThreads / 32];
     WarpTris& w = warp_tris[threadIdx.x >> 5];
     const uint32_t n_ext = *count;
@@ -694,9 +700,19 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
                 float tmax = 0.0f;
                 if (i < n_ext) {
                     ray = i;
-                    const float4 r0 = qr0[i];
-                    trav_init_record(st, s, qo[i], r0, qr1[i]);
-                    tmax = r0.w;
+                    if (FP16) {
+                        // the record of trav_init(o, decoded d, tmin by ray kind, 10000, any)
+                        const float4 o = qo[i];
+                        const bool any = (qp[i] & kAnyHitFlag) != 0;
+                        float4 r0, r1;
+                        ray_record(oct_decode(__float_as_uint(o.w)), 10000.0f, any, r0, r1);
+                        trav_init_record(st, s, make_float4(o.x, o.y, o.z, any ? 0.001f : 0.0001f), r0, r1);
+                        tmax = r0.w;
+                    } else {
+                        const float4 r0 = qr0[i];
+                        trav_init_record(st, s, qo[i], r0, qr1[i]);
+                        tmax = r0.w;
+                    }
                     w.rid[lane] = i;
                 } else if (i < n) {
                     ray = i - n_ext;
@@ -753,7 +769,8 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
         const uint32_t walking = __ballot_sync(0xffffffffu, has_node && tmask == 0);
         const uint32_t carried = __ballot_sync(0xffffffffu, tmask != 0);
         if (qn >= flush_tris || (uint32_t)__popc(parked) >= flush_parked || carried != 0 || (qn > 0 && walking == 0)) {
-            warp_test_tris<COUNT, WA>(w, lane, qn, s, qo, qr1, q.so, q.sr1, overflow, &cnt);
+            if (FP16) warp_test_tris_shfl<COUNT, WA>(w, lane, qn, s, st, overflow, &cnt);
+            else warp_test_tris<COUNT, WA>(w, lane, qn, s, qo, qr1, q.so, q.sr1, overflow, &cnt);
             qn = 0;
             queued = false;
         }
@@ -771,9 +788,12 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
                     }
                 } else {
                     const float2 uv = w.uv[lane];
-                    q.hit[ray] = best != kNoHit
-                                     ? make_float4(__uint_as_float((uint32_t)(key >> 32)), __uint_as_float(best), uv.x, uv.y)
-                                     : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
+                    if (FP16)
+                        reinterpret_cast<uint2*>(q.hit)[ray] = make_uint2(best, best != kNoHit ? half2_bits(uv.x, uv.y) : 0u);
+                    else
+                        q.hit[ray] = best != kNoHit
+                                         ? make_float4(__uint_as_float((uint32_t)(key >> 32)), __uint_as_float(best), uv.x, uv.y)
+                                         : make_float4(0.0f, __uint_as_float(kNoHit), 0.0f, 0.0f);
                     if (q.list_mode == 1u) shade_list_append(q, best == kNoHit, ray);
                 }
                 ray = kNoHit;
@@ -794,19 +814,19 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
 }
 
 // One traversal launch: the batched kernel for scenes under 2^27 triangles
-// with FP32 payloads, else the per-lane one; the WA instantiations (wide-alpha
-// any-hit path) only for scenes that need them.
+// (the queue's triangle index field), else the per-lane one; the WA
+// instantiations (wide-alpha any-hit path) only for scenes that need them.
 template <bool COUNT, bool FP16>
 static inline void launch_extend(const DevScene& s, const Queues& q, int grid_batched, int grid_trace, cudaStream_t st,
                                  const float4* qo, const float4* qr0, const float4* qr1, const uint32_t* qp,
                                  const uint32_t* count, uint32_t* fetch) {
-    if (!FP16 && s.num_prims < (1u << 27)) {
+    if (s.num_prims < (1u << 27)) {
         if (s.wide_alpha)
-            k_extend_batched<COUNT, true><<<grid_batched, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, count, fetch,
-                                                                                  kFlushTris, kFlushParked);
+            k_extend_batched<COUNT, true, FP16><<<grid_batched, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, count, fetch,
+                                                                                        kFlushTris, kFlushParked, qp);
         else
-            k_extend_batched<COUNT, false><<<grid_batched, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, count, fetch,
-                                                                                   kFlushTris, kFlushParked);
+            k_extend_batched<COUNT, false, FP16><<<grid_batched, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, count, fetch,
+                                                                                         kFlushTris, kFlushParked, qp);
     } else {
         if (s.wide_alpha)
             k_extend<COUNT, FP16, true><<<grid_trace, kTraceThreads, 0, st>>>(s, q, qo, qr0, qr1, qp, count, fetch);

@@ -245,6 +245,36 @@ def test_half_float_and_snorm_textures_match_oracle(gpu_ctx, case):
     sc.close()
 
 
+def test_wide_alpha_with_16bit_payloads_matches_oracle(gpu_ctx):
+    """The any-hit alpha test on an RGBA16F texture (the traversal's wide-alpha
+    instantiation) under 16-bit ray / hit payloads, against the oracle's
+    emulation of the same payload rounding."""
+    w, h = 24, 20
+    rng = np.random.default_rng(8)
+    texels = rng.uniform(0.0, 1.6, (h, w, 4)).astype(np.float16)
+    texels[..., 1] = rng.uniform(0.05, 0.95, (h, w)).astype(np.float16)
+    texels[..., 3] = np.where(rng.uniform(0, 1, (h, w)) < 0.3, 0.02, 1.0).astype(np.float16)
+    extra = dict(non_opaque=True, roughness_channel=1)
+    qs, sc = _hdr_quad(gpu_ctx, albedo=texels, albedo_format=hx.TEXTURE_RGBA16F, albedo_wh=(w, h), **extra)
+    oq = TexturedQuadScene(texels, albedo_srgb=False, normal_map=bump_normal_map(), albedo_format=hx.TEXTURE_RGBA16F,
+                           albedo_wh=(w, h), **extra)
+    osc = ob.OracleScene(oq)
+    W, H = 96, 64
+    d = integrator_desc(W, H, bounces=4, policy="reference")
+    d.policy.payload = hx.PAYLOAD_FP16
+    f = hx.frame_desc(qs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=4, policy=d.policy)
+    for frame in (0, 5):
+        g = it.sample_radiance(f, frame)
+        o, _ = osc.sample_radiance(d, f, frame, precision=32)
+        close = np.all(np.abs(g - o) <= 1e-4 * (1 + np.abs(o)), axis=1)
+        info = (frame, rel_rmse(g, o), int((~close).sum()))
+        assert close.mean() > 0.995, info
+        assert rel_rmse(g, o) < 1e-2, info
+    it.close()
+    sc.close()
+
+
 def test_bc6h_renders_like_its_rgba16f_texels(gpu_ctx):
     """A BC6H albedo texture (decoded at upload) gives the same accumulated
     image and albedo view, bit for bit, as uploading its RGBA16F decode; a
