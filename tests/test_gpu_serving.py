@@ -47,10 +47,12 @@ def _reference_image(ctx, scene, hs, w, h, spp, pol, bounces):
     return img
 
 
-def test_results_identical_alone_and_in_the_mix(gpu_ctx, scenes):
+@pytest.mark.parametrize("ray_offset", [hx.RAY_OFFSET_REFERENCE, hx.RAY_OFFSET_SCALED])
+def test_results_identical_alone_and_in_the_mix(gpu_ctx, scenes, ray_offset):
     (box, s_box), (ico, s_ico) = scenes
     pol = hx.policy_reference()
     pol.env_sampling = hx.ENV_SAMPLE_IMPORTANCE
+    pol.ray_offset = ray_offset
     srv = hx.Server(gpu_ctx, arena_bytes=1 << 30, max_paths_per_tick=1 << 20, max_ray_bounces=6, policy=pol)
     ib, ii = srv.add_scene(s_box), srv.add_scene(s_ico)
     srv.start()
