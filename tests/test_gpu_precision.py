@@ -114,6 +114,27 @@ def test_scaled_ray_offset_converges_to_fp64(gpu_ctx, terrain):
     assert err[hx.RAY_OFFSET_SCALED] < 2e-3, err
 
 
+def test_fp16_counting_mode_renders_the_same_image(gpu_ctx, terrain):
+    """16-bit payloads through the batched traversal in its counting
+    instantiation (node visits, triangle tests, SIMD counters) accumulate the
+    same image as without counting."""
+    hs, sc, _ = terrain
+    W, H = 320, 180
+    pol = _policy("reference", fp16=True, kahan=True)
+    f = hx.frame_desc(hs.camera(), W, H)
+    imgs, stats = [], None
+    for counting in (False, True):
+        it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=8, policy=pol)
+        it.set_counting(counting)
+        it.render(f, 2)
+        if counting:
+            stats = it.stats()
+        imgs.append(it.read_accumulation())
+        it.close()
+    assert imgs[0].tobytes() == imgs[1].tobytes()
+    assert stats.node_visits > 0 and stats.tri_tests > 0 and stats.warp_node_steps > 0
+
+
 def test_fp16_primary_hit_agreement(gpu_ctx, terrain):
     """Hit-ID agreement of primary rays whose directions went through the
     16-bit octahedral payload with FP32 rays.  The quantised BVH itself never
