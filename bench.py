@@ -372,6 +372,21 @@ def run_ours(args, dist):
     peaks = load_peaks()
     hbm_peak = peaks["hbm_gbs"]
     achieved = alg_bytes_per_launch / (ms_trace_per_launch / 1000.0) / 1e9
+    # the two-level model of the traversal launch: queue bytes (rays, hits,
+    # shadow entries) at the HBM peak, node and triangle bytes (cache-served)
+    # at this GPU's L2 read bandwidth, measured here (48 MiB working set)
+    l2_gbs = ctx.read_bandwidth(48 << 20, 200)
+    hbm_read_gbs = ctx.read_bandwidth(4 << 30, 3)
+    queue_b = (ext_rays * (36 + 16) + sh_rays * 48) / max(1, ct.trace_launches)
+    trav_b = trav_bytes / max(1, ct.trace_launches)
+    t_launch = ms_trace_per_launch / 1000.0
+    t_model = queue_b / (hbm_peak * 1e9) + trav_b / (l2_gbs * 1e9)
+    l2_model = {"l2_read_gbs": l2_gbs, "hbm_read_gbs": hbm_read_gbs,
+                "l2_source": "hx_measure_read_bandwidth: one launch reading a 48 MiB buffer 200 times, L1 bypassed "
+                             "(HBM: 4 GiB, 3 passes)",
+                "queue_bytes_per_launch": queue_b, "trav_bytes_per_launch": trav_b,
+                "trav_achieved_gbs": trav_b / t_launch / 1e9, "trav_frac_of_l2": trav_b / t_launch / 1e9 / l2_gbs,
+                "frac": t_model / t_launch}
     traffic = None
     ncu = {}
     try:
@@ -423,7 +438,7 @@ def run_ours(args, dist):
                              "bytes_per_launch": alg_bytes_per_launch, "ms_per_launch": ms_trace_per_launch,
                              "node_fetches_per_segment": ct.node_visits / max(1, ext_rays + sh_rays),
                              "tri_tests_per_segment": ct.tri_tests / max(1, ext_rays + sh_rays),
-                             "simd_lanes": simd},
+                             "simd_lanes": simd, "l2_model": l2_model},
                 "clocks": clk,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)

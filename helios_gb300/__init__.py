@@ -192,6 +192,7 @@ _SIGS = {
     "hx_context_destroy": (C.c_int, [_P]),
     "hx_context_synchronize": (C.c_int, [_P]),
     "hx_context_memory": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "hx_measure_read_bandwidth": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.POINTER(C.c_double)]),
     "hx_scene_upload": (C.c_int, [_P, C.POINTER(SceneDesc), C.POINTER(_P)]),
     "hx_scene_destroy": (C.c_int, [_P]),
     "hx_scene_info_get": (C.c_int, [_P, C.POINTER(SceneInfo)]),
@@ -424,6 +425,12 @@ class Context:
         u, b = C.c_uint64(), C.c_uint64()
         check(lib().hx_context_memory(self.handle, C.byref(u), C.byref(b)))
         return u.value, b.value
+
+    def read_bandwidth(self, nbytes, passes):
+        """GB/s of one launch reading an nbytes buffer `passes` times (L1 bypassed)."""
+        g = C.c_double()
+        check(lib().hx_measure_read_bandwidth(self.handle, nbytes, passes, C.byref(g)))
+        return g.value
 
     def rng_streams(self, kind, seeds, draws):
         seeds = np.ascontiguousarray(seeds, dtype=np.uint32)

@@ -115,6 +115,55 @@ extern "C" hx_status hx_context_memory(hx_context* ctx, uint64_t* used, uint64_t
     return HX_OK;
 }
 
+// One pass = every 16-byte word of the buffer read once (ld.global.cg: L2,
+// not L1); the XOR of the words is stored only if it equals a constant it
+// practically never equals, which keeps the loads without writing.
+__global__ void k_read_bandwidth(const uint4* __restrict__ buf, size_t n16, uint32_t passes, uint32_t* sink) {
+    uint32_t acc = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (uint32_t p = 0; p < passes; ++p)
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) {
+            const uint4 v = __ldcg(buf + i);
+            acc ^= v.x ^ v.y ^ v.z ^ v.w;
+        }
+    if (acc == 0x9e3779b9u) sink[blockIdx.x] = acc;
+}
+
+extern "C" hx_status hx_measure_read_bandwidth(hx_context* ctx, uint64_t bytes, uint32_t passes, double* gbs) {
+    HX_CHECK_ARG(ctx && gbs && passes > 0 && bytes >= (1u << 20) && bytes % 16 == 0,
+                 "hx_measure_read_bandwidth: bad argument");
+    HX_CUDA(cudaSetDevice(ctx->device));
+    const int blocks = 8 * ctx->num_sms, threads = 256;
+    DevBuffer buf, sink;
+    HX_TRY(buf.reserve(ctx, bytes));
+    HX_TRY(sink.reserve(ctx, 4 * (size_t)blocks));
+    cudaStream_t st = ctx->stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    hx_status rs = HX_OK;
+    float ms = 0.0f;
+    if (cudaMemsetAsync(buf.ptr, 0x5a, bytes, st) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+        rs = HX_ERR_DEVICE;
+    } else {
+        k_read_bandwidth<<<blocks, threads, 0, st>>>(buf.as<uint4>(), bytes / 16, 1, sink.as<uint32_t>());  // warm-up
+        cudaEventRecord(e0, st);
+        k_read_bandwidth<<<blocks, threads, 0, st>>>(buf.as<uint4>(), bytes / 16, passes, sink.as<uint32_t>());
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.0f)
+            rs = HX_ERR_DEVICE;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    buf.release();
+    sink.release();
+    if (rs != HX_OK) {
+        hx_set_error("hx_measure_read_bandwidth: CUDA error %s", cudaGetErrorString(cudaGetLastError()));
+        return rs;
+    }
+    *gbs = (double)bytes * passes / (ms * 1e-3) / 1e9;
+    return HX_OK;
+}
+
 struct hx_event {
     hx_context* ctx;
     cudaEvent_t ev;

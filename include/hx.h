@@ -388,6 +388,14 @@ HX_API hx_status   hx_context_create(int device, uint64_t hbm_budget_bytes, hx_c
 HX_API hx_status   hx_context_destroy(hx_context* ctx);
 HX_API hx_status   hx_context_synchronize(hx_context* ctx);
 HX_API hx_status   hx_context_memory(hx_context* ctx, uint64_t* used_bytes, uint64_t* budget_bytes);
+/* Read bandwidth of this GPU for a working set of `bytes` (a multiple of 16,
+ * at least 1 MiB): one launch reads the buffer `passes` times with 16-byte
+ * loads that bypass L1, timed with events on the context stream.  A working
+ * set well under the L2 (129 MB) gives the L2 read bandwidth, one of
+ * gigabytes the HBM read bandwidth: the denominators of the traversal's
+ * cache-served and DRAM bytes.  The buffer is allocated and freed inside the
+ * call (charged to the context's budget meanwhile). */
+HX_API hx_status   hx_measure_read_bandwidth(hx_context* ctx, uint64_t bytes, uint32_t passes, double* gb_per_s);
 HX_API const char* hx_last_error_string(void);
 HX_API const char* hx_version(void);
 

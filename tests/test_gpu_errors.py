@@ -94,3 +94,17 @@ def test_tensor_core_wait_timeout_is_reported_and_recovers(gpu_ctx):
     for b in (fb, tb, ob):
         b.close()
     dn.close()
+
+
+def test_read_bandwidth_probe(gpu_ctx):
+    """hx_measure_read_bandwidth: positive GB/s for an L2-sized and an
+    HBM-sized working set; malformed sizes are rejected before any launch."""
+    l2 = gpu_ctx.read_bandwidth(32 << 20, 50)
+    hbm = gpu_ctx.read_bandwidth(1 << 30, 2)
+    print("read bandwidth GB/s: 32 MiB", l2, "1 GiB", hbm)
+    assert l2 > 0 and hbm > 0
+    for nbytes, passes in (((32 << 20) + 8, 1), (1 << 10, 1), (32 << 20, 0)):
+        with pytest.raises(hx.HxError) as e:
+            gpu_ctx.read_bandwidth(nbytes, passes)
+        assert e.value.status == hx.HX_ERR_INVALID_ARG
+
