@@ -1,7 +1,7 @@
 """Benchmark: Mpaths/s of the wavefront path tracer on the 1M-triangle scene.
 
-Workload (config 1; one step = one progressive frame, K steps = the K-frame
-job, 256 by default): 12 instances of a level-6 icosphere (81,920 triangles
+Workload (one step = one progressive frame, K steps = the K-frame job, 256
+by default): 12 instances of a level-6 icosphere (81,920 triangles
 each) + a 2-triangle ground plane + 100k alpha-tested quads (64 distinct
 512x512 RGBA8 value-noise masks, 50% cut out), Hosek-Wilkie sky (sun
 elevation 30 deg, turbidity 3) baked to a 2048x1024 FP16 lat-long map with
@@ -47,7 +47,7 @@ METRIC = "Mpaths/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=256, help="frames (config 1: 256 frames of 1 spp)")
+    p.add_argument("--steps", type=int, default=256, help="frames (the 256-frame job of 1 spp each)")
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--frames-per-wavefront", type=int, default=64,
@@ -318,7 +318,7 @@ def run_ours(args, dist):
             "warp_tri_steps_per_node_step": ct.warp_tri_steps / max(1, ct.warp_node_steps),
             "alpha_tests_per_segment": ct.alpha_tests / max(1, ext_rays + sh_rays)}
 
-    # 3) the K-frame job (config 1: 1 spp per frame, K frames accumulated), fpw
+    # 3) the K-frame job (1 spp per frame, K frames accumulated), fpw
     #    frames per wavefront; device-timed with CUDA events on the library stream
     it.render(frame, max(args.warmup, fpw))
     ctx.synchronize()
@@ -576,7 +576,7 @@ def run_serving(args, dist):
 
 
 def run_precision(args, dist):
-    """Precision form at scale (config 2): 200 spheres + a terrain_size^2 fBm
+    """Precision form at scale: 200 spheres + a terrain_size^2 fBm
     heightfield, 1920x1080; 8-bit quantised BVH8 boxes, 16-bit ray/hit
     payloads, FP32 traversal, Kahan-compensated FP32 accumulation, to args.spp
     (4096) samples per pixel and on to args.ref_spp (16384).  The FP64

@@ -1,5 +1,5 @@
-// server.cu — resident render-serving loop (spec serving form; the
-// nearest reference hook is the per-frame Renderer::render,
+// server.cu — resident render-serving loop (no counterpart in the reference;
+// the nearest reference hook is the per-frame Renderer::render,
 // src/engine/gfx/renderer.cpp:107, driven once per window frame by the
 // application loop, src/engine/core/application.cpp:38-54).
 //
