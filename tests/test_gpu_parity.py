@@ -373,3 +373,46 @@ def test_importance_sampled_sky_samples_match_oracle(gpu_ctx, ico):
         assert close.mean() > 0.999, (frame, int((~close).sum()))
         assert rel_rmse(g, o) < 1e-4
     it.close()
+
+
+@pytest.mark.parametrize("case", ["one_triangle", "no_geometry", "no_lights"])
+def test_degenerate_scenes_match_oracle(gpu_ctx, case):
+    """Edge scenes: a single triangle (a one-leaf BVH), no geometry at all
+    (every ray misses; no BVH nodes), and geometry without any light (no NEE
+    draw).  Primary hits bit-exact and per-sample radiance against the
+    oracle; the accumulated image stays finite."""
+    from tests.helpers import TexturedQuadScene
+    q = TexturedQuadScene(np.full((8, 8, 4), 200, np.uint8), albedo_srgb=False)
+    if case == "one_triangle":
+        q._sub[0].index_count = 3
+        q._mesh[0].num_indices = 3
+    elif case == "no_geometry":
+        q._desc.num_meshes = 0
+        q._desc.num_instances = 0
+    else:
+        q._desc.num_punctual_lights = 0
+    sc = hx.Scene(gpu_ctx, q)
+    osc = ob.OracleScene(q)
+    W = H = 32
+    d = integrator_desc(W, H, bounces=4, policy="reference")
+    f = hx.frame_desc(q.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=4, policy=d.policy)
+    gh = it.primary_hits(f, 0)
+    oh = osc.trace(ob.primary_rays(d, f, 0), any_hit=True)
+    assert np.array_equal(gh["prim"], oh["prim"]) and np.array_equal(gh["t"], oh["t"])
+    if case == "no_geometry":
+        assert (gh["prim"] == hx.NO_HIT).all()
+    else:
+        assert (gh["prim"] != hx.NO_HIT).any()
+    for frame in (0, 3):
+        g = it.sample_radiance(f, frame)
+        o, _ = osc.sample_radiance(d, f, frame, precision=32)
+        assert np.all(np.abs(g - o) <= 1e-4 * (1 + np.abs(o))), (frame, rel_rmse(g, o))
+    it.render(f, 8)
+    acc = it.read_accumulation()
+    assert np.isfinite(acc).all()
+    if case != "one_triangle":
+        assert np.abs(acc[..., :3]).max() == 0.0
+    it.close()
+    sc.close()
+
