@@ -141,6 +141,8 @@ extern "C" hx_status hx_integrator_create(hx_context* ctx, const hx_scene* scene
                  "hx_integrator_create: bad extents %ux%u", desc->width, desc->height);
     HX_CHECK_ARG(desc->policy.rng <= 1 && desc->policy.accumulation <= 1 && desc->policy.ray_offset <= 1,
                  "hx_integrator_create: bad policy");
+    HX_CHECK_ARG(desc->max_ray_bounces <= 64, "hx_integrator_create: max_ray_bounces %u above 64",
+                 desc->max_ray_bounces);
     HX_CHECK_ARG(!(desc->policy.visualize_nans && desc->policy.accumulation == HX_ACCUM_KAHAN),
                  "hx_integrator_create: visualize_nans needs running-mean accumulation");
     HX_CUDA(cudaSetDevice(ctx->device));
@@ -315,8 +317,13 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
     }
     {
         // bounce b: k_extend traces the extension rays of b and the shadow
-        // rays of b - 1; a last launch traces the final bounce's shadow rays
-        for (uint32_t b = 0; b <= it->desc.max_ray_bounces; ++b) {
+        // rays of b - 1; a last launch traces the final bounce's shadow rays.
+        // The camera hit is always shaded (the closest-hit shader runs for
+        // every traced ray; only the indirect ray obeys (depth + 1) <
+        // max_ray_bounces, path_trace_rchit.glsl:577), so a limit of 0 traces
+        // like 1.
+        const uint32_t bounces = std::max<uint32_t>(1u, it->desc.max_ray_bounces);
+        for (uint32_t b = 0; b <= bounces; ++b) {
             const int cur = b & 1;
             {
                 StageTimer t(it, &it->stats.ms_trace);
@@ -335,7 +342,7 @@ static hx_status run_wavefront(hx_integrator* it, const hx_frame_desc& f, Rect r
                 it->stats.trace_launches++;
                 it->stats.kernel_launches++;
             }
-            if (b == it->desc.max_ray_bounces) break;
+            if (b == bounces) break;
             if (b == 0 && it->aov && accumulate) {
                 if (fp16)
                     k_aov_accumulate<true><<<it->grid_gen, kGenThreads, 0, st>>>(s, rect, frame0, nframes, it->q.hit, it->aov_a,
@@ -477,7 +484,7 @@ extern "C" hx_status hx_integrator_restart_bake(hx_integrator* it) {
     return HX_OK;
 }
 extern "C" hx_status hx_integrator_set_max_ray_bounces(hx_integrator* it, uint32_t n) {
-    HX_CHECK_ARG(it && n >= 1 && n <= 64, "hx_integrator_set_max_ray_bounces: bad value");
+    HX_CHECK_ARG(it && n <= 64, "hx_integrator_set_max_ray_bounces: bad value");
     it->desc.max_ray_bounces = n;
     return HX_OK;
 }

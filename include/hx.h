@@ -290,7 +290,8 @@ HX_API void hx_policy_spec(hx_policy* out);
 
 typedef struct hx_integrator_desc {
     uint32_t  width, height;       /* output extents (swap_chain_extents)          */
-    uint32_t  max_ray_bounces;     /* default 7, path_integrator.h:47               */
+    uint32_t  max_ray_bounces;     /* default 7, path_integrator.h:47; 0..64 (0 shades
+                                      the camera hit like 1: no indirect ray)     */
     uint32_t  max_samples;         /* default 5000, path_integrator.h:48            */
     float     shadow_ray_bias;     /* default 0, path_integrator.h:51               */
     uint32_t  tiled;               /* 128x128 tiles, path_integrator.cpp:7,312-336  */

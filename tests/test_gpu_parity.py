@@ -170,6 +170,26 @@ def test_sample_radiance_matches_oracle(which, policy, gpu_ctx, box, ico):
     it.close()
 
 
+@pytest.mark.parametrize("bounces", [0, 1, 2, 24])
+def test_sample_radiance_at_depth_limits_matches_oracle(bounces, gpu_ctx, ico):
+    """The depth limit's edges: 0 and 1 (the camera hit is shaded, emission and
+    NEE, but no indirect ray leaves it: (depth + 1) < max_ray_bounces fails for
+    both, as in the reference), two, and 24 (paths end by Russian roulette
+    long before the limit), per-sample against the oracle."""
+    hs, sc, osc = ico
+    W, H = 96, 54
+    d = integrator_desc(W, H, bounces=bounces, policy="spec")
+    f = hx.frame_desc(hs.camera(), W, H)
+    it = hx.PathIntegrator(gpu_ctx, sc, W, H, max_ray_bounces=bounces, policy=d.policy)
+    for frame in (0, 3):
+        g = it.sample_radiance(f, frame)
+        o, _ = osc.sample_radiance(d, f, frame, precision=32)
+        close = np.all(np.abs(g - o) <= 1e-4 * (1 + np.abs(o)), axis=1)
+        assert close.mean() > 0.995, (bounces, frame, rel_rmse(g, o))
+        assert rel_rmse(g, o) < 1e-2, (bounces, frame, rel_rmse(g, o))
+    it.close()
+
+
 def test_partitioned_shading_list_samples_match_oracle(gpu_ctx, ico):
     """A wavefront of 2^19 paths (1024 x 512, one frame) is shaded from the
     slot-order partition of each bounce's rays (misses ascending, hits
