@@ -809,8 +809,9 @@ __global__ void k_up_bwd(const bf16* __restrict__ gin, int h, int w, int C, int 
     reinterpret_cast<uint4*>(gout + ((size_t)(r.n * h + r.y) * w + r.x) * C)[r.g] = pack8(s);
 }
 
-// Features [n][h][w][12] (radiance rgb, -, albedo rgb, depth, normal xyz, -)
-// -> network input [n][H][W][32] BF16, zero outside h x w and beyond ch 9.
+// Features [n][h][w][12] (radiance rgb, noise level, albedo rgb, depth, normal
+// xyz, -) -> network input [n][H][W][32] BF16 (log1p radiance, albedo, normal,
+// depth, noise level), zero outside h x w and beyond channel 10.
 __global__ void k_pack_input(const float* __restrict__ feat, int h, int w, int H, int W, int nimg,
                              bf16* __restrict__ x) {
     const size_t total = (size_t)nimg * H * W;
@@ -833,6 +834,7 @@ __global__ void k_pack_input(const float* __restrict__ feat, int h, int w, int H
             f[7] = nm.y;
             f[8] = nm.z;
             f[9] = ad.w;
+            f[10] = r.w;
         }
         uint4* d = reinterpret_cast<uint4*>(x + p * 32);
 #pragma unroll

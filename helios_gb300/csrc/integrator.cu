@@ -925,7 +925,8 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     // (the progressive counter wraps to 0 when max_samples is reached, the
     // image and AOV buffers keep the finished frame)
     if (it->aov && it->aov_frames > 0) {
-        k_features_accumulated<<<it->grid_gen, kGenThreads, 0, st>>>(it->resolved, it->aov_a, it->aov_n, n, d_features);
+        k_features_accumulated<<<it->grid_gen, kGenThreads, 0, st>>>(it->resolved, it->aov_a, it->aov_n, n, it->count_map,
+                                                                     1u, d_features);
         HX_CUDA(cudaGetLastError());
         return HX_OK;
     }
@@ -934,7 +935,8 @@ extern "C" hx_status hx_integrator_features(hx_integrator* it, const hx_frame_de
     k_raygen<false><<<it->grid_gen, kGenThreads, 0, st>>>(*f, r, W, H, frame_index, 1, 0, W * H, P.rng, it->q);
     HX_CUDA(cudaMemsetAsync(it->q.counters + 4, 0, 24, st));
     launch_primary_trace(it, st);
-    k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, W, H, d_features);
+    k_features<<<it->grid_gen, kGenThreads, 0, st>>>(it->scene->d, it->q.hit, it->resolved, W, H, it->count_map,
+                                                      d_features);
     HX_CUDA(cudaGetLastError());
     HX_TRY(check_status(it));
     return HX_OK;

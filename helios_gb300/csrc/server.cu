@@ -565,7 +565,8 @@ static hx_status launch_tick(hx_server* s, SceneBatch* b, uint32_t scene_id) {
 // before tone mapping.
 static hx_status denoise_request(hx_server* s, SceneBatch* b, ServerRequest* r) {
     const uint32_t W = r->desc.width, H = r->desc.height;
-    k_features_accumulated<<<b->grid_gen, kGenThreads, 0, b->run>>>(r->acc, r->aov_a, r->aov_n, W * H, r->feat);
+    k_features_accumulated<<<b->grid_gen, kGenThreads, 0, b->run>>>(r->acc, r->aov_a, r->aov_n, W * H, nullptr,
+                                                                    r->desc.spp, r->feat);
     HX_CUDA(cudaGetLastError());
     HX_CUDA(cudaEventRecord(s->dn_ready, b->run));
     HX_CUDA(cudaStreamWaitEvent(s->ctx->stream, s->dn_ready, 0));

@@ -944,12 +944,18 @@ Policy make_policy(const hx_policy& p) {
 }
 
 
-// Denoiser features per pixel (12 floats): current image rgb, 0, albedo rgb,
-// depth feature log1p(t)/8, shading normal xyz, 0 — first-hit AOVs as the
-// reference's debug views define them (debug_visualization.frag:142-161:
-// base colour, shading normal); zeros on a miss.
+// Denoiser features per pixel (12 floats): current image rgb, noise level,
+// albedo rgb, depth feature log1p(t)/8, shading normal xyz, 0 — first-hit AOVs
+// as the reference's debug views define them (debug_visualization.frag:
+// 142-161: base colour, shading normal); zeros on a miss.  The noise level is
+// 1 / sqrt(samples in the pixel) (the Monte Carlo standard error's scale), from
+// the per-pixel count map, or `samples` for every pixel when it is null.
+HXD float noise_level(const uint32_t* count_map, uint32_t samples, uint32_t i) {
+    const uint32_t c = count_map ? count_map[i] : samples;
+    return 1.0f / sqrtf((float)(c > 0u ? c : 1u));
+}
 __global__ void k_features(DevScene s, const float4* __restrict__ hit, const float4* __restrict__ img, uint32_t W,
-                           uint32_t H, float* __restrict__ feat) {
+                           uint32_t H, const uint32_t* __restrict__ count_map, float* __restrict__ feat) {
     const Rect rect{0, 0, W, H};
     const uint32_t n = W * H;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -965,7 +971,7 @@ __global__ void k_features(DevScene s, const float4* __restrict__ hit, const flo
             depth = log1pf(h.x) * 0.125f;
         }
         float4* o = reinterpret_cast<float4*>(feat + 12 * (size_t)i);
-        o[0] = make_float4(r.x, r.y, r.z, 0.0f);
+        o[0] = make_float4(r.x, r.y, r.z, noise_level(count_map, 1u, i));
         o[1] = make_float4(alb.x, alb.y, alb.z, depth);
         o[2] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
     }
@@ -1021,13 +1027,16 @@ __global__ void k_aov_accumulate(DevScene s, Rect rect, uint32_t frame0, uint32_
     }
 }
 
-// Denoiser features from the accumulated image and accumulated AOVs.
+// Denoiser features from the accumulated image and accumulated AOVs (noise
+// level from count_map, or `samples` for every pixel when it is null).
 __global__ void k_features_accumulated(const float4* __restrict__ img, const float4* __restrict__ aov_a,
-                                       const float4* __restrict__ aov_n, uint32_t n, float* __restrict__ feat) {
+                                       const float4* __restrict__ aov_n, uint32_t n,
+                                       const uint32_t* __restrict__ count_map, uint32_t samples,
+                                       float* __restrict__ feat) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 r = img[i];
         float4* o = reinterpret_cast<float4*>(feat + 12 * (size_t)i);
-        o[0] = make_float4(r.x, r.y, r.z, 0.0f);
+        o[0] = make_float4(r.x, r.y, r.z, noise_level(count_map, samples, i));
         o[1] = aov_a[i];
         o[2] = aov_n[i];
     }

@@ -786,8 +786,9 @@ HX_API hx_status hx_hosek_wilkie_coefficients(const float sun_direction[3], floa
  * BF16 weights and activations with FP32 accumulation on the tensor cores,
  * trained by its own forward/backward kernels and Adam.
  *
- * Features: per pixel 12 floats, NHWC — radiance rgb, 0, albedo rgb, depth
- * feature log1p(t)/8 (0 on a miss), shading normal xyz, 0.  Targets: per
+ * Features: per pixel 12 floats, NHWC — radiance rgb, noise level
+ * 1/sqrt(samples in the pixel), albedo rgb, depth feature log1p(t)/8 (0 on a
+ * miss), shading normal xyz, 0.  Targets: per
  * pixel RGBA float radiance (alpha ignored).  The network predicts
  * log1p(radiance) as the input's log1p radiance plus a learned correction;
  * the loss is chosen by hx_denoiser_set_loss.  Parameters: one flat FP32 vector, per layer W[9][cout][cin]
@@ -843,10 +844,11 @@ HX_API hx_status hx_denoiser_read_output(hx_denoiser* dn, uint32_t training, flo
  * over the same frames as the image; off by default).  Switching it restarts
  * the progressive accumulation. */
 HX_API hx_status hx_integrator_set_aov_accumulation(hx_integrator* it, uint32_t enabled);
-/* Denoiser inputs from an integrator: the current accumulated image plus
- * albedo / normal / depth — the accumulated AOVs when AOV accumulation is on,
- * else those of the primary hits of sample frame_index — into d_features
- * (width*height*12 floats, device memory). */
+/* Denoiser inputs from an integrator: the current accumulated image, its
+ * noise level (1/sqrt of each pixel's sample count) and albedo / normal /
+ * depth — the accumulated AOVs when AOV accumulation is on, else those of the
+ * primary hits of sample frame_index — into d_features (width*height*12
+ * floats, device memory). */
 HX_API hx_status hx_integrator_features(hx_integrator* it, const hx_frame_desc* frame, uint32_t frame_index,
                                         float* d_features);
 /* The accumulated image (resolved RGBA floats) into device memory. */

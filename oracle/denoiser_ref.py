@@ -13,7 +13,7 @@ central differences of the forward pass.
 Network (5 levels, 3x3 'same' convolutions, ReLU, 2x2 average pooling,
 nearest 2x upsampling, skip connections by concatenation):
 
-    x   (32 ch: log1p radiance, albedo, normal, depth, zero padding)
+    x   (32 ch: log1p radiance, albedo, normal, depth, noise level, zero padding)
     a0  = relu(conv(x))            32   level 0
     a0b = relu(conv(a0))           32   level 0   (skip)
     a1  = relu(conv(pool(a0b)))    64   level 1   (skip)
@@ -99,7 +99,7 @@ def bf16(a):
 
 def pack_input(features, rnd=True):
     """features [n,h,w,12] float32 -> x [n,h,w,32]: log1p(max(radiance,0)),
-    albedo, normal, depth, then zeros."""
+    albedo, normal, depth, noise level (feature 3), then zeros."""
     f = np.asarray(features, np.float64)
     n, h, w, _ = f.shape
     x = np.zeros((n, h, w, IN_CHANNELS))
@@ -107,6 +107,7 @@ def pack_input(features, rnd=True):
     x[..., 3:6] = f[..., 4:7]
     x[..., 6:9] = f[..., 8:11]
     x[..., 9] = f[..., 7]
+    x[..., 10] = f[..., 3]
     return bf16(x) if rnd else x
 
 
