@@ -72,9 +72,9 @@ def parse():
     p.add_argument("--denoise-kernels", action="store_true",
                    help="denoiser kernel timing: 1080p inference and a 16 x 256^2 training step (random network)")
     p.add_argument("--dn-iters", type=int, default=20, help="timed iterations of --denoise-kernels")
-    p.add_argument("--dn-variants", type=int, default=512)
+    p.add_argument("--dn-variants", type=int, default=768)
     p.add_argument("--dn-target-spp", type=int, default=4096)
-    p.add_argument("--dn-steps", type=int, default=100000)
+    p.add_argument("--dn-steps", type=int, default=150000)
     p.add_argument("--dn-ref-spp", type=int, default=4096)
     p.add_argument("--dn-eval-seeds", type=int, nargs="+", default=[5000, 5001])
     p.add_argument("--dn-save", default="", help="directory for the trained parameters (one .npy per loss)")
