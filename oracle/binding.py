@@ -43,6 +43,7 @@ _SIGS = {
     "oracle_float_to_half": (C.c_uint16, [C.c_float]),
     "oracle_half_to_float": (C.c_float, [C.c_uint16]),
     "oracle_max_threads": (C.c_int, []),
+    "oracle_offset_origins": (None, [_P, _P, _P, C.c_uint32, _P]),
 }
 
 _lib = None

@@ -1826,4 +1826,18 @@ uint16_t oracle_float_to_half(float f) { return float_to_half(f); }
 float oracle_half_to_float(uint16_t h) { return half_to_float(h); }
 int oracle_max_threads(void) { return omp_get_max_threads(); }
 
+// HX_RAY_OFFSET_SCALED origins in FP32 for n points (p, geometric normal ng,
+// outgoing direction d; 3 floats each), for the property tests.
+void oracle_offset_origins(const float* p, const float* ng, const float* d, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = p + 3 * (size_t)i;
+        const float* b = ng + 3 * (size_t)i;
+        const float* c = d + 3 * (size_t)i;
+        V3<float> o = offset_origin(V3<float>(a[0], a[1], a[2]), V3<float>(b[0], b[1], b[2]), V3<float>(c[0], c[1], c[2]));
+        out[3 * (size_t)i] = o.x;
+        out[3 * (size_t)i + 1] = o.y;
+        out[3 * (size_t)i + 2] = o.z;
+    }
+}
+
 }  // extern "C"

@@ -177,6 +177,42 @@ def test_scaled_ray_offset_removes_the_fp32_bias_at_world_scale():
     assert rel_rmse(img64[hx.RAY_OFFSET_SCALED], img64[hx.RAY_OFFSET_REFERENCE]) < 5e-4
 
 
+def test_scaled_origins_leave_the_surface_at_world_scale():
+    """HX_RAY_OFFSET_SCALED as a property: FP32 hit points (barycentric
+    interpolation of triangles whose coordinates reach 4096) offset along the
+    FP32 geometric normal lie strictly on the side the ray leaves on, measured
+    against the exact (FP64) plane of the triangle, for every one of 200,000
+    hits; the raw FP32 hit points (the reference's origins) fall on the wrong
+    side or on the plane for a large share of them."""
+    import ctypes as C
+    rng = np.random.default_rng(21)
+    n = 200_000
+    c = rng.uniform(-4096, 4096, (n, 1, 3))
+    v = (c + rng.uniform(-4, 4, (n, 3, 3))).astype(np.float32)
+    b = rng.dirichlet((1, 1, 1), n).astype(np.float32)
+    p32 = (v[:, 0] * b[:, :1] + v[:, 1] * b[:, 1:2] + v[:, 2] * b[:, 2:3]).astype(np.float32)
+    e1, e2 = (v[:, 1] - v[:, 0]), (v[:, 2] - v[:, 0])
+    ng = np.cross(e1, e2).astype(np.float32)
+    ng /= np.linalg.norm(ng, axis=1, keepdims=True)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    out = np.zeros((n, 3), np.float32)
+    ptr = lambda a: np.ascontiguousarray(a, np.float32).ctypes.data_as(C.c_void_p)
+    p32c, ngc, dc = (np.ascontiguousarray(a, np.float32) for a in (p32, ng, d))
+    ob.lib().oracle_offset_origins(ptr(p32c), ptr(ngc), ptr(dc), n, out.ctypes.data_as(C.c_void_p))
+    v64 = v.astype(np.float64)
+    n64 = np.cross(v64[:, 1] - v64[:, 0], v64[:, 2] - v64[:, 0])
+    n64 /= np.linalg.norm(n64, axis=1, keepdims=True)
+    side = np.sign(np.einsum("ij,ij->i", d.astype(np.float64), n64))
+    keep = side != 0
+    dist_off = np.einsum("ij,ij->i", out.astype(np.float64) - v64[:, 0], n64) * side
+    dist_raw = np.einsum("ij,ij->i", p32.astype(np.float64) - v64[:, 0], n64) * side
+    assert (dist_off[keep] > 0).all(), np.sort(dist_off[keep])[:5]
+    wrong_raw = (dist_raw[keep] <= 0).mean()
+    print("raw FP32 hit points on the wrong side or on the plane:", wrong_raw)
+    assert wrong_raw > 0.2
+
+
 def test_light_list_reference_order():
     hs = small_icosphere_scene()
     osc = ob.OracleScene(hs)
